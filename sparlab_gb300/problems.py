@@ -1,0 +1,268 @@
+"""Structured cantilever problems on Q4 / Hex8 grids.
+
+These builders play the role of the reference's ``FemModel::finalize`` for the
+structured decks the SIMP loop runs on (``src/fem/FemModel.cpp:286-385``):
+box supports select nodes within ``1e-9 * diagonal`` of the box
+(``src/fem/Selector.cpp:12-52``), a point load spread over N nodes puts
+``force / N`` on each (``src/fem/BoundaryConditions.cpp:46-52``), and
+load-case weights are normalised to sum to one (``FemModel.cpp:412-420``).
+
+The seeded generator is SplitMix64 (Steele, Lea and Flood, 2014) so the CPU
+and GPU paths, and every machine, see identical bits.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Dict, List, Optional
+
+import numpy as np
+
+MASK64 = (1 << 64) - 1
+
+
+class SplitMix64:
+    """SplitMix64 stream; ``stream`` offsets the state by the golden gamma."""
+
+    def __init__(self, seed: int, stream: int = 0):
+        self.state = (seed * 0xD1B54A32D192ED03 + stream * 0x9E3779B97F4A7C15) & MASK64
+
+    def next_u64(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & MASK64
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+        return z ^ (z >> 31)
+
+    def uniform(self, lo: float = 0.0, hi: float = 1.0) -> float:
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / (1 << 53)))
+
+    def integers(self, lo: int, hi: int) -> int:
+        """Uniform integer in [lo, hi] inclusive."""
+        return lo + self.next_u64() % (hi - lo + 1)
+
+    def uniform_array(self, n: int, lo: float, hi: float) -> np.ndarray:
+        # vectorised SplitMix64 over a counter: identical to n calls of uniform()
+        idx = np.arange(1, n + 1, dtype=np.uint64)
+        with np.errstate(over="ignore"):
+            z = (np.uint64(self.state) + idx * np.uint64(0x9E3779B97F4A7C15))
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            z = z ^ (z >> np.uint64(31))
+        self.state = (self.state + n * 0x9E3779B97F4A7C15) & MASK64
+        u = (z >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))
+        return lo + (hi - lo) * u
+
+
+@dataclasses.dataclass
+class ProblemSpec:
+    dim: int
+    nx: int
+    ny: int
+    nz: int
+    lx: float
+    ly: float
+    lz: float
+    young: float = 1.0
+    poisson: float = 0.3
+    thickness: float = 1.0
+    fixed: Optional[np.ndarray] = None      # uint8 per DOF (node * dim + k)
+    loads: Optional[np.ndarray] = None      # (L, ndof)
+    weights: Optional[np.ndarray] = None    # (L,) raw weights
+    filter_radius: float = 1.5
+    volume_fraction: float = 0.5
+    initial_density: float = -1.0
+    penalty: float = 3.0
+    emin_ratio: float = 1e-9
+    move_limit: float = 0.2
+    damping: float = 0.5
+    rtol: float = 1e-8
+    max_cg_iterations: int = 0
+    warm_start: bool = True
+    amg: Dict = dataclasses.field(default_factory=dict)
+    name: str = ""
+
+    @property
+    def nodes_per_axis(self):
+        return (self.nx + 1, self.ny + 1, (self.nz + 1) if self.dim == 3 else 1)
+
+    @property
+    def num_nodes(self) -> int:
+        a, b, c = self.nodes_per_axis
+        return a * b * c
+
+    @property
+    def num_elements(self) -> int:
+        return self.nx * self.ny * (self.nz if self.dim == 3 else 1)
+
+    @property
+    def num_dofs(self) -> int:
+        return self.num_nodes * self.dim
+
+    def node_index(self, i, j, k=0) -> int:
+        nnx, nny, _ = self.nodes_per_axis
+        return (k * nny + j) * nnx + i
+
+    def node_coords(self) -> np.ndarray:
+        """(num_nodes, dim) coordinates, x0 + i * dx as the mesh generator forms them."""
+        nnx, nny, nnz = self.nodes_per_axis
+        dx, dy = self.lx / self.nx, self.ly / self.ny
+        i = np.arange(nnx) * dx
+        j = np.arange(nny) * dy
+        if self.dim == 2:
+            X, Y = np.meshgrid(i, j, indexing="xy")
+            return np.stack([X.ravel(), Y.ravel()], axis=1)
+        dz = self.lz / self.nz
+        k = np.arange(nnz) * dz
+        Z, Y, X = np.meshgrid(k, j, i, indexing="ij")
+        return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+
+    def free_dofs(self) -> np.ndarray:
+        return np.flatnonzero(self.fixed == 0).astype(np.int32)
+
+
+def _diag(spec: ProblemSpec) -> float:
+    if spec.dim == 2:
+        return math.hypot(spec.lx, spec.ly)
+    return math.sqrt(spec.lx ** 2 + spec.ly ** 2 + spec.lz ** 2)
+
+
+def clamp_left(spec: ProblemSpec, components=None) -> np.ndarray:
+    """Fix every component of the nodes on the x = 0 face (box xmax = 0)."""
+    tol = 1e-9 * max(_diag(spec), 1e-30)
+    x = spec.node_coords()[:, 0]
+    nodes = np.flatnonzero(x <= 0.0 + tol)
+    fixed = np.zeros(spec.num_dofs, np.uint8)
+    comps = range(spec.dim) if components is None else components
+    for k in comps:
+        fixed[nodes * spec.dim + k] = 1
+    return fixed
+
+
+def nearest_node(spec: ProblemSpec, point) -> int:
+    c = spec.node_coords()
+    p = np.zeros(spec.dim)
+    p[:] = point[: spec.dim]
+    d2 = ((c - p) ** 2).sum(axis=1)
+    return int(np.argmin(d2))   # first minimum, as the reference's strict '<' scan
+
+
+def point_load(spec: ProblemSpec, nodes, force) -> np.ndarray:
+    """Load vector with ``force`` spread equally over ``nodes``."""
+    f = np.zeros(spec.num_dofs)
+    nodes = np.atleast_1d(np.asarray(nodes, np.int64))
+    scale = 1.0 / len(nodes)
+    for n in nodes:
+        for k in range(spec.dim):
+            f[n * spec.dim + k] += scale * force[k]
+    return f
+
+
+# ---------------------------------------------------------------------------
+# The reference's own benchmark model (apps/sparlab_bench.cpp:87-127)
+# ---------------------------------------------------------------------------
+def bench_model(dim: int, nx: int, ny: int, nz: int = 0) -> ProblemSpec:
+    """lx=2, ly=1, lz=0.5; E=70e9, nu=0.3; t=0.01 in 2-D; x=0 clamped;
+    (0, -1000, 0) N at the node nearest (lx, 0, 0); solid density."""
+    spec = ProblemSpec(dim=dim, nx=nx, ny=ny, nz=nz if dim == 3 else 0, lx=2.0, ly=1.0,
+                       lz=0.5 if dim == 3 else 0.0, young=70.0e9, poisson=0.3,
+                       thickness=0.01 if dim == 2 else 1.0, filter_radius=0.0,
+                       name=f"bench_{'hex8' if dim == 3 else 'quad4'}_{nx}x{ny}" +
+                       (f"x{nz}" if dim == 3 else ""))
+    spec.fixed = clamp_left(spec)
+    tip = nearest_node(spec, (spec.lx, 0.0, 0.0))
+    spec.loads = point_load(spec, [tip], (0.0, -1000.0, 0.0))[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
+# ---------------------------------------------------------------------------
+# The five workload configurations
+# ---------------------------------------------------------------------------
+def q4_cantilever_120x40() -> ProblemSpec:
+    """Q4 120x40 unit cells, x=0 clamped, unit downward load at (120, 20)."""
+    spec = ProblemSpec(dim=2, nx=120, ny=40, nz=0, lx=120.0, ly=40.0, lz=0.0,
+                       thickness=1.0, filter_radius=1.5, volume_fraction=0.5,
+                       initial_density=0.5, rtol=1e-8, name="q4_120x40")
+    spec.fixed = clamp_left(spec)
+    spec.loads = point_load(spec, [spec.node_index(120, 20)], (0.0, -1.0))[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
+def q4_cantilever_600x200(seed: int = 2) -> ProblemSpec:
+    """Q4 600x200, r=3, vf=0.35, three unit loads at right-edge nodes j=50,
+    100, 150 in directions (sin t, -cos t), t ~ U[-90, 90] deg (stream i)."""
+    spec = ProblemSpec(dim=2, nx=600, ny=200, nz=0, lx=600.0, ly=200.0, lz=0.0,
+                       thickness=1.0, filter_radius=3.0, volume_fraction=0.35,
+                       rtol=1e-8, name="q4_600x200")
+    spec.fixed = clamp_left(spec)
+    loads = []
+    for i, j in enumerate((50, 100, 150)):
+        t = math.radians(SplitMix64(seed, i).uniform(-90.0, 90.0))
+        loads.append(point_load(spec, [spec.node_index(600, j)], (math.sin(t), -math.cos(t))))
+    spec.loads = np.stack(loads)
+    spec.weights = np.full(3, 1.0 / 3.0)
+    return spec
+
+
+def hex8_cantilever(nx: int, ny: int, nz: int, volume_fraction: float, name: str) -> ProblemSpec:
+    """Hex8 unit cells, x=0 face clamped, unit total load in -z spread over the
+    edge {i = nx, k = 0} (ny + 1 nodes)."""
+    spec = ProblemSpec(dim=3, nx=nx, ny=ny, nz=nz, lx=float(nx), ly=float(ny), lz=float(nz),
+                       filter_radius=1.5, volume_fraction=volume_fraction, rtol=1e-8, name=name)
+    spec.fixed = clamp_left(spec)
+    edge = [spec.node_index(nx, j, 0) for j in range(ny + 1)]
+    spec.loads = point_load(spec, edge, (0.0, 0.0, -1.0))[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
+def hex8_96x48x48() -> ProblemSpec:
+    return hex8_cantilever(96, 48, 48, 0.2, "hex8_96x48x48")
+
+
+def hex8_192x96x96() -> ProblemSpec:
+    return hex8_cantilever(192, 96, 96, 0.15, "hex8_192x96x96")
+
+
+def seeded_density(spec: ProblemSpec, seed: int = 3, lo: float = 0.01, hi: float = 1.0) -> np.ndarray:
+    """i.i.d. U[lo, hi] element densities (seeded SplitMix64)."""
+    return SplitMix64(seed).uniform_array(spec.num_elements, lo, hi)
+
+
+def batched_instances(seed: int = 4, count_q4: int = 48, count_hex: int = 16) -> List[ProblemSpec]:
+    """Uneven independent instances: Q4 nx~U{64..256}, ny~U{32..128}; Hex8
+    edges ~U{16..40}; clamped left face; 1-4 unit loads at random right-face
+    nodes; vf ~ U[0.2, 0.5]; p=3, r=1.5."""
+    rng = SplitMix64(seed)
+    out = []
+    for q in range(count_q4 + count_hex):
+        dim = 2 if q < count_q4 else 3
+        if dim == 2:
+            nx, ny, nz = rng.integers(64, 256), rng.integers(32, 128), 0
+        else:
+            nx, ny, nz = rng.integers(16, 40), rng.integers(16, 40), rng.integers(16, 40)
+        spec = ProblemSpec(dim=dim, nx=nx, ny=ny, nz=nz, lx=float(nx), ly=float(ny),
+                           lz=float(nz), filter_radius=1.5,
+                           volume_fraction=rng.uniform(0.2, 0.5), rtol=1e-8,
+                           name=f"inst{q}")
+        spec.fixed = clamp_left(spec)
+        loads = []
+        for _ in range(rng.integers(1, 4)):
+            j = rng.integers(0, ny)
+            k = rng.integers(0, nz) if dim == 3 else 0
+            if dim == 2:
+                t = rng.uniform(-math.pi / 2, math.pi / 2)
+                force = (math.sin(t), -math.cos(t))
+            else:
+                # uniform direction on the sphere
+                zc = rng.uniform(-1.0, 1.0)
+                ph = rng.uniform(0.0, 2.0 * math.pi)
+                s = math.sqrt(max(0.0, 1.0 - zc * zc))
+                force = (s * math.cos(ph), s * math.sin(ph), zc)
+            loads.append(point_load(spec, [spec.node_index(nx, j, k)], force))
+        spec.loads = np.stack(loads)
+        spec.weights = np.ones(len(loads))
+        out.append(spec)
+    return out
