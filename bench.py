@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""SIMP iterations per second of the GPU inner loop (one JSON line).
+
+A step is one SIMP iteration (filter, SIMP law, K_ff assembly, AMG setup,
+AMG-PCG per load case, sensitivities, filter pull-back, OC update) on the
+seeded synthetic Hex8 cantilever of 192 x 96 x 96 cells (1,769,472 elements,
+5,419,584 free DOFs), resident in GPU memory.  `value` is device-timed (CUDA
+events on the library's stream); `e2e` repeats the step through the public
+API with the design copied from pinned host memory and back every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl own|reference]
+                  [--config NAME] [--precision fp64|mixed]
+
+`--impl reference` times the CPU restatement of the reference's algorithm (the
+reference itself needs Eigen, which is absent) on the host cores, on a bounded
+sample of the workload (a geometrically similar grid with 1/64 of the cells,
+whose iteration time is scaled by the cell ratio: the reference's AMG-CG costs
+grow linearly, docs/benchmarks.md:1455-1458 of the reference).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from sparlab_gb300 import problems as P  # noqa: E402
+
+METRIC = "SIMP iter/s at Hex8 1.77M elts, compliance err<=1e-6: plain vs learned+mixed"
+
+WORKLOADS = {
+    "hex8_192x96x96": (P.hex8_192x96x96, (96, 48, 48)),
+    "hex8_96x48x48": (P.hex8_96x48x48, (48, 24, 24)),
+    "q4_600x200": (P.q4_cantilever_600x200, None),
+    "q4_120x40": (P.q4_cantilever_120x40, None),
+}
+
+
+def sample_spec(name):
+    """Bounded CPU sample: the same cantilever with every axis halved twice."""
+    make, sub = WORKLOADS[name]
+    full = make()
+    if sub is None:
+        return full, 1.0
+    nx, ny, nz = full.nx // 4, full.ny // 4, full.nz // 4
+    spec = P.hex8_cantilever(nx, ny, nz, full.volume_fraction, full.name + "_sample")
+    return spec, full.num_elements / spec.num_elements
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(name, steps=2):
+    """Oracle SIMP iterations on the bounded sample, all host threads."""
+    import oracle
+    spec, ratio = sample_spec(name)
+    pr = oracle.Problem(spec)
+    x = np.full(pr.ne, spec.volume_fraction)
+    ev = pr.evaluate(x)                      # first evaluation builds the hierarchy
+    x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ev = pr.evaluate(x)
+        x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    cores = os.cpu_count()
+    return {"value": 1.0 / (t * ratio), "unit": "iter/s", "cores": cores, "kind": "port",
+            "sample": f"{spec.nx}x{spec.ny}x{spec.nz} Hex8 cantilever (1/{ratio:.0f} of the cells), "
+                      f"min of {steps} SIMP iterations ({t:.3f} s each) after one setup iteration, "
+                      f"scaled by the cell ratio {ratio:.0f}"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    spec, ratio = sample_spec(args.config)
+    pr = oracle.Problem(spec)
+    x = np.full(pr.ne, spec.volume_fraction)
+    for _ in range(max(1, args.warmup)):
+        ev = pr.evaluate(x)
+        x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ev = pr.evaluate(x)
+        x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
+    el = time.perf_counter() - t0
+    per = el / args.steps
+    value = 1.0 / (per * ratio)
+    full = WORKLOADS[args.config][0]()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * ratio * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic seeded cantilever (no dataset)",
+        "config": {"workload": full.name, "elements": full.num_elements,
+                   "precision": "fp64", "host_threads": os.cpu_count()},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{spec.nx}x{spec.ny}x{spec.nz} Hex8 (1/{ratio:.0f} of the cells), "
+                                   f"{args.steps} SIMP iterations, scaled by the cell ratio"},
+        "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_own(args):
+    import torch
+    import torch.distributed as dist
+    from sparlab_gb300 import _lib
+    from sparlab_gb300.topopt import GpuSimpProblem
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    spec = WORKLOADS[args.config][0]()
+    prob = GpuSimpProblem(spec, precision=args.precision, device=local)
+    lib = _lib.load()
+
+    # warm-up: the first iteration builds the hierarchy
+    t_setup = time.perf_counter()
+    for _ in range(args.warmup):
+        prob.iterate()
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t_setup
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    barrier()
+    launches0 = lib.simp_kernel_launches()
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    recs = [prob.iterate() for _ in range(args.steps)]
+    e1.record()
+    barrier()
+    clocks = sampler.stop()
+    launches = lib.simp_kernel_launches() - launches0
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    per_step = ms / args.steps
+    value = world * args.steps / (ms * 1e-3)
+
+    # e2e: design from pinned host memory, iterate, design and compliance back
+    x_host = torch.empty(prob.ne, dtype=torch.float64, pin_memory=True).numpy()
+    x_host[:] = prob.design()
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(args.steps):
+        prob.set_design(x_host)
+        r = prob.iterate()
+        x_host[:] = prob.design()
+        _ = r.compliance
+    f1.record()
+    barrier()
+    e2e_ms = f0.elapsed_time(f1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # dominant kernel: the level-0 operator (CSR SpMV), timed alone
+    n = prob.nfree
+    xv = torch.rand(n, dtype=torch.float64, device=dev)
+    yv = torch.empty(n, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        prob.apply_operator(xv.data_ptr(), yv.data_ptr())
+    torch.cuda.synchronize()
+    reps = 20
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record()
+    for _ in range(reps):
+        prob.apply_operator(xv.data_ptr(), yv.data_ptr())
+    k1.record()
+    torch.cuda.synchronize()
+    kms = k0.elapsed_time(k1) / reps
+    nnz = prob.nnz
+    vbytes = 8
+    alg_bytes = nnz * (vbytes + 4) + 4 * (n + 1) + 2 * n * vbytes
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            d = json.load(f)
+        if d.get("workload") == spec.name and d.get("precision") == args.precision:
+            traffic = d.get("traffic_bytes_per_launch")
+
+    if rank != 0:
+        return
+    st = prob.amg_stats()
+    cpu = cpu_baseline(args.config) if world == 1 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic seeded cantilever (no dataset)",
+        "config": {"workload": spec.name, "elements": spec.num_elements, "free_dofs": prob.nfree,
+                   "nnz_kff": prob.nnz, "precision": args.precision, "replicas": world,
+                   "l2": "working set (K_ff %.2f GB) larger than L2" % (nnz * 12 / 1e9),
+                   "amg_levels": st["num_levels"],
+                   "operator_complexity": round(st["operator_complexity"], 6),
+                   "cg_iterations_per_step": [r.linear_iterations for r in recs],
+                   "compliance_last": recs[-1].compliance,
+                   "warmup_seconds_incl_setup": round(t_setup, 3)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_csr (level-0 K_ff SpMV, FP64 values, int32 columns)",
+                     "bytes_per_launch": alg_bytes, "ms_per_launch": kms,
+                     "peak_kind": f"{peak_kind} hbm_gbs (burst copy)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "iter/s",
+                "h2d_bytes_per_step": 8 * prob.ne, "d2h_bytes_per_step": 8 * prob.ne + 8},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="own", choices=["own", "reference"])
+    ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_own(args)
+
+
+if __name__ == "__main__":
+    main()

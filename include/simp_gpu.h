@@ -1,0 +1,231 @@
+/* simp_gpu.h - C ABI of the GB300 SIMP inner loop (libsimp_gb300.so).
+ *
+ * Two drop-in boundaries of SparLab:
+ *
+ *  1. The linear solver (sparlab::LinearSolver, include/sparlab/fem/
+ *     LinearSolver.hpp:64-109 of the reference): set_layout, factorize (AMG
+ *     setup, with aggregate reuse when the structure is unchanged, as
+ *     src/fem/Multigrid.cpp:959-966) and solve/solve_from (PCG per load case).
+ *     A caller that cannot change is served through this boundary alone.
+ *
+ *  2. The whole SIMP iteration (sparlab::ComplianceObjective::evaluate,
+ *     include/sparlab/topopt/Sensitivity.hpp:66-107, plus
+ *     optimality_criteria_update, include/sparlab/topopt/
+ *     OptimalityCriteria.hpp:45-77, driven as TopologyOptimizer::run_oc,
+ *     src/topopt/TopologyOptimizer.cpp:556-724): everything stays resident in
+ *     device memory between calls.
+ *
+ * Conventions: plain C types, host pointers unless named *_device, column
+ * indices int32, values FP64.  Every call returns a status code; on failure
+ * simp_last_error() holds a message worded as the reference's exceptions
+ * ("under-constrained", "did not converge", "not symmetric", ...).  A context
+ * is not thread-safe: use one per host thread.
+ */
+#ifndef SIMP_GPU_H
+#define SIMP_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  SIMP_BAD_INPUT / SIMP_BREAKDOWN / SIMP_UNDERCONSTRAINED /
+ * SIMP_NONFINITE map to sparlab::SolverError, SIMP_MAXITER to
+ * sparlab::ConvergenceError (src/fem/LinearSolver.cpp:268-280). */
+#define SIMP_OK 0
+#define SIMP_BAD_INPUT 1
+#define SIMP_BREAKDOWN 2
+#define SIMP_UNDERCONSTRAINED 3
+#define SIMP_MAXITER 4
+#define SIMP_NONFINITE 5
+#define SIMP_CUDA_ERROR 6
+
+/* Arithmetic of the operator, smoother and transfers.  CG scalars, the
+ * true-residual refinement and the coarsest dense Cholesky are FP64 in both. */
+#define SIMP_PRECISION_FP64 0
+#define SIMP_PRECISION_MIXED 1
+
+/* Options: AmgOptions (include/sparlab/fem/Multigrid.hpp:75-103) plus the
+ * iterative part of LinearSolverOptions (LinearSolver.hpp:36-61). */
+typedef struct {
+  double strength_threshold;     /* theta, 0.02 */
+  int32_t max_levels;            /* 12 */
+  int32_t coarse_size;           /* 1500 */
+  int32_t smoother_degree;       /* Chebyshev degree, 3 */
+  double chebyshev_ratio;        /* 30 */
+  double prolongator_damping;    /* omega * lambda_max, 4/3 */
+  int32_t lanczos_steps;         /* 12 */
+  double coarse_pivot_tolerance; /* 1e-13 */
+  int32_t reuse_aggregates;      /* 1 */
+  double iterative_tolerance;    /* relative residual, 1e-12 */
+  int32_t max_iterations;        /* 0 -> 1000 */
+  int32_t precision;             /* SIMP_PRECISION_* */
+  int32_t device;                /* CUDA device ordinal */
+} simp_solver_options;
+
+typedef struct {
+  int32_t num_levels;
+  int32_t reused_aggregates;
+  double operator_complexity;
+  double grid_complexity;
+  double coarse_pivot_ratio;
+  double setup_seconds;
+  int64_t storage_nonzeros;
+  int64_t level_rows[16];
+  int64_t level_nnz[16];
+  int64_t level_aggregates[16];
+  double level_lambda[16];
+} simp_amg_stats;
+
+typedef struct simp_ctx simp_ctx;
+
+void simp_default_options(simp_solver_options* opts);
+
+/* ---- Boundary 1: LinearSolver ------------------------------------------ */
+/* make_linear_solver(options) with type "gpu_amg_cg"
+ * (src/fem/LinearSolver.cpp:424-443). */
+int simp_ctx_create(const simp_solver_options* opts, simp_ctx** out);
+void simp_ctx_destroy(simp_ctx* ctx);
+/* Message of the last failed call on this context (thread-local when ctx is
+ * NULL, for failures of create). */
+const char* simp_last_error(const simp_ctx* ctx);
+
+/* LinearSolver::set_layout(DofLayout) (LinearSolver.hpp:87, Multigrid.hpp:
+ * 107-117): coordinates are dim x num_nodes (node-major), unknowns[i] is the
+ * global DOF node * ndpn + k of unknown i, ascending.  Copied. */
+int simp_set_layout(simp_ctx* ctx, int32_t dim, int32_t ndpn, const double* coords,
+                    int32_t num_nodes, const int32_t* unknowns, int32_t n);
+
+/* LinearSolver::factorize(const SparseMatrix&) (LinearSolver.hpp:71): the
+ * symmetric K_ff as CSR (the reference's column-major storage read as rows).
+ * Pattern and values are copied to the device; the aggregates of the last
+ * setup are reused when n, nnz and the layout are unchanged. */
+int simp_factorize(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx,
+                   const double* values);
+
+/* LinearSolver::solve / solve_from (LinearSolver.hpp:74-82) for nrhs
+ * right-hand sides stored one after another (n doubles each).  X0 may be NULL
+ * (zero guess).  iterations[k] and relres[k] (true relative residual) are
+ * written per right-hand side when non-NULL. */
+int simp_solve(simp_ctx* ctx, int32_t nrhs, const double* B, const double* X0, double* X,
+               int32_t* iterations, double* relres);
+
+/* AmgPreconditioner::apply (Multigrid.hpp:162): z = M^-1 r, one V-cycle. */
+int simp_apply_preconditioner(simp_ctx* ctx, const double* r, double* z);
+
+/* LinearSolver::amg_stats / last_iterations / storage_nonzeros. */
+int simp_stats(simp_ctx* ctx, simp_amg_stats* stats);
+
+/* Test access to the hierarchy (AmgPreconditioner, Multigrid.hpp:168-178):
+ * node-to-aggregate map of level `level` (count = number of nodes), the level
+ * operator A_l as CSR (call with NULL arrays for the sizes). */
+int simp_level_aggregates(simp_ctx* ctx, int32_t level, int32_t* agg, int32_t* count);
+int simp_level_matrix(simp_ctx* ctx, int32_t level, int32_t* rows, int64_t* nnz,
+                      int32_t* rowptr, int32_t* colidx, double* values);
+int simp_level_prolongator(simp_ctx* ctx, int32_t level, int32_t* rows, int32_t* cols,
+                           int64_t* nnz, int32_t* rowptr, int32_t* colidx, double* values);
+
+/* ---- Boundary 2: the whole SIMP iteration ------------------------------ */
+typedef struct simp_problem simp_problem;
+
+/* A structured Q4 / Hex8 problem: what FemModel, Assembler, DensityFilter,
+ * DesignDomain and the SIMP/OC options of the reference hold for it. */
+typedef struct {
+  int32_t dim;                  /* 2 (Q4 plane stress) or 3 (Hex8) */
+  int32_t nx, ny, nz;           /* cells per axis */
+  double lx, ly, lz;            /* extents, grid at the origin */
+  double thickness;             /* plane-stress thickness (2-D volumes); 1 in 3-D */
+  const double* element_matrix; /* K_e^0 (8x8 or 24x24, row-major), from the
+                                   caller's element (Assembler::element_stiffness) */
+  const uint8_t* fixed;         /* per DOF: 1 = clamped (homogeneous) */
+  int32_t num_loads;
+  const double* loads;          /* num_loads x num_dofs */
+  const double* weights;        /* raw load-case weights (normalised here) */
+  double filter_radius;         /* physical; <= 0: no filter */
+  double volume_fraction;
+  double initial_density;       /* < 0: the volume fraction */
+  double penalty, emin_ratio;   /* SimpOptions */
+  double move_limit, damping;   /* OptimalityCriteriaOptions */
+  int32_t warm_start;           /* LinearSolverOptions::warm_start */
+  int32_t block_pcg;            /* 1: all load cases as one block of RHS */
+} simp_problem_desc;
+
+/* ObjectiveEvaluation scalars (Sensitivity.hpp:66-107) and an OC step
+ * (OptimalityCriteria.hpp:53-60). */
+typedef struct {
+  double compliance;
+  double volume;
+  double volume_fraction;
+  int32_t linear_iterations;
+  double relres_max;
+} simp_evaluation;
+
+typedef struct {
+  double lambda;
+  double achieved_volume;
+  double max_change;
+  int32_t bisections;
+  int32_t volume_converged;
+} simp_oc_step;
+
+typedef struct {
+  double compliance, volume_fraction, max_change, lambda, gray_level;
+  int32_t linear_iterations, bisections;
+  double seconds;
+} simp_iteration_record;
+
+int simp_problem_create(const simp_problem_desc* desc, const simp_solver_options* opts,
+                        simp_problem** out);
+void simp_problem_destroy(simp_problem* p);
+const char* simp_problem_last_error(const simp_problem* p);
+/* ne, nn, ndof, nfree, nnz(K_ff) */
+int simp_problem_sizes(simp_problem* p, int64_t* sizes);
+
+/* Design vector on the device (host in / out). */
+int simp_set_design(simp_problem* p, const double* x);
+int simp_get_design(simp_problem* p, double* x);
+
+/* ComplianceObjective::evaluate(x, true) at the resident design.  Output
+ * arrays (host, may be NULL): physical density, dc/drho, dc/dx, dv/dx,
+ * element strain energy (ne each), displacements (num_loads x ndof). */
+int simp_evaluate(simp_problem* p, simp_evaluation* out, double* rho, double* dc_dphys,
+                  double* dc_dx, double* dv_dx, double* strain_energy, double* displacements);
+
+/* optimality_criteria_update with the resident gradients of the last
+ * evaluate; the new design replaces the resident one when `apply` != 0. */
+int simp_oc_update(simp_problem* p, int32_t apply, simp_oc_step* out, double* xnew);
+
+/* One run_oc iteration: evaluate + OC + clamp, device-resident. */
+int simp_iterate(simp_problem* p, simp_iteration_record* rec);
+
+/* AMG statistics of the problem's solver. */
+int simp_problem_stats(simp_problem* p, simp_amg_stats* stats);
+
+/* Density filter of the problem (DensityFilter::to_physical / pull_back). */
+int simp_filter_forward(simp_problem* p, const double* x, double* y);
+int simp_filter_adjoint(simp_problem* p, const double* v, double* g);
+
+/* Assembled K_ff of the problem at element factors `scale` (host), copied
+ * out as CSR (NULL arrays: sizes only).  Test access to the assembly. */
+int simp_problem_kff(simp_problem* p, const double* scale, int32_t* rowptr,
+                     int32_t* colidx, double* values);
+
+/* Element stiffness of a box cell (Quad4Element/Hex8Element::stiffness,
+ * src/elements/Quad4.cpp:117-137, src/elements/Hex8.cpp:172-192), for callers
+ * without an element library. */
+int simp_element_stiffness(int32_t dim, double hx, double hy, double hz, double young,
+                           double poisson, double thickness, double* ke);
+
+/* y = K_ff x with the problem's current level-0 operator (as assembled by
+ * the last evaluate), on device pointers of nfree doubles, on the library's
+ * stream.  Exposed so a caller can time the dominant kernel in isolation. */
+int simp_problem_apply_operator(simp_problem* p, const double* x_device, double* y_device);
+
+/* Number of kernels this library has launched (for launch accounting). */
+int64_t simp_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

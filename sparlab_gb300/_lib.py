@@ -1,0 +1,150 @@
+"""ctypes binding of libsimp_gb300.so (the C ABI of include/simp_gpu.h).
+
+The library is built in-tree by :mod:`sparlab_gb300.build`.  There is no CPU
+fallback: if the shared library is missing or fails to load, every entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+SIMP_OK = 0
+SIMP_BAD_INPUT = 1
+SIMP_BREAKDOWN = 2
+SIMP_UNDERCONSTRAINED = 3
+SIMP_MAXITER = 4
+SIMP_NONFINITE = 5
+SIMP_CUDA_ERROR = 6
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+EXPORTS = [
+    "simp_default_options", "simp_ctx_create", "simp_ctx_destroy", "simp_last_error",
+    "simp_set_layout", "simp_factorize", "simp_solve", "simp_apply_preconditioner",
+    "simp_stats", "simp_level_aggregates", "simp_level_matrix", "simp_level_prolongator",
+    "simp_problem_create", "simp_problem_destroy", "simp_problem_last_error",
+    "simp_problem_sizes", "simp_set_design", "simp_get_design", "simp_evaluate",
+    "simp_oc_update", "simp_iterate", "simp_problem_stats", "simp_filter_forward",
+    "simp_filter_adjoint", "simp_problem_kff", "simp_element_stiffness",
+    "simp_problem_apply_operator", "simp_kernel_launches",
+]
+
+
+class SolverOptions(C.Structure):
+    _fields_ = [("strength_threshold", C.c_double), ("max_levels", C.c_int32),
+                ("coarse_size", C.c_int32), ("smoother_degree", C.c_int32),
+                ("chebyshev_ratio", C.c_double), ("prolongator_damping", C.c_double),
+                ("lanczos_steps", C.c_int32), ("coarse_pivot_tolerance", C.c_double),
+                ("reuse_aggregates", C.c_int32), ("iterative_tolerance", C.c_double),
+                ("max_iterations", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32)]
+
+
+class AmgStats(C.Structure):
+    _fields_ = [("num_levels", C.c_int32), ("reused_aggregates", C.c_int32),
+                ("operator_complexity", C.c_double), ("grid_complexity", C.c_double),
+                ("coarse_pivot_ratio", C.c_double), ("setup_seconds", C.c_double),
+                ("storage_nonzeros", C.c_int64), ("level_rows", C.c_int64 * 16),
+                ("level_nnz", C.c_int64 * 16), ("level_aggregates", C.c_int64 * 16),
+                ("level_lambda", C.c_double * 16)]
+
+    def as_dict(self):
+        n = self.num_levels
+        return {
+            "num_levels": n, "reused_aggregates": bool(self.reused_aggregates),
+            "operator_complexity": self.operator_complexity,
+            "grid_complexity": self.grid_complexity,
+            "coarse_pivot_ratio": self.coarse_pivot_ratio,
+            "setup_seconds": self.setup_seconds, "storage_nonzeros": self.storage_nonzeros,
+            "levels": [{"unknowns": self.level_rows[k], "nonzeros": self.level_nnz[k],
+                        "aggregates": self.level_aggregates[k],
+                        "lambda_max": self.level_lambda[k]} for k in range(n)],
+        }
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+                ("thickness", C.c_double), ("element_matrix", C.POINTER(C.c_double)),
+                ("fixed", C.POINTER(C.c_uint8)), ("num_loads", C.c_int32),
+                ("loads", C.POINTER(C.c_double)), ("weights", C.POINTER(C.c_double)),
+                ("filter_radius", C.c_double), ("volume_fraction", C.c_double),
+                ("initial_density", C.c_double), ("penalty", C.c_double),
+                ("emin_ratio", C.c_double), ("move_limit", C.c_double), ("damping", C.c_double),
+                ("warm_start", C.c_int32), ("block_pcg", C.c_int32)]
+
+
+class Evaluation(C.Structure):
+    _fields_ = [("compliance", C.c_double), ("volume", C.c_double),
+                ("volume_fraction", C.c_double), ("linear_iterations", C.c_int32),
+                ("relres_max", C.c_double)]
+
+
+class OcStep(C.Structure):
+    _fields_ = [("lam", C.c_double), ("achieved_volume", C.c_double), ("max_change", C.c_double),
+                ("bisections", C.c_int32), ("volume_converged", C.c_int32)]
+
+
+class IterationRecord(C.Structure):
+    _fields_ = [("compliance", C.c_double), ("volume_fraction", C.c_double),
+                ("max_change", C.c_double), ("lam", C.c_double), ("gray_level", C.c_double),
+                ("linear_iterations", C.c_int32), ("bisections", C.c_int32),
+                ("seconds", C.c_double)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load the CUDA library (building it first when its sources are newer)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if build_if_missing and not _build.up_to_date():
+                _build.build()
+            if not os.path.exists(_build.LIB):
+                raise RuntimeError("libsimp_gb300.so is not built; run sparlab_gb300.build.build()")
+            lib = C.CDLL(_build.LIB)
+            lib.simp_last_error.restype = C.c_char_p
+            lib.simp_problem_last_error.restype = C.c_char_p
+            lib.simp_kernel_launches.restype = C.c_int64
+            _lib = lib
+    return _lib
+
+
+class SolverError(RuntimeError):
+    """Bad input, breakdown, under-constrained or non-finite (sparlab::SolverError)."""
+
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+class ConvergenceError(SolverError):
+    """Iteration budget spent (sparlab::ConvergenceError)."""
+
+
+def raise_for(code: int, msg: str):
+    if code == SIMP_OK:
+        return
+    if code == SIMP_MAXITER:
+        raise ConvergenceError(code, msg)
+    raise SolverError(code, msg)
+
+
+def default_options(**kw) -> SolverOptions:
+    o = SolverOptions()
+    load().simp_default_options(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown solver option {k!r}")
+        setattr(o, k, v)
+    return o
+
+
+def ptr(a, ctype=C.c_double):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ctype))

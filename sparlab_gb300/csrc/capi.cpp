@@ -1,0 +1,605 @@
+// extern "C" entry points of libsimp_gb300.so (declared in include/simp_gpu.h).
+#include "../../include/simp_gpu.h"
+
+#include "amg.h"
+#include "problem.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+using namespace simp;
+
+namespace {
+thread_local std::string g_create_error;
+
+AmgOptions convert(const simp_solver_options* o) {
+  AmgOptions a;
+  if (!o) return a;
+  a.theta = o->strength_threshold;
+  a.max_levels = o->max_levels;
+  a.coarse_size = o->coarse_size;
+  a.degree = o->smoother_degree;
+  a.cheb_ratio = o->chebyshev_ratio;
+  a.damping = o->prolongator_damping;
+  a.lanczos_steps = o->lanczos_steps;
+  a.pivot_tol = o->coarse_pivot_tolerance;
+  a.reuse = o->reuse_aggregates != 0;
+  a.rtol = o->iterative_tolerance;
+  a.maxit = o->max_iterations > 0 ? o->max_iterations : 1000;
+  a.precision = o->precision;
+  return a;
+}
+
+// Option checks of AmgPreconditioner's constructor (src/fem/Multigrid.cpp:907-925).
+void validate(const AmgOptions& o) {
+  if (!(o.theta >= 0.0 && o.theta < 1.0)) throw Error(kBadInput, "multigrid strength_threshold must lie in [0, 1)");
+  if (o.max_levels < 1) throw Error(kBadInput, "multigrid max_levels must be at least 1");
+  if (o.coarse_size < 1) throw Error(kBadInput, "multigrid coarse_size must be positive");
+  if (o.degree < 1) throw Error(kBadInput, "multigrid smoother_degree must be at least 1");
+  if (!(o.cheb_ratio > 1.0)) throw Error(kBadInput, "multigrid chebyshev_ratio must exceed 1");
+  if (!(o.damping > 0.0 && o.damping < 2.0)) throw Error(kBadInput, "multigrid prolongator_damping must lie in (0, 2)");
+  if (o.lanczos_steps < 2) throw Error(kBadInput, "multigrid lanczos_steps must be at least 2");
+  if (!(o.rtol > 0.0)) throw Error(kBadInput, "the iterative tolerance must be positive");
+  if (o.precision != SIMP_PRECISION_FP64 && o.precision != SIMP_PRECISION_MIXED)
+    throw Error(kBadInput, "unknown precision mode");
+}
+
+template <class F>
+int guarded(std::string& err, F&& f) {
+  try {
+    f();
+    return kOk;
+  } catch (const Error& e) {
+    err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    err = "out of host memory";
+    return kBadInput;
+  } catch (const std::exception& e) {
+    err = e.what();
+    return kBadInput;
+  }
+}
+
+void use_device(int dev) { SIMP_CUDA(cudaSetDevice(dev)); }
+
+}  // namespace
+
+struct simp_ctx {
+  AmgOptions opt;
+  int device = 0;
+  std::unique_ptr<GpuAmg> amg;
+  int dim = 0, ndpn = 0;
+  std::vector<double> coords;
+  i32 num_nodes = 0;
+  std::vector<i32> unknowns;
+  bool has_layout = false, layout_changed = true;
+  i32 fp_n = -1;
+  i64 fp_nnz = -1;
+  std::string err;
+  DBuf<double> db, dx;
+};
+
+struct simp_problem {
+  std::unique_ptr<GpuProblem> p;
+  int device = 0;
+  std::string err;
+};
+
+extern "C" {
+
+void simp_default_options(simp_solver_options* o) {
+  o->strength_threshold = 0.02;
+  o->max_levels = 12;
+  o->coarse_size = 1500;
+  o->smoother_degree = 3;
+  o->chebyshev_ratio = 30.0;
+  o->prolongator_damping = 4.0 / 3.0;
+  o->lanczos_steps = 12;
+  o->coarse_pivot_tolerance = 1.0e-13;
+  o->reuse_aggregates = 1;
+  o->iterative_tolerance = 1.0e-12;
+  o->max_iterations = 0;
+  o->precision = SIMP_PRECISION_FP64;
+  o->device = 0;
+}
+
+int simp_ctx_create(const simp_solver_options* opts, simp_ctx** out) {
+  return guarded(g_create_error, [&] {
+    if (!out) throw Error(kBadInput, "simp_ctx_create: out is NULL");
+    std::unique_ptr<simp_ctx> c(new simp_ctx());
+    simp_solver_options def;
+    simp_default_options(&def);
+    c->opt = convert(opts ? opts : &def);
+    validate(c->opt);
+    c->device = opts ? opts->device : 0;
+    use_device(c->device);
+    c->amg.reset(new GpuAmg(c->opt));
+    *out = c.release();
+  });
+}
+
+void simp_ctx_destroy(simp_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  delete ctx;
+}
+
+const char* simp_last_error(const simp_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int simp_set_layout(simp_ctx* ctx, int32_t dim, int32_t ndpn, const double* coords, int32_t num_nodes,
+                    const int32_t* unknowns, int32_t n) {
+  return guarded(ctx->err, [&] {
+    if (dim != 2 && dim != 3) throw Error(kBadInput, "multigrid: the DOF layout must be two- or three-dimensional");
+    const int nd = ndpn > 0 ? ndpn : dim;
+    if (nd != dim) {
+      std::ostringstream os;
+      os << "multigrid: a " << dim << "-D layout with " << nd
+         << " DOFs per node is not supported by the GPU solver (translations only)";
+      throw Error(kBadInput, os.str());
+    }
+    if (!coords || !unknowns || num_nodes < 0 || n < 0) throw Error(kBadInput, "multigrid: incomplete DOF layout");
+    std::vector<double> c(coords, coords + static_cast<size_t>(num_nodes) * dim);
+    std::vector<i32> u(unknowns, unknowns + n);
+    const bool same = ctx->has_layout && ctx->dim == dim && ctx->ndpn == nd && c == ctx->coords && u == ctx->unknowns;
+    if (!same) {
+      ctx->dim = dim;
+      ctx->ndpn = nd;
+      ctx->coords.swap(c);
+      ctx->unknowns.swap(u);
+      ctx->num_nodes = num_nodes;
+      ctx->layout_changed = true;
+    }
+    ctx->has_layout = true;
+  });
+}
+
+int simp_factorize(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx, const double* values) {
+  return guarded(ctx->err, [&] {
+    use_device(ctx->device);
+    const std::string who = "AMG-CG(chebyshev, GPU)";
+    if (n <= 0 || !rowptr) throw Error(kBadInput, who + " received an empty system");
+    if (!ctx->has_layout)
+      throw Error(kBadInput, who + " needs the DOF layout (node coordinates of the unknowns) to build its "
+                                   "rigid-body near-null space; the caller did not supply one");
+    if (static_cast<i32>(ctx->unknowns.size()) != n) {
+      std::ostringstream os;
+      os << "multigrid: the DOF layout lists " << ctx->unknowns.size() << " unknowns for a matrix of " << n << " rows";
+      throw Error(kBadInput, os.str());
+    }
+    const i64 nnz = rowptr[n];
+    if (rowptr[0] != 0 || nnz <= 0) throw Error(kBadInput, "multigrid: malformed row pointer");
+    for (i64 k = 0; k < nnz; ++k)
+      if (!std::isfinite(values[k])) throw Error(kNonFinite, "multigrid: the system matrix has a non-finite entry");
+    GpuAmg& amg = *ctx->amg;
+    const bool same = amg.ready() && ctx->fp_n == n && ctx->fp_nnz == nnz && !ctx->layout_changed;
+    if (!same) {
+      // symmetry check once per structure (Multigrid.cpp:968-991)
+      double mx = 0.0;
+      for (i64 k = 0; k < nnz; ++k) mx = std::max(mx, std::abs(values[k]));
+      for (i32 i = 0; i < n; ++i)
+        for (i32 k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+          const i32 j = colidx[k];
+          if (j < 0 || j >= n) throw Error(kBadInput, "multigrid: column index out of range");
+          const i32* b = colidx + rowptr[j];
+          const i32* e = colidx + rowptr[j + 1];
+          const i32* hit = std::lower_bound(b, e, i);
+          const double other = (hit != e && *hit == i) ? values[hit - colidx] : 0.0;
+          if (std::abs(other - values[k]) > 1.0e-10 * mx) {
+            std::ostringstream os;
+            os << "multigrid: the system matrix is not symmetric (entry (" << i << ", " << j << ") = " << values[k]
+               << " but (" << j << ", " << i << ") = " << other
+               << "); conjugate gradients needs a symmetric positive-definite matrix";
+            throw Error(kBadInput, os.str());
+          }
+        }
+      // unknowns grouped by node (Multigrid.cpp:383-412)
+      std::vector<i32> first(1, 0);
+      i32 prev = -1;
+      for (i32 i = 0; i < n; ++i) {
+        const i32 g = ctx->unknowns[i];
+        const i32 node = g / ctx->ndpn;
+        if (g < 0 || node >= ctx->num_nodes) {
+          std::ostringstream os;
+          os << "multigrid: unknown " << i << " maps to DOF " << g << ", outside the model's " << ctx->num_nodes
+             << " nodes";
+          throw Error(kBadInput, os.str());
+        }
+        if (i > 0 && g <= ctx->unknowns[i - 1])
+          throw Error(kBadInput, "multigrid: the DOF layout must list unknowns in ascending order");
+        if (node != prev) {
+          if (i > 0) first.push_back(i);
+          prev = node;
+        }
+      }
+      first.push_back(n);
+      NodePattern pat;
+      std::string why;
+      if (!derive_node_pattern(n, rowptr, colidx, first, pat, why))
+        throw Error(kBadInput, "multigrid: the matrix pattern is not node-blocked (" + why + ")");
+      const std::vector<i32> self = pattern_self_slots(pat);
+      for (size_t I = 0; I < self.size(); ++I)
+        if (self[I] < 0) {
+          std::ostringstream os;
+          os << "multigrid: node " << I << " has no diagonal block; a stiffness matrix must have a "
+                "positive diagonal";
+          throw Error(kBreakdown, os.str());
+        }
+      amg.levels.clear();
+      Level& l0 = amg.level0();
+      l0.n = n;
+      l0.nnodes = static_cast<i32>(first.size()) - 1;
+      l0.first = first;
+      l0.apat = std::move(pat);
+      l0.d_first.upload(l0.first);
+      l0.d_node_of.upload(node_of_unknowns(l0.first));
+      l0.d_apat.upload(l0.apat);
+      l0.d_self.upload(pattern_self_slots(l0.apat));
+      l0.a.rows = l0.a.cols = n;
+      l0.a.nnz = nnz;
+      l0.a.ptr.upload(rowptr, static_cast<size_t>(n) + 1);
+      l0.a.col.upload(colidx, static_cast<size_t>(nnz));
+      l0.null = rigid_body_modes(ctx->dim, ctx->ndpn, ctx->coords, ctx->num_nodes, ctx->unknowns);
+    }
+    Level& l0 = *amg.levels.front();
+    l0.a.v64.upload(values, static_cast<size_t>(nnz));
+    amg.setup(!same);
+    ctx->fp_n = n;
+    ctx->fp_nnz = nnz;
+    ctx->layout_changed = false;
+  });
+}
+
+int simp_solve(simp_ctx* ctx, int32_t nrhs, const double* B, const double* X0, double* X, int32_t* iterations,
+               double* relres) {
+  return guarded(ctx->err, [&] {
+    use_device(ctx->device);
+    GpuAmg& amg = *ctx->amg;
+    if (!amg.ready()) throw Error(kBadInput, "AMG-CG(chebyshev, GPU): solve called before factorize");
+    const i32 n = amg.levels.front()->n;
+    ctx->db.alloc(n);
+    ctx->dx.alloc(n);
+    for (int k = 0; k < nrhs; ++k) {
+      ctx->db.upload(B + static_cast<size_t>(k) * n, n, amg.stream);
+      if (X0) ctx->dx.upload(X0 + static_cast<size_t>(k) * n, n, amg.stream);
+      else ctx->dx.zero(amg.stream);
+      const GpuAmg::PcgResult r = amg.solve(ctx->db.p, ctx->dx.p);
+      ctx->dx.download(X + static_cast<size_t>(k) * n, n, amg.stream);
+      SIMP_CUDA(cudaStreamSynchronize(amg.stream));
+      if (iterations) iterations[k] = r.iterations;
+      if (relres) relres[k] = r.relres;
+      if (!r.converged) {
+        std::ostringstream os;
+        os << "AMG-CG(chebyshev, GPU) did not converge: " << r.iterations
+           << " iterations left a relative residual of " << r.relres << " against a tolerance of " << amg.opt.rtol
+           << " (" << amg.levels.size() << " levels, operator complexity " << amg.stats.operator_complexity
+           << "). Raise solver.linear.max_iterations, lower solver.linear.amg.strength_threshold, raise "
+              "amg.smoother_degree, or use \"simplicial_ldlt\"";
+        throw Error(kMaxIter, os.str());
+      }
+    }
+  });
+}
+
+int simp_apply_preconditioner(simp_ctx* ctx, const double* r, double* z) {
+  return guarded(ctx->err, [&] {
+    use_device(ctx->device);
+    GpuAmg& amg = *ctx->amg;
+    if (!amg.ready()) throw Error(kBadInput, "multigrid: apply() called before setup()");
+    const i32 n = amg.levels.front()->n;
+    ctx->db.upload(r, n, amg.stream);
+    ctx->dx.alloc(n);
+    amg.apply(ctx->db.p, ctx->dx.p);
+    ctx->dx.download(z, n, amg.stream);
+    SIMP_CUDA(cudaStreamSynchronize(amg.stream));
+  });
+}
+
+static void fill_stats(const GpuAmg& amg, simp_amg_stats* s) {
+  std::memset(s, 0, sizeof(*s));
+  s->num_levels = amg.stats.num_levels;
+  s->reused_aggregates = amg.stats.reused ? 1 : 0;
+  s->operator_complexity = amg.stats.operator_complexity;
+  s->grid_complexity = amg.stats.grid_complexity;
+  s->coarse_pivot_ratio = amg.stats.pivot_ratio;
+  s->setup_seconds = amg.stats.setup_seconds;
+  s->storage_nonzeros = amg.stats.storage;
+  for (size_t k = 0; k < amg.levels.size() && k < 16; ++k) {
+    s->level_rows[k] = amg.levels[k]->n;
+    s->level_nnz[k] = amg.levels[k]->a.nnz;
+    s->level_aggregates[k] = k + 1 < amg.levels.size() ? amg.levels[k + 1]->nnodes : 0;
+    s->level_lambda[k] = amg.levels[k]->lambda;
+  }
+}
+
+int simp_stats(simp_ctx* ctx, simp_amg_stats* s) {
+  return guarded(ctx->err, [&] { fill_stats(*ctx->amg, s); });
+}
+
+static void copy_level_matrix(GpuAmg& amg, int level, int32_t* rows, int64_t* nnz, int32_t* rowptr, int32_t* col,
+                              double* val) {
+  if (level < 0 || level >= static_cast<int>(amg.levels.size())) throw Error(kBadInput, "no such level");
+  const Level& lv = *amg.levels[level];
+  if (rows) *rows = lv.n;
+  if (nnz) *nnz = lv.a.nnz;
+  if (rowptr) lv.a.ptr.download(rowptr, static_cast<size_t>(lv.n) + 1);
+  if (col) lv.a.col.download(col, static_cast<size_t>(lv.a.nnz));
+  if (val) lv.a.v64.download(val, static_cast<size_t>(lv.a.nnz));
+  SIMP_CUDA(cudaDeviceSynchronize());
+}
+
+int simp_level_aggregates(simp_ctx* ctx, int32_t level, int32_t* agg, int32_t* count) {
+  return guarded(ctx->err, [&] {
+    GpuAmg& amg = *ctx->amg;
+    if (level < 0 || level >= static_cast<int>(amg.levels.size())) throw Error(kBadInput, "no such level");
+    const Level& lv = *amg.levels[level];
+    if (count) *count = lv.nnodes;
+    if (agg) {
+      if (lv.agg.empty()) std::fill(agg, agg + lv.nnodes, -1);
+      else std::copy(lv.agg.begin(), lv.agg.end(), agg);
+    }
+  });
+}
+
+int simp_level_matrix(simp_ctx* ctx, int32_t level, int32_t* rows, int64_t* nnz, int32_t* rowptr, int32_t* col,
+                      double* val) {
+  return guarded(ctx->err, [&] {
+    use_device(ctx->device);
+    copy_level_matrix(*ctx->amg, level, rows, nnz, rowptr, col, val);
+  });
+}
+
+int simp_level_prolongator(simp_ctx* ctx, int32_t level, int32_t* rows, int32_t* cols, int64_t* nnz,
+                           int32_t* rowptr, int32_t* col, double* val) {
+  return guarded(ctx->err, [&] {
+    use_device(ctx->device);
+    GpuAmg& amg = *ctx->amg;
+    if (level < 0 || level + 1 >= static_cast<int>(amg.levels.size())) throw Error(kBadInput, "no such transfer level");
+    const Level& lv = *amg.levels[level];
+    if (rows) *rows = lv.p.rows;
+    if (cols) *cols = lv.p.cols;
+    if (nnz) *nnz = lv.p.nnz;
+    if (rowptr) lv.p.ptr.download(rowptr, static_cast<size_t>(lv.p.rows) + 1);
+    if (col) lv.p.col.download(col, static_cast<size_t>(lv.p.nnz));
+    if (val) lv.p.v64.download(val, static_cast<size_t>(lv.p.nnz));
+    SIMP_CUDA(cudaDeviceSynchronize());
+  });
+}
+
+// ---- whole SIMP iteration ----
+
+int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options* opts, simp_problem** out) {
+  return guarded(g_create_error, [&] {
+    if (!dsc || !out) throw Error(kBadInput, "simp_problem_create: NULL argument");
+    simp_solver_options def;
+    simp_default_options(&def);
+    const simp_solver_options* o = opts ? opts : &def;
+    AmgOptions ao = convert(o);
+    validate(ao);
+    use_device(o->device);
+    ProblemDesc d;
+    d.dim = dsc->dim;
+    d.nx = dsc->nx;
+    d.ny = dsc->ny;
+    d.nz = dsc->dim == 3 ? dsc->nz : 1;
+    d.lx = dsc->lx;
+    d.ly = dsc->ly;
+    d.lz = dsc->lz;
+    d.thickness = dsc->thickness;
+    if (d.dim != 2 && d.dim != 3) throw Error(kBadInput, "dim must be 2 or 3");
+    const int ed = d.dim == 3 ? 24 : 8;
+    if (!dsc->element_matrix || !dsc->fixed || !dsc->loads || !dsc->weights)
+      throw Error(kBadInput, "simp_problem_create: missing element matrix, supports or loads");
+    d.ke.assign(dsc->element_matrix, dsc->element_matrix + ed * ed);
+    const i64 nn = static_cast<i64>(d.nx + 1) * (d.ny + 1) * (d.dim == 3 ? d.nz + 1 : 1);
+    const i64 ndof = nn * d.dim;
+    d.fixed.assign(dsc->fixed, dsc->fixed + ndof);
+    d.nloads = dsc->num_loads;
+    if (d.nloads < 1) throw Error(kBadInput, "at least one load case is needed");
+    d.loads.assign(dsc->loads, dsc->loads + ndof * d.nloads);
+    double ws = 0.0;
+    for (int l = 0; l < d.nloads; ++l) ws += dsc->weights[l];
+    if (!(ws > 0.0)) throw Error(kBadInput, "load-case weights must have a positive sum");
+    for (int l = 0; l < d.nloads; ++l) d.weights.push_back(dsc->weights[l] / ws);
+    d.radius = dsc->filter_radius;
+    d.vf = dsc->volume_fraction;
+    if (!(d.vf > 0.0 && d.vf <= 1.0)) throw Error(kBadInput, "volume fraction must lie in (0, 1]");
+    d.x0 = dsc->initial_density >= 0.0 ? dsc->initial_density : dsc->volume_fraction;
+    d.penalty = dsc->penalty;
+    d.emin = dsc->emin_ratio;
+    if (!(d.emin > 0.0 && d.emin < 1.0)) throw Error(kBadInput, "SIMP emin_ratio must lie in (0, 1)");
+    d.move = dsc->move_limit;
+    if (!(d.move > 0.0 && d.move <= 1.0)) throw Error(kBadInput, "optimizer.move_limit must lie in (0, 1]");
+    d.damping = dsc->damping;
+    if (!(d.damping > 0.0 && d.damping <= 1.0)) throw Error(kBadInput, "optimizer.damping must lie in (0, 1]");
+    d.warm = dsc->warm_start != 0;
+    d.block_pcg = dsc->block_pcg != 0;
+    std::unique_ptr<simp_problem> p(new simp_problem());
+    p->device = o->device;
+    p->p.reset(new GpuProblem(d, ao));
+    *out = p.release();
+  });
+}
+
+void simp_problem_destroy(simp_problem* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  delete p;
+}
+
+const char* simp_problem_last_error(const simp_problem* p) { return p ? p->err.c_str() : g_create_error.c_str(); }
+
+int simp_problem_sizes(simp_problem* p, int64_t* s) {
+  return guarded(p->err, [&] {
+    s[0] = p->p->ne;
+    s[1] = p->p->nn;
+    s[2] = p->p->ndof;
+    s[3] = p->p->nfree;
+    s[4] = p->p->amg.levels.front()->a.nnz;
+  });
+}
+
+int simp_set_design(simp_problem* p, const double* x) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    for (i64 e = 0; e < p->p->ne; ++e)
+      if (!std::isfinite(x[e])) throw Error(kBadInput, "design vector contains NaN or Inf");
+    p->p->set_design(x);
+  });
+}
+
+int simp_get_design(simp_problem* p, double* x) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    p->p->get_design(x);
+  });
+}
+
+int simp_evaluate(simp_problem* p, simp_evaluation* out, double* rho, double* dcp, double* dcx, double* dvx,
+                  double* se, double* disp) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuProblem& g = *p->p;
+    const Evaluation ev = g.evaluate();
+    if (out) {
+      out->compliance = ev.compliance;
+      out->volume = ev.volume;
+      out->volume_fraction = ev.volume_fraction;
+      out->linear_iterations = ev.linear_iterations;
+      out->relres_max = ev.relres_max;
+    }
+    cudaStream_t s = g.amg.stream;
+    const size_t ne = static_cast<size_t>(g.ne);
+    if (rho) g.rho.download(rho, ne, s);
+    if (dcp) g.dc_dphys.download(dcp, ne, s);
+    if (dcx) g.dc_dx.download(dcx, ne, s);
+    if (dvx) g.dv_dx.download(dvx, ne, s);
+    if (se) g.se.download(se, ne, s);
+    if (disp) {
+      std::vector<double> uf(static_cast<size_t>(g.nfree) * g.d.nloads);
+      g.u.download(uf.data(), uf.size(), s);
+      const std::vector<i32> map = g.dof_map.to_host(s);
+      for (int l = 0; l < g.d.nloads; ++l)
+        for (i64 k = 0; k < g.ndof; ++k)
+          disp[l * g.ndof + k] = map[k] >= 0 ? uf[static_cast<size_t>(l) * g.nfree + map[k]] : 0.0;
+    }
+    SIMP_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int simp_oc_update(simp_problem* p, int32_t apply, simp_oc_step* out, double* xnew) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    const OcStep st = p->p->oc_update(apply != 0, xnew);
+    if (out) {
+      out->lambda = st.lambda;
+      out->achieved_volume = st.volume;
+      out->max_change = st.max_change;
+      out->bisections = st.bisections;
+      out->volume_converged = st.converged ? 1 : 0;
+    }
+  });
+}
+
+int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuProblem& g = *p->p;
+    cudaEvent_t e0, e1;
+    SIMP_CUDA(cudaEventCreate(&e0));
+    SIMP_CUDA(cudaEventCreate(&e1));
+    SIMP_CUDA(cudaEventRecord(e0, g.amg.stream));
+    const Evaluation ev = g.evaluate();
+    const OcStep st = g.oc_update(true, nullptr);
+    SIMP_CUDA(cudaEventRecord(e1, g.amg.stream));
+    SIMP_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    SIMP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rec) {
+      rec->compliance = ev.compliance;
+      rec->volume_fraction = ev.volume_fraction;
+      rec->max_change = st.max_change;
+      rec->lambda = st.lambda;
+      rec->gray_level = g.gray;
+      rec->linear_iterations = ev.linear_iterations;
+      rec->bisections = st.bisections;
+      rec->seconds = ms * 1e-3;
+    }
+  });
+}
+
+int simp_problem_stats(simp_problem* p, simp_amg_stats* s) {
+  return guarded(p->err, [&] { fill_stats(p->p->amg, s); });
+}
+
+int simp_filter_forward(simp_problem* p, const double* x, double* y) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuProblem& g = *p->p;
+    const size_t ne = static_cast<size_t>(g.ne);
+    DBuf<double> a, b(ne);
+    a.upload(x, ne);
+    g.filter_forward(a.p, b.p);
+    b.download(y, ne);
+    SIMP_CUDA(cudaDeviceSynchronize());
+  });
+}
+
+int simp_filter_adjoint(simp_problem* p, const double* v, double* gout) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuProblem& g = *p->p;
+    const size_t ne = static_cast<size_t>(g.ne);
+    DBuf<double> a, b(ne);
+    a.upload(v, ne);
+    g.filter_adjoint(a.p, b.p);
+    b.download(gout, ne);
+    SIMP_CUDA(cudaDeviceSynchronize());
+  });
+}
+
+int simp_problem_kff(simp_problem* p, const double* scale, int32_t* rowptr, int32_t* col, double* val) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuProblem& g = *p->p;
+    Level& l0 = *g.amg.levels.front();
+    if (val) {
+      if (!scale) throw Error(kBadInput, "simp_problem_kff: values need element factors");
+      DBuf<double> s;
+      s.upload(scale, static_cast<size_t>(g.ne));
+      g.assemble(s.p);
+      l0.a.v64.download(val, static_cast<size_t>(l0.a.nnz));
+    }
+    if (rowptr) l0.a.ptr.download(rowptr, static_cast<size_t>(l0.n) + 1);
+    if (col) l0.a.col.download(col, static_cast<size_t>(l0.a.nnz));
+    SIMP_CUDA(cudaDeviceSynchronize());
+  });
+}
+
+int simp_element_stiffness(int32_t dim, double hx, double hy, double hz, double young, double poisson,
+                           double thickness, double* ke) {
+  return guarded(g_create_error, [&] {
+    if (dim != 2 && dim != 3) throw Error(kBadInput, "dim must be 2 or 3");
+    element_stiffness(dim, hx, hy, hz, young, poisson, thickness, ke);
+  });
+}
+
+int simp_problem_apply_operator(simp_problem* p, const double* x, double* y) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuAmg& amg = p->p->amg;
+    if (!amg.ready()) throw Error(kBadInput, "the operator is assembled by the first evaluate");
+    amg.spmv0(x, y);
+  });
+}
+
+int64_t simp_kernel_launches(void) { return g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,525 @@
+// Device kernels of the AMG-PCG solve: deterministic reductions, CSR
+// operator applications with fused smoother epilogues, the Galerkin numeric
+// products over node-level patterns, and the PCG vector updates.
+//
+// Determinism: every reduction has a fixed shape (grid, block, tree), every
+// output entry is written by one thread that sums its terms in a fixed order,
+// and no value path uses atomics, so results are bitwise reproducible run to
+// run.  The setup products sum in exactly the order of the reference's
+// multiply/multiply_numeric (src/fem/Multigrid.cpp:121-225) with rounded
+// (unfused) multiply-adds, so their FP64 values equal the CPU oracle's.
+#pragma once
+
+#include "common.h"
+
+#include <cuda_runtime.h>
+
+namespace simp {
+
+// Scalar column indices of a CSR from its node pattern (defined in amg.cu).
+__global__ void k_expand_columns(i32 n, const i32* __restrict__ node_of, NodeView p,
+                                 const i32* __restrict__ col_first, const i32* __restrict__ rowptr,
+                                 i32* __restrict__ col);
+
+constexpr int kRedBlocks = 1024;   // fixed reduction grid
+constexpr int kRedThreads = 256;
+
+// Kernels below have internal linkage: every translation unit instantiates
+// the ones it launches.
+namespace {
+// ---------------------------------------------------------------------------
+// exact-order arithmetic (no contraction into FMA)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+
+template <class T>
+__device__ __forceinline__ double todbl(T v) { return static_cast<double>(v); }
+
+// Block-wide sum of one double per thread (fixed tree), valid in thread 0.
+template <int BS>
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double warp_part[BS / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) warp_part[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (w == 0) {
+    s = l < BS / 32 ? warp_part[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  }
+  __syncthreads();
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// elementwise
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_fill(T* __restrict__ x, T v, i64 n) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) x[i] = v;
+}
+
+template <class A, class B>
+__global__ void k_convert(const A* __restrict__ a, B* __restrict__ b, i64 n) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+    b[i] = static_cast<B>(a[i]);
+}
+
+// ---------------------------------------------------------------------------
+// deterministic two-stage reductions
+// ---------------------------------------------------------------------------
+template <class TA, class TB>
+__global__ void __launch_bounds__(kRedThreads) k_dot_partial(const TA* __restrict__ a,
+                                                             const TB* __restrict__ b, i64 n,
+                                                             double* __restrict__ part) {
+  double s = 0.0;
+  for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads)
+    s += todbl(a[i]) * todbl(b[i]);
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// out = sum(part[0..m)) ; optional sqrt
+__global__ void __launch_bounds__(kRedThreads) k_reduce_final(const double* __restrict__ part, int m,
+                                                              double* __restrict__ out, int take_sqrt) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < m; i += kRedThreads) s += part[i];
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) *out = take_sqrt ? sqrt(s) : s;
+}
+
+// ---------------------------------------------------------------------------
+// PCG scalars and vector updates (FP64 CG scalars in device memory)
+// ---------------------------------------------------------------------------
+struct PcgScalars {
+  double rz;       // r^T z of the current direction
+  double pq;       // p^T A p
+  double alpha, beta;
+  double rr;       // ||r||^2 after the update
+  double rz_new;
+  int status;      // 0 ok, 2 breakdown (p^T A p <= 0 or non-finite)
+  int pad;
+};
+
+__global__ void __launch_bounds__(kRedThreads) k_pcg_alpha(const double* __restrict__ part, int m,
+                                                           PcgScalars* sc) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < m; i += kRedThreads) s += part[i];
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) {
+    sc->pq = s;
+    if (!(s > 0.0) || !isfinite(s)) {
+      sc->status = 2;
+      sc->alpha = 0.0;
+    } else {
+      sc->alpha = sc->rz / s;
+    }
+  }
+}
+
+// rz_new = sum(part); beta = rz_new / rz; rz = rz_new
+__global__ void __launch_bounds__(kRedThreads) k_pcg_beta(const double* __restrict__ part, int m,
+                                                          PcgScalars* sc) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < m; i += kRedThreads) s += part[i];
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) {
+    sc->rz_new = s;
+    sc->beta = s / sc->rz;
+    sc->rz = s;
+  }
+}
+
+// x += alpha p ; r -= alpha q ; partial ||r||^2
+__global__ void __launch_bounds__(kRedThreads) k_pcg_update(double* __restrict__ x, double* __restrict__ r,
+                                                            const double* __restrict__ p,
+                                                            const double* __restrict__ q, i64 n,
+                                                            const PcgScalars* __restrict__ sc,
+                                                            double* __restrict__ part) {
+  const double alpha = sc->alpha;
+  double s = 0.0;
+  for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    s += ri * ri;
+  }
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// p = z + beta p
+__global__ void k_pcg_direction(double* __restrict__ p, const double* __restrict__ z, i64 n,
+                                const PcgScalars* __restrict__ sc) {
+  const double beta = sc->beta;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+// ---------------------------------------------------------------------------
+// CSR operator applications: VS lanes per row, butterfly reduction
+// ---------------------------------------------------------------------------
+template <int VS, class TV, class TX, class TA>
+__device__ __forceinline__ TA csr_row_dot(const i32* __restrict__ ptr, const i32* __restrict__ col,
+                                          const TV* __restrict__ val, const TX* __restrict__ x,
+                                          i32 row, bool valid, int lane) {
+  TA s = TA(0);
+  if (valid) {
+    const i32 e = ptr[row + 1];
+    for (i32 k = ptr[row] + lane; k < e; k += VS) s += static_cast<TA>(val[k]) * static_cast<TA>(x[col[k]]);
+  }
+#pragma unroll
+  for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, VS);
+  return s;
+}
+
+// mode 0: y = A x ; 1: y = b - A x ; 2: y += A x
+template <int VS, int MODE, class TV, class TX>
+__global__ void __launch_bounds__(256) k_csr(i32 rows, const i32* __restrict__ ptr,
+                                             const i32* __restrict__ col, const TV* __restrict__ val,
+                                             const TX* __restrict__ x, TX* __restrict__ y,
+                                             const TX* __restrict__ b) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  const bool valid = row < rows;
+  const TX s = csr_row_dot<VS, TV, TX, TX>(ptr, col, val, x, row, valid, lane);
+  if (valid && lane == 0) {
+    if (MODE == 0) y[row] = s;
+    else if (MODE == 1) y[row] = b[row] - s;
+    else y[row] += s;
+  }
+}
+
+// Chebyshev step (Saad, Alg. 12.1 in D^-1 A; src/fem/Multigrid.cpp:828-853):
+//   r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ dprev]) + dn
+template <int VS, class TV, class TX>
+__global__ void __launch_bounds__(256) k_cheb_step(i32 rows, const i32* __restrict__ ptr,
+                                                   const i32* __restrict__ col, const TV* __restrict__ val,
+                                                   const TX* __restrict__ d, const TX* __restrict__ r_in,
+                                                   TX* __restrict__ r, TX* __restrict__ dn,
+                                                   TX* __restrict__ x, const TX* __restrict__ dinv,
+                                                   TX c1, TX c2, int add_d_first) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  const bool valid = row < rows;
+  const TX s = csr_row_dot<VS, TV, TX, TX>(ptr, col, val, d, row, valid, lane);
+  if (valid && lane == 0) {
+    const TX ri = r_in[row] - s;
+    r[row] = ri;
+    const TX di = c1 * d[row] + c2 * dinv[row] * ri;
+    dn[row] = di;
+    TX xi = x[row];
+    if (add_d_first) xi = xi + d[row];
+    x[row] = xi + di;
+  }
+}
+
+// r = b - A x ; d = dinv r / theta   (start of a smoothing from a guess)
+template <int VS, class TV, class TX>
+__global__ void __launch_bounds__(256) k_cheb_first(i32 rows, const i32* __restrict__ ptr,
+                                                    const i32* __restrict__ col, const TV* __restrict__ val,
+                                                    const TX* __restrict__ x, const TX* __restrict__ b,
+                                                    TX* __restrict__ r, TX* __restrict__ d,
+                                                    const TX* __restrict__ dinv, TX inv_theta) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  const bool valid = row < rows;
+  const TX s = csr_row_dot<VS, TV, TX, TX>(ptr, col, val, x, row, valid, lane);
+  if (valid && lane == 0) {
+    const TX ri = b[row] - s;
+    r[row] = ri;
+    d[row] = dinv[row] * ri * inv_theta;
+  }
+}
+
+// zero guess: d = dinv b / theta ; x = d
+template <class TX>
+__global__ void k_cheb_zero(i64 n, const TX* __restrict__ b, const TX* __restrict__ dinv,
+                            TX* __restrict__ d, TX* __restrict__ x, TX inv_theta) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    const TX di = dinv[i] * b[i] * inv_theta;
+    d[i] = di;
+    x[i] = di;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos pieces (src/fem/Multigrid.cpp:288-327)
+// ---------------------------------------------------------------------------
+// w = s .* (A (s .* v)) - beta vp   with tmp = s .* v precomputed
+template <int VS, class TV>
+__global__ void __launch_bounds__(256) k_lanczos_apply(i32 rows, const i32* __restrict__ ptr,
+                                                       const i32* __restrict__ col, const TV* __restrict__ val,
+                                                       const double* __restrict__ tmp,
+                                                       const double* __restrict__ s,
+                                                       const double* __restrict__ vp, double beta,
+                                                       double* __restrict__ w) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  const bool valid = row < rows;
+  const double acc = csr_row_dot<VS, TV, double, double>(ptr, col, val, tmp, row, valid, lane);
+  if (valid && lane == 0) {
+    double wi = acc * s[row];
+    if (vp) wi -= beta * vp[row];
+    w[row] = wi;
+  }
+}
+
+// w -= a v ; partial ||w||^2
+__global__ void __launch_bounds__(kRedThreads) k_axpy_norm(double* __restrict__ w, const double* __restrict__ v,
+                                                           const double* __restrict__ a_dev, i64 n,
+                                                           double* __restrict__ part) {
+  const double a = *a_dev;
+  double s = 0.0;
+  for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads) {
+    const double wi = w[i] - a * v[i];
+    w[i] = wi;
+    s += wi * wi;
+  }
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// vp = v ; v = w / b ; tmp = s .* v
+__global__ void k_lanczos_shift(double* __restrict__ v, double* __restrict__ vp, const double* __restrict__ w,
+                                const double* __restrict__ s, double* __restrict__ tmp, double bj, i64 n) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    vp[i] = v[i];
+    const double vi = w[i] / bj;
+    v[i] = vi;
+    tmp[i] = s[i] * vi;
+  }
+}
+
+// v = v / nrm ; tmp = s .* v ; s = sqrt(dinv)
+__global__ void k_lanczos_start(double* __restrict__ v, const double* __restrict__ nrm,
+                                const double* __restrict__ dinv, double* __restrict__ s,
+                                double* __restrict__ tmp, i64 n) {
+  const double inv = *nrm;
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    const double si = sqrt(dinv[i]);
+    s[i] = si;
+    const double vi = v[i] / inv;
+    v[i] = vi;
+    tmp[i] = si * vi;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Setup numerics over node-level patterns
+// ---------------------------------------------------------------------------
+// 1 / diagonal; status 1 when a diagonal is not positive
+template <class TV>
+__global__ void k_inv_diag(i32 n, const i32* __restrict__ node_of, const i32* __restrict__ first,
+                           const i32* __restrict__ self_slot, NodeView a, const i32* __restrict__ rowptr,
+                           const TV* __restrict__ val, double* __restrict__ dinv, int* __restrict__ bad) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    const i32 I = node_of[i];
+    const i32 li = static_cast<i32>(i) - first[I];
+    const double d = static_cast<double>(val[rowptr[i] + a.off[self_slot[I]] + li]);
+    if (!(d > 0.0)) {
+      atomicMin(bad, static_cast<int>(i));
+      dinv[i] = 0.0;
+    } else {
+      dinv[i] = 1.0 / d;
+    }
+  }
+}
+
+// Block sums of squares per node-level slot (strength of connection,
+// src/fem/Multigrid.cpp:460-513): rows of the row node in order, then the
+// slot's columns in order.
+__global__ void k_block_sumsq(i32 nnodes, const i32* __restrict__ first, NodeView a,
+                              const i32* __restrict__ col_first, const i32* __restrict__ rowptr,
+                              const double* __restrict__ val, double* __restrict__ acc) {
+  for (i64 I = blockIdx.x * (i64)blockDim.x + threadIdx.x; I < nnodes; I += (i64)gridDim.x * blockDim.x) {
+    for (i32 t = a.ptr[I]; t < a.ptr[I + 1]; ++t) {
+      const i32 J = a.nbr[t];
+      const i32 sz = col_first[J + 1] - col_first[J];
+      double s = 0.0;
+      for (i32 i = first[I]; i < first[I + 1]; ++i) {
+        const double* v = val + rowptr[i] + a.off[t];
+        for (i32 k = 0; k < sz; ++k) s = xadd(s, xmul(v[k], v[k]));
+      }
+      acc[t] = s;
+    }
+  }
+}
+
+// P = (I - omega D^-1 A) P-hat over P's node pattern
+// (src/fem/Multigrid.cpp:671-716).  One TPR-lane group per fine row.
+template <int TPR, class T>
+__global__ void __launch_bounds__(256) k_prolongator(
+    i32 n, const i32* __restrict__ node_of, const i32* __restrict__ first,
+    const i32* __restrict__ first1, const i32* __restrict__ agg, NodeView a,
+    const i32* __restrict__ arow, const T* __restrict__ aval, NodeView p,
+    const i32* __restrict__ prow, T* __restrict__ pval, const i32* __restrict__ phat_ptr,
+    const T* __restrict__ phat, const double* __restrict__ dinv, double omega) {
+  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 i = static_cast<i32>(t0 / TPR);
+  const int lane = static_cast<int>(t0 % TPR);
+  if (i >= n) return;
+  const i32 I = node_of[i];
+  const T scale = static_cast<T>(omega * dinv[i]);
+  const i32 aI = agg[I];
+  for (i32 s = p.ptr[I] + lane; s < p.ptr[I + 1]; s += TPR) {
+    const i32 g = p.nbr[s];
+    const i32 rg = first1[g + 1] - first1[g];
+    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    for (i32 t = a.ptr[I]; t < a.ptr[I + 1]; ++t) {
+      const i32 J = a.nbr[t];
+      if (agg[J] != g) continue;
+      const i32 sJ = first[J + 1] - first[J];
+      const T* av = aval + arow[i] + a.off[t];
+      for (i32 kb = 0; kb < sJ; ++kb) {
+        const T v = av[kb];
+        const T* ph = phat + phat_ptr[first[J] + kb];
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+          if (j < rg) acc[j] = xadd(acc[j], xmul(v, ph[j]));
+      }
+    }
+    T* out = pval + prow[i] + p.off[s];
+    const T* own = phat + phat_ptr[i];
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+      if (j < rg) {
+        T v = xmul(acc[j], -scale);
+        if (aI == g) v = xadd(v, own[j]);
+        out[j] = v;
+      }
+  }
+}
+
+// R = P^T refill: R(c, (I, ka)) = P((I, ka), c)
+template <int TPR, class T>
+__global__ void __launch_bounds__(256) k_restriction(
+    i32 nc, const i32* __restrict__ node_of1, const i32* __restrict__ first1,
+    const i32* __restrict__ first, NodeView r, const i32* __restrict__ rrow, T* __restrict__ rval,
+    const i32* __restrict__ r_to_p, NodeView p, const i32* __restrict__ prow,
+    const T* __restrict__ pval) {
+  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 c = static_cast<i32>(t0 / TPR);
+  const int lane = static_cast<int>(t0 % TPR);
+  if (c >= nc) return;
+  const i32 g = node_of1[c];
+  const i32 lc = c - first1[g];
+  for (i32 t = r.ptr[g] + lane; t < r.ptr[g + 1]; t += TPR) {
+    const i32 I = r.nbr[t];
+    const i32 u = r_to_p[t];
+    T* out = rval + rrow[c] + r.off[t];
+    for (i32 ka = 0; ka < first[I + 1] - first[I]; ++ka) out[ka] = pval[prow[first[I] + ka] + p.off[u] + lc];
+  }
+}
+
+// AP = A P over AP's node pattern (multiply_numeric order).
+template <int TPR, class T>
+__global__ void __launch_bounds__(256) k_product_ap(
+    i32 n, const i32* __restrict__ node_of, const i32* __restrict__ first,
+    const i32* __restrict__ first1, NodeView a, const i32* __restrict__ arow,
+    const T* __restrict__ aval, NodeView p, const i32* __restrict__ prow,
+    const T* __restrict__ pval, NodeView ap, const i32* __restrict__ aprow, T* __restrict__ apval) {
+  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 i = static_cast<i32>(t0 / TPR);
+  const int lane = static_cast<int>(t0 % TPR);
+  if (i >= n) return;
+  const i32 I = node_of[i];
+  for (i32 s = ap.ptr[I] + lane; s < ap.ptr[I + 1]; s += TPR) {
+    const i32 h = ap.nbr[s];
+    const i32 rh = first1[h + 1] - first1[h];
+    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    for (i32 t = a.ptr[I]; t < a.ptr[I + 1]; ++t) {
+      const i32 J = a.nbr[t];
+      i32 u = p.ptr[J];
+      const i32 ue = p.ptr[J + 1];
+      while (u < ue && p.nbr[u] < h) ++u;
+      if (u == ue || p.nbr[u] != h) continue;
+      const i32 sJ = first[J + 1] - first[J];
+      const T* av = aval + arow[i] + a.off[t];
+      for (i32 kb = 0; kb < sJ; ++kb) {
+        const T v = av[kb];
+        const T* pv = pval + prow[first[J] + kb] + p.off[u];
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+          if (j < rh) acc[j] = xadd(acc[j], xmul(v, pv[j]));
+      }
+    }
+    T* out = apval + aprow[i] + ap.off[s];
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+      if (j < rh) out[j] = acc[j];
+  }
+}
+
+// RAW = R (AP) over the coarse node pattern (multiply_numeric order).
+template <int TPR, class T>
+__global__ void __launch_bounds__(256) k_product_rap(
+    i32 nc, const i32* __restrict__ node_of1, const i32* __restrict__ first1,
+    const i32* __restrict__ first, NodeView r, const i32* __restrict__ rrow,
+    const T* __restrict__ rval, NodeView ap, const i32* __restrict__ aprow,
+    const T* __restrict__ apval, NodeView c, const i32* __restrict__ crow, T* __restrict__ cval) {
+  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t0 / TPR);
+  const int lane = static_cast<int>(t0 % TPR);
+  if (row >= nc) return;
+  const i32 g = node_of1[row];
+  for (i32 s = c.ptr[g] + lane; s < c.ptr[g + 1]; s += TPR) {
+    const i32 h = c.nbr[s];
+    const i32 rh = first1[h + 1] - first1[h];
+    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    for (i32 t = r.ptr[g]; t < r.ptr[g + 1]; ++t) {
+      const i32 I = r.nbr[t];
+      i32 u = ap.ptr[I];
+      const i32 ue = ap.ptr[I + 1];
+      while (u < ue && ap.nbr[u] < h) ++u;
+      if (u == ue || ap.nbr[u] != h) continue;
+      const i32 sI = first[I + 1] - first[I];
+      const T* rv = rval + rrow[row] + r.off[t];
+      for (i32 ka = 0; ka < sI; ++ka) {
+        const T v = rv[ka];
+        const T* apv = apval + aprow[first[I] + ka] + ap.off[u];
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+          if (j < rh) acc[j] = xadd(acc[j], xmul(v, apv[j]));
+      }
+    }
+    T* out = cval + crow[row] + c.off[s];
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+      if (j < rh) out[j] = acc[j];
+  }
+}
+
+// A_c = (RAW + RAW^T) / 2 on the (structurally symmetric) coarse pattern.
+template <class T, class TO>
+__global__ void k_symmetrize(i32 nc, const i32* __restrict__ node_of1, const i32* __restrict__ first1,
+                             NodeView c, const i32* __restrict__ crow, const i32* __restrict__ tslot,
+                             const T* __restrict__ raw, TO* __restrict__ out, double* __restrict__ out64) {
+  for (i64 row = blockIdx.x * (i64)blockDim.x + threadIdx.x; row < nc; row += (i64)gridDim.x * blockDim.x) {
+    const i32 g = node_of1[row];
+    const i32 lc = static_cast<i32>(row) - first1[g];
+    for (i32 s = c.ptr[g]; s < c.ptr[g + 1]; ++s) {
+      const i32 h = c.nbr[s];
+      const i32 st = tslot[s];
+      const i32 base = crow[row] + c.off[s];
+      for (i32 j = 0; j < first1[h + 1] - first1[h]; ++j) {
+        const T a = raw[base + j];
+        const T b = raw[crow[first1[h] + j] + c.off[st] + lc];
+        const T v = xmul(T(0.5), xadd(a, b));
+        out[base + j] = static_cast<TO>(v);
+        if (out64) out64[base + j] = static_cast<double>(v);
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace simp

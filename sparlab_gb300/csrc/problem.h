@@ -1,0 +1,88 @@
+// The whole SIMP iteration on the GPU for a structured Q4 / Hex8 problem:
+// ComplianceObjective::evaluate (src/topopt/Sensitivity.cpp:110-237),
+// optimality_criteria_update (src/topopt/OptimalityCriteria.cpp:40-149) and
+// one iteration of TopologyOptimizer::run_oc (src/topopt/TopologyOptimizer.cpp:
+// 608-705), with the design, densities, displacements and gradients resident
+// in device memory.
+#pragma once
+
+#include "amg.h"
+#include "common.h"
+
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace simp {
+
+struct ProblemDesc {
+  int dim = 3;
+  i32 nx = 0, ny = 0, nz = 1;
+  double lx = 0, ly = 0, lz = 0;
+  double thickness = 1.0;
+  std::vector<double> ke;       // element matrix, row-major
+  std::vector<uint8_t> fixed;   // per DOF
+  int nloads = 0;
+  std::vector<double> loads;    // nloads x ndof
+  std::vector<double> weights;  // normalised
+  double radius = 1.5, vf = 0.5, x0 = 0.5, penalty = 3.0, emin = 1e-9, move = 0.2, damping = 0.5;
+  bool warm = true;
+  bool block_pcg = false;
+};
+
+struct Evaluation {
+  double compliance = 0, volume = 0, volume_fraction = 0, relres_max = 0;
+  int linear_iterations = 0;
+};
+
+struct OcStep {
+  double lambda = 0, volume = 0, max_change = 0;
+  int bisections = 0;
+  bool converged = false;
+};
+
+class GpuProblem {
+ public:
+  GpuProblem(const ProblemDesc& d, const AmgOptions& o);
+  ~GpuProblem();
+
+  ProblemDesc d;
+  GpuAmg amg;
+  i64 ne = 0, nn = 0, ndof = 0;
+  i32 nfree = 0;
+  double hx = 0, hy = 0, hz = 0, elem_volume = 0, domain_volume = 0;
+
+  void set_design(const double* h);
+  void get_design(double* h);
+  Evaluation evaluate();
+  OcStep oc_update(bool apply, double* xnew_host);
+  void filter_forward(const double* x, double* y);   // device pointers
+  void filter_adjoint(const double* v, double* g);   // device pointers
+  void assemble(const double* scale_device);
+
+  // device state
+  DBuf<double> x, xnew, rho, sf, df, dc_dphys, dc_dx, dv_dx, se, vols, tmp;
+  DBuf<double> b, u;        // free load vectors / displacements, nloads x nfree
+  DBuf<i32> dof_map;        // DOF -> free index or -1
+  DBuf<double> ke_d, weights_d;
+  DBuf<double> hw;          // filter weights, slot-major
+  DBuf<i32> gnode;
+  DBuf<uint8_t> cmask, ucomp;
+  DBuf<double> opart;
+  void* stencil_d = nullptr;
+  std::vector<double> last_compliance;
+  bool evaluated = false;
+  int evaluations = 0;
+  double gray = 0.0;
+
+ private:
+  bool structure_built_ = false;
+  int stencil_count_ = 0;
+  std::vector<i32> free_dofs_;
+  void build();
+};
+
+void element_stiffness(int dim, double hx, double hy, double hz, double young, double nu, double thick,
+                       double* ke);
+
+}  // namespace simp

@@ -1,0 +1,265 @@
+// Device kernels of the SIMP iteration on a structured Q4 / Hex8 grid:
+// value assembly of K_ff, the density filter as a stencil, the SIMP law,
+// element strain energies / compliance sensitivities, and the OC candidate
+// with its filtered volume.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace simp {
+namespace {
+
+struct GridView {
+  int dim;            // 2 or 3
+  i32 nx, ny, nz;     // cells (nz = 1 in 2-D)
+  i32 nnx, nny, nnz;  // nodes per axis
+};
+
+// VTK corner index of the node at offset (dx, dy, dz) in {0,1}^3 of its cell
+// (src/mesh/StructuredMesh.cpp:221-236).
+__device__ __forceinline__ int corner_of(int dx, int dy, int dz) { return 4 * dz + (dy ? 3 - dx : dx); }
+
+// K_ff values into the free-free pattern, row-owner gather: entry
+// (row (I, ka), column (J, kb)) = sum over the cells shared by I and J, in
+// ascending cell order, of s_e * K_e^0(J kb, I ka), with rounded products and
+// sums in the order of the reference's scatter (src/fem/Assembler.cpp:
+// 182-214), so the FP64 values equal a sequential assembly bit for bit.
+template <int TPR, class TO>
+__global__ void __launch_bounds__(256) k_assemble(
+    GridView g, i32 n, const i32* __restrict__ node_of, const i32* __restrict__ gnode,
+    const uint8_t* __restrict__ cmask, const uint8_t* __restrict__ ucomp, NodeView a,
+    const i32* __restrict__ rowptr, const double* __restrict__ ke, const double* __restrict__ scale,
+    TO* __restrict__ val, double* __restrict__ val64) {
+  __shared__ double ks[24 * 24];
+  const int ed = g.dim == 3 ? 24 : 8;
+  for (int e = threadIdx.x; e < ed * ed; e += blockDim.x) ks[e] = ke[e];
+  __syncthreads();
+  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 i = static_cast<i32>(t0 / TPR);
+  const int lane = static_cast<int>(t0 % TPR);
+  if (i >= n) return;
+  const i32 I = node_of[i];
+  const int ka = ucomp[i];
+  const i32 gi = gnode[I];
+  const i32 ix = gi % g.nnx, iy = (gi / g.nnx) % g.nny, iz = gi / (g.nnx * g.nny);
+  for (i32 t = a.ptr[I] + lane; t < a.ptr[I + 1]; t += TPR) {
+    const i32 J = a.nbr[t];
+    const i32 gj = gnode[J];
+    const i32 jx = gj % g.nnx, jy = (gj / g.nnx) % g.nny, jz = gj / (g.nnx * g.nny);
+    const int mask = cmask[J];
+    double acc[3] = {0.0, 0.0, 0.0};
+    const i32 z0 = max(max(iz, jz) - 1, 0), z1 = min(min(iz, jz), g.nz - 1);
+    const i32 y0 = max(max(iy, jy) - 1, 0), y1 = min(min(iy, jy), g.ny - 1);
+    const i32 x0 = max(max(ix, jx) - 1, 0), x1 = min(min(ix, jx), g.nx - 1);
+    for (i32 cz = z0; cz <= z1; ++cz)
+      for (i32 cy = y0; cy <= y1; ++cy)
+        for (i32 cx = x0; cx <= x1; ++cx) {
+          const i64 e = (static_cast<i64>(cz) * g.ny + cy) * g.nx + cx;
+          const double s = scale[e];
+          const int aI = corner_of(ix - cx, iy - cy, g.dim == 3 ? iz - cz : 0);
+          const int aJ = corner_of(jx - cx, jy - cy, g.dim == 3 ? jz - cz : 0);
+          int q = 0;
+          for (int kb = 0; kb < g.dim; ++kb) {
+            if (!(mask & (1 << kb))) continue;
+            acc[q] = xadd(acc[q], xmul(s, ks[(g.dim * aJ + kb) * ed + g.dim * aI + ka]));
+            ++q;
+          }
+        }
+    const i32 base = rowptr[i] + a.off[t];
+    int q = 0;
+    for (int kb = 0; kb < g.dim; ++kb) {
+      if (!(mask & (1 << kb))) continue;
+      val[base + q] = static_cast<TO>(acc[q]);
+      if (val64) val64[base + q] = acc[q];
+      ++q;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// density filter as a stencil: H(e, e + o_s) = w[s][e] (w / row sum, FP64)
+// ---------------------------------------------------------------------------
+struct Stencil {
+  int count;
+  int dx[128], dy[128], dz[128];  // offsets, ascending linear order
+};
+
+__device__ __forceinline__ bool in_grid(const GridView& g, i32 x, i32 y, i32 z) {
+  return x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz;
+}
+
+// y = H x (ascending neighbour order, as Eigen's column-major product sums);
+// clamp01 != 0 also clamps the result to [0, 1]; vol != NULL accumulates
+// sum_e v_e y_e into per-block partials.
+__global__ void __launch_bounds__(kRedThreads) k_filter_forward(GridView g, const Stencil* __restrict__ st,
+                                                                const double* __restrict__ w, i64 ne,
+                                                                const double* __restrict__ x,
+                                                                double* __restrict__ y, int clamp01,
+                                                                const double* __restrict__ volumes,
+                                                                double* __restrict__ part) {
+  double vs = 0.0;
+  for (i64 e = blockIdx.x * (i64)kRedThreads + threadIdx.x; e < ne; e += (i64)gridDim.x * kRedThreads) {
+    const i32 ex = static_cast<i32>(e % g.nx), ey = static_cast<i32>((e / g.nx) % g.ny),
+              ez = static_cast<i32>(e / ((i64)g.nx * g.ny));
+    double s = 0.0;
+    for (int k = 0; k < st->count; ++k) {
+      const i32 qx = ex + st->dx[k], qy = ey + st->dy[k], qz = ez + st->dz[k];
+      if (!in_grid(g, qx, qy, qz)) continue;
+      const i64 q = (static_cast<i64>(qz) * g.ny + qy) * g.nx + qx;
+      s = xadd(s, xmul(w[k * ne + e], x[q]));
+    }
+    if (clamp01) s = fmin(fmax(s, 0.0), 1.0);
+    if (y) y[e] = s;
+    if (part) vs += s * volumes[e];
+  }
+  if (part) {
+    vs = block_sum<kRedThreads>(vs);
+    if (threadIdx.x == 0) part[blockIdx.x] = vs;
+  }
+}
+
+// g = H^T v: column j of H summed over ascending rows e = j - o_s.
+__global__ void k_filter_adjoint(GridView g, const Stencil* __restrict__ st, const double* __restrict__ w,
+                                 i64 ne, const double* __restrict__ v, double* __restrict__ out) {
+  for (i64 j = blockIdx.x * (i64)blockDim.x + threadIdx.x; j < ne; j += (i64)gridDim.x * blockDim.x) {
+    const i32 jx = static_cast<i32>(j % g.nx), jy = static_cast<i32>((j / g.nx) % g.ny),
+              jz = static_cast<i32>(j / ((i64)g.nx * g.ny));
+    double s = 0.0;
+    for (int k = st->count - 1; k >= 0; --k) {
+      const i32 ex = jx - st->dx[k], ey = jy - st->dy[k], ez = jz - st->dz[k];
+      if (!in_grid(g, ex, ey, ez)) continue;
+      const i64 e = (static_cast<i64>(ez) * g.ny + ey) * g.nx + ex;
+      s = xadd(s, xmul(w[k * ne + e], v[e]));
+    }
+    out[j] = s;
+  }
+}
+
+// Correctly rounded r^3 (double-double product): the FP64 SIMP law with the
+// penalty 3 of every configuration gives the same factors as a correctly
+// rounded pow.
+__device__ __forceinline__ double cube_rn(double r) {
+  const double h = r * r;
+  const double l = fma(r, r, -h);            // r^2 = h + l exactly
+  const double p = h * r;
+  const double pe = fma(h, r, -p);           // h r = p + pe exactly
+  return p + fma(l, r, pe);
+}
+
+__device__ __forceinline__ double simp_pow(double r, double p) {
+  if (p == 3.0) return cube_rn(r);
+  return pow(r, p);
+}
+
+// rho -> stiffness factor and its derivative (src/topopt/SimpInterpolation.cpp:59-70)
+__global__ void k_simp(i64 ne, const double* __restrict__ rho, double pen, double emin,
+                       double* __restrict__ sf, double* __restrict__ df) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x) {
+    const double r = fmin(fmax(rho[e], 0.0), 1.0);
+    sf[e] = xadd(emin, xmul(1.0 - emin, simp_pow(r, pen)));
+    df[e] = xmul(xmul(pen, 1.0 - emin), pen == 3.0 ? xmul(r, r) : pow(r, pen - 1.0));
+  }
+}
+
+// Element energies u_e^T K_e^0 u_e for every load case (src/topopt/
+// Sensitivity.cpp:182-189): dc/drho_e -= w_l dE_e q, SE_e += w_l / 2 E_e q.
+__global__ void __launch_bounds__(128) k_sensitivities(GridView g, i64 ne, int nloads,
+                                                       const double* __restrict__ u, i64 ldu,
+                                                       const i32* __restrict__ dof_map,
+                                                       const double* __restrict__ ke,
+                                                       const double* __restrict__ weights,
+                                                       const double* __restrict__ sf,
+                                                       const double* __restrict__ df,
+                                                       double* __restrict__ dc, double* __restrict__ se) {
+  __shared__ double ks[24 * 24];
+  const int ed = g.dim == 3 ? 24 : 8;
+  for (int k = threadIdx.x; k < ed * ed; k += blockDim.x) ks[k] = ke[k];
+  __syncthreads();
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x) {
+    const i32 ex = static_cast<i32>(e % g.nx), ey = static_cast<i32>((e / g.nx) % g.ny),
+              ez = static_cast<i32>(e / ((i64)g.nx * g.ny));
+    const i64 n0 = (static_cast<i64>(ez) * g.nny + ey) * g.nnx + ex;
+    const i64 layer = static_cast<i64>(g.nnx) * g.nny;
+    i64 nodes[8];
+    nodes[0] = n0;
+    nodes[1] = n0 + 1;
+    nodes[2] = n0 + g.nnx + 1;
+    nodes[3] = n0 + g.nnx;
+    if (g.dim == 3) {
+      for (int a = 0; a < 4; ++a) nodes[4 + a] = nodes[a] + layer;
+    }
+    const int npe = g.dim == 3 ? 8 : 4;
+    double dcs = 0.0, ses = 0.0;
+    for (int l = 0; l < nloads; ++l) {
+      double ue[24];
+      for (int a = 0; a < npe; ++a)
+        for (int k = 0; k < g.dim; ++k) {
+          const i32 f = dof_map[nodes[a] * g.dim + k];
+          ue[g.dim * a + k] = f >= 0 ? u[l * ldu + f] : 0.0;
+        }
+      double quad = 0.0;
+      for (int r = 0; r < ed; ++r) {
+        double kr = 0.0;
+        for (int c = 0; c < ed; ++c) kr += ks[r * ed + c] * ue[c];
+        quad += ue[r] * kr;
+      }
+      ses += weights[l] * 0.5 * sf[e] * quad;
+      dcs -= weights[l] * df[e] * quad;
+    }
+    dc[e] = dcs;
+    se[e] = ses;
+  }
+}
+
+// OC candidate (src/topopt/OptimalityCriteria.cpp:14-36)
+__global__ void k_oc_candidate(i64 ne, const double* __restrict__ x, const double* __restrict__ dc,
+                               const double* __restrict__ dv, double lam, double move, double damping,
+                               double* __restrict__ xn) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x) {
+    const double xe = x[e];
+    const double lo = fmax(0.0, xe - move), hi = fmin(1.0, xe + move);
+    const double den = lam * dv[e];
+    double b = 0.0;
+    if (den > 0.0) b = fmax(0.0, -dc[e] / den);
+    const double f = damping == 0.5 ? sqrt(b) : pow(b, damping);
+    xn[e] = fmin(fmax(xe * f, lo), hi);
+  }
+}
+
+// max |a - b| and sum rho (1 - rho) partials
+__global__ void __launch_bounds__(kRedThreads) k_change_gray(i64 ne, const double* __restrict__ a,
+                                                             const double* __restrict__ b,
+                                                             const double* __restrict__ rho,
+                                                             double* __restrict__ part_max,
+                                                             double* __restrict__ part_gray) {
+  double m = 0.0, gsum = 0.0;
+  for (i64 e = blockIdx.x * (i64)kRedThreads + threadIdx.x; e < ne; e += (i64)gridDim.x * kRedThreads) {
+    m = fmax(m, fabs(a[e] - b[e]));
+    if (rho) gsum += rho[e] * (1.0 - rho[e]);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double wm[kRedThreads / 32];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  gsum = block_sum<kRedThreads>(gsum);
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int k = 0; k < kRedThreads / 32; ++k) mm = fmax(mm, wm[k]);
+    part_max[blockIdx.x] = mm;
+    if (part_gray) part_gray[blockIdx.x] = gsum;
+  }
+}
+
+__global__ void k_clamp01(i64 ne, double* __restrict__ x) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x)
+    x[e] = fmin(fmax(x[e], 0.0), 1.0);
+}
+
+// gather the free part of full-length load vectors: b[l][i] = f[l][free[i]]
+__global__ void k_gather(i64 n, int nl, const double* __restrict__ f, i64 ldf, const i32* __restrict__ free_dofs,
+                         double* __restrict__ b) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+    for (int l = 0; l < nl; ++l) b[l * n + i] = f[l * ldf + free_dofs[i]];
+}
+
+}  // namespace
+}  // namespace simp

@@ -1,0 +1,231 @@
+"""The SIMP iteration over the C ABI, with the reference's interfaces.
+
+``ComplianceObjective.evaluate`` mirrors ``sparlab::ComplianceObjective::
+evaluate`` (src/topopt/Sensitivity.cpp:110-237), ``optimality_criteria_update``
+mirrors src/topopt/OptimalityCriteria.cpp:40-149, and
+``TopologyOptimizer.run`` drives them as ``TopologyOptimizer::run_oc``
+(src/topopt/TopologyOptimizer.cpp:556-724).  The design, densities,
+displacements and gradients live in GPU memory; arrays are copied to the host
+only when asked for.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import time
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import ptr
+from .problems import ProblemSpec
+
+
+def element_stiffness(dim, hx, hy, hz, young, poisson, thickness=1.0) -> np.ndarray:
+    ed = 8 if dim == 2 else 24
+    ke = np.zeros((ed, ed))
+    code = _lib.load().simp_element_stiffness(C.c_int32(dim), C.c_double(hx), C.c_double(hy),
+                                              C.c_double(hz), C.c_double(young),
+                                              C.c_double(poisson), C.c_double(thickness), ptr(ke))
+    if code:
+        _lib.raise_for(code, _lib.load().simp_last_error(None).decode())
+    return ke
+
+
+@dataclasses.dataclass
+class ObjectiveEvaluation:
+    compliance: float
+    volume: float
+    volume_fraction: float
+    linear_iterations: int
+    relres_max: float
+    physical_density: Optional[np.ndarray] = None
+    dc_dphysical: Optional[np.ndarray] = None
+    dc_dx: Optional[np.ndarray] = None
+    dv_dx: Optional[np.ndarray] = None
+    element_strain_energy: Optional[np.ndarray] = None
+    displacements: Optional[np.ndarray] = None
+
+
+@dataclasses.dataclass
+class OptimalityCriteriaStep:
+    x: Optional[np.ndarray]
+    lam: float
+    achieved_volume: float
+    max_change: float
+    bisections: int
+    volume_converged: bool
+
+
+@dataclasses.dataclass
+class TopologyIteration:
+    iteration: int
+    compliance: float
+    volume_fraction: float
+    max_change: float
+    lam: float
+    gray_level: float
+    linear_iterations: int
+    bisections: int
+    seconds: float
+
+
+class GpuSimpProblem:
+    """A structured SIMP problem resident on the GPU (boundary 2 of the C ABI)."""
+
+    def __init__(self, spec: ProblemSpec, precision="fp64", element_matrix=None, device=0,
+                 block_pcg=False, **amg):
+        self._lib = _lib.load()
+        self.spec = spec
+        hx, hy = spec.lx / spec.nx, spec.ly / spec.ny
+        hz = spec.lz / spec.nz if spec.dim == 3 else 0.0
+        if element_matrix is None:
+            element_matrix = element_stiffness(spec.dim, hx, hy, hz, spec.young, spec.poisson,
+                                               spec.thickness if spec.dim == 2 else 1.0)
+        self._ke = np.ascontiguousarray(element_matrix, np.float64)
+        self._fixed = np.ascontiguousarray(spec.fixed, np.uint8)
+        self._loads = np.ascontiguousarray(np.atleast_2d(spec.loads), np.float64)
+        self._weights = np.ascontiguousarray(spec.weights, np.float64)
+        d = _lib.ProblemDesc()
+        d.dim, d.nx, d.ny, d.nz = spec.dim, spec.nx, spec.ny, spec.nz
+        d.lx, d.ly, d.lz = spec.lx, spec.ly, spec.lz
+        d.thickness = spec.thickness if spec.dim == 2 else 1.0
+        d.element_matrix = ptr(self._ke)
+        d.fixed = ptr(self._fixed, C.c_uint8)
+        d.num_loads = self._loads.shape[0]
+        d.loads = ptr(self._loads)
+        d.weights = ptr(self._weights)
+        d.filter_radius = spec.filter_radius
+        d.volume_fraction = spec.volume_fraction
+        d.initial_density = spec.initial_density
+        d.penalty, d.emin_ratio = spec.penalty, spec.emin_ratio
+        d.move_limit, d.damping = spec.move_limit, spec.damping
+        d.warm_start = int(spec.warm_start)
+        d.block_pcg = int(block_pcg)
+        prec = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
+        opts = dict(spec.amg)
+        opts.update(amg)
+        self.options = _lib.default_options(iterative_tolerance=spec.rtol,
+                                            max_iterations=spec.max_cg_iterations,
+                                            precision=prec, device=device, **opts)
+        self._h = C.c_void_p()
+        code = self._lib.simp_problem_create(C.byref(d), C.byref(self.options), C.byref(self._h))
+        if code:
+            _lib.raise_for(code, self._lib.simp_problem_last_error(None).decode())
+        s = np.zeros(5, np.int64)
+        self._check(self._lib.simp_problem_sizes(self._h, ptr(s, C.c_int64)))
+        self.ne, self.nn, self.ndof, self.nfree, self.nnz = (int(v) for v in s)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.simp_problem_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def _check(self, code):
+        if code:
+            _lib.raise_for(code, self._lib.simp_problem_last_error(self._h).decode())
+
+    def set_design(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        self._check(self._lib.simp_set_design(self._h, ptr(x)))
+
+    def design(self) -> np.ndarray:
+        x = np.zeros(self.ne)
+        self._check(self._lib.simp_get_design(self._h, ptr(x)))
+        return x
+
+    def evaluate(self, arrays=True, displacements=False) -> ObjectiveEvaluation:
+        ev = _lib.Evaluation()
+        out = {k: (np.zeros(self.ne) if arrays else None)
+               for k in ("rho", "dcp", "dcx", "dvx", "se")}
+        u = np.zeros((self._loads.shape[0], self.ndof)) if displacements else None
+        self._check(self._lib.simp_evaluate(self._h, C.byref(ev), ptr(out["rho"]), ptr(out["dcp"]),
+                                            ptr(out["dcx"]), ptr(out["dvx"]), ptr(out["se"]),
+                                            ptr(u)))
+        return ObjectiveEvaluation(ev.compliance, ev.volume, ev.volume_fraction,
+                                   ev.linear_iterations, ev.relres_max, out["rho"], out["dcp"],
+                                   out["dcx"], out["dvx"], out["se"], u)
+
+    def oc_update(self, apply=True, download=True) -> OptimalityCriteriaStep:
+        st = _lib.OcStep()
+        xn = np.zeros(self.ne) if download else None
+        self._check(self._lib.simp_oc_update(self._h, C.c_int32(int(apply)), C.byref(st), ptr(xn)))
+        return OptimalityCriteriaStep(xn, st.lam, st.achieved_volume, st.max_change, st.bisections,
+                                      bool(st.volume_converged))
+
+    def iterate(self) -> _lib.IterationRecord:
+        rec = _lib.IterationRecord()
+        self._check(self._lib.simp_iterate(self._h, C.byref(rec)))
+        return rec
+
+    def amg_stats(self) -> dict:
+        s = _lib.AmgStats()
+        self._check(self._lib.simp_problem_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def apply_operator(self, x_device_ptr: int, y_device_ptr: int):
+        """y = K_ff x on device pointers (nfree doubles each)."""
+        self._check(self._lib.simp_problem_apply_operator(self._h, C.c_void_p(x_device_ptr),
+                                                          C.c_void_p(y_device_ptr)))
+
+    def filter_forward(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.ne)
+        self._check(self._lib.simp_filter_forward(self._h, ptr(x), ptr(y)))
+        return y
+
+    def filter_adjoint(self, v):
+        v = np.ascontiguousarray(v, np.float64)
+        g = np.zeros(self.ne)
+        self._check(self._lib.simp_filter_adjoint(self._h, ptr(v), ptr(g)))
+        return g
+
+    def kff(self, scale=None):
+        p = np.zeros(self.nfree + 1, np.int32)
+        c = np.zeros(self.nnz, np.int32)
+        v = None if scale is None else np.zeros(self.nnz)
+        scale = None if scale is None else np.ascontiguousarray(scale, np.float64)
+        self._check(self._lib.simp_problem_kff(self._h, ptr(scale), ptr(p, C.c_int32),
+                                               ptr(c, C.c_int32), ptr(v)))
+        return p, c, v
+
+
+class ComplianceObjective:
+    """``ComplianceObjective`` over a :class:`GpuSimpProblem`."""
+
+    def __init__(self, problem: GpuSimpProblem):
+        self.problem = problem
+
+    def evaluate(self, x, need_gradients=True) -> ObjectiveEvaluation:
+        self.problem.set_design(x)
+        return self.problem.evaluate(arrays=True)
+
+
+def optimality_criteria_update(problem: GpuSimpProblem) -> OptimalityCriteriaStep:
+    """OC step with the gradients of the problem's last evaluation (the volume
+    callback of the reference is the problem's own filter)."""
+    return problem.oc_update(apply=False, download=True)
+
+
+class TopologyOptimizer:
+    """``run_oc`` with the evaluation, OC update and clamp on the GPU."""
+
+    def __init__(self, problem: GpuSimpProblem, max_iterations=200, change_tolerance=1e-3):
+        self.problem = problem
+        self.max_iterations = max_iterations
+        self.change_tolerance = change_tolerance
+
+    def run(self) -> List[TopologyIteration]:
+        history = []
+        for it in range(1, self.max_iterations + 1):
+            t0 = time.perf_counter()
+            r = self.problem.iterate()
+            history.append(TopologyIteration(it, r.compliance, r.volume_fraction, r.max_change,
+                                             r.lam, r.gray_level, r.linear_iterations,
+                                             r.bisections, time.perf_counter() - t0))
+            if self.change_tolerance > 0 and r.max_change <= self.change_tolerance:
+                break
+        return history

@@ -1,0 +1,73 @@
+"""CPU checks of the C-ABI library: it builds for sm_103a, loads, exports
+every entry point include/simp_gpu.h declares, and its host-only helpers
+agree with the oracle.  No kernel runs here."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from sparlab_gb300 import _lib, build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "simp_gpu.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(simp_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_builds_for_sm103a():
+    path = build.build()
+    assert os.path.exists(path)
+    assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
+
+
+def test_every_declared_symbol_is_exported():
+    lib = _lib.load()
+    names = declared_functions()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(_lib.EXPORTS)
+
+
+def test_default_options_match_reference_defaults():
+    o = _lib.default_options()
+    assert o.strength_threshold == 0.02 and o.max_levels == 12 and o.coarse_size == 1500
+    assert o.smoother_degree == 3 and o.chebyshev_ratio == 30.0
+    assert o.prolongator_damping == pytest.approx(4.0 / 3.0) and o.lanczos_steps == 12
+    assert o.coarse_pivot_tolerance == 1e-13 and o.reuse_aggregates == 1
+    assert o.iterative_tolerance == 1e-12
+
+
+@pytest.mark.parametrize("dim,h", [(2, (1.0, 1.0, 0.0)), (2, (0.25, 0.1, 0.0)),
+                                   (3, (1.0, 1.0, 1.0)), (3, (0.25, 0.25, 0.25)),
+                                   (3, (0.5, 0.2, 0.125))])
+def test_element_stiffness_matches_oracle(dim, h):
+    from sparlab_gb300.topopt import element_stiffness
+    ke = element_stiffness(dim, *h, 70e9, 0.3, 0.01 if dim == 2 else 1.0)
+    ko = oracle.element_stiffness(dim, *h, 70e9, 0.3, 0.01 if dim == 2 else 1.0)
+    assert np.abs(ke - ko).max() <= 1e-14 * np.abs(ko).max()
+    assert np.array_equal(ke, ke.T)
+    # rigid translations are in the null space
+    n = ke.shape[0]
+    for k in range(dim):
+        t = np.zeros(n)
+        t[k::dim] = 1.0
+        assert np.abs(ke @ t).max() <= 1e-12 * np.abs(ke).max()
+
+
+def test_context_creation_reports_cuda_errors_without_a_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = _lib.load()
+    h = C.c_void_p()
+    code = lib.simp_ctx_create(None, C.byref(h))
+    assert code == _lib.SIMP_CUDA_ERROR
+    assert lib.simp_last_error(None)

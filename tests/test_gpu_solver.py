@@ -1,0 +1,165 @@
+"""GPU parity of the LinearSolver boundary (C ABI) against the CPU oracle.
+
+Integer work is compared bit for bit (aggregates of every level); values
+within the stated tolerances: displacements 1e-9 relative at rtol 1e-12,
+Galerkin level operators 1e-12 relative, compliance of the reference's
+bench model within 1e-9 of its published value."""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+import oracle
+from sparlab_gb300 import problems as P
+from sparlab_gb300.linear_solver import ConvergenceError, GpuAmgCgSolver, SolverError
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "solver_scaling.json")
+
+
+def system(spec, scale=None):
+    pr = oracle.Problem(spec)
+    ptr, col, val = pr.kff(scale)
+    return pr, ptr, col, val
+
+
+def both(spec, scale=None, rtol=1e-12, **amg):
+    pr, ptr, col, val = system(spec, scale)
+    ref = oracle.Solver(rtol=rtol, **amg)
+    ref.factorize(ptr, col, val, spec.dim, pr.coords(), pr.free_dofs())
+    gpu = GpuAmgCgSolver(iterative_tolerance=rtol, **amg)
+    gpu.set_layout(spec.dim, pr.coords(), pr.free_dofs())
+    gpu.factorize(ptr, col, val)
+    return pr, (ptr, col, val), ref, gpu
+
+
+@pytest.mark.parametrize("dim,nx,ny,nz", [(3, 8, 4, 2), (3, 16, 8, 4), (2, 40, 20, 0),
+                                          (3, 48, 24, 12), (2, 160, 80, 0)])
+def test_bench_model_matches_published_compliance(dim, nx, ny, nz):
+    with open(GOLDEN) as f:
+        rows = [r for r in json.load(f)["rows"] if r["solver"] == "amg" and r["nx"] == nx
+                and r["ny"] == ny and r["element"] == ("Hex8" if dim == 3 else "Quad4")]
+    gold = rows[0]
+    spec = P.bench_model(dim, nx, ny, nz)
+    pr, _, ref, gpu = both(spec, rtol=1e-10)
+    f = spec.loads[0][pr.free_dofs()]
+    x = gpu.solve(f)
+    assert abs(f @ x / gold["compliance"] - 1) < 1e-9
+    st = gpu.amg_stats()
+    assert st["num_levels"] == gold["levels"]
+    assert st["operator_complexity"] == gold["operator_complexity"]
+    assert abs(gpu.last_iterations() - gold["iterations"]) <= 1
+
+
+def test_aggregates_bit_exact_and_levels_match_oracle():
+    spec = P.bench_model(3, 24, 12, 8)
+    rng = P.SplitMix64(7)
+    rho = rng.uniform_array(spec.num_elements, 0.01, 1.0)
+    scale = 1e-9 + (1 - 1e-9) * rho ** 3
+    pr, (ptr, col, val), ref, gpu = both(spec, scale, coarse_size=60)
+    assert gpu.amg_stats()["num_levels"] == ref.num_levels()
+    for lvl in range(ref.num_levels() - 1):
+        np.testing.assert_array_equal(gpu.aggregates(lvl), ref.aggregates(lvl))
+    for lvl in range(1, ref.num_levels()):
+        gp, gc, gv = gpu.level_matrix(lvl)
+        rp, rc, rv = ref.level_matrix(lvl)
+        np.testing.assert_array_equal(gp, rp)
+        np.testing.assert_array_equal(gc, rc)
+        assert np.abs(gv - rv).max() <= 1e-12 * np.abs(rv).max()
+
+
+def test_solution_matches_oracle_and_direct():
+    spec = P.bench_model(3, 20, 10, 6)
+    pr, (ptr, col, val), ref, gpu = both(spec, coarse_size=60)
+    f = spec.loads[0][pr.free_dofs()]
+    xg = gpu.solve(f)
+    xr, itr, _ = ref.solve(f)
+    n = len(ptr) - 1
+    u = spla.spsolve(sp.csr_matrix((val, col, ptr), shape=(n, n)).tocsc(), f)
+    assert np.linalg.norm(xg - xr) <= 1e-9 * np.linalg.norm(xr)
+    assert np.linalg.norm(xg - u) <= 1e-8 * np.linalg.norm(u)
+    assert abs(gpu.last_iterations() - itr) <= 1
+    assert gpu.last_error() <= 1e-12
+
+
+def test_vcycle_symmetric_and_matches_oracle():
+    spec = P.bench_model(3, 12, 6, 4)
+    pr, (ptr, col, val), ref, gpu = both(spec, coarse_size=60)
+    n = len(ptr) - 1
+    i = np.arange(n)
+    x = np.sin(0.37 * i + 0.1) + 0.2
+    y = np.sin(0.37 * i + 1.3) + 0.2
+    mx, my = gpu.apply_preconditioner(x), gpu.apply_preconditioner(y)
+    assert abs(x @ my - y @ mx) <= 1e-11 * abs(x @ my)
+    rx = ref.apply(x)
+    assert np.linalg.norm(mx - rx) <= 1e-10 * np.linalg.norm(rx)
+
+
+def test_simp_contrast_reuse_and_warm_start():
+    spec = P.bench_model(3, 16, 8, 4)
+    rng = P.SplitMix64(11)
+    rho = rng.uniform_array(spec.num_elements, 0.0, 1.0)
+    rho[rho < 0.4] = 0.001
+    scale = 1e-9 + (1 - 1e-9) * rho ** 3
+    pr, (ptr, col, val), ref, gpu = both(spec, scale, rtol=1e-10, coarse_size=60)
+    f = spec.loads[0][pr.free_dofs()]
+    x = gpu.solve(f)
+    xr, _, _ = ref.solve(f)
+    assert abs((f @ x) / (f @ xr) - 1) < 1e-8
+    gpu.factorize(ptr, col, val)
+    assert gpu.amg_stats()["reused_aggregates"]
+    x2 = gpu.solve_from(f, x)
+    assert gpu.last_iterations() == 0
+    assert np.array_equal(x2, x)
+
+
+def test_deterministic_runs():
+    spec = P.bench_model(3, 16, 8, 4)
+    pr, (ptr, col, val), ref, gpu = both(spec, coarse_size=60)
+    f = spec.loads[0][pr.free_dofs()]
+    a = gpu.solve(f)
+    b = gpu.solve(f)
+    assert np.array_equal(a, b)
+
+
+def test_errors_are_reported_and_context_survives():
+    spec = P.bench_model(3, 8, 4, 2)
+    spec.fixed = np.zeros_like(spec.fixed)
+    pr, ptr, col, val = system(spec)
+    gpu = GpuAmgCgSolver(coarse_size=60)
+    gpu.set_layout(3, pr.coords(), pr.free_dofs())
+    with pytest.raises(SolverError) as e:
+        gpu.factorize(ptr, col, val)
+    assert "under-constrained" in str(e.value)
+    # not symmetric
+    spec = P.bench_model(3, 8, 4, 2)
+    pr, ptr, col, val = system(spec)
+    bad = val.copy()
+    bad[5] *= 1.5
+    gpu = GpuAmgCgSolver(coarse_size=60)
+    gpu.set_layout(3, pr.coords(), pr.free_dofs())
+    with pytest.raises(SolverError) as e:
+        gpu.factorize(ptr, col, bad)
+    assert "not symmetric" in str(e.value)
+    nan = val.copy()
+    nan[3] = np.nan
+    with pytest.raises(SolverError):
+        gpu.factorize(ptr, col, nan)
+    # iteration budget
+    gpu = GpuAmgCgSolver(iterative_tolerance=1e-14, max_iterations=1, coarse_size=60)
+    spec = P.bench_model(3, 16, 8, 4)
+    pr, ptr, col, val = system(spec)
+    gpu.set_layout(3, pr.coords(), pr.free_dofs())
+    gpu.factorize(ptr, col, val)
+    with pytest.raises(ConvergenceError) as e:
+        gpu.solve(spec.loads[0][pr.free_dofs()])
+    assert "did not converge" in str(e.value)
+    # the context is still usable
+    gpu2 = GpuAmgCgSolver(iterative_tolerance=1e-10, coarse_size=60)
+    gpu2.set_layout(3, pr.coords(), pr.free_dofs())
+    gpu2.factorize(ptr, col, val)
+    gpu2.solve(spec.loads[0][pr.free_dofs()])
