@@ -222,6 +222,21 @@ int simp_element_stiffness(int32_t dim, double hx, double hy, double hz, double 
  * stream.  Exposed so a caller can time the dominant kernel in isolation. */
 int simp_problem_apply_operator(simp_problem* p, const double* x_device, double* y_device);
 
+/* No counterpart in the reference.  rho = clamp(H x, 0, 1) and the volume
+ * sum_e v_e rho_e of the problem's density filter -- the physical density and
+ * volume simp_evaluate reports for design x -- on device pointers (x and rho:
+ * num_elements doubles, volume: one double), launched on the library's stream.
+ * It allocates no device memory: its partial sums live in a fixed 128 KiB
+ * device array of the library, so a caller that must not call cudaMalloc at
+ * that point (an optimiser evaluating many trial designs per iteration
+ * without device synchronisation, an application running under its own
+ * memory pool) can use it.  At most 67,108,864 elements (SIMP_BAD_INPUT
+ * beyond).  The first call on a device sets the array up and should come
+ * before any stream capture; calls that overlap on the GPU share the array
+ * and race. */
+int simp_filter_volume_noalloc(simp_problem* p, const double* x_device, double* rho_device,
+                               double* volume_device);
+
 /* Number of kernels this library has launched (for launch accounting). */
 int64_t simp_kernel_launches(void);
 

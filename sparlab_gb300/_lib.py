@@ -30,7 +30,7 @@ EXPORTS = [
     "simp_problem_sizes", "simp_set_design", "simp_get_design", "simp_evaluate",
     "simp_oc_update", "simp_iterate", "simp_problem_stats", "simp_filter_forward",
     "simp_filter_adjoint", "simp_problem_kff", "simp_element_stiffness",
-    "simp_problem_apply_operator", "simp_kernel_launches",
+    "simp_problem_apply_operator", "simp_filter_volume_noalloc", "simp_kernel_launches",
 ]
 
 

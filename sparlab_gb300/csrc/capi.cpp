@@ -600,6 +600,13 @@ int simp_problem_apply_operator(simp_problem* p, const double* x, double* y) {
   });
 }
 
+int simp_filter_volume_noalloc(simp_problem* p, const double* x, double* rho, double* volume) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    filter_volume_noalloc(*p->p, x, rho, volume);
+  });
+}
+
 int64_t simp_kernel_launches(void) { return g_launches.load(); }
 
 }  // extern "C"

@@ -85,4 +85,7 @@ class GpuProblem {
 void element_stiffness(int dim, double hx, double hy, double hz, double young, double nu, double thick,
                        double* ke);
 
+// rho = clamp(H x, 0, 1) and sum_e v_e rho_e without allocating (noalloc.cu).
+void filter_volume_noalloc(GpuProblem& p, const double* x, double* rho, double* volume);
+
 }  // namespace simp
