@@ -149,6 +149,7 @@ typedef struct {
   double move_limit, damping;   /* OptimalityCriteriaOptions */
   int32_t warm_start;           /* LinearSolverOptions::warm_start */
   int32_t block_pcg;            /* 1: all load cases as one block of RHS */
+  int32_t optimizer;            /* simp_iterate's update: 0 OC, 1 MMA */
 } simp_problem_desc;
 
 /* ObjectiveEvaluation scalars (Sensitivity.hpp:66-107) and an OC step
@@ -196,7 +197,15 @@ int simp_evaluate(simp_problem* p, simp_evaluation* out, double* rho, double* dc
  * evaluate; the new design replaces the resident one when `apply` != 0. */
 int simp_oc_update(simp_problem* p, int32_t apply, simp_oc_step* out, double* xnew);
 
-/* One run_oc iteration: evaluate + OC + clamp, device-resident. */
+/* MmaOptimizer::update (src/topopt/Mma.cpp:63-157) as run_mma drives it
+ * (src/topopt/TopologyOptimizer.cpp:831-905): objective c / c_1, one
+ * constraint V / V* - 1, with the resident gradients of the last evaluate.
+ * out->lambda is the volume multiplier, out->bisections the subproblem's
+ * Newton iterations; achieved_volume is not computed (0). */
+int simp_mma_update(simp_problem* p, int32_t apply, simp_oc_step* out, double* xnew);
+
+/* One run_oc (or run_mma, per desc->optimizer) iteration: evaluate + update +
+ * clamp, device-resident. */
 int simp_iterate(simp_problem* p, simp_iteration_record* rec);
 
 /* AMG statistics of the problem's solver. */
@@ -221,6 +230,13 @@ int simp_element_stiffness(int32_t dim, double hx, double hy, double hz, double 
  * the last evaluate), on device pointers of nfree doubles, on the library's
  * stream.  Exposed so a caller can time the dominant kernel in isolation. */
 int simp_problem_apply_operator(simp_problem* p, const double* x_device, double* y_device);
+
+/* Times `reps` launches of the level-0 operator application the V-cycle uses
+ * (FP64 values, or FP32 in mixed precision) with CUDA events on the library's
+ * stream: average milliseconds per launch and its algorithmic bytes (values,
+ * block pattern, x read and y written once). */
+int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms_per_launch,
+                               double* bytes_per_launch);
 
 /* No counterpart in the reference.  rho = clamp(H x, 0, 1) and the volume
  * sum_e v_e rho_e of the problem's density filter -- the physical density and

@@ -309,6 +309,13 @@ class Problem:
         return xn, dict(lam=out[0], volume=out[1], max_change=out[2], bisections=int(out[3]),
                         converged=bool(out[4]))
 
+    def run_mma(self, iterations):
+        x = np.zeros(self.ne)
+        hist = np.zeros((iterations, 6))
+        done = C.c_int32()
+        _check(lib().orc_run_mma(self._h, C.c_int32(iterations), _p(x), _p(hist), C.byref(done)))
+        return x, hist[: done.value]
+
     def run(self, iterations, change_tol=0.0):
         x = np.zeros(self.ne)
         hist = np.zeros((iterations, 6))

@@ -1642,6 +1642,208 @@ OcStep oc_update(const Problem& p, const double* x, const double* dc, const doub
   return st;
 }
 
+// ---------------------------------------------------------------------------
+// MMA (src/topopt/Mma.cpp:63-409), restated for one constraint row (the
+// volume): the (lambda, z) Newton system of the subproblem is 2 x 2.
+// ---------------------------------------------------------------------------
+struct MmaState {
+  int iteration = 0;
+  Vec xold1, xold2, low, upp;
+  double move = 0.2, asy_init = 0.5, asy_inc = 1.2, asy_dec = 0.7, albefa = 0.1, raa0 = 1.0e-5;
+  double a0 = 1.0, c = 1000.0, d = 1.0, epsimin = 1.0e-7, scale_cap = 10.0;
+  int max_inner = 500;
+};
+
+struct MmaResult {
+  Vec x;
+  double lam = 0.0, y = 0.0, z = 0.0, max_change = 0.0;
+  int iterations = 0;
+};
+
+// xmin = 0, xmax = 1 for every variable (no passive regions)
+MmaResult mma_update(MmaState& st, const Vec& x, const Vec& df0, double fval, const Vec& dfdx) {
+  const size_t n = x.size();
+  if (st.xold1.empty()) {
+    st.xold1.assign(n, 0.0);
+    st.xold2.assign(n, 0.0);
+    st.low.assign(n, 0.0);
+    st.upp.assign(n, 1.0);
+  }
+  ++st.iteration;
+  const double xmami = 1.0;  // xmax - xmin
+  Vec& low = st.low;
+  Vec& upp = st.upp;
+  if (st.iteration <= 2) {
+    for (size_t j = 0; j < n; ++j) {
+      low[j] = x[j] - st.asy_init * xmami;
+      upp[j] = x[j] + st.asy_init * xmami;
+    }
+  } else {
+    for (size_t j = 0; j < n; ++j) {
+      const double zzz = (x[j] - st.xold1[j]) * (st.xold1[j] - st.xold2[j]);
+      double f = 1.0;
+      if (zzz > 0.0) f = st.asy_inc;
+      if (zzz < 0.0) f = st.asy_dec;
+      low[j] = x[j] - f * (st.xold1[j] - low[j]);
+      upp[j] = x[j] + f * (upp[j] - st.xold1[j]);
+      low[j] = std::min(std::max(low[j], x[j] - 10.0 * xmami), x[j] - 0.01 * xmami);
+      upp[j] = std::min(std::max(upp[j], x[j] + 0.01 * xmami), x[j] + 10.0 * xmami);
+    }
+  }
+  Vec alfa(n), beta(n), p0(n), q0(n), p(n), q(n);
+  const double xmamiinv = 1.0 / std::max(xmami, 1.0e-5);
+  // row scale of the constraint (Mma.cpp:141-149)
+  double dmax = 0.0;
+  for (size_t j = 0; j < n; ++j) dmax = std::max(dmax, std::abs(dfdx[j]));
+  const double magnitude = std::max(std::abs(fval), dmax * st.move * xmami);
+  const double row_scale = magnitude > st.scale_cap ? st.scale_cap / magnitude : 1.0;
+  const double fs = row_scale * fval;
+  double bsum = 0.0;
+  for (size_t j = 0; j < n; ++j) {
+    alfa[j] = std::max({low[j] + st.albefa * (x[j] - low[j]), x[j] - st.move * xmami, 0.0});
+    beta[j] = std::min({upp[j] - st.albefa * (upp[j] - x[j]), x[j] + st.move * xmami, 1.0});
+    const double ux1 = upp[j] - x[j], xl1 = x[j] - low[j];
+    const double ux2 = ux1 * ux1, xl2 = xl1 * xl1;
+    double pp0 = std::max(df0[j], 0.0), qq0 = std::max(-df0[j], 0.0);
+    const double pq0 = 0.001 * (pp0 + qq0) + st.raa0 * xmamiinv;
+    p0[j] = (pp0 + pq0) * ux2;
+    q0[j] = (qq0 + pq0) * xl2;
+    const double ds = row_scale * dfdx[j];
+    double pp = std::max(ds, 0.0), qq = std::max(-ds, 0.0);
+    const double pq = 0.001 * (pp + qq) + st.raa0 * xmamiinv;
+    p[j] = (pp + pq) * ux2;
+    q[j] = (qq + pq) * xl2;
+    bsum += p[j] / ux1 + q[j] / xl1;
+  }
+  const double b = bsum - fs;
+  // primal-dual subproblem (Mma.cpp:158-395)
+  const double a = 0.0, c = st.c, d = st.d, a0 = st.a0;
+  double epsi = 1.0;
+  Vec xx(n), xsi(n), eta(n);
+  for (size_t j = 0; j < n; ++j) {
+    xx[j] = 0.5 * (alfa[j] + beta[j]);
+    xsi[j] = std::max(1.0 / (xx[j] - alfa[j]), 1.0);
+    eta[j] = std::max(1.0 / (beta[j] - xx[j]), 1.0);
+  }
+  double y = 1.0, z = 1.0, lam = 1.0, mu = std::max(0.5 * c, 1.0), zet = 1.0, s = 1.0;
+  auto residual = [&](const Vec& xv, double yv, double zv, double lv, const Vec& xsiv, const Vec& etav,
+                      double muv, double zetv, double sv, double& norm) {
+    double sq = 0.0, mx = 0.0, gvec = 0.0;
+    for (size_t j = 0; j < n; ++j) {
+      const double ux1 = upp[j] - xv[j], xl1 = xv[j] - low[j];
+      const double plam = p0[j] + p[j] * lv, qlam = q0[j] + q[j] * lv;
+      gvec += p[j] / ux1 + q[j] / xl1;
+      const double dpsidx = plam / (ux1 * ux1) - qlam / (xl1 * xl1);
+      const double rex = dpsidx - xsiv[j] + etav[j];
+      const double rexsi = xsiv[j] * (xv[j] - alfa[j]) - epsi;
+      const double reeta = etav[j] * (beta[j] - xv[j]) - epsi;
+      sq += rex * rex + rexsi * rexsi + reeta * reeta;
+      mx = std::max({mx, std::abs(rex), std::abs(rexsi), std::abs(reeta)});
+    }
+    const double rey = c + d * yv - muv - lv;
+    const double rez = a0 - zetv - a * lv;
+    const double relam = gvec - a * zv - yv + sv - b;
+    const double remu = muv * yv - epsi, rezet = zetv * zv - epsi, res = lv * sv - epsi;
+    sq += rey * rey + rez * rez + relam * relam + remu * remu + rezet * rezet + res * res;
+    mx = std::max({mx, std::abs(rey), std::abs(rez), std::abs(relam), std::abs(remu), std::abs(rezet),
+                   std::abs(res)});
+    norm = std::isfinite(sq) ? std::sqrt(sq) : std::numeric_limits<double>::infinity();
+    return std::isfinite(sq) ? mx : std::numeric_limits<double>::infinity();
+  };
+  int total = 0;
+  Vec dx(n), dxsi(n), deta(n), xo(n), xsio(n), etao(n);
+  while (epsi > st.epsimin) {
+    double cur_norm;
+    double cur_max = residual(xx, y, z, lam, xsi, eta, mu, zet, s, cur_norm);
+    int ittt = 0;
+    while (cur_max > 0.9 * epsi && ittt < st.max_inner) {
+      ++ittt;
+      ++total;
+      double sgd = 0.0, sgg = 0.0, gvec = 0.0;
+      Vec delx(n), diagx(n), gg(n);
+      for (size_t j = 0; j < n; ++j) {
+        const double ux1 = upp[j] - xx[j], xl1 = xx[j] - low[j];
+        const double ux2 = ux1 * ux1, xl2 = xl1 * xl1;
+        const double plam = p0[j] + p[j] * lam, qlam = q0[j] + q[j] * lam;
+        gvec += p[j] / ux1 + q[j] / xl1;
+        gg[j] = p[j] / ux2 - q[j] / xl2;
+        const double dpsidx = plam / ux2 - qlam / xl2;
+        const double xa = xx[j] - alfa[j], bx = beta[j] - xx[j];
+        delx[j] = dpsidx - epsi / xa + epsi / bx;
+        diagx[j] = 2.0 * (plam / (ux2 * ux1) + qlam / (xl2 * xl1)) + xsi[j] / xa + eta[j] / bx;
+        sgd += gg[j] * (delx[j] / diagx[j]);
+        sgg += gg[j] * gg[j] / diagx[j];
+      }
+      const double dely = c + d * y - lam - epsi / y;
+      const double delz = a0 - a * lam - epsi / z;
+      const double dellam = gvec - a * z - y - b + epsi / lam;
+      const double diagy = d + mu / y;
+      const double diaglamyi = s / lam + 1.0 / diagy;
+      const double blam = dellam + dely / diagy - sgd;
+      // [alam a; a -zet/z] [dlam; dz] = [blam; delz]
+      const double alam = diaglamyi + sgg;
+      const double a11 = alam, a12 = a, a21 = a, a22 = -zet / z;
+      const double det = a11 * a22 - a12 * a21;
+      const double dlam = (blam * a22 - a12 * delz) / det;
+      const double dz = (a11 * delz - a21 * blam) / det;
+      for (size_t j = 0; j < n; ++j) dx[j] = -delx[j] / diagx[j] - (gg[j] * dlam) / diagx[j];
+      const double dy = -dely / diagy + dlam / diagy;
+      double stmxx = std::max({-1.01 * dy / y, -1.01 * dz / z, -1.01 * dlam / lam});
+      for (size_t j = 0; j < n; ++j) {
+        const double xa = xx[j] - alfa[j], bx = beta[j] - xx[j];
+        dxsi[j] = -xsi[j] + epsi / xa - (xsi[j] * dx[j]) / xa;
+        deta[j] = -eta[j] + epsi / bx + (eta[j] * dx[j]) / bx;
+        stmxx = std::max({stmxx, -1.01 * dxsi[j] / xsi[j], -1.01 * deta[j] / eta[j], -1.01 * dx[j] / xa,
+                          1.01 * dx[j] / bx});
+      }
+      const double dmu = -mu + epsi / y - (mu * dy) / y;
+      const double dzet = -zet + epsi / z - zet * dz / z;
+      const double dss = -s + epsi / lam - (s * dlam) / lam;
+      stmxx = std::max({stmxx, -1.01 * dmu / mu, -1.01 * dzet / zet, -1.01 * dss / s});
+      const double stminv = std::max(stmxx, 1.0);
+      double steg = 1.0 / stminv;
+      xo = xx;
+      xsio = xsi;
+      etao = eta;
+      const double yo = y, zo = z, lamo = lam, muo = mu, zeto = zet, so = s;
+      int itto = 0;
+      double trial_norm = 2.0 * cur_norm, trial_max = cur_max;
+      while (trial_norm > cur_norm && itto < 50) {
+        ++itto;
+        for (size_t j = 0; j < n; ++j) {
+          xx[j] = xo[j] + steg * dx[j];
+          xsi[j] = xsio[j] + steg * dxsi[j];
+          eta[j] = etao[j] + steg * deta[j];
+        }
+        y = yo + steg * dy;
+        z = zo + steg * dz;
+        lam = lamo + steg * dlam;
+        mu = muo + steg * dmu;
+        zet = zeto + steg * dzet;
+        s = so + steg * dss;
+        trial_max = residual(xx, y, z, lam, xsi, eta, mu, zet, s, trial_norm);
+        steg *= 0.5;
+      }
+      cur_norm = trial_norm;
+      cur_max = trial_max;
+    }
+    if (ittt >= st.max_inner) throw Error(kMaxIter, "the MMA subproblem solver did not converge");
+    epsi *= 0.1;
+  }
+  MmaResult r;
+  r.x = xx;
+  r.lam = lam * row_scale;
+  r.y = y / row_scale;
+  r.z = z;
+  r.iterations = total;
+  double mc = 0.0;
+  for (size_t j = 0; j < n; ++j) mc = std::max(mc, std::abs(xx[j] - x[j]));
+  r.max_change = mc;
+  st.xold2 = st.xold1;
+  st.xold1 = x;
+  return r;
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1957,6 +2159,44 @@ int orc_oc_update(orc_problem* h, const double* x, const double* dc, const doubl
     out[2] = st.max_change;
     out[3] = st.bisections;
     out[4] = st.converged ? 1.0 : 0.0;
+  });
+}
+
+// run_mma (src/topopt/TopologyOptimizer.cpp:730-905) for the compliance /
+// volume problem: f0 = c / c_1, f1 = V / V* - 1.  history: compliance, volume
+// fraction, max change, lambda, linear iterations, subproblem iterations.
+int orc_run_mma(orc_problem* h, int32_t iterations, double* x, double* hist, int32_t* performed) {
+  return guarded([&] {
+    Problem& p = h->p;
+    Vec xv(static_cast<size_t>(p.ne), p.x0);
+    for (auto& v : xv) v = std::min(std::max(v, 0.0), 1.0);
+    MmaState st;
+    st.move = p.move;
+    double c_ref = 0.0;
+    const double target = p.vf * p.domain_volume;
+    int it = 0;
+    for (it = 1; it <= iterations; ++it) {
+      Evaluation ev;
+      evaluate(p, xv.data(), ev);
+      if (it == 1) c_ref = ev.compliance;
+      Vec df0(static_cast<size_t>(p.ne)), dfdx(static_cast<size_t>(p.ne));
+      for (Index e = 0; e < p.ne; ++e) {
+        df0[e] = ev.dc_dx[e] / c_ref;
+        dfdx[e] = ev.dv_dx[e] / target;
+      }
+      const MmaResult r = mma_update(st, xv, df0, ev.volume / target - 1.0, dfdx);
+      double* row = hist + static_cast<size_t>(it - 1) * 6;
+      row[0] = ev.compliance;
+      row[1] = ev.volume_fraction;
+      row[2] = r.max_change;
+      row[3] = r.lam;
+      row[4] = ev.linear_iterations;
+      row[5] = r.iterations;
+      xv = r.x;
+      for (auto& v : xv) v = std::min(std::max(v, 0.0), 1.0);
+    }
+    *performed = std::min(it, iterations);
+    std::copy(xv.begin(), xv.end(), x);
   });
 }
 

@@ -112,6 +112,11 @@ int orc_oc_update(orc_problem* p, const double* x, const double* dc_dx,
  * linear iterations, bisections. */
 int orc_run(orc_problem* p, int32_t iterations, double change_tol, double* x,
             double* history, int32_t* performed);
+/* run_mma for `iterations` iterations (MMA with the volume constraint); history:
+ * compliance, volume fraction, max change, lambda, linear iterations,
+ * subproblem Newton iterations. */
+int orc_run_mma(orc_problem* p, int32_t iterations, double* x, double* history,
+                int32_t* performed);
 
 #ifdef __cplusplus
 }

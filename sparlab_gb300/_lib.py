@@ -28,9 +28,10 @@ EXPORTS = [
     "simp_stats", "simp_level_aggregates", "simp_level_matrix", "simp_level_prolongator",
     "simp_problem_create", "simp_problem_destroy", "simp_problem_last_error",
     "simp_problem_sizes", "simp_set_design", "simp_get_design", "simp_evaluate",
-    "simp_oc_update", "simp_iterate", "simp_problem_stats", "simp_filter_forward",
+    "simp_oc_update", "simp_mma_update", "simp_iterate", "simp_problem_stats", "simp_filter_forward",
     "simp_filter_adjoint", "simp_problem_kff", "simp_element_stiffness",
-    "simp_problem_apply_operator", "simp_filter_volume_noalloc", "simp_kernel_launches",
+    "simp_problem_apply_operator", "simp_problem_time_operator", "simp_filter_volume_noalloc",
+    "simp_kernel_launches",
 ]
 
 
@@ -74,7 +75,7 @@ class ProblemDesc(C.Structure):
                 ("filter_radius", C.c_double), ("volume_fraction", C.c_double),
                 ("initial_density", C.c_double), ("penalty", C.c_double),
                 ("emin_ratio", C.c_double), ("move_limit", C.c_double), ("damping", C.c_double),
-                ("warm_start", C.c_int32), ("block_pcg", C.c_int32)]
+                ("warm_start", C.c_int32), ("block_pcg", C.c_int32), ("optimizer", C.c_int32)]
 
 
 class Evaluation(C.Structure):

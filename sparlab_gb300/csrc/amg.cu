@@ -5,11 +5,16 @@
 #include "amg.h"
 #include "dense.cuh"
 #include "kernels.cuh"
+#include "mfree.cuh"
+#include "nbspmv.cuh"
+
+#include <cuda_profiler_api.h>
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <sstream>
+#include <type_traits>
 
 namespace simp {
 
@@ -36,91 +41,264 @@ __global__ void k_expand_columns(i32 n, const i32* __restrict__ node_of, NodeVie
 
 namespace {
 
-int lanes_for(const DevCsr& a) {
-  const double avg = a.rows > 0 ? static_cast<double>(a.nnz) / a.rows : 1.0;
-  if (avg <= 3) return 2;
-  if (avg <= 10) return 4;
-  if (avg <= 24) return 8;
-  if (avg <= 64) return 16;
-  return 32;
+// w = s .* w - beta vp
+__global__ void k_lanczos_finish(double* __restrict__ w, const double* __restrict__ s,
+                                 const double* __restrict__ vp, double beta, i64 n) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    double wi = w[i] * s[i];
+    if (vp) wi -= beta * vp[i];
+    w[i] = wi;
+  }
 }
 
-template <int VS, int MODE>
-void launch_csr_vs(const DevCsr& a, const double* x, double* y, const double* b, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(a.rows) * VS;
-  k_csr<VS, MODE, double, double><<<grid_for(threads, 256), 256, 0, s>>>(a.rows, a.ptr.p, a.col.p, a.v64.p, x, y, b);
+template <int B, int MODE, class TV, class TX, class TA>
+void nb_apply_b(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cudaStream_t s) {
+  const i64 threads = static_cast<i64>(op.nodes) * 32;
+  k_chunk_apply<B, MODE, TV, TX, TA><<<grid_for(threads, 256), 256, 0, s>>>(op.nodes, op.row_first, op.pat,
+                                                                            op.rowptr, op.col, val, x, y, b);
   SIMP_CHECK_LAUNCH();
+}
+
+template <int VS, int B, int MODE, class TV, class TX, class TA>
+void rows_apply_b(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cudaStream_t s) {
+  const i64 threads = static_cast<i64>(op.rows) * VS;
+  k_rows_apply<VS, B, MODE, TV, TX, TA><<<grid_for(threads, 256), 256, 0, s>>>(
+      op.nodes, op.row_first, op.node_of, op.pat, op.rowptr, op.col, val, x, y, b, op.rows);
+  SIMP_CHECK_LAUNCH();
+}
+
+template <int MODE, class TV, class TX, class TA>
+void nb_apply(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cudaStream_t s) {
+  if constexpr (std::is_same<TA, double>::value) {
+    // FP64 arithmetic bound: few lanes per row
+    const bool wide = op.lanes > 4;
+    switch (op.block) {
+      case 2:
+        wide ? rows_apply_b<8, 2, MODE, TV, TX, TA>(op, val, x, y, b, s) : rows_apply_b<4, 2, MODE, TV, TX, TA>(op, val, x, y, b, s);
+        break;
+      case 3:
+        wide ? rows_apply_b<8, 3, MODE, TV, TX, TA>(op, val, x, y, b, s) : rows_apply_b<4, 3, MODE, TV, TX, TA>(op, val, x, y, b, s);
+        break;
+      default:
+        wide ? rows_apply_b<8, 0, MODE, TV, TX, TA>(op, val, x, y, b, s) : rows_apply_b<4, 0, MODE, TV, TX, TA>(op, val, x, y, b, s);
+        break;
+    }
+    return;
+  }
+  switch (op.block) {
+    case 2: nb_apply_b<2, MODE, TV, TX, TA>(op, val, x, y, b, s); break;
+    case 3: nb_apply_b<3, MODE, TV, TX, TA>(op, val, x, y, b, s); break;
+    default: nb_apply_b<0, MODE, TV, TX, TA>(op, val, x, y, b, s); break;
+  }
+}
+
+template <int B, class T>
+void nb_cheb_step_b(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
+                    double c1, double c2, int add_d, cudaStream_t s) {
+  const i64 threads = static_cast<i64>(op.nodes) * 32;
+  k_chunk_cheb_step<B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.nodes, op.row_first, op.pat, op.rowptr, op.col,
+                                                                 val, d, rin, r, dn, x, dinv, static_cast<T>(c1),
+                                                                 static_cast<T>(c2), add_d);
+  SIMP_CHECK_LAUNCH();
+}
+
+template <int VS, int B, class T>
+void rows_cheb_step_b(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
+                      double c1, double c2, int add_d, cudaStream_t s) {
+  const i64 threads = static_cast<i64>(op.rows) * VS;
+  k_rows_cheb_step<VS, B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.rows, op.node_of, op.pat, op.rowptr, op.col,
+                                                                    val, d, rin, r, dn, x, dinv, static_cast<T>(c1),
+                                                                    static_cast<T>(c2), add_d);
+  SIMP_CHECK_LAUNCH();
+}
+
+template <int VS, int B, class T>
+void rows_cheb_first_b(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
+                       double inv_theta, cudaStream_t s) {
+  const i64 threads = static_cast<i64>(op.rows) * VS;
+  k_rows_cheb_first<VS, B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.rows, op.node_of, op.pat, op.rowptr, op.col,
+                                                                     val, x, b, r, d, dinv,
+                                                                     static_cast<T>(inv_theta));
+  SIMP_CHECK_LAUNCH();
+}
+
+template <class T>
+void nb_cheb_step(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
+                  double c1, double c2, int add_d, cudaStream_t s) {
+  if constexpr (std::is_same<T, double>::value) {
+    const bool wide = op.lanes > 4;
+    switch (op.block) {
+      case 2:
+        wide ? rows_cheb_step_b<8, 2, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s)
+             : rows_cheb_step_b<4, 2, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s);
+        break;
+      case 3:
+        wide ? rows_cheb_step_b<8, 3, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s)
+             : rows_cheb_step_b<4, 3, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s);
+        break;
+      default:
+        wide ? rows_cheb_step_b<8, 0, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s)
+             : rows_cheb_step_b<4, 0, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s);
+        break;
+    }
+    return;
+  }
+  switch (op.block) {
+    case 2: nb_cheb_step_b<2, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
+    case 3: nb_cheb_step_b<3, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
+    default: nb_cheb_step_b<0, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
+  }
+}
+
+template <int B, class T>
+void nb_cheb_first_b(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
+                     double inv_theta, cudaStream_t s) {
+  const i64 threads = static_cast<i64>(op.nodes) * 32;
+  k_chunk_cheb_first<B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.nodes, op.row_first, op.pat, op.rowptr,
+                                                                  op.col, val, x, b, r, d, dinv,
+                                                                  static_cast<T>(inv_theta));
+  SIMP_CHECK_LAUNCH();
+}
+
+template <class T>
+void nb_cheb_first(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
+                   double inv_theta, cudaStream_t s) {
+  if constexpr (std::is_same<T, double>::value) {
+    const bool wide = op.lanes > 4;
+    switch (op.block) {
+      case 2:
+        wide ? rows_cheb_first_b<8, 2, T>(op, val, x, b, r, d, dinv, inv_theta, s)
+             : rows_cheb_first_b<4, 2, T>(op, val, x, b, r, d, dinv, inv_theta, s);
+        break;
+      case 3:
+        wide ? rows_cheb_first_b<8, 3, T>(op, val, x, b, r, d, dinv, inv_theta, s)
+             : rows_cheb_first_b<4, 3, T>(op, val, x, b, r, d, dinv, inv_theta, s);
+        break;
+      default:
+        wide ? rows_cheb_first_b<8, 0, T>(op, val, x, b, r, d, dinv, inv_theta, s)
+             : rows_cheb_first_b<4, 0, T>(op, val, x, b, r, d, dinv, inv_theta, s);
+        break;
+    }
+    return;
+  }
+  switch (op.block) {
+    case 2: nb_cheb_first_b<2, T>(op, val, x, b, r, d, dinv, inv_theta, s); break;
+    case 3: nb_cheb_first_b<3, T>(op, val, x, b, r, d, dinv, inv_theta, s); break;
+    default: nb_cheb_first_b<0, T>(op, val, x, b, r, d, dinv, inv_theta, s); break;
+  }
+}
+
+// Uniform B x B blocks with node I's unknowns at B*I: the column-free path.
+int uniform_block(const std::vector<i32>& row_first, const std::vector<i32>& col_first) {
+  for (int b : {3, 2}) {
+    bool ok = row_first == col_first;
+    for (size_t I = 0; ok && I < row_first.size(); ++I) ok = row_first[I] == b * static_cast<i32>(I);
+    if (ok) return b;
+  }
+  return 0;
+}
+
+// Per-precision views of a level's arrays.
+template <class T>
+struct V;
+template <>
+struct V<double> {
+  static const double* a(const DevCsr& c) { return c.v64.p; }
+  static double* x(Level& l) { return l.x64.p; }
+  static double* b(Level& l) { return l.b64.p; }
+  static double* r(Level& l) { return l.r64.p; }
+  static double* d(Level& l) { return l.d64.p; }
+  static double* e(Level& l) { return l.e64.p; }
+  static const double* dinv(Level& l) { return l.dinv64.p; }
+};
+template <>
+struct V<float> {
+  static const float* a(const DevCsr& c) { return c.v32.p; }
+  static float* x(Level& l) { return l.x32.p; }
+  static float* b(Level& l) { return l.b32.p; }
+  static float* r(Level& l) { return l.r32.p; }
+  static float* d(Level& l) { return l.d32.p; }
+  static float* e(Level& l) { return l.e32.p; }
+  static const float* dinv(Level& l) { return l.dinv32.p; }
+};
+
+template <class A, class B>
+void convert(const A* a, B* b, i64 n, cudaStream_t s) {
+  k_convert<A, B><<<grid_for(n, 256, 4096), 256, 0, s>>>(a, b, n);
+  SIMP_CHECK_LAUNCH();
+}
+
+MfView mf_view(const MfOp& o) {
+  MfView v;
+  v.dim = o.dim;
+  v.nx = o.nx;
+  v.ny = o.ny;
+  v.nz = o.nz;
+  v.nnx = o.nnx;
+  v.nny = o.nny;
+  v.gnode = o.gnode;
+  v.nindex = o.nindex;
+  v.ke = o.ke;
+  v.scale = o.scale;
+  return v;
 }
 
 template <int MODE>
-void launch_csr(const DevCsr& a, const double* x, double* y, const double* b, cudaStream_t s) {
-  switch (lanes_for(a)) {
-    case 2: launch_csr_vs<2, MODE>(a, x, y, b, s); break;
-    case 4: launch_csr_vs<4, MODE>(a, x, y, b, s); break;
-    case 8: launch_csr_vs<8, MODE>(a, x, y, b, s); break;
-    case 16: launch_csr_vs<16, MODE>(a, x, y, b, s); break;
-    default: launch_csr_vs<32, MODE>(a, x, y, b, s); break;
-  }
-}
-
-template <int VS>
-void launch_cheb_step_vs(const DevCsr& a, const double* d, const double* rin, double* r, double* dn,
-                         double* x, const double* dinv, double c1, double c2, int add_d, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(a.rows) * VS;
-  k_cheb_step<VS, double, double><<<grid_for(threads, 256), 256, 0, s>>>(
-      a.rows, a.ptr.p, a.col.p, a.v64.p, d, rin, r, dn, x, dinv, c1, c2, add_d);
+void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
+  const dim3 grid((mf.nnx + kTX - 1) / kTX, (mf.nny + kTY - 1) / kTY, (mf.nz + 1 + kTZ - 1) / kTZ);
+  k_mf3_tile<MODE><<<grid, kTX * kTY * kTZ, 0, s>>>(mf_view(mf), a);
   SIMP_CHECK_LAUNCH();
 }
 
-void launch_cheb_step(const DevCsr& a, const double* d, const double* rin, double* r, double* dn,
-                      double* x, const double* dinv, double c1, double c2, int add_d, cudaStream_t s) {
-  switch (lanes_for(a)) {
-    case 2: launch_cheb_step_vs<2>(a, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
-    case 4: launch_cheb_step_vs<4>(a, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
-    case 8: launch_cheb_step_vs<8>(a, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
-    case 16: launch_cheb_step_vs<16>(a, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
-    default: launch_cheb_step_vs<32>(a, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
+// Matrix-free level-0 pieces of the FP32 cycle (tiled in 3-D).
+void mf_cheb_first(const MfOp& mf, i32 nodes, const float* x, const float* b, float* r, float* d,
+                   const float* dinv, float inv_theta, cudaStream_t s) {
+  if (mf.dim == 3) {
+    MfArgs a{};
+    a.x = x;
+    a.b = b;
+    a.r = r;
+    a.dn = d;
+    a.dinv = dinv;
+    a.inv_theta = inv_theta;
+    mf3<4>(mf, a, s);
+    return;
   }
-}
-
-template <int VS>
-void launch_cheb_first_vs(const DevCsr& a, const double* x, const double* b, double* r, double* d,
-                          const double* dinv, double inv_theta, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(a.rows) * VS;
-  k_cheb_first<VS, double, double><<<grid_for(threads, 256), 256, 0, s>>>(
-      a.rows, a.ptr.p, a.col.p, a.v64.p, x, b, r, d, dinv, inv_theta);
+  k_mf_cheb_first<<<grid_for(nodes, 256), 256, 0, s>>>(mf_view(mf), nodes, x, b, r, d, dinv, inv_theta);
   SIMP_CHECK_LAUNCH();
 }
 
-void launch_cheb_first(const DevCsr& a, const double* x, const double* b, double* r, double* d,
-                       const double* dinv, double inv_theta, cudaStream_t s) {
-  switch (lanes_for(a)) {
-    case 2: launch_cheb_first_vs<2>(a, x, b, r, d, dinv, inv_theta, s); break;
-    case 4: launch_cheb_first_vs<4>(a, x, b, r, d, dinv, inv_theta, s); break;
-    case 8: launch_cheb_first_vs<8>(a, x, b, r, d, dinv, inv_theta, s); break;
-    case 16: launch_cheb_first_vs<16>(a, x, b, r, d, dinv, inv_theta, s); break;
-    default: launch_cheb_first_vs<32>(a, x, b, r, d, dinv, inv_theta, s); break;
+void mf_cheb_step(const MfOp& mf, i32 nodes, const float* d, const float* rin, float* r, float* dn, float* x,
+                  const float* dinv, float c1, float c2, int add_d, cudaStream_t s) {
+  if (mf.dim == 3) {
+    MfArgs a{};
+    a.x = d;
+    a.b = rin;
+    a.r = r;
+    a.dn = dn;
+    a.xs = x;
+    a.dinv = dinv;
+    a.c1 = c1;
+    a.c2 = c2;
+    a.add_d = add_d;
+    mf3<3>(mf, a, s);
+    return;
   }
-}
-
-template <int VS>
-void launch_lanczos_vs(const DevCsr& a, const double* tmp, const double* s, const double* vp, double beta,
-                       double* w, cudaStream_t st) {
-  const i64 threads = static_cast<i64>(a.rows) * VS;
-  k_lanczos_apply<VS, double><<<grid_for(threads, 256), 256, 0, st>>>(a.rows, a.ptr.p, a.col.p, a.v64.p,
-                                                                      tmp, s, vp, beta, w);
+  k_mf_cheb_step<<<grid_for(nodes, 256), 256, 0, s>>>(mf_view(mf), nodes, d, rin, r, dn, x, dinv, c1, c2, add_d);
   SIMP_CHECK_LAUNCH();
 }
 
-void launch_lanczos(const DevCsr& a, const double* tmp, const double* s, const double* vp, double beta,
-                    double* w, cudaStream_t st) {
-  switch (lanes_for(a)) {
-    case 2: launch_lanczos_vs<2>(a, tmp, s, vp, beta, w, st); break;
-    case 4: launch_lanczos_vs<4>(a, tmp, s, vp, beta, w, st); break;
-    case 8: launch_lanczos_vs<8>(a, tmp, s, vp, beta, w, st); break;
-    case 16: launch_lanczos_vs<16>(a, tmp, s, vp, beta, w, st); break;
-    default: launch_lanczos_vs<32>(a, tmp, s, vp, beta, w, st); break;
+void mf_residual(const MfOp& mf, i32 nodes, const float* x, float* r, const float* b, cudaStream_t s) {
+  if (mf.dim == 3) {
+    MfArgs a{};
+    a.x = x;
+    a.y = r;
+    a.b = b;
+    mf3<1>(mf, a, s);
+    return;
   }
+  k_mf_apply<1, float><<<grid_for(nodes, 256), 256, 0, s>>>(mf_view(mf), nodes, x, r, b);
+  SIMP_CHECK_LAUNCH();
 }
 
 double seconds_since(std::chrono::steady_clock::time_point t0) {
@@ -128,8 +306,6 @@ double seconds_since(std::chrono::steady_clock::time_point t0) {
 }
 
 }  // namespace
-
-void csr_apply(const DevCsr& a, const double* x, double* y, cudaStream_t s) { launch_csr<0>(a, x, y, nullptr, s); }
 
 GpuAmg::GpuAmg(const AmgOptions& o) : opt(o) {
   part.alloc(kRedBlocks);
@@ -155,17 +331,112 @@ double GpuAmg::dot(const double* a, const double* b, i64 n) {
   return h;
 }
 
-void GpuAmg::spmv0(const double* x, double* y) { launch_csr<0>(levels.front()->a, x, y, nullptr, stream); }
+void GpuAmg::make_ops(size_t l) {
+  Level& lv = *levels[l];
+  lv.opA.nodes = lv.nnodes;
+  lv.opA.row_first = lv.d_first.p;
+  lv.opA.pat = lv.d_apat.view();
+  lv.opA.rowptr = lv.a.ptr.p;
+  lv.opA.col = lv.a.col.p;
+  lv.opA.block = uniform_block(lv.first, lv.first);
+  lv.opA.node_of = lv.d_node_of.p;
+  lv.opA.rows = lv.n;
+  auto lanes = [](const DevCsr& c) { return c.rows > 0 && c.nnz / c.rows > 100 ? 8 : 4; };
+  lv.opA.lanes = lanes(lv.a);
+  if (l + 1 < levels.size()) {
+    Level& nv = *levels[l + 1];
+    lv.opP.nodes = lv.nnodes;
+    lv.opP.row_first = lv.d_first.p;
+    lv.opP.pat = lv.d_ppat.view();
+    lv.opP.rowptr = lv.p.ptr.p;
+    lv.opP.col = lv.p.col.p;
+    lv.opP.block = 0;
+    lv.opP.node_of = lv.d_node_of.p;
+    lv.opP.rows = lv.n;
+    lv.opP.lanes = lanes(lv.p);
+    lv.opR.nodes = nv.nnodes;
+    lv.opR.row_first = nv.d_first.p;
+    lv.opR.pat = lv.d_rpat.view();
+    lv.opR.rowptr = lv.r.ptr.p;
+    lv.opR.col = lv.r.col.p;
+    lv.opR.block = 0;
+    lv.opR.node_of = nv.d_node_of.p;
+    lv.opR.rows = nv.n;
+    lv.opR.lanes = lanes(lv.r);
+  }
+}
+
+void GpuAmg::spmv0(const double* x, double* y) {
+  Level& l0 = *levels.front();
+  nb_apply<0, double, double, double>(l0.opA, l0.a.v64.p, x, y, nullptr, stream);
+}
+
+void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
+  if (!ready_) throw Error(kBadInput, "the operator is built by the first setup");
+  Level& l0 = *levels.front();
+  const i32 n = l0.n;
+  const bool f32 = mixed();
+  const size_t vs = f32 ? sizeof(float) : sizeof(double);
+  DBuf<double> x64, y64;
+  DBuf<float> x32, y32;
+  if (f32) {
+    x32.alloc(n);
+    y32.alloc(n);
+    k_fill<float><<<grid_for(n, 256), 256, 0, stream>>>(x32.p, 1.0f, n);
+  } else {
+    x64.alloc(n);
+    y64.alloc(n);
+    k_fill<double><<<grid_for(n, 256), 256, 0, stream>>>(x64.p, 1.0, n);
+  }
+  SIMP_CHECK_LAUNCH();
+  auto launch = [&]() {
+    if (f32) nb_apply<0, float, float, float>(l0.opA, l0.a.v32.p, x32.p, y32.p, nullptr, stream);
+    else nb_apply<0, double, double, double>(l0.opA, l0.a.v64.p, x64.p, y64.p, nullptr, stream);
+  };
+  for (int k = 0; k < 3; ++k) launch();
+  // the timed launches are the profiler's capture window when one is attached
+  cudaProfilerStart();
+  cudaEvent_t e0, e1;
+  SIMP_CUDA(cudaEventCreate(&e0));
+  SIMP_CUDA(cudaEventCreate(&e1));
+  SIMP_CUDA(cudaEventRecord(e0, stream));
+  for (int k = 0; k < reps; ++k) launch();
+  SIMP_CUDA(cudaEventRecord(e1, stream));
+  SIMP_CUDA(cudaEventSynchronize(e1));
+  cudaProfilerStop();
+  float t = 0.0f;
+  SIMP_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t / std::max(reps, 1);
+  // values + node pattern (nbr, off per slot; ptr per node) + row pointers + x + y
+  *bytes = static_cast<double>(l0.a.nnz) * vs + static_cast<double>(l0.apat.slots()) * 8.0 +
+           static_cast<double>(l0.nnodes + 1) * 8.0 + static_cast<double>(n + 1) * 4.0 +
+           2.0 * static_cast<double>(n) * vs;
+}
+
+void GpuAmg::refresh_level0_fp32() {
+  Level& l0 = *levels.front();
+  l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
+  convert(l0.a.v64.p, l0.a.v32.p, l0.a.nnz, stream);
+}
 
 // inverse diagonal and lambda_max(D^-1 A) of one level (Multigrid.cpp:718-747)
 void GpuAmg::numeric_level(size_t l) {
   Level& lv = *levels[l];
   const i32 n = lv.n;
+  const bool fp32 = mixed() && ready_ && lv.a.v32.p != nullptr;
+  make_ops(l);
   lv.dinv64.alloc(n);
   SIMP_CUDA(cudaMemsetAsync(dstatus.p, 0x7f, sizeof(int), stream));
-  k_inv_diag<double><<<grid_for(n, 256), 256, 0, stream>>>(n, lv.d_node_of.p, lv.d_first.p, lv.d_self.p,
-                                                           lv.d_apat.view(), lv.a.ptr.p, lv.a.v64.p,
-                                                           lv.dinv64.p, dstatus.p);
+  if (fp32)
+    k_inv_diag<float><<<grid_for(n, 256), 256, 0, stream>>>(n, lv.d_node_of.p, lv.d_first.p, lv.d_self.p,
+                                                            lv.d_apat.view(), lv.a.ptr.p, lv.a.v32.p, lv.dinv64.p,
+                                                            dstatus.p);
+  else
+    k_inv_diag<double><<<grid_for(n, 256), 256, 0, stream>>>(n, lv.d_node_of.p, lv.d_first.p, lv.d_self.p,
+                                                             lv.d_apat.view(), lv.a.ptr.p, lv.a.v64.p, lv.dinv64.p,
+                                                             dstatus.p);
   SIMP_CHECK_LAUNCH();
   int bad = 0;
   SIMP_CUDA(cudaMemcpyAsync(&bad, dstatus.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -176,6 +447,10 @@ void GpuAmg::numeric_level(size_t l) {
        << " is not positive; a stiffness matrix must have a positive diagonal. The model has an "
           "unconnected degree of freedom or a non-positive stiffness";
     throw Error(kBreakdown, os.str());
+  }
+  if (mixed()) {
+    lv.dinv32.alloc(n);
+    convert(lv.dinv64.p, lv.dinv32.p, n, stream);
   }
   // Lanczos on D^-1/2 A D^-1/2 with the reference's start vector.
   DBuf<double> v(n), vp(n), w(n), s(n), tmp(n);
@@ -191,7 +466,18 @@ void GpuAmg::numeric_level(size_t l) {
   std::vector<double> alpha, beta;
   const int m = std::max(1, std::min<int>(opt.lanczos_steps, n));
   for (int j = 0; j < m; ++j) {
-    launch_lanczos(lv.a, tmp.p, s.p, j > 0 ? vp.p : nullptr, j > 0 ? beta.back() : 0.0, w.p, stream);
+    if (fp32) {
+      // FP32 operator on FP32 copies of the Lanczos vectors
+      lv.x32.alloc(n);
+      lv.b32.alloc(n);
+      convert(tmp.p, lv.x32.p, n, stream);
+      nb_apply<0, float, float, float>(lv.opA, lv.a.v32.p, lv.x32.p, lv.b32.p, nullptr, stream);
+      convert(lv.b32.p, w.p, n, stream);
+    }
+    else nb_apply<0, double, double, double>(lv.opA, lv.a.v64.p, tmp.p, w.p, nullptr, stream);
+    k_lanczos_finish<<<grid_for(n, 256), 256, 0, stream>>>(w.p, s.p, j > 0 ? vp.p : nullptr,
+                                                          j > 0 ? beta.back() : 0.0, n);
+    SIMP_CHECK_LAUNCH();
     const double aj = dot(w.p, v.p, n);
     alpha.push_back(aj);
     SIMP_CUDA(cudaMemcpyAsync(scal.p + 2, &aj, sizeof(double), cudaMemcpyHostToDevice, stream));
@@ -229,11 +515,19 @@ void GpuAmg::numeric_level(size_t l) {
     lv.c2.push_back(2.0 * rn / delta);
     rho = rn;
   }
-  lv.x64.alloc(n);
-  lv.b64.alloc(n);
-  lv.r64.alloc(n);
-  lv.d64.alloc(n);
-  lv.e64.alloc(n);
+  if (mixed()) {
+    lv.x32.alloc(n);
+    lv.b32.alloc(n);
+    lv.r32.alloc(n);
+    lv.d32.alloc(n);
+    lv.e32.alloc(n);
+  } else {
+    lv.x64.alloc(n);
+    lv.b64.alloc(n);
+    lv.r64.alloc(n);
+    lv.d64.alloc(n);
+    lv.e64.alloc(n);
+  }
 }
 
 // Aggregates, tentative prolongator and symbolic patterns of level l -> l+1.
@@ -270,6 +564,10 @@ void GpuAmg::build_transfer(size_t l) {
   lv.d_agg.upload(lv.agg, stream);
   lv.phat_ptr.upload(t.phat_ptr, stream);
   lv.phat64.upload(t.phat, stream);
+  if (mixed()) {
+    lv.phat32.alloc(t.phat.size());
+    convert(lv.phat64.p, lv.phat32.p, static_cast<i64>(t.phat.size()), stream);
+  }
   // symbolic patterns
   lv.ppat = pattern_prolongator(lv.apat, lv.agg, lv.naggs);
   finish_offsets(lv.ppat, nv.first);
@@ -302,52 +600,75 @@ void GpuAmg::build_transfer(size_t l) {
                                                                 d_col_first.p, c.ptr.p, c.col.p);
     SIMP_CHECK_LAUNCH();
     c.v64.alloc(static_cast<size_t>(c.nnz));
+    if (mixed()) c.v32.alloc(static_cast<size_t>(c.nnz));
   };
   make(lv.p, lv.ppat, lv.first, nv.first, lv.d_node_of, lv.d_ppat, nv.d_first);
   make(lv.r, lv.rpat, nv.first, lv.first, nv.d_node_of, lv.d_rpat, lv.d_first);
   make(lv.ap, lv.appat, lv.first, nv.first, lv.d_node_of, lv.d_appat, nv.d_first);
   make(nv.a, nv.apat, nv.first, nv.first, nv.d_node_of, nv.d_apat, nv.d_first);
   lv.raw64.alloc(static_cast<size_t>(nv.a.nnz));
+  if (mixed()) lv.raw32.alloc(static_cast<size_t>(nv.a.nnz));
   levels.push_back(std::move(nx));
 }
 
 // Numeric P, R, AP, RAP and symmetrisation (Multigrid.cpp:671-716, 1047-1055).
-void GpuAmg::galerkin(size_t l) {
-  Level& lv = *levels[l];
-  Level& nv = *levels[l + 1];
-  const double omega = opt.damping / lv.lambda;
+template <class T>
+static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t stream) {
+  const bool f32 = sizeof(T) == 4;
+  auto A = [&](DevCsr& c) -> T* { return f32 ? reinterpret_cast<T*>(c.v32.p) : reinterpret_cast<T*>(c.v64.p); };
+  const T* phat = f32 ? reinterpret_cast<const T*>(lv.phat32.p) : reinterpret_cast<const T*>(lv.phat64.p);
+  T* raw = f32 ? reinterpret_cast<T*>(lv.raw32.p) : reinterpret_cast<T*>(lv.raw64.p);
+  const double omega = g.opt.damping / lv.lambda;
   {
     const i64 th = static_cast<i64>(lv.n) * 8;
-    k_prolongator<8, double><<<grid_for(th, 256), 256, 0, stream>>>(
-        lv.n, lv.d_node_of.p, lv.d_first.p, nv.d_first.p, lv.d_agg.p, lv.d_apat.view(), lv.a.ptr.p,
-        lv.a.v64.p, lv.d_ppat.view(), lv.p.ptr.p, lv.p.v64.p, lv.phat_ptr.p, lv.phat64.p, lv.dinv64.p, omega);
+    k_prolongator<8, T><<<grid_for(th, 256), 256, 0, stream>>>(
+        lv.n, lv.d_node_of.p, lv.d_first.p, nv.d_first.p, lv.d_agg.p, lv.d_apat.view(), lv.a.ptr.p, A(lv.a),
+        lv.d_ppat.view(), lv.p.ptr.p, A(lv.p), lv.phat_ptr.p, phat, lv.dinv64.p, omega);
     SIMP_CHECK_LAUNCH();
   }
   {
     const i64 th = static_cast<i64>(nv.n) * 32;
-    k_restriction<32, double><<<grid_for(th, 256), 256, 0, stream>>>(
-        nv.n, nv.d_node_of.p, nv.d_first.p, lv.d_first.p, lv.d_rpat.view(), lv.r.ptr.p, lv.r.v64.p,
-        lv.d_r_to_p.p, lv.d_ppat.view(), lv.p.ptr.p, lv.p.v64.p);
+    k_restriction<32, T><<<grid_for(th, 256), 256, 0, stream>>>(
+        nv.n, nv.d_node_of.p, nv.d_first.p, lv.d_first.p, lv.d_rpat.view(), lv.r.ptr.p, A(lv.r), lv.d_r_to_p.p,
+        lv.d_ppat.view(), lv.p.ptr.p, A(lv.p));
     SIMP_CHECK_LAUNCH();
   }
   {
     const i64 th = static_cast<i64>(lv.n) * 32;
-    k_product_ap<32, double><<<grid_for(th, 256), 256, 0, stream>>>(
-        lv.n, lv.d_node_of.p, lv.d_first.p, nv.d_first.p, lv.d_apat.view(), lv.a.ptr.p, lv.a.v64.p,
-        lv.d_ppat.view(), lv.p.ptr.p, lv.p.v64.p, lv.d_appat.view(), lv.ap.ptr.p, lv.ap.v64.p);
+    k_product_ap<32, T><<<grid_for(th, 256), 256, 0, stream>>>(
+        lv.n, lv.d_node_of.p, lv.d_first.p, nv.d_first.p, lv.d_apat.view(), lv.a.ptr.p, A(lv.a),
+        lv.d_ppat.view(), lv.p.ptr.p, A(lv.p), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap));
     SIMP_CHECK_LAUNCH();
   }
   {
     const i64 th = static_cast<i64>(nv.n) * 32;
-    k_product_rap<32, double><<<grid_for(th, 256), 256, 0, stream>>>(
-        nv.n, nv.d_node_of.p, nv.d_first.p, lv.d_first.p, lv.d_rpat.view(), lv.r.ptr.p, lv.r.v64.p,
-        lv.d_appat.view(), lv.ap.ptr.p, lv.ap.v64.p, nv.d_apat.view(), nv.a.ptr.p, lv.raw64.p);
+    k_product_rap<32, T><<<grid_for(th, 256), 256, 0, stream>>>(
+        nv.n, nv.d_node_of.p, nv.d_first.p, lv.d_first.p, lv.d_rpat.view(), lv.r.ptr.p, A(lv.r),
+        lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap), nv.d_apat.view(), nv.a.ptr.p, raw);
     SIMP_CHECK_LAUNCH();
   }
-  k_symmetrize<double, double><<<grid_for(nv.n, 128), 128, 0, stream>>>(
-      nv.n, nv.d_node_of.p, nv.d_first.p, nv.d_apat.view(), nv.a.ptr.p, lv.d_sym_t.p, lv.raw64.p, nv.a.v64.p,
-      nullptr);
+  // FP64 copy of the coarse operator where the FP64 path or the coarse
+  // factorisation needs it
+  double* out64 = (!f32 || last) ? nv.a.v64.p : nullptr;
+  k_symmetrize<T, T><<<grid_for(nv.n, 128), 128, 0, stream>>>(nv.n, nv.d_node_of.p, nv.d_first.p, nv.d_apat.view(),
+                                                              nv.a.ptr.p, lv.d_sym_t.p, raw, A(nv.a), f32 ? out64 : nullptr);
   SIMP_CHECK_LAUNCH();
+}
+
+void GpuAmg::galerkin(size_t l, bool fp32) {
+  Level& lv = *levels[l];
+  Level& nv = *levels[l + 1];
+  const bool last = l + 2 == levels.size();
+  if (fp32) {
+    galerkin_t<float>(*this, lv, nv, last, stream);
+  } else {
+    galerkin_t<double>(*this, lv, nv, last, stream);
+    if (mixed()) {
+      convert(lv.p.v64.p, lv.p.v32.p, lv.p.nnz, stream);
+      convert(lv.r.v64.p, lv.r.v32.p, lv.r.nnz, stream);
+      convert(nv.a.v64.p, nv.a.v32.p, nv.a.nnz, stream);
+    }
+  }
 }
 
 // Dense FP64 Cholesky of the coarsest operator and W = L^-1.
@@ -400,7 +721,7 @@ void GpuAmg::coarse_factorize() {
        << "level, so the model is under-constrained: too few supports, or a part connected to nothing";
     throw Error(kUnderConstrained, os.str());
   }
-  // W = L^-1 into inv_t_ (row-major, lower), then keep W in inv_t_ and W^T in dense_
+  // W = L^-1 into inv_t_ (row-major, lower); W^T into dense_
   k_identity<<<grid_for(static_cast<i64>(nn), 256), 256, 0, stream>>>(inv_t_.p, n);
   SIMP_CHECK_LAUNCH();
   for (int k0 = 0; k0 < n; k0 += kNB) {
@@ -419,13 +740,14 @@ void GpuAmg::coarse_factorize() {
   SIMP_CHECK_LAUNCH();
 }
 
-// x = W^T (W b) at the coarsest level
-void GpuAmg::coarse_solve(const Level& lv) {
+// x = W^T (W b) at the coarsest level, in FP64
+template <class T>
+void GpuAmg::coarse_solve(Level& lv) {
   const int n = nc_;
   const i64 th = static_cast<i64>(n) * 32;
-  k_gemv<double, double><<<grid_for(th, 256), 256, 0, stream>>>(inv_t_.p, n, lv.b64.p, tmp_.p, 1);
+  k_gemv<T, double><<<grid_for(th, 256), 256, 0, stream>>>(inv_t_.p, n, V<T>::b(lv), tmp_.p, 1);
   SIMP_CHECK_LAUNCH();
-  k_gemv<double, double><<<grid_for(th, 256), 256, 0, stream>>>(dense_.p, n, tmp_.p, lv.x64.p, 2);
+  k_gemv<double, T><<<grid_for(th, 256), 256, 0, stream>>>(dense_.p, n, tmp_.p, V<T>::x(lv), 2);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -433,12 +755,17 @@ void GpuAmg::setup(bool structure_changed) {
   const auto t0 = std::chrono::steady_clock::now();
   const bool reuse = opt.reuse && !structure_changed && ready_;
   if (!reuse) {
-    // drop the coarse levels of an earlier structure
     while (levels.size() > 1) levels.pop_back();
     Level& l0 = *levels.front();
     l0.agg.clear();
     l0.naggs = 0;
+    ready_ = false;
   }
+  // Reused structure in mixed mode: FP32 numerics; a new structure is set up
+  // in FP64 so the aggregates come from the FP64 values.
+  const bool fp32 = mixed() && reuse;
+  if (mixed() && !level0_fp32_fresh) refresh_level0_fp32();
+  level0_fp32_fresh = false;
   const size_t reused_levels = levels.size();
   size_t l = 0;
   while (true) {
@@ -451,12 +778,12 @@ void GpuAmg::setup(bool structure_changed) {
       build_transfer(l);
       if (levels.size() == l + 1) break;  // coarsening stalled
     }
-    galerkin(l);
+    galerkin(l, fp32);
     ++l;
   }
   levels.resize(l + 1);
+  for (size_t k = 0; k < levels.size(); ++k) make_ops(k);
   coarse_factorize();
-  // PCG workspace
   const i32 n0 = levels.front()->n;
   pr.alloc(n0);
   pz.alloc(n0);
@@ -487,72 +814,99 @@ void GpuAmg::compute_stats() {
 }
 
 // Chebyshev smoothing of x (Multigrid.cpp:783-855) on level l.
+template <class T>
 void GpuAmg::smooth(size_t l, bool zero_guess) {
   Level& lv = *levels[l];
   const i32 n = lv.n;
-  double* d = lv.d64.p;
-  double* e = lv.e64.p;
+  const T* A = V<T>::a(lv.a);
+  T* x = V<T>::x(lv);
+  T* b = V<T>::b(lv);
+  T* r = V<T>::r(lv);
+  T* d = V<T>::d(lv);
+  T* e = V<T>::e(lv);
+  const T* dinv = V<T>::dinv(lv);
+  bool matrix_free = false;
+  if constexpr (std::is_same<T, float>::value) matrix_free = l == 0 && mf.enabled;
   if (zero_guess) {
-    k_cheb_zero<double><<<grid_for(n, 256), 256, 0, stream>>>(n, lv.b64.p, lv.dinv64.p, d, lv.x64.p, lv.inv_theta);
+    k_cheb_zero<T><<<grid_for(n, 256), 256, 0, stream>>>(n, b, dinv, d, x, static_cast<T>(lv.inv_theta));
     SIMP_CHECK_LAUNCH();
+  } else if (matrix_free) {
+    if constexpr (std::is_same<T, float>::value)
+      mf_cheb_first(mf, lv.nnodes, x, b, r, d, dinv, static_cast<float>(lv.inv_theta), stream);
   } else {
-    launch_cheb_first(lv.a, lv.x64.p, lv.b64.p, lv.r64.p, d, lv.dinv64.p, lv.inv_theta, stream);
+    nb_cheb_first<T>(lv.opA, A, x, b, r, d, dinv, lv.inv_theta, stream);
   }
   for (int k = 1; k < opt.degree; ++k) {
-    const double* rin = (k == 1 && zero_guess) ? lv.b64.p : lv.r64.p;
+    const T* rin = (k == 1 && zero_guess) ? b : r;
     const int add_d = (k == 1 && !zero_guess) ? 1 : 0;
-    launch_cheb_step(lv.a, d, rin, lv.r64.p, e, lv.x64.p, lv.dinv64.p, lv.c1[k - 1], lv.c2[k - 1], add_d,
-                     stream);
+    if (matrix_free) {
+      if constexpr (std::is_same<T, float>::value)
+        mf_cheb_step(mf, lv.nnodes, d, rin, r, e, x, dinv, static_cast<float>(lv.c1[k - 1]),
+                     static_cast<float>(lv.c2[k - 1]), add_d, stream);
+    } else {
+      nb_cheb_step<T>(lv.opA, A, d, rin, r, e, x, dinv, lv.c1[k - 1], lv.c2[k - 1], add_d, stream);
+    }
     std::swap(d, e);
   }
-  if (opt.degree == 1 && !zero_guess) {
-    // x += d (degree 1 from a guess)
-    launch_cheb_step(lv.a, d, lv.r64.p, lv.r64.p, e, lv.x64.p, lv.dinv64.p, 0.0, 0.0, 1, stream);
-  }
+  if (opt.degree == 1 && !zero_guess) nb_cheb_step<T>(lv.opA, A, d, r, r, e, x, dinv, 0.0, 0.0, 1, stream);
 }
 
+template <class T>
 void GpuAmg::cycle(size_t l) {
   Level& lv = *levels[l];
   if (l + 1 == levels.size()) {
-    coarse_solve(lv);
+    coarse_solve<T>(lv);
     return;
   }
   Level& nv = *levels[l + 1];
-  smooth(l, true);
-  launch_csr<1>(lv.a, lv.x64.p, lv.r64.p, lv.b64.p, stream);     // residual
-  launch_csr<0>(lv.r, lv.r64.p, nv.b64.p, nullptr, stream);      // restrict
-  cycle(l + 1);
-  launch_csr<2>(lv.p, nv.x64.p, lv.x64.p, nullptr, stream);      // x += P x_c
-  smooth(l, false);
+  smooth<T>(l, true);
+  bool matrix_free = false;
+  if constexpr (std::is_same<T, float>::value) matrix_free = l == 0 && mf.enabled;
+  if (matrix_free) {  // residual
+    if constexpr (std::is_same<T, float>::value) mf_residual(mf, lv.nnodes, V<T>::x(lv), V<T>::r(lv), V<T>::b(lv), stream);
+  } else {
+    nb_apply<1, T, T, T>(lv.opA, V<T>::a(lv.a), V<T>::x(lv), V<T>::r(lv), V<T>::b(lv), stream);
+  }
+  nb_apply<0, T, T, T>(lv.opR, V<T>::a(lv.r), V<T>::r(lv), V<T>::b(nv), nullptr, stream);      // restrict
+  cycle<T>(l + 1);
+  nb_apply<2, T, T, T>(lv.opP, V<T>::a(lv.p), V<T>::x(nv), V<T>::x(lv), nullptr, stream);      // x += P x_c
+  smooth<T>(l, false);
 }
 
 void GpuAmg::apply(const double* r, double* z) {
   if (!ready_) throw Error(kBadInput, "multigrid: apply() called before setup()");
   Level& f = *levels.front();
-  SIMP_CUDA(cudaMemcpyAsync(f.b64.p, r, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, stream));
-  cycle(0);
-  SIMP_CUDA(cudaMemcpyAsync(z, f.x64.p, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, stream));
+  if (mixed()) {
+    convert(r, f.b32.p, f.n, stream);
+    cycle<float>(0);
+    convert(f.x32.p, z, f.n, stream);
+  } else {
+    SIMP_CUDA(cudaMemcpyAsync(f.b64.p, r, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, stream));
+    cycle<double>(0);
+    SIMP_CUDA(cudaMemcpyAsync(z, f.x64.p, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, stream));
+  }
 }
 
-GpuAmg::PcgResult GpuAmg::solve(const double* b, double* x) {
-  if (!ready_) throw Error(kBadInput, "solve called before factorize");
+// Preconditioned CG on A x = b (FP64 operator and vectors) from the guess in
+// x; `restarts` follows the reference's true-residual restarts.  Stops when
+// the recursive residual reaches `target` or the iteration `budget` is spent.
+GpuAmg::PcgResult GpuAmg::pcg(const double* b, double* x, double target, int budget, bool restarts,
+                              double bnorm) {
   Level& f = *levels.front();
   const i32 n = f.n;
   PcgResult res;
-  const double bnorm = std::sqrt(dot(b, b, n));
-  if (bnorm == 0.0) {
-    SIMP_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, stream));
-    res.converged = true;
-    return res;
-  }
-  const double target = opt.rtol * bnorm;
   PcgScalars* sc = reinterpret_cast<PcgScalars*>(scal.p + 8);
   static_assert(sizeof(PcgScalars) <= 8 * sizeof(double), "scalar block");
+  auto op = [&](const double* in, double* out, const double* rhs) {
+    if (rhs) nb_apply<1, double, double, double>(f.opA, f.a.v64.p, in, out, rhs, stream);
+    else nb_apply<0, double, double, double>(f.opA, f.a.v64.p, in, out, nullptr, stream);
+  };
   int total = 0;
   bool rec_conv = false;
   double best = std::numeric_limits<double>::max();
-  for (int restart = 0; restart < 3; ++restart) {
-    launch_csr<1>(f.a, x, pr.p, b, stream);
+  const int rounds = restarts ? 3 : 1;
+  for (int restart = 0; restart < rounds; ++restart) {
+    op(x, pr.p, b);
     double rnorm = std::sqrt(dot(pr.p, pr.p, n));
     res.relres = rnorm / bnorm;
     if (rnorm <= target) { res.converged = true; break; }
@@ -565,8 +919,8 @@ GpuAmg::PcgResult GpuAmg::solve(const double* b, double* x) {
       SIMP_CUDA(cudaMemcpyAsync(sc, &h, sizeof(h), cudaMemcpyHostToDevice, stream));
     }
     bool conv = false;
-    while (total < opt.maxit) {
-      launch_csr<0>(f.a, pp.p, pq.p, nullptr, stream);
+    while (total < budget) {
+      op(pp.p, pq.p, nullptr);
       k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(pp.p, pq.p, n, part.p);
       SIMP_CHECK_LAUNCH();
       k_pcg_alpha<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, sc);
@@ -596,9 +950,14 @@ GpuAmg::PcgResult GpuAmg::solve(const double* b, double* x) {
       k_pcg_direction<<<grid_for(n, 256), 256, 0, stream>>>(pp.p, pz.p, n, sc);
       SIMP_CHECK_LAUNCH();
     }
-    launch_csr<1>(f.a, x, pr.p, b, stream);
+    if (!restarts) {
+      res.converged = conv;
+      res.relres = rnorm / bnorm;
+      break;
+    }
+    op(x, pr.p, b);
     res.relres = std::sqrt(dot(pr.p, pr.p, n)) / bnorm;
-    if (res.relres <= opt.rtol) { res.converged = true; break; }
+    if (res.relres * bnorm <= target) { res.converged = true; break; }
     if (!conv) break;
     rec_conv = true;
     if (!(res.relres < 0.5 * best)) break;
@@ -607,6 +966,26 @@ GpuAmg::PcgResult GpuAmg::solve(const double* b, double* x) {
   if (!res.converged && rec_conv) res.converged = true;
   res.iterations = total;
   return res;
+}
+
+GpuAmg::PcgResult GpuAmg::solve(const double* b, double* x) {
+  if (!ready_) throw Error(kBadInput, "solve called before factorize");
+  Level& f = *levels.front();
+  const i32 n = f.n;
+  const double bnorm = std::sqrt(dot(b, b, n));
+  if (bnorm == 0.0) {
+    SIMP_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, stream));
+    PcgResult r;
+    r.converged = true;
+    return r;
+  }
+  const double target = opt.rtol * bnorm;
+  // The CG operator and the true-residual restarts are FP64 in both modes; in
+  // mixed precision the preconditioner (V-cycle) runs in FP32.  CG with an
+  // FP32 operator converges towards the FP32 matrix's solution: with the SIMP
+  // stiffness contrast it needed up to twice the CG iterations even with
+  // FP64 residual replacement, so the outer operator stays FP64.
+  return pcg(b, x, target, opt.maxit, true, bnorm);
 }
 
 }  // namespace simp

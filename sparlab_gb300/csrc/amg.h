@@ -2,6 +2,15 @@
 // src/fem/Multigrid.cpp with every per-setup numeric product, the V-cycle and
 // PCG on the device, and the once-per-structure aggregation, QR and symbolic
 // patterns on the host.
+//
+// Precision: SIMP_PRECISION_FP64 runs everything in FP64 (the reference's
+// arithmetic).  SIMP_PRECISION_MIXED keeps FP32 copies of every operator,
+// prolongator and restriction and runs the V-cycle (smoother, residuals,
+// transfers; level 0 matrix-free on structured grids), the Lanczos estimates
+// and the reused-structure Galerkin products in FP32.  CG itself -- its
+// operator, vectors, scalars and the true-residual restarts -- and the
+// coarsest dense Cholesky stay FP64 in both modes, so both stop on the same
+// FP64 residual test.
 #pragma once
 
 #include "common.h"
@@ -25,7 +34,7 @@ struct AmgOptions {
   bool reuse = true;
   double rtol = 1.0e-12;
   int maxit = 1000;
-  int precision = 0;  // 0 FP64, 1 mixed (FP32 operator / smoother / transfers)
+  int precision = 0;  // 0 FP64, 1 mixed
 };
 
 struct DevPattern {
@@ -42,6 +51,19 @@ struct DevCsr {
   DBuf<float> v32;
 };
 
+// A node-chunked matrix as the operator kernels see it (see nbspmv.cuh).
+struct NbOp {
+  i32 nodes = 0;                // row nodes
+  const i32* row_first = nullptr;
+  NodeView pat{nullptr, nullptr, nullptr};
+  const i32* rowptr = nullptr;
+  const i32* col = nullptr;
+  int block = 0;                // uniform B x B blocks without columns (2, 3), or 0
+  const i32* node_of = nullptr; // row -> row node
+  i32 rows = 0;
+  int lanes = 4;                // lanes per row of the FP64 kernel
+};
+
 struct Level {
   i32 n = 0, nnodes = 0;
   std::vector<i32> first;
@@ -50,6 +72,7 @@ struct Level {
   DevPattern d_apat;
   DBuf<i32> d_self;
   DevCsr a;
+  NbOp opA, opP, opR;
   DBuf<double> dinv64;
   DBuf<float> dinv32;
   double lambda = 0.0;
@@ -73,6 +96,18 @@ struct Level {
   double inv_theta = 0.0;
 };
 
+// Matrix-free level-0 operator of a structured grid (see mfree.cuh), used
+// by the FP32 V-cycle and the mixed-precision CG operator when enabled.
+struct MfOp {
+  bool enabled = false;
+  int dim = 3;
+  i32 nx = 0, ny = 0, nz = 1, nnx = 0, nny = 0;
+  const i32* gnode = nullptr;   // free node -> grid node
+  const i32* nindex = nullptr;  // grid node -> free node or -1
+  const float* ke = nullptr;    // K_e^0, FP32
+  const float* scale = nullptr; // s_e, FP32
+};
+
 struct AmgStats {
   int num_levels = 0;
   bool reused = false;
@@ -90,50 +125,57 @@ class GpuAmg {
   AmgStats stats;
   cudaStream_t stream = 0;
 
-  // Level 0: the caller fills levels[0]->a (device CSR, FP64 values), its
-  // node layout (first) and pattern (apat), and the near-null space.
+  bool mixed() const { return opt.precision == 1; }
+  // Set by an assembler that wrote level 0's FP32 values itself; otherwise
+  // setup converts them from the FP64 values (mixed mode).
+  bool level0_fp32_fresh = false;
+  MfOp mf;
+  // Level 0: the caller fills levels[0]->a (device CSR with FP64 values, and
+  // FP32 values in mixed mode), its node layout (first) and pattern (apat),
+  // and the near-null space.
   Level& level0();
   // structure_changed: rebuild aggregates / patterns (first setup or a new
   // structure); otherwise reuse them when opt.reuse.
   void setup(bool structure_changed);
   bool ready() const { return ready_; }
+  // level-0 FP32 values from the FP64 ones (mixed mode)
+  void refresh_level0_fp32();
 
   // z = M^-1 r (FP64 device vectors of level-0 length).
   void apply(const double* r, double* z);
-  // PCG (src/fem/Multigrid.cpp:1152-1237); x holds the guess on entry.
   struct PcgResult {
     int iterations = 0;
     double relres = 0.0;
     bool converged = false;
   };
+  // PCG (src/fem/Multigrid.cpp:1152-1237); x holds the guess on entry.
   PcgResult solve(const double* b, double* x);
-  // y = A0 x
+  // y = A0 x in FP64
   void spmv0(const double* x, double* y);
+  // CUDA-event time of the cycle's level-0 operator launch (ms) and its
+  // algorithmic bytes
+  void time_operator(int reps, double* ms, double* bytes);
 
-  // scratch for reductions and PCG
   DBuf<double> part, scal;
   DBuf<double> pr, pz, pp, pq;
   DBuf<int> dstatus;
 
  private:
   bool ready_ = false;
-  // coarse direct solve
   i32 nc_ = 0;
   DBuf<double> dense_, inv_t_, piv_, tmp_;
-  std::vector<double> lanczos_start_;
 
   void numeric_level(size_t l);
   void build_transfer(size_t l);
-  void galerkin(size_t l);
+  void galerkin(size_t l, bool fp32);
   void coarse_factorize();
-  void coarse_solve(const Level& lv);
-  void smooth(size_t l, bool zero_guess);
-  void cycle(size_t l);
+  void make_ops(size_t l);
+  template <class T> void coarse_solve(Level& lv);
+  template <class T> void smooth(size_t l, bool zero_guess);
+  template <class T> void cycle(size_t l);
   double dot(const double* a, const double* b, i64 n);
+  PcgResult pcg(const double* b, double* x, double target, int budget, bool restarts, double bnorm);
   void compute_stats();
 };
-
-// y = A x for a level operator (selects lanes per row from the row length).
-void csr_apply(const DevCsr& a, const double* x, double* y, cudaStream_t s);
 
 }  // namespace simp

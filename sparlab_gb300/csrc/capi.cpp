@@ -419,6 +419,8 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     if (!(d.damping > 0.0 && d.damping <= 1.0)) throw Error(kBadInput, "optimizer.damping must lie in (0, 1]");
     d.warm = dsc->warm_start != 0;
     d.block_pcg = dsc->block_pcg != 0;
+    if (dsc->optimizer != 0 && dsc->optimizer != 1) throw Error(kBadInput, "unknown optimizer (expected 0 OC, 1 MMA)");
+    d.optimizer = dsc->optimizer;
     std::unique_ptr<simp_problem> p(new simp_problem());
     p->device = o->device;
     p->p.reset(new GpuProblem(d, ao));
@@ -506,6 +508,20 @@ int simp_oc_update(simp_problem* p, int32_t apply, simp_oc_step* out, double* xn
   });
 }
 
+int simp_mma_update(simp_problem* p, int32_t apply, simp_oc_step* out, double* xnew) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    const OcStep st = p->p->mma_update(apply != 0, xnew);
+    if (out) {
+      out->lambda = st.lambda;
+      out->achieved_volume = st.volume;
+      out->max_change = st.max_change;
+      out->bisections = st.bisections;
+      out->volume_converged = st.converged ? 1 : 0;
+    }
+  });
+}
+
 int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
   return guarded(p->err, [&] {
     use_device(p->device);
@@ -515,7 +531,7 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
     SIMP_CUDA(cudaEventCreate(&e1));
     SIMP_CUDA(cudaEventRecord(e0, g.amg.stream));
     const Evaluation ev = g.evaluate();
-    const OcStep st = g.oc_update(true, nullptr);
+    const OcStep st = g.d.optimizer == 1 ? g.mma_update(true, nullptr) : g.oc_update(true, nullptr);
     SIMP_CUDA(cudaEventRecord(e1, g.amg.stream));
     SIMP_CUDA(cudaEventSynchronize(e1));
     float ms = 0.0f;
@@ -574,7 +590,7 @@ int simp_problem_kff(simp_problem* p, const double* scale, int32_t* rowptr, int3
       if (!scale) throw Error(kBadInput, "simp_problem_kff: values need element factors");
       DBuf<double> s;
       s.upload(scale, static_cast<size_t>(g.ne));
-      g.assemble(s.p);
+      g.assemble(s.p, true);
       l0.a.v64.download(val, static_cast<size_t>(l0.a.nnz));
     }
     if (rowptr) l0.a.ptr.download(rowptr, static_cast<size_t>(l0.n) + 1);
@@ -597,6 +613,16 @@ int simp_problem_apply_operator(simp_problem* p, const double* x, double* y) {
     GpuAmg& amg = p->p->amg;
     if (!amg.ready()) throw Error(kBadInput, "the operator is assembled by the first evaluate");
     amg.spmv0(x, y);
+  });
+}
+
+int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms, double* bytes) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    double m = 0.0, b = 0.0;
+    p->p->amg.time_operator(reps, &m, &b);
+    if (ms) *ms = m;
+    if (bytes) *bytes = b;
   });
 }
 

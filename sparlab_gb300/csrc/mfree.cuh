@@ -1,0 +1,258 @@
+// Matrix-free level-0 operator of a structured Q4 / Hex8 grid (FP32).
+//
+// y_I = sum over the cells e around node I of s_e sum_J K_e^0(I, J) x_J, with
+// one thread per free node gathering its (at most 8) cells: every output is
+// written once, no atomics, and the result does not depend on the launch
+// shape.  The 8 (4) cells around a node are visited in a fixed order, so all
+// threads of a warp read the same K_e^0 rows at the same time (a broadcast
+// from shared memory).  Used where every node is either fully free or fully
+// clamped (the free DOFs of node I are 3I', 3I'+1, 3I'+2 for its free index
+// I'); the assembled operator is used otherwise.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace simp {
+namespace {
+
+struct MfView {
+  int dim;             // 2 or 3
+  i32 nx, ny, nz;      // cells (nz = 1 in 2-D)
+  i32 nnx, nny;        // nodes per axis in x, y
+  const i32* gnode;    // free node -> grid node
+  const i32* nindex;   // grid node -> free node or -1
+  const float* ke;     // K_e^0 (ed x ed, row-major)
+  const float* scale;  // s_e
+};
+
+// Per-node product (A x)_I for the free node I; out[k], k < dim.
+template <class TX>
+__device__ __forceinline__ void mf_node_apply(const MfView& m, const float* __restrict__ ks, i32 I,
+                                              const TX* __restrict__ x, float (&out)[3]) {
+  const int dim = m.dim;
+  const int ed = dim == 3 ? 24 : 8;
+  out[0] = out[1] = out[2] = 0.0f;
+  const i32 g = m.gnode[I];
+  const i32 ix = g % m.nnx, iy = (g / m.nnx) % m.nny, iz = g / (m.nnx * m.nny);
+  const int zlo = dim == 3 ? -1 : 0;
+  for (int dz = zlo; dz <= 0; ++dz)
+    for (int dy = -1; dy <= 0; ++dy)
+      for (int dx = -1; dx <= 0; ++dx) {
+        const i32 cx = ix + dx, cy = iy + dy, cz = iz + dz;
+        if (cx < 0 || cx >= m.nx || cy < 0 || cy >= m.ny || cz < 0 || cz >= m.nz) continue;
+        const float s = m.scale[(static_cast<i64>(cz) * m.ny + cy) * m.nx + cx];
+        // corner index of node I in cell c: offsets (-dx, -dy, -dz)
+        const int ox = -dx, oy = -dy, oz = -dz;
+        const int aI = 4 * oz + (oy ? 3 - ox : ox);
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        const int npe = dim == 3 ? 8 : 4;
+        for (int b = 0; b < npe; ++b) {
+          const int bx = (b == 1 || b == 2 || b == 5 || b == 6) ? 1 : 0;
+          const int by = (b == 2 || b == 3 || b == 6 || b == 7) ? 1 : 0;
+          const int bz = b >= 4 ? 1 : 0;
+          const i64 gj = (static_cast<i64>(cz + bz) * m.nny + (cy + by)) * m.nnx + (cx + bx);
+          const i32 J = m.nindex[gj];
+          if (J < 0) continue;
+          float xj[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) xj[k] = k < dim ? static_cast<float>(x[static_cast<i64>(J) * dim + k]) : 0.0f;
+#pragma unroll
+          for (int ka = 0; ka < 3; ++ka) {
+            if (ka < dim) {
+              const float* row = ks + (dim * aI + ka) * ed + dim * b;
+#pragma unroll
+              for (int kb = 0; kb < 3; ++kb)
+                if (kb < dim) acc[ka] = fmaf(row[kb], xj[kb], acc[ka]);
+            }
+          }
+        }
+#pragma unroll
+        for (int ka = 0; ka < 3; ++ka) out[ka] = fmaf(s, acc[ka], out[ka]);
+      }
+}
+
+// mode 0: y = A x ; 1: y = b - A x ; 2: y += A x
+template <int MODE, class TX>
+__global__ void __launch_bounds__(256) k_mf_apply(MfView m, i32 nodes, const TX* __restrict__ x, TX* __restrict__ y,
+                                                  const TX* __restrict__ b) {
+  __shared__ float ks[24 * 24];
+  const int ed = m.dim == 3 ? 24 : 8;
+  for (int k = threadIdx.x; k < ed * ed; k += blockDim.x) ks[k] = m.ke[k];
+  __syncthreads();
+  const i32 I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nodes) return;
+  float out[3];
+  mf_node_apply<TX>(m, ks, I, x, out);
+  for (int k = 0; k < m.dim; ++k) {
+    const i64 row = static_cast<i64>(I) * m.dim + k;
+    if (MODE == 0) y[row] = static_cast<TX>(out[k]);
+    else if (MODE == 1) y[row] = b[row] - static_cast<TX>(out[k]);
+    else y[row] += static_cast<TX>(out[k]);
+  }
+}
+
+// Chebyshev step: r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ d]) + dn
+__global__ void __launch_bounds__(256) k_mf_cheb_step(MfView m, i32 nodes, const float* __restrict__ d,
+                                                      const float* __restrict__ r_in, float* __restrict__ r,
+                                                      float* __restrict__ dn, float* __restrict__ x,
+                                                      const float* __restrict__ dinv, float c1, float c2,
+                                                      int add_d) {
+  __shared__ float ks[24 * 24];
+  const int ed = m.dim == 3 ? 24 : 8;
+  for (int k = threadIdx.x; k < ed * ed; k += blockDim.x) ks[k] = m.ke[k];
+  __syncthreads();
+  const i32 I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nodes) return;
+  float out[3];
+  mf_node_apply<float>(m, ks, I, d, out);
+  for (int k = 0; k < m.dim; ++k) {
+    const i64 row = static_cast<i64>(I) * m.dim + k;
+    const float ri = r_in[row] - out[k];
+    r[row] = ri;
+    const float di = c1 * d[row] + c2 * dinv[row] * ri;
+    dn[row] = di;
+    float xi = x[row];
+    if (add_d) xi = xi + d[row];
+    x[row] = xi + di;
+  }
+}
+
+// r = b - A x ; d = dinv r / theta
+__global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, const float* __restrict__ x,
+                                                       const float* __restrict__ b, float* __restrict__ r,
+                                                       float* __restrict__ d, const float* __restrict__ dinv,
+                                                       float inv_theta) {
+  __shared__ float ks[24 * 24];
+  const int ed = m.dim == 3 ? 24 : 8;
+  for (int k = threadIdx.x; k < ed * ed; k += blockDim.x) ks[k] = m.ke[k];
+  __syncthreads();
+  const i32 I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nodes) return;
+  float out[3];
+  mf_node_apply<float>(m, ks, I, x, out);
+  for (int k = 0; k < m.dim; ++k) {
+    const i64 row = static_cast<i64>(I) * m.dim + k;
+    const float ri = b[row] - out[k];
+    r[row] = ri;
+    d[row] = dinv[row] * ri * inv_theta;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tiled 3-D variant: a block owns a 32 x 4 x 2 tile of grid nodes; the tile's
+// node values plus a one-node halo, the scales of the 33 x 5 x 3 cells that
+// touch it and K_e^0 (as float4 rows of its 3 x 3 node blocks) are staged in
+// shared memory once, so each node's 64 (cell, corner) terms read shared
+// memory only.  Modes: 0 y = A x, 1 y = b - A x, 3 Chebyshev step, 4 Chebyshev
+// first step (same epilogues as the other operator kernels).
+// ---------------------------------------------------------------------------
+constexpr int kTX = 32, kTY = 4, kTZ = 2;
+
+struct MfArgs {
+  const float* x;     // input (d for the Chebyshev step)
+  float* y;           // mode 0/1: output
+  const float* b;     // mode 1/4: right-hand side; mode 3: r_in
+  float* r;           // mode 3/4: residual out
+  float* dn;          // mode 3: new direction; mode 4: d out
+  float* xs;          // mode 3: smoothed iterate (updated)
+  const float* dinv;  // mode 3/4
+  float c1, c2, inv_theta;
+  int add_d;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a) {
+  __shared__ float4 xh[kTZ + 2][kTY + 2][kTX + 2];
+  __shared__ float sc[kTZ + 1][kTY + 1][kTX + 1];
+  __shared__ float4 kq[8][8][3];
+  const int tid = threadIdx.x;
+  const i32 x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * kTZ;
+  const i32 nnz = m.nz + 1;
+  // K_e^0 blocks: kq[aI][b][ka] = row 3 aI + ka, columns 3 b .. 3 b + 2
+  for (int e = tid; e < 8 * 8 * 3; e += kTX * kTY * kTZ) {
+    const int aI = e / 24, b = (e / 3) % 8, ka = e % 3;
+    const float* row = m.ke + (3 * aI + ka) * 24 + 3 * b;
+    kq[aI][b][ka] = make_float4(row[0], row[1], row[2], 0.0f);
+  }
+  // node values of the tile and its halo (zero outside the grid / clamped)
+  for (int e = tid; e < (kTZ + 2) * (kTY + 2) * (kTX + 2); e += kTX * kTY * kTZ) {
+    const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
+    const i32 gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (gx >= 0 && gx < m.nnx && gy >= 0 && gy < m.nny && gz >= 0 && gz < nnz) {
+      const i32 J = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
+      if (J >= 0) {
+        const float* p = a.x + static_cast<i64>(J) * 3;
+        v = make_float4(p[0], p[1], p[2], 0.0f);
+      }
+    }
+    xh[hz][hy][hx] = v;
+  }
+  // cell scales (zero outside the grid)
+  for (int e = tid; e < (kTZ + 1) * (kTY + 1) * (kTX + 1); e += kTX * kTY * kTZ) {
+    const int cx = e % (kTX + 1), cy = (e / (kTX + 1)) % (kTY + 1), cz = e / ((kTX + 1) * (kTY + 1));
+    const i32 gx = x0 - 1 + cx, gy = y0 - 1 + cy, gz = z0 - 1 + cz;
+    float s = 0.0f;
+    if (gx >= 0 && gx < m.nx && gy >= 0 && gy < m.ny && gz >= 0 && gz < m.nz)
+      s = m.scale[(static_cast<i64>(gz) * m.ny + gy) * m.nx + gx];
+    sc[cz][cy][cx] = s;
+  }
+  __syncthreads();
+  const int tx = tid % kTX, ty = (tid / kTX) % kTY, tz = tid / (kTX * kTY);
+  const i32 gx = x0 + tx, gy = y0 + ty, gz = z0 + tz;
+  if (gx >= m.nnx || gy >= m.nny || gz >= nnz) return;
+  const i32 I = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
+  if (I < 0) return;
+  float out0 = 0.0f, out1 = 0.0f, out2 = 0.0f;
+#pragma unroll
+  for (int dz = -1; dz <= 0; ++dz)
+#pragma unroll
+    for (int dy = -1; dy <= 0; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 0; ++dx) {
+        const float s = sc[tz + dz + 1][ty + dy + 1][tx + dx + 1];
+        const int ox = -dx, oy = -dy, oz = -dz;
+        const int aI = 4 * oz + (oy ? 3 - ox : ox);
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          const int bx = (b == 1 || b == 2 || b == 5 || b == 6) ? 1 : 0;
+          const int by = (b == 2 || b == 3 || b == 6 || b == 7) ? 1 : 0;
+          const int bz = b >= 4 ? 1 : 0;
+          const float4 xv = xh[tz + dz + 1 + bz][ty + dy + 1 + by][tx + dx + 1 + bx];
+          const float4 k0 = kq[aI][b][0], k1 = kq[aI][b][1], k2 = kq[aI][b][2];
+          a0 = fmaf(k0.x, xv.x, fmaf(k0.y, xv.y, fmaf(k0.z, xv.z, a0)));
+          a1 = fmaf(k1.x, xv.x, fmaf(k1.y, xv.y, fmaf(k1.z, xv.z, a1)));
+          a2 = fmaf(k2.x, xv.x, fmaf(k2.y, xv.y, fmaf(k2.z, xv.z, a2)));
+        }
+        out0 = fmaf(s, a0, out0);
+        out1 = fmaf(s, a1, out1);
+        out2 = fmaf(s, a2, out2);
+      }
+  const float o[3] = {out0, out1, out2};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const i64 row = static_cast<i64>(I) * 3 + k;
+    if (MODE == 0) {
+      a.y[row] = o[k];
+    } else if (MODE == 1) {
+      a.y[row] = a.b[row] - o[k];
+    } else if (MODE == 3) {
+      const float ri = a.b[row] - o[k];
+      a.r[row] = ri;
+      const float dv = a.x[row];
+      const float di = a.c1 * dv + a.c2 * a.dinv[row] * ri;
+      a.dn[row] = di;
+      float xi = a.xs[row];
+      if (a.add_d) xi = xi + dv;
+      a.xs[row] = xi + di;
+    } else {
+      const float ri = a.b[row] - o[k];
+      a.r[row] = ri;
+      a.dn[row] = a.dinv[row] * ri * a.inv_theta;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace simp

@@ -1,13 +1,16 @@
-// Node-block sparse operator applications.
+// Node-chunked sparse operator applications.
 //
-// Every level operator (A_l, P_l, R_l) is stored as scalar rows whose column
-// lists are shared by all rows of a node and grouped by whole column nodes
-// (see structure.h).  A group of G lanes owns one row node: lanes stride over
-// its node-level slots, each lane multiplies the slot's (rows x cols) block by
-// the column node's entries of x (loaded once for all rows of the node), and
-// the per-row sums are reduced across the group with a fixed butterfly.  Index
-// traffic is one slot record per block instead of one column per entry, and
-// x is read once per block instead of once per row.
+// Every level operator (A_l, P_l, R_l) is a scalar CSR whose rows of one
+// node share their length and column list, and are stored back to back.  One
+// warp owns one row node: for each of its (<= 6) rows the lanes stride across
+// the row's contiguous values (coalesced loads), then the row sums are
+// reduced with a fixed butterfly and lane r writes row r, so every output is
+// written once and the result does not depend on timing.
+//
+// Level 0 of a grid whose nodes are all fully free or fully clamped has
+// uniform B x B blocks (B = 2 or 3); there the column of entry w of a row is
+// B * nbr[slot w / B] + w % B, so the column array is not read at all and the
+// index traffic is one slot record per block.
 #pragma once
 
 #include "kernels.cuh"
@@ -17,18 +20,13 @@ namespace {
 
 constexpr int kMaxNode = 6;  // unknowns per node: 2-3 on level 0, rank <= 6 below
 
-template <class T>
-struct Acc {
-  using type = T;
-};
-
-// Per-row dot products of one row node; returns with acc[r] (r < nr) summed
-// over the group in every lane.
-template <int G, class TV, class TX, class TA>
-__device__ __forceinline__ void nb_row_dots(i32 I, int lane, unsigned mask, bool valid, const i32* __restrict__ row_first,
-                                            const i32* __restrict__ col_first, NodeView pat,
-                                            const i32* __restrict__ rowptr, const TV* __restrict__ val,
-                                            const TX* __restrict__ x, int& nr, i32& r0, TA (&acc)[kMaxNode]) {
+// Row sums of one row node; returns with acc[r] (r < nr) summed over the warp
+// in every lane.  B > 0: uniform-block level 0 without the column array.
+template <int B, class TV, class TX, class TA>
+__device__ __forceinline__ void chunk_row_dots(i32 I, int lane, bool valid, const i32* __restrict__ row_first,
+                                               NodeView pat, const i32* __restrict__ rowptr,
+                                               const i32* __restrict__ col, const TV* __restrict__ val,
+                                               const TX* __restrict__ x, int& nr, i32& r0, TA (&acc)[kMaxNode]) {
 #pragma unroll
   for (int r = 0; r < kMaxNode; ++r) acc[r] = TA(0);
   nr = 0;
@@ -36,60 +34,50 @@ __device__ __forceinline__ void nb_row_dots(i32 I, int lane, unsigned mask, bool
   if (valid) {
     r0 = row_first[I];
     nr = row_first[I + 1] - r0;
-    i32 rp[kMaxNode];
+    const i32 base = rowptr[r0];
+    const i32 len = nr > 0 ? rowptr[r0 + 1] - base : 0;
+    const i32 s0 = pat.ptr[I];
 #pragma unroll
-    for (int r = 0; r < kMaxNode; ++r) rp[r] = r < nr ? rowptr[r0 + r] : 0;
-    const i32 te = pat.ptr[I + 1];
-    for (i32 t = pat.ptr[I] + lane; t < te; t += G) {
-      const i32 J = pat.nbr[t];
-      const i32 c0 = col_first[J];
-      const int nc = col_first[J + 1] - c0;
-      const i32 o = pat.off[t];
-      TA xv[kMaxNode];
-#pragma unroll
-      for (int k = 0; k < kMaxNode; ++k) xv[k] = k < nc ? static_cast<TA>(x[c0 + k]) : TA(0);
-#pragma unroll
-      for (int r = 0; r < kMaxNode; ++r) {
-        if (r < nr) {
-          const TV* v = val + rp[r] + o;
-#pragma unroll
-          for (int k = 0; k < kMaxNode; ++k)
-            if (k < nc) acc[r] += static_cast<TA>(v[k]) * xv[k];
+    for (int r = 0; r < kMaxNode; ++r) {
+      if (r < nr) {
+        const TV* v = val + base + r * len;
+        TA s = TA(0);
+        if constexpr (B > 0) {
+          for (i32 w = lane; w < len; w += 32) {
+            const i32 t = w / B;
+            const i32 c = B * pat.nbr[s0 + t] + (w - B * t);
+            s += static_cast<TA>(v[w]) * static_cast<TA>(x[c]);
+          }
+        } else {
+          const i32* cl = col + base + r * len;
+          for (i32 w = lane; w < len; w += 32) s += static_cast<TA>(v[w]) * static_cast<TA>(x[cl[w]]);
         }
+        acc[r] = s;
       }
     }
   }
 #pragma unroll
   for (int r = 0; r < kMaxNode; ++r) {
+    if (r < nr) {
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(mask, acc[r], o, G);
+      for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+    }
   }
 }
 
-template <int G>
-__device__ __forceinline__ unsigned group_mask() {
-  if (G == 32) return 0xffffffffu;
-  const int base = (threadIdx.x & 31) & ~(G - 1);
-  return ((1u << G) - 1u) << base;
-}
-
 // mode 0: y = A x ; 1: y = b - A x ; 2: y += A x
-template <int G, int MODE, class TV, class TX, class TA>
-__global__ void __launch_bounds__(256) k_nb_apply(i32 nodes, const i32* __restrict__ row_first,
-                                                  const i32* __restrict__ col_first, NodeView pat,
-                                                  const i32* __restrict__ rowptr, const TV* __restrict__ val,
-                                                  const TX* __restrict__ x, TX* __restrict__ y,
-                                                  const TX* __restrict__ b) {
-  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  const i32 I = static_cast<i32>(t0 / G);
-  const int lane = static_cast<int>(t0 % G);
-  const bool valid = I < nodes;
+template <int B, int MODE, class TV, class TX, class TA>
+__global__ void __launch_bounds__(256) k_chunk_apply(i32 nodes, const i32* __restrict__ row_first, NodeView pat,
+                                                     const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                                     const TV* __restrict__ val, const TX* __restrict__ x,
+                                                     TX* __restrict__ y, const TX* __restrict__ b) {
+  const i32 I = static_cast<i32>((blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (I >= nodes) return;  // whole warps leave together
   TA acc[kMaxNode];
   int nr;
   i32 r0;
-  nb_row_dots<G, TV, TX, TA>(I, lane, group_mask<G>(), valid, row_first, col_first, pat, rowptr, val, x, nr, r0,
-                             acc);
-  if (!valid) return;
+  chunk_row_dots<B, TV, TX, TA>(I, lane, true, row_first, pat, rowptr, col, val, x, nr, r0, acc);
 #pragma unroll
   for (int r = 0; r < kMaxNode; ++r) {
     if (r < nr && lane == r) {
@@ -102,30 +90,29 @@ __global__ void __launch_bounds__(256) k_nb_apply(i32 nodes, const i32* __restri
 }
 
 // Chebyshev step: r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ d]) + dn
-template <int G, class TV, class TX>
-__global__ void __launch_bounds__(256) k_nb_cheb_step(i32 nodes, const i32* __restrict__ first, NodeView pat,
-                                                      const i32* __restrict__ rowptr, const TV* __restrict__ val,
-                                                      const TX* __restrict__ d, const TX* __restrict__ r_in,
-                                                      TX* __restrict__ r, TX* __restrict__ dn, TX* __restrict__ x,
-                                                      const TX* __restrict__ dinv, TX c1, TX c2, int add_d) {
-  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  const i32 I = static_cast<i32>(t0 / G);
-  const int lane = static_cast<int>(t0 % G);
-  const bool valid = I < nodes;
-  TX acc[kMaxNode];
+template <int B, class T>
+__global__ void __launch_bounds__(256) k_chunk_cheb_step(i32 nodes, const i32* __restrict__ first, NodeView pat,
+                                                         const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                                         const T* __restrict__ val, const T* __restrict__ d,
+                                                         const T* __restrict__ r_in, T* __restrict__ r,
+                                                         T* __restrict__ dn, T* __restrict__ x,
+                                                         const T* __restrict__ dinv, T c1, T c2, int add_d) {
+  const i32 I = static_cast<i32>((blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (I >= nodes) return;
+  T acc[kMaxNode];
   int nr;
   i32 r0;
-  nb_row_dots<G, TV, TX, TX>(I, lane, group_mask<G>(), valid, first, first, pat, rowptr, val, d, nr, r0, acc);
-  if (!valid) return;
+  chunk_row_dots<B, T, T, T>(I, lane, true, first, pat, rowptr, col, val, d, nr, r0, acc);
 #pragma unroll
   for (int q = 0; q < kMaxNode; ++q) {
     if (q < nr && lane == q) {
       const i32 row = r0 + q;
-      const TX ri = r_in[row] - acc[q];
+      const T ri = r_in[row] - acc[q];
       r[row] = ri;
-      const TX di = c1 * d[row] + c2 * dinv[row] * ri;
+      const T di = c1 * d[row] + c2 * dinv[row] * ri;
       dn[row] = di;
-      TX xi = x[row];
+      T xi = x[row];
       if (add_d) xi = xi + d[row];
       x[row] = xi + di;
     }
@@ -133,29 +120,133 @@ __global__ void __launch_bounds__(256) k_nb_cheb_step(i32 nodes, const i32* __re
 }
 
 // r = b - A x ; d = dinv r / theta
-template <int G, class TV, class TX>
-__global__ void __launch_bounds__(256) k_nb_cheb_first(i32 nodes, const i32* __restrict__ first, NodeView pat,
-                                                       const i32* __restrict__ rowptr, const TV* __restrict__ val,
-                                                       const TX* __restrict__ x, const TX* __restrict__ b,
-                                                       TX* __restrict__ r, TX* __restrict__ d,
-                                                       const TX* __restrict__ dinv, TX inv_theta) {
-  const i64 t0 = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  const i32 I = static_cast<i32>(t0 / G);
-  const int lane = static_cast<int>(t0 % G);
-  const bool valid = I < nodes;
-  TX acc[kMaxNode];
+template <int B, class T>
+__global__ void __launch_bounds__(256) k_chunk_cheb_first(i32 nodes, const i32* __restrict__ first, NodeView pat,
+                                                          const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                                          const T* __restrict__ val, const T* __restrict__ x,
+                                                          const T* __restrict__ b, T* __restrict__ r,
+                                                          T* __restrict__ d, const T* __restrict__ dinv,
+                                                          T inv_theta) {
+  const i32 I = static_cast<i32>((blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (I >= nodes) return;
+  T acc[kMaxNode];
   int nr;
   i32 r0;
-  nb_row_dots<G, TV, TX, TX>(I, lane, group_mask<G>(), valid, first, first, pat, rowptr, val, x, nr, r0, acc);
-  if (!valid) return;
+  chunk_row_dots<B, T, T, T>(I, lane, true, first, pat, rowptr, col, val, x, nr, r0, acc);
 #pragma unroll
   for (int q = 0; q < kMaxNode; ++q) {
     if (q < nr && lane == q) {
       const i32 row = r0 + q;
-      const TX ri = b[row] - acc[q];
+      const T ri = b[row] - acc[q];
       r[row] = ri;
       d[row] = dinv[row] * ri * inv_theta;
     }
+  }
+}
+
+// VS lanes per scalar row (VS = 4 or 8), for operators whose arithmetic is
+// the bottleneck (FP64 on GB300 runs at 1/64 of the FP32 rate): a VS-lane
+// reduction costs log2(VS) adds per row instead of five.  Lanes of a row
+// read consecutive values (32-byte sectors fully used).
+template <int VS, int B, int MODE, class TV, class TX, class TA>
+__global__ void __launch_bounds__(256) k_rows_apply(i32 nodes, const i32* __restrict__ row_first,
+                                                    const i32* __restrict__ node_of, NodeView pat,
+                                                    const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                                    const TV* __restrict__ val, const TX* __restrict__ x,
+                                                    TX* __restrict__ y, const TX* __restrict__ b, i32 rows) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  TA s = TA(0);
+  if (row < rows) {
+    const i32 k0 = rowptr[row], len = rowptr[row + 1] - k0;
+    const TV* v = val + k0;
+    if constexpr (B > 0) {
+      const i32 s0 = pat.ptr[node_of[row]];
+      for (i32 w = lane; w < len; w += VS) {
+        const i32 tt = w / B;
+        s += static_cast<TA>(v[w]) * static_cast<TA>(x[B * pat.nbr[s0 + tt] + (w - B * tt)]);
+      }
+    } else {
+      const i32* cl = col + k0;
+      for (i32 w = lane; w < len; w += VS) s += static_cast<TA>(v[w]) * static_cast<TA>(x[cl[w]]);
+    }
+  }
+#pragma unroll
+  for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, VS);
+  if (row < rows && lane == 0) {
+    if (MODE == 0) y[row] = static_cast<TX>(s);
+    else if (MODE == 1) y[row] = b[row] - static_cast<TX>(s);
+    else y[row] += static_cast<TX>(s);
+  }
+  (void)row_first;
+  (void)nodes;
+}
+
+template <int VS, int B, class TV, class TX>
+__device__ __forceinline__ TX rows_dot(i32 row, int lane, bool valid, const i32* __restrict__ node_of, NodeView pat,
+                                       const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                       const TV* __restrict__ val, const TX* __restrict__ x) {
+  TX s = TX(0);
+  if (valid) {
+    const i32 k0 = rowptr[row], len = rowptr[row + 1] - k0;
+    const TV* v = val + k0;
+    if constexpr (B > 0) {
+      const i32 s0 = pat.ptr[node_of[row]];
+      for (i32 w = lane; w < len; w += VS) {
+        const i32 tt = w / B;
+        s += static_cast<TX>(v[w]) * x[B * pat.nbr[s0 + tt] + (w - B * tt)];
+      }
+    } else {
+      const i32* cl = col + k0;
+      for (i32 w = lane; w < len; w += VS) s += static_cast<TX>(v[w]) * x[cl[w]];
+    }
+  }
+#pragma unroll
+  for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, VS);
+  return s;
+}
+
+// Chebyshev step with VS lanes per row (FP64 path).
+template <int VS, int B, class T>
+__global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __restrict__ node_of, NodeView pat,
+                                                        const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                                        const T* __restrict__ val, const T* __restrict__ d,
+                                                        const T* __restrict__ r_in, T* __restrict__ r,
+                                                        T* __restrict__ dn, T* __restrict__ x,
+                                                        const T* __restrict__ dinv, T c1, T c2, int add_d) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  const bool valid = row < rows;
+  const T s = rows_dot<VS, B, T, T>(row, lane, valid, node_of, pat, rowptr, col, val, d);
+  if (valid && lane == 0) {
+    const T ri = r_in[row] - s;
+    r[row] = ri;
+    const T di = c1 * d[row] + c2 * dinv[row] * ri;
+    dn[row] = di;
+    T xi = x[row];
+    if (add_d) xi = xi + d[row];
+    x[row] = xi + di;
+  }
+}
+
+template <int VS, int B, class T>
+__global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __restrict__ node_of, NodeView pat,
+                                                         const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                                         const T* __restrict__ val, const T* __restrict__ x,
+                                                         const T* __restrict__ b, T* __restrict__ r,
+                                                         T* __restrict__ d, const T* __restrict__ dinv, T inv_theta) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  const bool valid = row < rows;
+  const T s = rows_dot<VS, B, T, T>(row, lane, valid, node_of, pat, rowptr, col, val, x);
+  if (valid && lane == 0) {
+    const T ri = b[row] - s;
+    r[row] = ri;
+    d[row] = dinv[row] * ri * inv_theta;
   }
 }
 

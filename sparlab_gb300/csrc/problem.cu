@@ -189,6 +189,7 @@ void GpuProblem::build() {
   pat.rows = pat.cols = nfn;
   pat.ptr.assign(static_cast<size_t>(nfn) + 1, 0);
   pat.nbr.reserve(static_cast<size_t>(nfn) * (dim == 3 ? 27 : 9));
+  std::vector<uint32_t> nmask_h(static_cast<size_t>(nfn), 0u);
   for (i32 I = 0; I < nfn; ++I) {
     const i64 gi = gnode_h[I];
     const i32 ix = static_cast<i32>(gi % g.nnx), iy = static_cast<i32>((gi / g.nnx) % g.nny),
@@ -199,10 +200,15 @@ void GpuProblem::build() {
           const i32 jx = ix + dx, jy = iy + dy, jz = iz + dz;
           if (jx < 0 || jx >= g.nnx || jy < 0 || jy >= g.nny || jz < 0 || jz >= g.nnz) continue;
           const i64 gj = (static_cast<i64>(jz) * g.nny + jy) * g.nnx + jx;
-          if (node_index[gj] >= 0) pat.nbr.push_back(node_index[gj]);
+          if (node_index[gj] >= 0) {
+            pat.nbr.push_back(node_index[gj]);
+            const int o = (dim == 3 ? (dz + 1) * 9 : 0) + (dy + 1) * 3 + (dx + 1);
+            nmask_h[I] |= 1u << o;
+          }
         }
     pat.ptr[I + 1] = static_cast<i32>(pat.nbr.size());
   }
+  nmask.upload(nmask_h);
   finish_offsets(pat, first);
   // AMG level 0
   Level& l0 = amg.level0();
@@ -238,6 +244,30 @@ void GpuProblem::build() {
   }
   gnode.upload(gnode_h);
   cmask.upload(cmask_h);
+  // matrix-free level-0 operator where every node is fully free or clamped
+  {
+    const uint8_t full = static_cast<uint8_t>((1 << dim) - 1);
+    bool all_or_nothing = true;
+    for (uint8_t m : cmask_h) all_or_nothing = all_or_nothing && m == full;
+    if (amg.mixed() && all_or_nothing) {
+      std::vector<float> k32(d.ke.begin(), d.ke.end());
+      ke32.upload(k32);
+      sf32.alloc(static_cast<size_t>(ne));
+      nindex.upload(node_index);
+      MfOp& mf = amg.mf;
+      mf.enabled = true;
+      mf.dim = dim;
+      mf.nx = d.nx;
+      mf.ny = d.ny;
+      mf.nz = d.nz;
+      mf.nnx = g.nnx;
+      mf.nny = g.nny;
+      mf.gnode = gnode.p;
+      mf.nindex = nindex.p;
+      mf.ke = ke32.p;
+      mf.scale = sf32.p;
+    }
+  }
   std::vector<uint8_t> uc(ucomp_h.begin(), ucomp_h.end());
   ucomp.upload(uc);
   dof_map.upload(map);
@@ -399,19 +429,32 @@ void GpuProblem::get_design(double* h) {
   SIMP_CUDA(cudaStreamSynchronize(amg.stream));
 }
 
-void GpuProblem::assemble(const double* scale) {
+void GpuProblem::assemble(const double* scale, bool exact) {
   Level& l0 = *amg.levels.front();
   const GridView g = grid_of(d);
-  if (d.dim == 3) {
-    const i64 th = static_cast<i64>(nfree) * 32;
-    k_assemble<32, double><<<grid_for(th, 256), 256, 0, amg.stream>>>(
-        g, nfree, l0.d_node_of.p, gnode.p, cmask.p, ucomp.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale,
-        l0.a.v64.p, nullptr);
+  const dim3 grid(static_cast<unsigned>((l0.nnodes + 255) / 256), d.dim == 3 ? 27 : 9);
+  // FP64 values always (CG operator, aggregation); FP32 values in the same
+  // pass for the mixed-precision preconditioner
+  if (amg.mixed()) {
+    l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
+    if (exact)
+      k_assemble_offsets<true, float><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
+                                                                    nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
+                                                                    scale, l0.a.v32.p, l0.a.v64.p);
+    else
+      k_assemble_offsets<false, float><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
+                                                                     nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
+                                                                     scale, l0.a.v32.p, l0.a.v64.p);
+    amg.level0_fp32_fresh = true;
   } else {
-    const i64 th = static_cast<i64>(nfree) * 16;
-    k_assemble<16, double><<<grid_for(th, 256), 256, 0, amg.stream>>>(
-        g, nfree, l0.d_node_of.p, gnode.p, cmask.p, ucomp.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale,
-        l0.a.v64.p, nullptr);
+    if (exact)
+      k_assemble_offsets<true, double><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
+                                                                     nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
+                                                                     scale, l0.a.v64.p, nullptr);
+    else
+      k_assemble_offsets<false, double><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
+                                                                      nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
+                                                                      scale, l0.a.v64.p, nullptr);
   }
   SIMP_CHECK_LAUNCH();
 }
@@ -425,7 +468,13 @@ Evaluation GpuProblem::evaluate() {
   SIMP_CHECK_LAUNCH();
   k_simp<<<grid_for(ne, 256), 256, 0, s>>>(ne, rho.p, d.penalty, d.emin, sf.p, df.p);
   SIMP_CHECK_LAUNCH();
-  assemble(sf.p);
+  if (amg.mf.enabled) {
+    k_convert<double, float><<<grid_for(ne, 256), 256, 0, s>>>(sf.p, sf32.p, ne);
+    SIMP_CHECK_LAUNCH();
+  }
+  // the structure-defining first assembly is bit-exact (the aggregates come
+  // from its values); later ones use fused multiply-adds
+  assemble(sf.p, !structure_built_);
   amg.setup(!structure_built_);
   structure_built_ = true;
   // one PCG per load case, warm-started from the previous displacement
@@ -471,6 +520,7 @@ Evaluation GpuProblem::evaluate() {
   ev.volume_fraction = ev.volume / domain_volume;
   if (!std::isfinite(ev.compliance)) throw Error(kNonFinite, "the compliance objective evaluated to a non-finite value");
   evaluated = true;
+  last_evaluation = ev;
   return ev;
 }
 

@@ -28,6 +28,7 @@ struct ProblemDesc {
   double radius = 1.5, vf = 0.5, x0 = 0.5, penalty = 3.0, emin = 1e-9, move = 0.2, damping = 0.5;
   bool warm = true;
   bool block_pcg = false;
+  int optimizer = 0;  // 0 OC, 1 MMA
 };
 
 struct Evaluation {
@@ -56,9 +57,14 @@ class GpuProblem {
   void get_design(double* h);
   Evaluation evaluate();
   OcStep oc_update(bool apply, double* xnew_host);
+  // MMA step with the gradients of the last evaluate (mma.cu); lambda is the
+  // volume multiplier, `bisections` the subproblem's Newton iterations.
+  OcStep mma_update(bool apply, double* xnew_host);
   void filter_forward(const double* x, double* y);   // device pointers
   void filter_adjoint(const double* v, double* g);   // device pointers
-  void assemble(const double* scale_device);
+  // exact: rounded products and sums in element order (the structure-
+  // defining first assembly); otherwise fused multiply-adds
+  void assemble(const double* scale_device, bool exact);
 
   // device state
   DBuf<double> x, xnew, rho, sf, df, dc_dphys, dc_dx, dv_dx, se, vols, tmp;
@@ -68,9 +74,22 @@ class GpuProblem {
   DBuf<double> hw;          // filter weights, slot-major
   DBuf<i32> gnode;
   DBuf<uint8_t> cmask, ucomp;
+  DBuf<uint32_t> nmask;     // per free node: free neighbours by offset
   DBuf<double> opart;
+  // matrix-free level-0 operator (mixed precision, fully free / clamped nodes)
+  DBuf<float> ke32, sf32;
+  DBuf<i32> nindex;
   void* stencil_d = nullptr;
   std::vector<double> last_compliance;
+  Evaluation last_evaluation;
+  // MMA state: previous designs, asymptotes, subproblem vectors
+  bool mma_ready = false;
+  int mma_iteration = 0;
+  double c_ref = 0.0;
+  DBuf<double> m_x1, m_x2, m_low, m_upp, m_alfa, m_beta, m_p0, m_q0, m_p, m_q, m_x, m_xsi, m_eta, m_xo, m_xsio,
+      m_etao, m_dx, m_dxsi, m_deta, m_delx, m_diagx, m_gg, mpart;
+  void mma_reduce(int k, std::vector<double>& out);
+  double mma_reduce_max(int which);
   bool evaluated = false;
   int evaluations = 0;
   double gray = 0.0;

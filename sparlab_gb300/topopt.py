@@ -75,7 +75,7 @@ class GpuSimpProblem:
     """A structured SIMP problem resident on the GPU (boundary 2 of the C ABI)."""
 
     def __init__(self, spec: ProblemSpec, precision="fp64", element_matrix=None, device=0,
-                 block_pcg=False, **amg):
+                 block_pcg=False, optimizer="oc", **amg):
         self._lib = _lib.load()
         self.spec = spec
         hx, hy = spec.lx / spec.nx, spec.ly / spec.ny
@@ -103,6 +103,7 @@ class GpuSimpProblem:
         d.move_limit, d.damping = spec.move_limit, spec.damping
         d.warm_start = int(spec.warm_start)
         d.block_pcg = int(block_pcg)
+        d.optimizer = {"oc": 0, "mma": 1}[optimizer]
         prec = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
         opts = dict(spec.amg)
         opts.update(amg)
@@ -156,6 +157,15 @@ class GpuSimpProblem:
         return OptimalityCriteriaStep(xn, st.lam, st.achieved_volume, st.max_change, st.bisections,
                                       bool(st.volume_converged))
 
+    def mma_update(self, apply=True, download=True) -> OptimalityCriteriaStep:
+        """MMA step (``MmaOptimizer::update``) with the last evaluation's
+        gradients; ``bisections`` holds the subproblem's Newton iterations."""
+        st = _lib.OcStep()
+        xn = np.zeros(self.ne) if download else None
+        self._check(self._lib.simp_mma_update(self._h, C.c_int32(int(apply)), C.byref(st), ptr(xn)))
+        return OptimalityCriteriaStep(xn, st.lam, st.achieved_volume, st.max_change, st.bisections,
+                                      bool(st.volume_converged))
+
     def iterate(self) -> _lib.IterationRecord:
         rec = _lib.IterationRecord()
         self._check(self._lib.simp_iterate(self._h, C.byref(rec)))
@@ -170,6 +180,14 @@ class GpuSimpProblem:
         """y = K_ff x on device pointers (nfree doubles each)."""
         self._check(self._lib.simp_problem_apply_operator(self._h, C.c_void_p(x_device_ptr),
                                                           C.c_void_p(y_device_ptr)))
+
+    def time_operator(self, reps: int = 20):
+        """(ms per launch, algorithmic bytes per launch) of the level-0
+        operator application the V-cycle uses, timed with CUDA events."""
+        ms, by = C.c_double(), C.c_double()
+        self._check(self._lib.simp_problem_time_operator(self._h, C.c_int32(reps), C.byref(ms),
+                                                         C.byref(by)))
+        return ms.value, by.value
 
     def filter_volume_noalloc(self, x_device_ptr: int, rho_device_ptr: int,
                               volume_device_ptr: int):

@@ -105,3 +105,33 @@ def test_first_setup_aggregates_match_oracle_linear_solver():
     for lvl in range(solver.num_levels()):
         assert st["levels"][lvl]["unknowns"] == solver.level_info(lvl)[0]
         assert st["levels"][lvl]["nonzeros"] == solver.level_info(lvl)[1]
+
+
+def test_mma_run_matches_oracle_history():
+    """run_mma on the GPU against the oracle's restatement of the reference's
+    MMA: same compliance and volume history, same subproblem iteration counts
+    within one."""
+    spec = small_q4(30, 15)
+    spec.volume_fraction = 0.4
+    spec.initial_density = 0.4
+    ref, gpu = pair(spec, optimizer="mma")
+    _, hist = ref.run_mma(10)
+    recs = TopologyOptimizer(gpu, max_iterations=10, change_tolerance=0).run()
+    for k, r in enumerate(recs):
+        assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
+        assert abs(r.volume_fraction - hist[k, 1]) < 1e-8
+        assert abs(r.lam / hist[k, 3] - 1) < 1e-5
+        assert abs(r.bisections - hist[k, 5]) <= 1
+    assert recs[-1].compliance < 0.6 * recs[0].compliance
+
+
+def test_mixed_precision_iteration_matches_oracle():
+    spec = small_hex(20, 10, 10)
+    spec.rtol = 1e-8
+    spec.initial_density = 0.2
+    ref = oracle.Problem(spec)
+    _, hist = ref.run(4)
+    gpu = GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision="mixed")
+    recs = TopologyOptimizer(gpu, max_iterations=4, change_tolerance=0).run()
+    for k, r in enumerate(recs):
+        assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])

@@ -163,3 +163,29 @@ def test_errors_are_reported_and_context_survives():
     gpu2.set_layout(3, pr.coords(), pr.free_dofs())
     gpu2.factorize(ptr, col, val)
     gpu2.solve(spec.loads[0][pr.free_dofs()])
+
+
+def test_mixed_precision_matches_fp64_solution():
+    """FP32 operator / V-cycle with FP64 refinement reaches the same
+    tolerance on the FP64 residual: solution within 1e-6 of the FP64 one."""
+    spec = P.bench_model(3, 24, 12, 8)
+    rng = P.SplitMix64(5)
+    rho = rng.uniform_array(spec.num_elements, 0.01, 1.0)
+    scale = 1e-9 + (1 - 1e-9) * rho ** 3
+    pr, ptr, col, val = system(spec, scale)
+    f = spec.loads[0][pr.free_dofs()]
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = GpuAmgCgSolver(iterative_tolerance=1e-8, precision=prec, coarse_size=60)
+        s.set_layout(3, pr.coords(), pr.free_dofs())
+        s.factorize(ptr, col, val)
+        x = s.solve(f)
+        assert s.last_error() <= 1e-8
+        out[prec] = (x, s.last_iterations())
+        s.factorize(ptr, col, val)          # reused structure: FP32 setup products
+        x2 = s.solve(f)
+        assert s.amg_stats()["reused_aggregates"]
+        assert np.linalg.norm(x2 - x) <= 1e-6 * np.linalg.norm(x)
+    xa, xb = out["fp64"][0], out["mixed"][0]
+    assert np.linalg.norm(xa - xb) <= 1e-6 * np.linalg.norm(xa)
+    assert abs((f @ xa) / (f @ xb) - 1) <= 1e-7

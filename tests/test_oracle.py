@@ -218,6 +218,23 @@ def test_finite_difference_sensitivities():
         assert abs(fd - ev["dc_dx"][e]) <= 1e-5 * abs(ev["compliance"])
 
 
+def test_mma_reaches_the_oc_optimum():
+    """tests/test_mma.cpp:419 of the reference: MMA and OC end at the same
+    design quality on the compliance problem; MMA keeps V <= V* at the end."""
+    spec = P.q4_cantilever_120x40()
+    spec.nx, spec.ny, spec.lx, spec.ly = 30, 15, 30.0, 15.0
+    spec.fixed = P.clamp_left(spec)
+    spec.loads = P.point_load(spec, [spec.node_index(30, 7)], (0.0, -1.0))[None, :]
+    spec.volume_fraction = 0.4
+    spec.initial_density = 0.4
+    pr = oracle.Problem(spec)
+    _, hm = pr.run_mma(40)
+    _, ho = pr.run(40)
+    assert abs(hm[-1, 0] / ho[-1, 0] - 1) < 0.03
+    assert hm[-1, 1] <= 0.4 + 1e-3
+    assert np.all(hm[:, 5] > 0)
+
+
 def test_oc_meets_volume_and_end_to_end_run_improves():
     spec = P.q4_cantilever_120x40()
     spec.nx, spec.ny, spec.lx, spec.ly = 30, 15, 30.0, 15.0
