@@ -10,6 +10,7 @@ API with the design copied from pinned host memory and back every step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl own|reference]
                   [--config NAME] [--precision fp64|mixed]
+                  [--warm zero|previous|projection]
 
 `--impl reference` times the CPU restatement of the reference's algorithm (the
 reference itself needs Eigen, which is absent) on the host cores, on a bounded
@@ -35,6 +36,9 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 from sparlab_gb300 import problems as P  # noqa: E402
+
+# PCG initial guess per load case (simp_problem_desc.warm_start)
+WARM = {"zero": 0, "previous": 1, "projection": 2}
 
 METRIC = "SIMP iter/s at Hex8 1.77M elts, compliance err<=1e-6: plain vs learned+mixed"
 
@@ -190,6 +194,7 @@ def run_own(args):
     dev = torch.device("cuda", local)
 
     spec = WORKLOADS[args.config][0]()
+    spec.warm_start = WARM[args.warm]
     prob = GpuSimpProblem(spec, precision=args.precision, device=local)
     lib = _lib.load()
 
@@ -268,7 +273,8 @@ def run_own(args):
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic seeded cantilever (no dataset)",
         "config": {"workload": spec.name, "elements": spec.num_elements, "free_dofs": prob.nfree,
-                   "nnz_kff": prob.nnz, "precision": args.precision, "replicas": world,
+                   "nnz_kff": prob.nnz, "precision": args.precision, "warm_start": args.warm,
+                   "replicas": world,
                    "l2": "working set (K_ff %.2f GB) larger than L2" % (nnz * 12 / 1e9),
                    "amg_levels": st["num_levels"],
                    "operator_complexity": round(st["operator_complexity"], 6),
@@ -300,6 +306,9 @@ def main():
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--warm", default="previous", choices=sorted(WARM),
+                    help="PCG initial guess: zero, the previous displacement (the reference's "
+                         "warm start) or the energy-optimal combination of the last three")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

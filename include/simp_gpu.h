@@ -147,7 +147,9 @@ typedef struct {
   double initial_density;       /* < 0: the volume fraction */
   double penalty, emin_ratio;   /* SimpOptions */
   double move_limit, damping;   /* OptimalityCriteriaOptions */
-  int32_t warm_start;           /* LinearSolverOptions::warm_start */
+  int32_t warm_start;           /* 0: zero guess; 1: previous displacement
+                                   (LinearSolverOptions::warm_start); 2: energy-
+                                   optimal combination of the last 3 displacements */
   int32_t block_pcg;            /* 1: all load cases as one block of RHS */
   int32_t optimizer;            /* simp_iterate's update: 0 OC, 1 MMA */
 } simp_problem_desc;

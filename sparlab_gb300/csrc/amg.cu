@@ -4,6 +4,7 @@
 // pcg_solve (:1152-1237).
 #include "amg.h"
 #include "dense.cuh"
+#include "galerkin.cuh"
 #include "kernels.cuh"
 #include "mfree.cuh"
 #include "nbspmv.cuh"
@@ -51,151 +52,86 @@ __global__ void k_lanczos_finish(double* __restrict__ w, const double* __restric
   }
 }
 
-template <int B, int MODE, class TV, class TX, class TA>
-void nb_apply_b(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(op.nodes) * 32;
-  k_chunk_apply<B, MODE, TV, TX, TA><<<grid_for(threads, 256), 256, 0, s>>>(op.nodes, op.row_first, op.pat,
-                                                                            op.rowptr, op.col, val, x, y, b);
-  SIMP_CHECK_LAUNCH();
+// Every operator application runs the VS-lanes-per-row kernels of
+// nbspmv.cuh; (VS, B) come from the operator's shape: B = the uniform width of
+// its column nodes (column-free decode) or 0, VS = the lanes per row chosen
+// for the arithmetic type.
+template <class TA, class F>
+void with_shape(const NbOp& op, F&& f) {
+  auto lanes = [&](auto b) {
+    switch (std::is_same<TA, double>::value ? op.lanes64 : op.lanes32) {
+      case 32: f(std::integral_constant<int, 32>{}, b); break;
+      case 8: f(std::integral_constant<int, 8>{}, b); break;
+      default: f(std::integral_constant<int, 4>{}, b); break;
+    }
+  };
+  switch (op.block) {
+    case 2: lanes(std::integral_constant<int, 2>{}); break;
+    case 3: lanes(std::integral_constant<int, 3>{}); break;
+    case 6: lanes(std::integral_constant<int, 6>{}); break;
+    default: lanes(std::integral_constant<int, 0>{}); break;
+  }
 }
 
-template <int VS, int B, int MODE, class TV, class TX, class TA>
-void rows_apply_b(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(op.rows) * VS;
-  k_rows_apply<VS, B, MODE, TV, TX, TA><<<grid_for(threads, 256), 256, 0, s>>>(
-      op.nodes, op.row_first, op.node_of, op.pat, op.rowptr, op.col, val, x, y, b, op.rows);
-  SIMP_CHECK_LAUNCH();
+// One thread per (row, lane); no grid-stride loop in the row kernels.
+unsigned rows_grid(const NbOp& op, int vs) {
+  const i64 blocks = (static_cast<i64>(op.rows) * vs + 255) / 256;
+  return static_cast<unsigned>(std::max<i64>(blocks, 1));
 }
 
 template <int MODE, class TV, class TX, class TA>
 void nb_apply(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cudaStream_t s) {
-  if constexpr (std::is_same<TA, double>::value) {
-    // FP64 arithmetic bound: few lanes per row
-    const bool wide = op.lanes > 4;
-    switch (op.block) {
-      case 2:
-        wide ? rows_apply_b<8, 2, MODE, TV, TX, TA>(op, val, x, y, b, s) : rows_apply_b<4, 2, MODE, TV, TX, TA>(op, val, x, y, b, s);
-        break;
-      case 3:
-        wide ? rows_apply_b<8, 3, MODE, TV, TX, TA>(op, val, x, y, b, s) : rows_apply_b<4, 3, MODE, TV, TX, TA>(op, val, x, y, b, s);
-        break;
-      default:
-        wide ? rows_apply_b<8, 0, MODE, TV, TX, TA>(op, val, x, y, b, s) : rows_apply_b<4, 0, MODE, TV, TX, TA>(op, val, x, y, b, s);
-        break;
-    }
-    return;
-  }
-  switch (op.block) {
-    case 2: nb_apply_b<2, MODE, TV, TX, TA>(op, val, x, y, b, s); break;
-    case 3: nb_apply_b<3, MODE, TV, TX, TA>(op, val, x, y, b, s); break;
-    default: nb_apply_b<0, MODE, TV, TX, TA>(op, val, x, y, b, s); break;
-  }
-}
-
-template <int B, class T>
-void nb_cheb_step_b(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
-                    double c1, double c2, int add_d, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(op.nodes) * 32;
-  k_chunk_cheb_step<B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.nodes, op.row_first, op.pat, op.rowptr, op.col,
-                                                                 val, d, rin, r, dn, x, dinv, static_cast<T>(c1),
-                                                                 static_cast<T>(c2), add_d);
-  SIMP_CHECK_LAUNCH();
-}
-
-template <int VS, int B, class T>
-void rows_cheb_step_b(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
-                      double c1, double c2, int add_d, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(op.rows) * VS;
-  k_rows_cheb_step<VS, B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.rows, op.node_of, op.pat, op.rowptr, op.col,
-                                                                    val, d, rin, r, dn, x, dinv, static_cast<T>(c1),
-                                                                    static_cast<T>(c2), add_d);
-  SIMP_CHECK_LAUNCH();
-}
-
-template <int VS, int B, class T>
-void rows_cheb_first_b(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
-                       double inv_theta, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(op.rows) * VS;
-  k_rows_cheb_first<VS, B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.rows, op.node_of, op.pat, op.rowptr, op.col,
-                                                                     val, x, b, r, d, dinv,
-                                                                     static_cast<T>(inv_theta));
+  with_shape<TA>(op, [&](auto vs, auto blk) {
+    constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
+    k_rows_apply<VS, B, MODE, TV, TX, TA><<<rows_grid(op, VS), 256, 0, s>>>(
+        op.node_of, op.pat, op.rowptr, op.col, val, x, y, b, op.rows);
+  });
   SIMP_CHECK_LAUNCH();
 }
 
 template <class T>
 void nb_cheb_step(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
                   double c1, double c2, int add_d, cudaStream_t s) {
-  if constexpr (std::is_same<T, double>::value) {
-    const bool wide = op.lanes > 4;
-    switch (op.block) {
-      case 2:
-        wide ? rows_cheb_step_b<8, 2, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s)
-             : rows_cheb_step_b<4, 2, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s);
-        break;
-      case 3:
-        wide ? rows_cheb_step_b<8, 3, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s)
-             : rows_cheb_step_b<4, 3, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s);
-        break;
-      default:
-        wide ? rows_cheb_step_b<8, 0, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s)
-             : rows_cheb_step_b<4, 0, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s);
-        break;
-    }
-    return;
-  }
-  switch (op.block) {
-    case 2: nb_cheb_step_b<2, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
-    case 3: nb_cheb_step_b<3, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
-    default: nb_cheb_step_b<0, T>(op, val, d, rin, r, dn, x, dinv, c1, c2, add_d, s); break;
-  }
-}
-
-template <int B, class T>
-void nb_cheb_first_b(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
-                     double inv_theta, cudaStream_t s) {
-  const i64 threads = static_cast<i64>(op.nodes) * 32;
-  k_chunk_cheb_first<B, T><<<grid_for(threads, 256), 256, 0, s>>>(op.nodes, op.row_first, op.pat, op.rowptr,
-                                                                  op.col, val, x, b, r, d, dinv,
-                                                                  static_cast<T>(inv_theta));
+  with_shape<T>(op, [&](auto vs, auto blk) {
+    constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
+    k_rows_cheb_step<VS, B, T><<<rows_grid(op, VS), 256, 0, s>>>(
+        op.rows, op.node_of, op.pat, op.rowptr, op.col, val, d, rin, r, dn, x, dinv, static_cast<T>(c1),
+        static_cast<T>(c2), add_d);
+  });
   SIMP_CHECK_LAUNCH();
 }
 
 template <class T>
 void nb_cheb_first(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
                    double inv_theta, cudaStream_t s) {
-  if constexpr (std::is_same<T, double>::value) {
-    const bool wide = op.lanes > 4;
-    switch (op.block) {
-      case 2:
-        wide ? rows_cheb_first_b<8, 2, T>(op, val, x, b, r, d, dinv, inv_theta, s)
-             : rows_cheb_first_b<4, 2, T>(op, val, x, b, r, d, dinv, inv_theta, s);
-        break;
-      case 3:
-        wide ? rows_cheb_first_b<8, 3, T>(op, val, x, b, r, d, dinv, inv_theta, s)
-             : rows_cheb_first_b<4, 3, T>(op, val, x, b, r, d, dinv, inv_theta, s);
-        break;
-      default:
-        wide ? rows_cheb_first_b<8, 0, T>(op, val, x, b, r, d, dinv, inv_theta, s)
-             : rows_cheb_first_b<4, 0, T>(op, val, x, b, r, d, dinv, inv_theta, s);
-        break;
-    }
-    return;
-  }
-  switch (op.block) {
-    case 2: nb_cheb_first_b<2, T>(op, val, x, b, r, d, dinv, inv_theta, s); break;
-    case 3: nb_cheb_first_b<3, T>(op, val, x, b, r, d, dinv, inv_theta, s); break;
-    default: nb_cheb_first_b<0, T>(op, val, x, b, r, d, dinv, inv_theta, s); break;
-  }
+  with_shape<T>(op, [&](auto vs, auto blk) {
+    constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
+    k_rows_cheb_first<VS, B, T><<<rows_grid(op, VS), 256, 0, s>>>(
+        op.rows, op.node_of, op.pat, op.rowptr, op.col, val, x, b, r, d, dinv, static_cast<T>(inv_theta));
+  });
+  SIMP_CHECK_LAUNCH();
 }
 
-// Uniform B x B blocks with node I's unknowns at B*I: the column-free path.
-int uniform_block(const std::vector<i32>& row_first, const std::vector<i32>& col_first) {
-  for (int b : {3, 2}) {
-    bool ok = row_first == col_first;
-    for (size_t I = 0; ok && I < row_first.size(); ++I) ok = row_first[I] == b * static_cast<i32>(I);
+// Width B of every column node (node J's unknowns at B*J .. B*J+B-1), or 0:
+// the column-free decode of nbspmv.cuh needs it.
+int uniform_block(const std::vector<i32>& col_first) {
+  for (int b : {6, 3, 2}) {
+    bool ok = !col_first.empty();
+    for (size_t J = 0; ok && J < col_first.size(); ++J) ok = col_first[J] == b * static_cast<i32>(J);
     if (ok) return b;
   }
   return 0;
+}
+
+// Lanes per row: FP64 products are arithmetic bound on GB300 (1/64 of the
+// FP32 rate), so FP64 rows get few lanes and short reductions; FP32 rows are
+// bandwidth bound and get 8 lanes (one 32-byte sector per step) or a whole
+// warp for long rows.
+template <class T>
+int row_lanes(const DevCsr& c) {
+  const i64 avg = c.rows > 0 ? c.nnz / c.rows : 0;
+  if (std::is_same<T, double>::value) return avg > 100 ? 8 : 4;
+  return avg >= 256 ? 32 : 8;
 }
 
 // Per-precision views of a level's arrays.
@@ -246,7 +182,9 @@ MfView mf_view(const MfOp& o) {
 template <int MODE>
 void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
   const dim3 grid((mf.nnx + kTX - 1) / kTX, (mf.nny + kTY - 1) / kTY, (mf.nz + 1 + kTZ - 1) / kTZ);
-  k_mf3_tile<MODE><<<grid, kTX * kTY * kTZ, 0, s>>>(mf_view(mf), a);
+  KeF32 ke;
+  std::copy(mf.ke_host, mf.ke_host + 24 * 24, ke.k);
+  k_mf3_tile<MODE><<<grid, kTX * kTY * kTZ, 0, s>>>(mf_view(mf), a, ke);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -285,6 +223,18 @@ void mf_cheb_step(const MfOp& mf, i32 nodes, const float* d, const float* rin, f
     return;
   }
   k_mf_cheb_step<<<grid_for(nodes, 256), 256, 0, s>>>(mf_view(mf), nodes, d, rin, r, dn, x, dinv, c1, c2, add_d);
+  SIMP_CHECK_LAUNCH();
+}
+
+void mf_apply(const MfOp& mf, i32 nodes, const float* x, float* y, cudaStream_t s) {
+  if (mf.dim == 3) {
+    MfArgs a{};
+    a.x = x;
+    a.y = y;
+    mf3<0>(mf, a, s);
+    return;
+  }
+  k_mf_apply<0, float><<<grid_for(nodes, 256), 256, 0, s>>>(mf_view(mf), nodes, x, y, nullptr);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -338,11 +288,11 @@ void GpuAmg::make_ops(size_t l) {
   lv.opA.pat = lv.d_apat.view();
   lv.opA.rowptr = lv.a.ptr.p;
   lv.opA.col = lv.a.col.p;
-  lv.opA.block = uniform_block(lv.first, lv.first);
+  lv.opA.block = uniform_block(lv.first);
   lv.opA.node_of = lv.d_node_of.p;
   lv.opA.rows = lv.n;
-  auto lanes = [](const DevCsr& c) { return c.rows > 0 && c.nnz / c.rows > 100 ? 8 : 4; };
-  lv.opA.lanes = lanes(lv.a);
+  lv.opA.lanes32 = row_lanes<float>(lv.a);
+  lv.opA.lanes64 = row_lanes<double>(lv.a);
   if (l + 1 < levels.size()) {
     Level& nv = *levels[l + 1];
     lv.opP.nodes = lv.nnodes;
@@ -350,19 +300,21 @@ void GpuAmg::make_ops(size_t l) {
     lv.opP.pat = lv.d_ppat.view();
     lv.opP.rowptr = lv.p.ptr.p;
     lv.opP.col = lv.p.col.p;
-    lv.opP.block = 0;
+    lv.opP.block = uniform_block(nv.first);
     lv.opP.node_of = lv.d_node_of.p;
     lv.opP.rows = lv.n;
-    lv.opP.lanes = lanes(lv.p);
+    lv.opP.lanes32 = row_lanes<float>(lv.p);
+    lv.opP.lanes64 = row_lanes<double>(lv.p);
     lv.opR.nodes = nv.nnodes;
     lv.opR.row_first = nv.d_first.p;
     lv.opR.pat = lv.d_rpat.view();
     lv.opR.rowptr = lv.r.ptr.p;
     lv.opR.col = lv.r.col.p;
-    lv.opR.block = 0;
+    lv.opR.block = uniform_block(lv.first);
     lv.opR.node_of = nv.d_node_of.p;
     lv.opR.rows = nv.n;
-    lv.opR.lanes = lanes(lv.r);
+    lv.opR.lanes32 = row_lanes<float>(lv.r);
+    lv.opR.lanes64 = row_lanes<double>(lv.r);
   }
 }
 
@@ -471,7 +423,9 @@ void GpuAmg::numeric_level(size_t l) {
       lv.x32.alloc(n);
       lv.b32.alloc(n);
       convert(tmp.p, lv.x32.p, n, stream);
-      nb_apply<0, float, float, float>(lv.opA, lv.a.v32.p, lv.x32.p, lv.b32.p, nullptr, stream);
+      // level 0 of a structured grid: the matrix-free operator the smoother uses
+      if (l == 0 && mf.enabled) mf_apply(mf, lv.nnodes, lv.x32.p, lv.b32.p, stream);
+      else nb_apply<0, float, float, float>(lv.opA, lv.a.v32.p, lv.x32.p, lv.b32.p, nullptr, stream);
       convert(lv.b32.p, w.p, n, stream);
     }
     else nb_apply<0, double, double, double>(lv.opA, lv.a.v64.p, tmp.p, w.p, nullptr, stream);
@@ -579,6 +533,21 @@ void GpuAmg::build_transfer(size_t l) {
   nv.apat = pattern_product(lv.rpat, lv.appat);
   finish_offsets(nv.apat, nv.first);
   const std::vector<i32> sym_t = pattern_transpose_slots(nv.apat);
+  // shared-memory shapes of the warp-per-node products
+  auto shape = [](const NodePattern& out, const std::vector<i32>& row_first, const NodePattern* inner) {
+    WarpRows w;
+    for (i32 I = 0; I < out.rows; ++I) {
+      const i64 acc = static_cast<i64>(row_first[I + 1] - row_first[I]) * out.rowlen[I];
+      w.acc = static_cast<int>(std::max<i64>(w.acc, std::min<i64>(acc, 1 << 30)));
+      w.slots = std::max(w.slots, out.ptr[I + 1] - out.ptr[I]);
+    }
+    if (inner)
+      for (i32 J = 0; J < inner->rows; ++J) w.inner = std::max(w.inner, inner->ptr[J + 1] - inner->ptr[J]);
+    return w;
+  };
+  lv.wr_p = shape(lv.ppat, lv.first, nullptr);
+  lv.wr_ap = shape(lv.appat, lv.first, &lv.ppat);
+  lv.wr_rap = shape(nv.apat, nv.first, &lv.appat);
   lv.d_ppat.upload(lv.ppat);
   lv.d_rpat.upload(lv.rpat);
   lv.d_appat.upload(lv.appat);
@@ -611,6 +580,23 @@ void GpuAmg::build_transfer(size_t l) {
   levels.push_back(std::move(nx));
 }
 
+// Launches a warp-per-row-node product with its shared-memory shape; false
+// (nothing launched) when one warp's accumulator would not fit.
+template <class T, class... KArgs, class... Args>
+bool launch_rows(void (*kernel)(i32, WarpRows, KArgs...), i32 nodes, const WarpRows& w, cudaStream_t s,
+                 Args... args) {
+  const size_t per_warp = static_cast<size_t>(w.acc) * sizeof(T) + static_cast<size_t>(2 * w.slots + w.inner) * 4;
+  if (per_warp > 200 * 1024) return false;
+  const int warps = static_cast<int>(std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp)));
+  const size_t smem = per_warp * warps;
+  if (smem > 48 * 1024)
+    SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  const i64 blocks = std::max<i64>(1, std::min<i64>((static_cast<i64>(nodes) + warps - 1) / warps, 152 * 64));
+  kernel<<<static_cast<unsigned>(blocks), warps * 32, smem, s>>>(nodes, w, args...);
+  SIMP_CHECK_LAUNCH();
+  return true;
+}
+
 // Numeric P, R, AP, RAP and symmetrisation (Multigrid.cpp:671-716, 1047-1055).
 template <class T>
 static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t stream) {
@@ -619,7 +605,10 @@ static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t 
   const T* phat = f32 ? reinterpret_cast<const T*>(lv.phat32.p) : reinterpret_cast<const T*>(lv.phat64.p);
   T* raw = f32 ? reinterpret_cast<T*>(lv.raw32.p) : reinterpret_cast<T*>(lv.raw64.p);
   const double omega = g.opt.damping / lv.lambda;
-  {
+  const int b1 = uniform_block(nv.first);
+  if (!launch_rows<T>(k_prolongator_rows<T>, lv.nnodes, lv.wr_p, stream, lv.d_first.p, nv.d_first.p, lv.d_agg.p,
+                      lv.d_apat.view(), lv.a.ptr.p, A(lv.a), lv.d_ppat.view(), lv.p.ptr.p, A(lv.p),
+                      lv.phat_ptr.p, phat, lv.dinv64.p, omega)) {
     const i64 th = static_cast<i64>(lv.n) * 8;
     k_prolongator<8, T><<<grid_for(th, 256), 256, 0, stream>>>(
         lv.n, lv.d_node_of.p, lv.d_first.p, nv.d_first.p, lv.d_agg.p, lv.d_apat.view(), lv.a.ptr.p, A(lv.a),
@@ -633,14 +622,17 @@ static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t 
         lv.d_ppat.view(), lv.p.ptr.p, A(lv.p));
     SIMP_CHECK_LAUNCH();
   }
-  {
+  if (!launch_rows<T>(k_ap_rows<T>, lv.nnodes, lv.wr_ap, stream, lv.d_first.p, b1, lv.d_apat.view(), lv.a.ptr.p,
+                      A(lv.a), lv.d_ppat.view(), lv.p.ptr.p, A(lv.p), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap))) {
     const i64 th = static_cast<i64>(lv.n) * 32;
     k_product_ap<32, T><<<grid_for(th, 256), 256, 0, stream>>>(
         lv.n, lv.d_node_of.p, lv.d_first.p, nv.d_first.p, lv.d_apat.view(), lv.a.ptr.p, A(lv.a),
         lv.d_ppat.view(), lv.p.ptr.p, A(lv.p), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap));
     SIMP_CHECK_LAUNCH();
   }
-  {
+  if (!launch_rows<T>(k_rap_rows<T>, nv.nnodes, lv.wr_rap, stream, nv.d_first.p, lv.d_first.p, b1,
+                      lv.d_rpat.view(), lv.r.ptr.p, A(lv.r), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap),
+                      nv.d_apat.view(), nv.a.ptr.p, raw)) {
     const i64 th = static_cast<i64>(nv.n) * 32;
     k_product_rap<32, T><<<grid_for(th, 256), 256, 0, stream>>>(
         nv.n, nv.d_node_of.p, nv.d_first.p, lv.d_first.p, lv.d_rpat.view(), lv.r.ptr.p, A(lv.r),

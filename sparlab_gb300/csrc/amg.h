@@ -58,10 +58,17 @@ struct NbOp {
   NodeView pat{nullptr, nullptr, nullptr};
   const i32* rowptr = nullptr;
   const i32* col = nullptr;
-  int block = 0;                // uniform B x B blocks without columns (2, 3), or 0
+  int block = 0;                // uniform column-node width (2, 3, 6): no column reads; or 0
   const i32* node_of = nullptr; // row -> row node
   i32 rows = 0;
-  int lanes = 4;                // lanes per row of the FP64 kernel
+  int lanes32 = 8, lanes64 = 4; // lanes per row of the FP32 / FP64 kernels
+};
+
+// Shared-memory shape of a warp-per-row-node product (galerkin.cuh).
+struct WarpRows {
+  int acc = 0;    // max rows x row length of the output, per row node
+  int slots = 0;  // max output slots per row node
+  int inner = 0;  // max slots of an inner row
 };
 
 struct Level {
@@ -84,6 +91,7 @@ struct Level {
   DBuf<double> phat64;
   DBuf<float> phat32;
   NodePattern ppat, rpat, appat;
+  WarpRows wr_p, wr_ap, wr_rap;
   DevPattern d_ppat, d_rpat, d_appat;
   DBuf<i32> d_r_to_p, d_sym_t;
   DevCsr p, r, ap;
@@ -106,6 +114,7 @@ struct MfOp {
   const i32* nindex = nullptr;  // grid node -> free node or -1
   const float* ke = nullptr;    // K_e^0, FP32
   const float* scale = nullptr; // s_e, FP32
+  float ke_host[24 * 24] = {};  // K_e^0, FP32 (kernel parameter of the tiled 3-D kernel)
 };
 
 struct AmgStats {

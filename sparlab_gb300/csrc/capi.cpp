@@ -417,7 +417,8 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     if (!(d.move > 0.0 && d.move <= 1.0)) throw Error(kBadInput, "optimizer.move_limit must lie in (0, 1]");
     d.damping = dsc->damping;
     if (!(d.damping > 0.0 && d.damping <= 1.0)) throw Error(kBadInput, "optimizer.damping must lie in (0, 1]");
-    d.warm = dsc->warm_start != 0;
+    if (dsc->warm_start < 0 || dsc->warm_start > 2) throw Error(kBadInput, "warm_start must be 0, 1 or 2");
+    d.warm = dsc->warm_start;
     d.block_pcg = dsc->block_pcg != 0;
     if (dsc->optimizer != 0 && dsc->optimizer != 1) throw Error(kBadInput, "unknown optimizer (expected 0 OC, 1 MMA)");
     d.optimizer = dsc->optimizer;

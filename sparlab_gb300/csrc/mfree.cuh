@@ -140,13 +140,20 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 
 // ---------------------------------------------------------------------------
 // Tiled 3-D variant: a block owns a 32 x 4 x 2 tile of grid nodes; the tile's
-// node values plus a one-node halo, the scales of the 33 x 5 x 3 cells that
-// touch it and K_e^0 (as float4 rows of its 3 x 3 node blocks) are staged in
-// shared memory once, so each node's 64 (cell, corner) terms read shared
-// memory only.  Modes: 0 y = A x, 1 y = b - A x, 3 Chebyshev step, 4 Chebyshev
-// first step (same epilogues as the other operator kernels).
+// node values plus a one-node halo (one shared array per component) and the
+// scales of the 33 x 5 x 3 cells that touch it are staged in shared memory
+// once.  Each thread loads its 27 neighbour values into registers and sums
+// the 64 (cell, corner) 3 x 3 block products with K_e^0 taken from the kernel
+// parameter (a __grid_constant__ struct indexed by compile-time constants,
+// so its entries are constant-bank operands of the FMAs rather than loads).
+// Modes: 0 y = A x, 1 y = b - A x, 3 Chebyshev step, 4 Chebyshev first step
+// (same epilogues as the other operator kernels).
 // ---------------------------------------------------------------------------
 constexpr int kTX = 32, kTY = 4, kTZ = 2;
+
+struct KeF32 {
+  float k[24 * 24];  // K_e^0, row-major
+};
 
 struct MfArgs {
   const float* x;     // input (d for the Chebyshev step)
@@ -161,32 +168,29 @@ struct MfArgs {
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a) {
-  __shared__ float4 xh[kTZ + 2][kTY + 2][kTX + 2];
+__global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, const __grid_constant__ KeF32 ke) {
+  __shared__ float xh[3][kTZ + 2][kTY + 2][kTX + 2];
   __shared__ float sc[kTZ + 1][kTY + 1][kTX + 1];
-  __shared__ float4 kq[8][8][3];
   const int tid = threadIdx.x;
   const i32 x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * kTZ;
   const i32 nnz = m.nz + 1;
-  // K_e^0 blocks: kq[aI][b][ka] = row 3 aI + ka, columns 3 b .. 3 b + 2
-  for (int e = tid; e < 8 * 8 * 3; e += kTX * kTY * kTZ) {
-    const int aI = e / 24, b = (e / 3) % 8, ka = e % 3;
-    const float* row = m.ke + (3 * aI + ka) * 24 + 3 * b;
-    kq[aI][b][ka] = make_float4(row[0], row[1], row[2], 0.0f);
-  }
   // node values of the tile and its halo (zero outside the grid / clamped)
   for (int e = tid; e < (kTZ + 2) * (kTY + 2) * (kTX + 2); e += kTX * kTY * kTZ) {
     const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
     const i32 gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
-    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
     if (gx >= 0 && gx < m.nnx && gy >= 0 && gy < m.nny && gz >= 0 && gz < nnz) {
       const i32 J = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
       if (J >= 0) {
         const float* p = a.x + static_cast<i64>(J) * 3;
-        v = make_float4(p[0], p[1], p[2], 0.0f);
+        v0 = p[0];
+        v1 = p[1];
+        v2 = p[2];
       }
     }
-    xh[hz][hy][hx] = v;
+    xh[0][hz][hy][hx] = v0;
+    xh[1][hz][hy][hx] = v1;
+    xh[2][hz][hy][hx] = v2;
   }
   // cell scales (zero outside the grid)
   for (int e = tid; e < (kTZ + 1) * (kTY + 1) * (kTX + 1); e += kTX * kTY * kTZ) {
@@ -203,6 +207,16 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a) 
   if (gx >= m.nnx || gy >= m.nny || gz >= nnz) return;
   const i32 I = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
   if (I < 0) return;
+  // the 27 neighbour values, nb[k][z][y][x] for offsets z, y, x in {0, 1, 2}
+  float nb[3][3][3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int z = 0; z < 3; ++z)
+#pragma unroll
+      for (int y = 0; y < 3; ++y)
+#pragma unroll
+        for (int x = 0; x < 3; ++x) nb[k][z][y][x] = xh[k][tz + z][ty + y][tx + x];
   float out0 = 0.0f, out1 = 0.0f, out2 = 0.0f;
 #pragma unroll
   for (int dz = -1; dz <= 0; ++dz)
@@ -219,11 +233,14 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a) 
           const int bx = (b == 1 || b == 2 || b == 5 || b == 6) ? 1 : 0;
           const int by = (b == 2 || b == 3 || b == 6 || b == 7) ? 1 : 0;
           const int bz = b >= 4 ? 1 : 0;
-          const float4 xv = xh[tz + dz + 1 + bz][ty + dy + 1 + by][tx + dx + 1 + bx];
-          const float4 k0 = kq[aI][b][0], k1 = kq[aI][b][1], k2 = kq[aI][b][2];
-          a0 = fmaf(k0.x, xv.x, fmaf(k0.y, xv.y, fmaf(k0.z, xv.z, a0)));
-          a1 = fmaf(k1.x, xv.x, fmaf(k1.y, xv.y, fmaf(k1.z, xv.z, a1)));
-          a2 = fmaf(k2.x, xv.x, fmaf(k2.y, xv.y, fmaf(k2.z, xv.z, a2)));
+          const int nz_ = dz + 1 + bz, ny_ = dy + 1 + by, nx_ = dx + 1 + bx;
+#pragma unroll
+          for (int kb = 0; kb < 3; ++kb) {
+            const float xv = nb[kb][nz_][ny_][nx_];
+            a0 = fmaf(ke.k[(3 * aI + 0) * 24 + 3 * b + kb], xv, a0);
+            a1 = fmaf(ke.k[(3 * aI + 1) * 24 + 3 * b + kb], xv, a1);
+            a2 = fmaf(ke.k[(3 * aI + 2) * 24 + 3 * b + kb], xv, a2);
+          }
         }
         out0 = fmaf(s, a0, out0);
         out1 = fmaf(s, a1, out1);

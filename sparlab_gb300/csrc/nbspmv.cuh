@@ -1,16 +1,17 @@
-// Node-chunked sparse operator applications.
+// Sparse operator applications of the AMG levels (A_l, P_l, R_l).
 //
-// Every level operator (A_l, P_l, R_l) is a scalar CSR whose rows of one
-// node share their length and column list, and are stored back to back.  One
-// warp owns one row node: for each of its (<= 6) rows the lanes stride across
-// the row's contiguous values (coalesced loads), then the row sums are
-// reduced with a fixed butterfly and lane r writes row r, so every output is
-// written once and the result does not depend on timing.
+// Every level operator is a scalar CSR whose rows of one node share their
+// length and column list (grouped by whole column nodes), stored back to
+// back.  VS consecutive lanes own one row: they stride across its contiguous
+// values (VS = 8 FP32 lanes read one 32-byte sector per step), then reduce
+// with a fixed log2(VS)-step butterfly, so every output is written once by
+// lane 0 of its group and the result does not depend on timing.
 //
-// Level 0 of a grid whose nodes are all fully free or fully clamped has
-// uniform B x B blocks (B = 2 or 3); there the column of entry w of a row is
-// B * nbr[slot w / B] + w % B, so the column array is not read at all and the
-// index traffic is one slot record per block.
+// Where every column node has the same width B (B = 2 or 3 on a level 0 whose
+// nodes are fully free or fully clamped, B = 6 (3-D) or 3 (2-D) on coarse
+// levels of full-rank aggregates), the column of entry w of a row is
+// B * nbr[slot w / B] + w % B: the column array is not read and the index
+// traffic is one slot record per block.
 #pragma once
 
 #include "kernels.cuh"
@@ -18,140 +19,11 @@
 namespace simp {
 namespace {
 
-constexpr int kMaxNode = 6;  // unknowns per node: 2-3 on level 0, rank <= 6 below
-
-// Row sums of one row node; returns with acc[r] (r < nr) summed over the warp
-// in every lane.  B > 0: uniform-block level 0 without the column array.
-template <int B, class TV, class TX, class TA>
-__device__ __forceinline__ void chunk_row_dots(i32 I, int lane, bool valid, const i32* __restrict__ row_first,
-                                               NodeView pat, const i32* __restrict__ rowptr,
-                                               const i32* __restrict__ col, const TV* __restrict__ val,
-                                               const TX* __restrict__ x, int& nr, i32& r0, TA (&acc)[kMaxNode]) {
-#pragma unroll
-  for (int r = 0; r < kMaxNode; ++r) acc[r] = TA(0);
-  nr = 0;
-  r0 = 0;
-  if (valid) {
-    r0 = row_first[I];
-    nr = row_first[I + 1] - r0;
-    const i32 base = rowptr[r0];
-    const i32 len = nr > 0 ? rowptr[r0 + 1] - base : 0;
-    const i32 s0 = pat.ptr[I];
-#pragma unroll
-    for (int r = 0; r < kMaxNode; ++r) {
-      if (r < nr) {
-        const TV* v = val + base + r * len;
-        TA s = TA(0);
-        if constexpr (B > 0) {
-          for (i32 w = lane; w < len; w += 32) {
-            const i32 t = w / B;
-            const i32 c = B * pat.nbr[s0 + t] + (w - B * t);
-            s += static_cast<TA>(v[w]) * static_cast<TA>(x[c]);
-          }
-        } else {
-          const i32* cl = col + base + r * len;
-          for (i32 w = lane; w < len; w += 32) s += static_cast<TA>(v[w]) * static_cast<TA>(x[cl[w]]);
-        }
-        acc[r] = s;
-      }
-    }
-  }
-#pragma unroll
-  for (int r = 0; r < kMaxNode; ++r) {
-    if (r < nr) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
-    }
-  }
-}
-
-// mode 0: y = A x ; 1: y = b - A x ; 2: y += A x
-template <int B, int MODE, class TV, class TX, class TA>
-__global__ void __launch_bounds__(256) k_chunk_apply(i32 nodes, const i32* __restrict__ row_first, NodeView pat,
-                                                     const i32* __restrict__ rowptr, const i32* __restrict__ col,
-                                                     const TV* __restrict__ val, const TX* __restrict__ x,
-                                                     TX* __restrict__ y, const TX* __restrict__ b) {
-  const i32 I = static_cast<i32>((blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (I >= nodes) return;  // whole warps leave together
-  TA acc[kMaxNode];
-  int nr;
-  i32 r0;
-  chunk_row_dots<B, TV, TX, TA>(I, lane, true, row_first, pat, rowptr, col, val, x, nr, r0, acc);
-#pragma unroll
-  for (int r = 0; r < kMaxNode; ++r) {
-    if (r < nr && lane == r) {
-      const i32 row = r0 + r;
-      if (MODE == 0) y[row] = static_cast<TX>(acc[r]);
-      else if (MODE == 1) y[row] = b[row] - static_cast<TX>(acc[r]);
-      else y[row] += static_cast<TX>(acc[r]);
-    }
-  }
-}
-
-// Chebyshev step: r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ d]) + dn
-template <int B, class T>
-__global__ void __launch_bounds__(256) k_chunk_cheb_step(i32 nodes, const i32* __restrict__ first, NodeView pat,
-                                                         const i32* __restrict__ rowptr, const i32* __restrict__ col,
-                                                         const T* __restrict__ val, const T* __restrict__ d,
-                                                         const T* __restrict__ r_in, T* __restrict__ r,
-                                                         T* __restrict__ dn, T* __restrict__ x,
-                                                         const T* __restrict__ dinv, T c1, T c2, int add_d) {
-  const i32 I = static_cast<i32>((blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (I >= nodes) return;
-  T acc[kMaxNode];
-  int nr;
-  i32 r0;
-  chunk_row_dots<B, T, T, T>(I, lane, true, first, pat, rowptr, col, val, d, nr, r0, acc);
-#pragma unroll
-  for (int q = 0; q < kMaxNode; ++q) {
-    if (q < nr && lane == q) {
-      const i32 row = r0 + q;
-      const T ri = r_in[row] - acc[q];
-      r[row] = ri;
-      const T di = c1 * d[row] + c2 * dinv[row] * ri;
-      dn[row] = di;
-      T xi = x[row];
-      if (add_d) xi = xi + d[row];
-      x[row] = xi + di;
-    }
-  }
-}
-
-// r = b - A x ; d = dinv r / theta
-template <int B, class T>
-__global__ void __launch_bounds__(256) k_chunk_cheb_first(i32 nodes, const i32* __restrict__ first, NodeView pat,
-                                                          const i32* __restrict__ rowptr, const i32* __restrict__ col,
-                                                          const T* __restrict__ val, const T* __restrict__ x,
-                                                          const T* __restrict__ b, T* __restrict__ r,
-                                                          T* __restrict__ d, const T* __restrict__ dinv,
-                                                          T inv_theta) {
-  const i32 I = static_cast<i32>((blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (I >= nodes) return;
-  T acc[kMaxNode];
-  int nr;
-  i32 r0;
-  chunk_row_dots<B, T, T, T>(I, lane, true, first, pat, rowptr, col, val, x, nr, r0, acc);
-#pragma unroll
-  for (int q = 0; q < kMaxNode; ++q) {
-    if (q < nr && lane == q) {
-      const i32 row = r0 + q;
-      const T ri = b[row] - acc[q];
-      r[row] = ri;
-      d[row] = dinv[row] * ri * inv_theta;
-    }
-  }
-}
-
-// VS lanes per scalar row (VS = 4 or 8), for operators whose arithmetic is
-// the bottleneck (FP64 on GB300 runs at 1/64 of the FP32 rate): a VS-lane
-// reduction costs log2(VS) adds per row instead of five.  Lanes of a row
-// read consecutive values (32-byte sectors fully used).
+// mode 0: y = A x ; 1: y = b - A x ; 2: y += A x.  TA is the arithmetic
+// type (FP64 rows get VS = 4: GB300's FP64 rate is 1/64 of FP32, and a short
+// reduction keeps the FP64 pipe on the products).
 template <int VS, int B, int MODE, class TV, class TX, class TA>
-__global__ void __launch_bounds__(256) k_rows_apply(i32 nodes, const i32* __restrict__ row_first,
-                                                    const i32* __restrict__ node_of, NodeView pat,
+__global__ void __launch_bounds__(256) k_rows_apply(const i32* __restrict__ node_of, NodeView pat,
                                                     const i32* __restrict__ rowptr, const i32* __restrict__ col,
                                                     const TV* __restrict__ val, const TX* __restrict__ x,
                                                     TX* __restrict__ y, const TX* __restrict__ b, i32 rows) {
@@ -180,8 +52,6 @@ __global__ void __launch_bounds__(256) k_rows_apply(i32 nodes, const i32* __rest
     else if (MODE == 1) y[row] = b[row] - static_cast<TX>(s);
     else y[row] += static_cast<TX>(s);
   }
-  (void)row_first;
-  (void)nodes;
 }
 
 template <int VS, int B, class TV, class TX>
@@ -208,7 +78,7 @@ __device__ __forceinline__ TX rows_dot(i32 row, int lane, bool valid, const i32*
   return s;
 }
 
-// Chebyshev step with VS lanes per row (FP64 path).
+// Chebyshev step: r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ d]) + dn
 template <int VS, int B, class T>
 __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __restrict__ node_of, NodeView pat,
                                                         const i32* __restrict__ rowptr, const i32* __restrict__ col,
@@ -232,6 +102,7 @@ __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __r
   }
 }
 
+// r = b - A x ; d = dinv r / theta
 template <int VS, int B, class T>
 __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __restrict__ node_of, NodeView pat,
                                                          const i32* __restrict__ rowptr, const i32* __restrict__ col,

@@ -265,6 +265,7 @@ void GpuProblem::build() {
       mf.gnode = gnode.p;
       mf.nindex = nindex.p;
       mf.ke = ke32.p;
+      std::copy(k32.begin(), k32.end(), mf.ke_host);
       mf.scale = sf32.p;
     }
   }
@@ -291,6 +292,12 @@ void GpuProblem::build() {
     for (i32 i = 0; i < nfree; ++i) bh[static_cast<size_t>(l) * nfree + i] = d.loads[l * ndof + free_dofs_[i]];
   b.upload(bh);
   u.alloc(static_cast<size_t>(nfree) * d.nloads);
+  if (d.warm == 2) {
+    hist.alloc(static_cast<size_t>(nfree) * d.nloads * kHistory);
+    khist.alloc(static_cast<size_t>(nfree) * kHistory);
+    hpart.alloc(static_cast<size_t>(kRedBlocks) * (kHistory * (kHistory + 1) / 2 + kHistory));
+    hist_count.assign(static_cast<size_t>(d.nloads), 0);
+  }
   u.zero();
   weights_d.upload(d.weights);
   // element volumes (uniform cells)
@@ -432,31 +439,28 @@ void GpuProblem::get_design(double* h) {
 void GpuProblem::assemble(const double* scale, bool exact) {
   Level& l0 = *amg.levels.front();
   const GridView g = grid_of(d);
-  const dim3 grid(static_cast<unsigned>((l0.nnodes + 255) / 256), d.dim == 3 ? 27 : 9);
+  const int offsets = d.dim == 3 ? 27 : 9;
+  const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
+  const size_t smem = assemble_smem(d.dim);
   // FP64 values always (CG operator, aggregation); FP32 values in the same
   // pass for the mixed-precision preconditioner
+  auto launch = [&](auto kernel, auto* out, double* out64) {
+    SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    kernel<<<blocks, offsets * kAsmTile, smem, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p, nmask.p,
+                                                              l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale, out,
+                                                              out64);
+    SIMP_CHECK_LAUNCH();
+  };
+  if (l0.nnodes == 0) return;
   if (amg.mixed()) {
     l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
-    if (exact)
-      k_assemble_offsets<true, float><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
-                                                                    nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
-                                                                    scale, l0.a.v32.p, l0.a.v64.p);
-    else
-      k_assemble_offsets<false, float><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
-                                                                     nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
-                                                                     scale, l0.a.v32.p, l0.a.v64.p);
+    if (exact) launch(k_assemble_tiles<true, float>, l0.a.v32.p, l0.a.v64.p);
+    else launch(k_assemble_tiles<false, float>, l0.a.v32.p, l0.a.v64.p);
     amg.level0_fp32_fresh = true;
   } else {
-    if (exact)
-      k_assemble_offsets<true, double><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
-                                                                     nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
-                                                                     scale, l0.a.v64.p, nullptr);
-    else
-      k_assemble_offsets<false, double><<<grid, 256, 0, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
-                                                                      nmask.p, l0.d_apat.view(), l0.a.ptr.p, ke_d.p,
-                                                                      scale, l0.a.v64.p, nullptr);
+    if (exact) launch(k_assemble_tiles<true, double>, l0.a.v64.p, nullptr);
+    else launch(k_assemble_tiles<false, double>, l0.a.v64.p, nullptr);
   }
-  SIMP_CHECK_LAUNCH();
 }
 
 Evaluation GpuProblem::evaluate() {
@@ -482,7 +486,8 @@ Evaluation GpuProblem::evaluate() {
   for (int l = 0; l < d.nloads; ++l) {
     double* ul = u.p + static_cast<size_t>(l) * nfree;
     const double* bl = b.p + static_cast<size_t>(l) * nfree;
-    if (!d.warm || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, s));
+    if (d.warm == 0 || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, s));
+    else if (d.warm == 2 && hist_count[l] > 0) projected_start(l, ul);
     const GpuAmg::PcgResult r = amg.solve(bl, ul);
     if (!r.converged) {
       std::ostringstream os;
@@ -502,6 +507,7 @@ Evaluation GpuProblem::evaluate() {
     SIMP_CUDA(cudaMemcpyAsync(&c, amg.scal.p + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
     SIMP_CUDA(cudaStreamSynchronize(s));
     last_compliance[l] = c;
+    if (d.warm == 2) record_history(l, ul);
     ev.compliance += d.weights[l] * c;
   }
   ++evaluations;

@@ -15,6 +15,8 @@
 
 namespace simp {
 
+constexpr int kHistory = 3;  // displacements kept per load case by warm start 2
+
 struct ProblemDesc {
   int dim = 3;
   i32 nx = 0, ny = 0, nz = 1;
@@ -26,7 +28,7 @@ struct ProblemDesc {
   std::vector<double> loads;    // nloads x ndof
   std::vector<double> weights;  // normalised
   double radius = 1.5, vf = 0.5, x0 = 0.5, penalty = 3.0, emin = 1e-9, move = 0.2, damping = 0.5;
-  bool warm = true;
+  int warm = 1;  // 0 zero start, 1 previous displacement, 2 projection on the last kHistory
   bool block_pcg = false;
   int optimizer = 0;  // 0 OC, 1 MMA
 };
@@ -90,6 +92,11 @@ class GpuProblem {
       m_etao, m_dx, m_dxsi, m_deta, m_delx, m_diagx, m_gg, mpart;
   void mma_reduce(int k, std::vector<double>& out);
   double mma_reduce_max(int which);
+  // warm start 2 (warmstart.cu): newest-first displacement history per load
+  DBuf<double> hist, khist, hpart;
+  std::vector<int> hist_count;
+  void projected_start(int l, double* ul);
+  void record_history(int l, const double* ul);
   bool evaluated = false;
   int evaluations = 0;
   double gray = 0.0;

@@ -21,73 +21,93 @@ __device__ __forceinline__ int corner_of(int dx, int dy, int dz) { return 4 * dz
 
 // K_ff values into the free-free pattern, row-owner gather: entry
 // (row (I, ka), column (J, kb)) = sum over the cells shared by I and J, in
-// ascending cell order, of s_e * K_e^0(J kb, I ka), with rounded products and
-// sums in the order of the reference's scatter (src/fem/Assembler.cpp:
-// 182-214), so the FP64 values equal a sequential assembly bit for bit.
-// Offset-major assembly: blockIdx.y selects one of the 27 (9) neighbour
-// offsets o, threads run over free nodes I, so for a given o all lanes walk
-// the same cells with the same corner indices and read the same K_e^0
-// entries (shared-memory broadcast).  nmask[I] has bit o set when the
-// neighbour at offset o is a free node; its slot is the rank of o among the
-// set bits (the node pattern lists neighbours in ascending order, which is
-// ascending offset order).  EXACT: rounded products and sums in element order
-// (bit-identical to a sequential scatter); otherwise fused multiply-adds.
+// ascending cell order, of s_e * K_e^0(J kb, I ka).  EXACT: rounded products
+// and sums in the order of the reference's scatter (src/fem/Assembler.cpp:
+// 182-214), so the FP64 values equal a sequential assembly bit for bit;
+// otherwise fused multiply-adds.
+//
+// One block per tile of 32 consecutive free nodes; warp o of the block owns
+// neighbour offset o (27 in 3-D, 9 in 2-D) and lane i node I0 + i, so a
+// warp's lanes walk the same cells with the same corner indices (uniform
+// trip counts, K_e^0 read as a shared-memory broadcast).  Each thread's 3 x 3
+// block goes to a shared staging copy of the tile's rows, which are one
+// contiguous range of the CSR values; the block then writes that range with
+// coalesced stores.  nmask[I] has bit o set when the neighbour at offset o is
+// a free node; its slot is the rank of o among the set bits (the node
+// pattern lists neighbours in ascending order = ascending offset order).
+constexpr int kAsmTile = 32;
+
+inline size_t assemble_smem(int dim) {
+  const int ed = dim == 3 ? 24 : 8, rowvals = dim == 3 ? 3 * 81 : 2 * 18;
+  return sizeof(double) * (static_cast<size_t>(ed) * ed + static_cast<size_t>(kAsmTile) * rowvals);
+}
+
 template <bool EXACT, class TO>
-__global__ void __launch_bounds__(256) k_assemble_offsets(
+__global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
     GridView g, i32 nodes, const i32* __restrict__ first, const i32* __restrict__ gnode,
     const uint8_t* __restrict__ cmask, const uint32_t* __restrict__ nmask, NodeView a,
     const i32* __restrict__ rowptr, const double* __restrict__ ke, const double* __restrict__ scale,
     TO* __restrict__ val, double* __restrict__ val64) {
-  __shared__ double ks[24 * 24];
+  extern __shared__ double smem_asm[];
   const int ed = g.dim == 3 ? 24 : 8;
+  double* ks = smem_asm;
+  double* stage = smem_asm + ed * ed;
   for (int e = threadIdx.x; e < ed * ed; e += blockDim.x) ks[e] = ke[e];
+  const i32 I0 = blockIdx.x * kAsmTile;
+  const i32 I1 = min(I0 + kAsmTile, nodes);
+  const i32 base = rowptr[first[I0]], end = rowptr[first[I1]];
   __syncthreads();
-  const int o = blockIdx.y;
-  const int odx = o % 3 - 1, ody = (o / 3) % 3 - 1, odz = g.dim == 3 ? o / 9 - 1 : 0;
-  const i32 I = blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= nodes) return;
-  const uint32_t mk = nmask[I];
-  if (!(mk & (1u << o))) return;
-  const i32 t = a.ptr[I] + __popc(mk & ((1u << o) - 1u));
-  const i32 gi = gnode[I];
-  const i32 ix = gi % g.nnx, iy = (gi / g.nnx) % g.nny, iz = gi / (g.nnx * g.nny);
-  const i32 jx = ix + odx, jy = iy + ody, jz = iz + odz;
-  const i32 J = a.nbr[t];
-  const int maskI = cmask[I], maskJ = cmask[J];
-  double acc[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
-  const i32 z0 = max(max(iz, jz) - 1, 0), z1 = min(min(iz, jz), g.nz - 1);
-  const i32 y0 = max(max(iy, jy) - 1, 0), y1 = min(min(iy, jy), g.ny - 1);
-  const i32 x0 = max(max(ix, jx) - 1, 0), x1 = min(min(ix, jx), g.nx - 1);
-  for (i32 cz = z0; cz <= z1; ++cz)
-    for (i32 cy = y0; cy <= y1; ++cy)
-      for (i32 cx = x0; cx <= x1; ++cx) {
-        const double s = scale[(static_cast<i64>(cz) * g.ny + cy) * g.nx + cx];
-        const int aI = corner_of(ix - cx, iy - cy, g.dim == 3 ? iz - cz : 0);
-        const int aJ = corner_of(jx - cx, jy - cy, g.dim == 3 ? jz - cz : 0);
+  const int o = threadIdx.x >> 5;
+  const i32 I = I0 + (threadIdx.x & 31);
+  const uint32_t mk = I < I1 ? nmask[I] : 0u;
+  if (mk & (1u << o)) {
+    const int odx = o % 3 - 1, ody = (o / 3) % 3 - 1, odz = g.dim == 3 ? o / 9 - 1 : 0;
+    const i32 t = a.ptr[I] + __popc(mk & ((1u << o) - 1u));
+    const i32 gi = gnode[I];
+    const i32 ix = gi % g.nnx, iy = (gi / g.nnx) % g.nny, iz = gi / (g.nnx * g.nny);
+    const i32 jx = ix + odx, jy = iy + ody, jz = iz + odz;
+    const i32 J = a.nbr[t];
+    const int maskI = cmask[I], maskJ = cmask[J];
+    double acc[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    const i32 z0 = max(max(iz, jz) - 1, 0), z1 = min(min(iz, jz), g.nz - 1);
+    const i32 y0 = max(max(iy, jy) - 1, 0), y1 = min(min(iy, jy), g.ny - 1);
+    const i32 x0 = max(max(ix, jx) - 1, 0), x1 = min(min(ix, jx), g.nx - 1);
+    for (i32 cz = z0; cz <= z1; ++cz)
+      for (i32 cy = y0; cy <= y1; ++cy)
+        for (i32 cx = x0; cx <= x1; ++cx) {
+          const double s = scale[(static_cast<i64>(cz) * g.ny + cy) * g.nx + cx];
+          const int aI = corner_of(ix - cx, iy - cy, g.dim == 3 ? iz - cz : 0);
+          const int aJ = corner_of(jx - cx, jy - cy, g.dim == 3 ? jz - cz : 0);
 #pragma unroll
-        for (int ka = 0; ka < 3; ++ka)
+          for (int ka = 0; ka < 3; ++ka)
 #pragma unroll
-          for (int kb = 0; kb < 3; ++kb)
-            if (ka < g.dim && kb < g.dim) {
-              const double k = ks[(g.dim * aJ + kb) * ed + g.dim * aI + ka];
-              acc[ka][kb] = EXACT ? xadd(acc[ka][kb], xmul(s, k)) : fma(s, k, acc[ka][kb]);
-            }
+            for (int kb = 0; kb < 3; ++kb)
+              if (ka < g.dim && kb < g.dim) {
+                const double k = ks[(g.dim * aJ + kb) * ed + g.dim * aI + ka];
+                acc[ka][kb] = EXACT ? xadd(acc[ka][kb], xmul(s, k)) : fma(s, k, acc[ka][kb]);
+              }
+        }
+    const i32 r0 = first[I];
+    int qa = 0;
+#pragma unroll
+    for (int ka = 0; ka < 3; ++ka) {
+      if (ka >= g.dim || !(maskI & (1 << ka))) continue;
+      const i32 rb = rowptr[r0 + qa] + a.off[t] - base;
+      int qb = 0;
+#pragma unroll
+      for (int kb = 0; kb < 3; ++kb) {
+        if (kb >= g.dim || !(maskJ & (1 << kb))) continue;
+        stage[rb + qb] = acc[ka][kb];
+        ++qb;
       }
-  const i32 r0 = first[I];
-  int qa = 0;
-#pragma unroll
-  for (int ka = 0; ka < 3; ++ka) {
-    if (ka >= g.dim || !(maskI & (1 << ka))) continue;
-    const i32 base = rowptr[r0 + qa] + a.off[t];
-    int qb = 0;
-#pragma unroll
-    for (int kb = 0; kb < 3; ++kb) {
-      if (kb >= g.dim || !(maskJ & (1 << kb))) continue;
-      val[base + qb] = static_cast<TO>(acc[ka][kb]);
-      if (val64) val64[base + qb] = acc[ka][kb];
-      ++qb;
+      ++qa;
     }
-    ++qa;
+  }
+  __syncthreads();
+  for (i32 k = threadIdx.x; k < end - base; k += blockDim.x) {
+    const double v = stage[k];
+    val[base + k] = static_cast<TO>(v);
+    if (val64) val64[base + k] = v;
   }
 }
 

@@ -1,0 +1,144 @@
+// Projected initial guess for the per-load PCG (warm_start = 2).
+//
+// The reference warm-starts each solve from the previous iteration's
+// displacement (StaticAnalysis::solve_load_vector with LinearSolverOptions::
+// warm_start, src/fem/StaticAnalysis.cpp:134-143).  Mode 2 keeps the last
+// kHistory displacements U = [u_1 .. u_k] of the load case and starts from
+// the energy-optimal combination over their span under the NEW stiffness:
+//
+//   x0 = U c,  (U^T K U) c = U^T f,
+//
+// which is never worse in the energy norm than x0 = u_1 (c = e_1 lies in the
+// search space).  Nearly dependent history vectors are dropped by a pivoted
+// LDL^T of the k x k Gram matrix.  Cost: k FP64 operator applications and one
+// fused multi-dot pass; the PCG itself is unchanged.
+#include "kernels.cuh"
+#include "problem.h"
+
+#include <cmath>
+
+namespace simp {
+
+namespace {
+
+constexpr int kDots = kHistory * (kHistory + 1) / 2 + kHistory;
+
+// partials of u_i . (K u_j) (i <= j) and u_i . f, per block
+__global__ void __launch_bounds__(kRedThreads) k_history_dots(i64 n, int k, const double* __restrict__ u,
+                                                              const double* __restrict__ ku,
+                                                              const double* __restrict__ f,
+                                                              double* __restrict__ part) {
+  double acc[kDots];
+#pragma unroll
+  for (int q = 0; q < kDots; ++q) acc[q] = 0.0;
+  for (i64 e = blockIdx.x * (i64)kRedThreads + threadIdx.x; e < n; e += (i64)gridDim.x * kRedThreads) {
+    double ue[kHistory], ke[kHistory];
+#pragma unroll
+    for (int i = 0; i < kHistory; ++i) {
+      ue[i] = i < k ? u[i * n + e] : 0.0;
+      ke[i] = i < k ? ku[i * n + e] : 0.0;
+    }
+    const double fe = f[e];
+    int q = 0;
+#pragma unroll
+    for (int i = 0; i < kHistory; ++i)
+#pragma unroll
+      for (int j = i; j < kHistory; ++j) acc[q++] += ue[i] * ke[j];
+#pragma unroll
+    for (int i = 0; i < kHistory; ++i) acc[q++] += ue[i] * fe;
+  }
+#pragma unroll
+  for (int q = 0; q < kDots; ++q) {
+    const double s = block_sum<kRedThreads>(acc[q]);
+    if (threadIdx.x == 0) part[q * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+struct Coefs {
+  double c[kHistory];
+};
+
+__global__ void k_history_combine(i64 n, int k, const double* __restrict__ u, Coefs c, double* __restrict__ x) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < k; ++i) s += c.c[i] * u[i * n + e];
+    x[e] = s;
+  }
+}
+
+}  // namespace
+
+void GpuProblem::projected_start(int l, double* ul) {
+  cudaStream_t s = amg.stream;
+  const int k = hist_count[l];
+  const i64 n = nfree;
+  const double* U = hist.p + static_cast<size_t>(l) * kHistory * n;
+  const double* f = b.p + static_cast<size_t>(l) * n;
+  for (int i = 0; i < k; ++i) amg.spmv0(U + i * n, khist.p + i * n);
+  k_history_dots<<<kRedBlocks, kRedThreads, 0, s>>>(n, k, U, khist.p, f, hpart.p);
+  SIMP_CHECK_LAUNCH();
+  std::vector<double> hp(static_cast<size_t>(kDots) * kRedBlocks);
+  SIMP_CUDA(cudaMemcpyAsync(hp.data(), hpart.p, sizeof(double) * hp.size(), cudaMemcpyDeviceToHost, s));
+  SIMP_CUDA(cudaStreamSynchronize(s));
+  double dots[kDots];
+  for (int q = 0; q < kDots; ++q) {
+    double t = 0.0;
+    for (int p = 0; p < kRedBlocks; ++p) t += hp[static_cast<size_t>(q) * kRedBlocks + p];
+    dots[q] = t;
+  }
+  double G[kHistory][kHistory] = {}, g[kHistory] = {};
+  int q = 0;
+  for (int i = 0; i < kHistory; ++i)
+    for (int j = i; j < kHistory; ++j) {
+      G[i][j] = G[j][i] = dots[q];
+      ++q;
+    }
+  for (int i = 0; i < kHistory; ++i) g[i] = dots[q++];
+  // LDL^T in history order (newest first); a pivot below 1e-10 of its
+  // diagonal marks a dependent vector, whose coefficient is zero
+  double L[kHistory][kHistory] = {}, D[kHistory] = {};
+  bool keep[kHistory] = {};
+  for (int j = 0; j < k; ++j) {
+    double dj = G[j][j];
+    for (int p = 0; p < j; ++p)
+      if (keep[p]) dj -= L[j][p] * L[j][p] * D[p];
+    keep[j] = dj > 1.0e-10 * G[j][j] && G[j][j] > 0.0;
+    D[j] = keep[j] ? dj : 0.0;
+    for (int i = j + 1; i < k; ++i) {
+      double v = G[i][j];
+      for (int p = 0; p < j; ++p)
+        if (keep[p]) v -= L[i][p] * L[j][p] * D[p];
+      L[i][j] = keep[j] ? v / dj : 0.0;
+    }
+  }
+  Coefs c{};
+  double y[kHistory] = {};
+  for (int i = 0; i < k; ++i) {
+    double v = g[i];
+    for (int p = 0; p < i; ++p) v -= L[i][p] * y[p];
+    y[i] = keep[i] ? v : 0.0;
+  }
+  for (int i = k - 1; i >= 0; --i) {
+    double v = keep[i] ? y[i] / D[i] : 0.0;
+    for (int p = i + 1; p < k; ++p) v -= L[p][i] * c.c[p];
+    c.c[i] = keep[i] ? v : 0.0;
+  }
+  bool finite = true;
+  for (int i = 0; i < k; ++i) finite = finite && std::isfinite(c.c[i]);
+  if (!finite) return;  // keep the previous displacement
+  k_history_combine<<<grid_for(n, 256, 8192), 256, 0, s>>>(n, k, U, c, ul);
+  SIMP_CHECK_LAUNCH();
+}
+
+void GpuProblem::record_history(int l, const double* ul) {
+  const i64 n = nfree;
+  double* U = hist.p + static_cast<size_t>(l) * kHistory * n;
+  // newest first: shift the older vectors down one slot
+  const int k = std::min(hist_count[l] + 1, kHistory);
+  for (int i = k - 1; i > 0; --i)
+    SIMP_CUDA(cudaMemcpyAsync(U + i * n, U + (i - 1) * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, amg.stream));
+  SIMP_CUDA(cudaMemcpyAsync(U, ul, sizeof(double) * n, cudaMemcpyDeviceToDevice, amg.stream));
+  hist_count[l] = k;
+}
+
+}  // namespace simp

@@ -78,7 +78,7 @@ class ProblemSpec:
     damping: float = 0.5
     rtol: float = 1e-8
     max_cg_iterations: int = 0
-    warm_start: bool = True
+    warm_start: int = 1  # 0 zero guess, 1 previous displacement, 2 projection on the last 3
     amg: Dict = dataclasses.field(default_factory=dict)
     name: str = ""
 

@@ -135,3 +135,25 @@ def test_mixed_precision_iteration_matches_oracle():
     recs = TopologyOptimizer(gpu, max_iterations=4, change_tolerance=0).run()
     for k, r in enumerate(recs):
         assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_projected_warm_start_matches_oracle(precision):
+    """warm_start 2 (energy-optimal start over the last three displacements)
+    changes only the PCG's initial guess: the compliance history still matches
+    the oracle's (which warm-starts from the previous displacement), and the
+    solves need no more iterations in total than with warm_start 1."""
+    spec = small_hex(20, 10, 10)
+    spec.rtol = 1e-8
+    spec.initial_density = 0.2
+    ref = oracle.Problem(spec)
+    _, hist = ref.run(8)
+    its = {}
+    for mode in (1, 2):
+        spec.warm_start = mode
+        gpu = GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision=precision)
+        recs = TopologyOptimizer(gpu, max_iterations=8, change_tolerance=0).run()
+        for k, r in enumerate(recs):
+            assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (mode, k, r.compliance, hist[k, 0])
+        its[mode] = sum(r.linear_iterations for r in recs)
+    assert its[2] <= its[1], its
