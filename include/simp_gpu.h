@@ -233,10 +233,10 @@ int simp_element_stiffness(int32_t dim, double hx, double hy, double hz, double 
  * stream.  Exposed so a caller can time the dominant kernel in isolation. */
 int simp_problem_apply_operator(simp_problem* p, const double* x_device, double* y_device);
 
-/* Times `reps` launches of the level-0 operator application the V-cycle uses
- * (FP64 values, or FP32 in mixed precision) with CUDA events on the library's
- * stream: average milliseconds per launch and its algorithmic bytes (values,
- * block pattern, x read and y written once). */
+/* Times `reps` launches of the FP64 level-0 operator application (the CG
+ * operator of both precision modes) with CUDA events on the library's stream:
+ * average milliseconds per launch and its algorithmic bytes (values, the
+ * index data the kernel reads, x read and y written once). */
 int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms_per_launch,
                                double* bytes_per_launch);
 

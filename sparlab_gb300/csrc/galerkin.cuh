@@ -19,18 +19,45 @@
 namespace simp {
 namespace {
 
+constexpr int kChunk = 32;  // left-operand slots whose metadata a warp stages at once
+
+// Per-warp shared memory: the accumulator (T), then int arrays: output slots
+// and offsets, the chunk's slot metadata, and the (slot, inner slot) positions.
+struct WarpSmem {
+  int* sl;    // output slots (column nodes), ascending
+  int* soff;  // their offsets in the output row
+  int* mj;    // chunk: inner row node's first unknown
+  int* msj;   // chunk: its unknown count
+  int* mrow;  // chunk: start of its first inner row's values
+  int* mlen;  // chunk: inner row length
+  int* mu0;   // chunk: first inner slot
+  int* mpre;  // chunk: exclusive prefix of inner slot counts (kChunk + 1)
+  int* maux;  // chunk: left operand's slot offset (a.off / r.off)
+  int* upos;  // pair positions in the accumulator row
+};
+
+constexpr int kMetaInts = 8 * kChunk + 1;
+
 template <class T>
-__device__ __forceinline__ void warp_row_setup(const WarpRows& w, int warps, int warp, unsigned char* smem, T*& acc,
-                                               i32*& sl, i32*& soff, i32*& upos) {
-  acc = reinterpret_cast<T*>(smem) + static_cast<size_t>(warp) * w.acc;
-  i32* base = reinterpret_cast<i32*>(reinterpret_cast<T*>(smem) + static_cast<size_t>(warps) * w.acc);
-  sl = base + static_cast<size_t>(warp) * (2 * w.slots + w.inner);
-  soff = sl + w.slots;
-  upos = soff + w.slots;
+__device__ __forceinline__ T* warp_setup(const WarpRows& w, int warps, int warp, unsigned char* smem, WarpSmem& m) {
+  T* acc = reinterpret_cast<T*>(smem) + static_cast<size_t>(warp) * w.acc;
+  int* base = reinterpret_cast<int*>(reinterpret_cast<T*>(smem) + static_cast<size_t>(warps) * w.acc) +
+              static_cast<size_t>(warp) * (2 * w.slots + kMetaInts + w.inner);
+  m.sl = base;
+  m.soff = m.sl + w.slots;
+  m.mj = m.soff + w.slots;
+  m.msj = m.mj + kChunk;
+  m.mrow = m.msj + kChunk;
+  m.mlen = m.mrow + kChunk;
+  m.mu0 = m.mlen + kChunk;
+  m.maux = m.mu0 + kChunk;
+  m.mpre = m.maux + kChunk;
+  m.upos = m.mpre + kChunk + 1;
+  return acc;
 }
 
 // first index q of the sorted sl[0..ns) with sl[q] >= h (ns >= 1)
-__device__ __forceinline__ int lower_slot(const i32* sl, int ns, i32 h) {
+__device__ __forceinline__ int lower_slot(const int* sl, int ns, i32 h) {
   int lo = 0, hi = ns - 1;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
@@ -40,22 +67,81 @@ __device__ __forceinline__ int lower_slot(const i32* sl, int ns, i32 h) {
   return lo;
 }
 
-// position of column c of an inner row (slots of width b, or described by
-// off when b == 0) in the accumulator row
-__device__ __forceinline__ int inner_pos(int c, int b, const i32* __restrict__ off, i32 u0, i32 nu,
-                                         const i32* upos) {
-  if (b > 0) {
-    const int u = c / b;
-    return upos[u] + (c - u * b);
+// Stage the output slots of a row node and zero its accumulator rows.
+template <class T>
+__device__ __forceinline__ void warp_begin(NodeView out, i32 node, int nrows, int len, int lane, const WarpSmem& m,
+                                           T* acc) {
+  const i32 s0 = out.ptr[node], ns = out.ptr[node + 1] - s0;
+  for (int q = lane; q < ns; q += 32) {
+    m.sl[q] = out.nbr[s0 + q];
+    m.soff[q] = out.off[s0 + q];
   }
-  int u = 0;
-  while (u + 1 < nu && off[u0 + u + 1] <= c) ++u;
-  return upos[u] + (c - off[u0 + u]);
+  for (int q = lane; q < nrows * len; q += 32) acc[q] = T(0);
+  __syncwarp();
+}
+
+// Phase 1 + 2 for one chunk of the left operand's slots [t0, t0 + nt):
+// metadata of each slot's inner row node (lanes over slots), then the
+// accumulator position of every (slot, inner slot) pair (lanes over pairs).
+// left: the left operand's node pattern; inner: the inner rows' pattern.
+__device__ __forceinline__ void warp_chunk(NodeView left, i32 t0, int nt, const i32* __restrict__ first,
+                                           NodeView inner, const i32* __restrict__ irow, int ns, int lane,
+                                           const WarpSmem& m) {
+  int nu = 0;
+  if (lane < nt) {
+    const i32 J = left.nbr[t0 + lane];
+    const i32 kj = first[J], sJ = first[J + 1] - kj;
+    const i32 u0 = inner.ptr[J];
+    nu = sJ > 0 ? inner.ptr[J + 1] - u0 : 0;
+    m.mj[lane] = kj;
+    m.msj[lane] = sJ;
+    m.mrow[lane] = sJ > 0 ? irow[kj] : 0;
+    m.mlen[lane] = sJ > 0 ? irow[kj + 1] - irow[kj] : 0;
+    m.mu0[lane] = u0;
+    m.maux[lane] = left.off[t0 + lane];
+  }
+  int incl = nu;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane < nt) m.mpre[lane] = incl - nu;
+  const int npairs = __shfl_sync(0xffffffffu, incl, 31);
+  if (lane == 0) m.mpre[nt] = npairs;
+  __syncwarp();
+  for (int q = lane; q < npairs; q += 32) {
+    int lo = 0, hi = nt - 1;  // the last slot t with mpre[t] <= q
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (m.mpre[mid] <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    const int u = q - m.mpre[lo];
+    m.upos[q] = m.soff[lower_slot(m.sl, ns, inner.nbr[m.mu0[lo] + u])];
+  }
+  __syncwarp();
+}
+
+// Accumulator position of column c of the inner row of chunk slot t.
+template <int B1>
+__device__ __forceinline__ int pair_pos(int c, int t, const WarpSmem& m, const i32* __restrict__ ioff) {
+  const int pb = m.mpre[t];
+  if constexpr (B1 > 0) {
+    const int u = c / B1;
+    return m.upos[pb + u] + (c - u * B1);
+  } else {
+    const int nu = m.mpre[t + 1] - pb, u0 = m.mu0[t];
+    int u = 0;
+    while (u + 1 < nu && ioff[u0 + u + 1] <= c) ++u;
+    return m.upos[pb + u] + (c - ioff[u0 + u]);
+  }
 }
 
 // AP = A P: warp per fine node I; inner rows are P's rows of I's neighbours J.
-template <class T>
-__global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i32* __restrict__ first, int b1,
+// acc(ka, pos(c)) += sum_kb A((I,ka),(J,kb)) P((J,kb), c), kb ascending.
+template <class T, int B1>
+__global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i32* __restrict__ first,
                                                  NodeView a, const i32* __restrict__ arow,
                                                  const T* __restrict__ aval, NodeView p,
                                                  const i32* __restrict__ prow, const T* __restrict__ pval,
@@ -63,38 +149,46 @@ __global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i3
                                                  T* __restrict__ apval) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* acc;
-  i32 *sl, *soff, *upos;
-  warp_row_setup<T>(w, warps, warp, smem, acc, sl, soff, upos);
+  WarpSmem m;
+  T* acc = warp_setup<T>(w, warps, warp, smem, m);
   for (i32 I = blockIdx.x * warps + warp; I < nodes; I += gridDim.x * warps) {
     const i32 r0 = first[I], nr = first[I + 1] - r0;
-    const i32 s0 = ap.ptr[I], ns = ap.ptr[I + 1] - s0;
+    const int ns = ap.ptr[I + 1] - ap.ptr[I];
     if (nr == 0 || ns == 0) continue;
     const i32 L = aprow[r0 + 1] - aprow[r0];
-    for (int q = lane; q < ns; q += 32) {
-      sl[q] = ap.nbr[s0 + q];
-      soff[q] = ap.off[s0 + q];
-    }
-    for (int q = lane; q < nr * L; q += 32) acc[q] = T(0);
-    __syncwarp();
-    for (i32 t = a.ptr[I]; t < a.ptr[I + 1]; ++t) {
-      const i32 J = a.nbr[t];
-      const i32 kj = first[J], sJ = first[J + 1] - kj;
-      const i32 u0 = p.ptr[J], nu = p.ptr[J + 1] - u0;
-      if (sJ == 0 || nu == 0) continue;
-      for (int u = lane; u < nu; u += 32) upos[u] = soff[lower_slot(sl, ns, p.nbr[u0 + u])];
-      __syncwarp();
-      const i32 Lp = prow[kj + 1] - prow[kj];
-      const i32 aoff = a.off[t];
-      for (int q = lane; q < nr * Lp; q += 32) {
-        const int ka = q / Lp, c = q - ka * Lp;
-        const int pos = ka * L + inner_pos(c, b1, p.off, u0, nu, upos);
-        const T* av = aval + arow[r0 + ka] + aoff;
-        T v = acc[pos];
-        for (int kb = 0; kb < sJ; ++kb) v = xadd(v, xmul(av[kb], pval[prow[kj + kb] + c]));
-        acc[pos] = v;
+    const i32 abase = arow[r0], LA = arow[r0 + 1] - arow[r0];
+    warp_begin<T>(ap, I, nr, L, lane, m, acc);
+    for (i32 t0 = a.ptr[I]; t0 < a.ptr[I + 1]; t0 += kChunk) {
+      const int nt = min(kChunk, a.ptr[I + 1] - t0);
+      warp_chunk(a, t0, nt, first, p, prow, ns, lane, m);
+      for (int t = 0; t < nt; ++t) {
+        const int sJ = m.msj[t], Lp = m.mlen[t];
+        if (sJ == 0) continue;
+        T ar[6][6];
+        const T* av = aval + abase + m.maux[t];
+#pragma unroll
+        for (int ka = 0; ka < 6; ++ka)
+#pragma unroll
+          for (int kb = 0; kb < 6; ++kb) ar[ka][kb] = (ka < nr && kb < sJ) ? av[ka * LA + kb] : T(0);
+        const T* pv = pval + m.mrow[t];
+        for (int c = lane; c < Lp; c += 32) {
+          T pc[6];
+#pragma unroll
+          for (int kb = 0; kb < 6; ++kb) pc[kb] = kb < sJ ? pv[kb * Lp + c] : T(0);
+          const int pos = pair_pos<B1>(c, t, m, p.off);
+#pragma unroll
+          for (int ka = 0; ka < 6; ++ka) {
+            if (ka < nr) {
+              T v = acc[ka * L + pos];
+#pragma unroll
+              for (int kb = 0; kb < 6; ++kb)
+                if (kb < sJ) v = xadd(v, xmul(ar[ka][kb], pc[kb]));
+              acc[ka * L + pos] = v;
+            }
+          }
+        }
+        __syncwarp();
       }
-      __syncwarp();
     }
     for (int ka = 0; ka < nr; ++ka) {
       T* out = apval + aprow[r0 + ka];
@@ -104,49 +198,57 @@ __global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i3
   }
 }
 
-// RAW = R (AP): warp per coarse node g; inner rows are AP's rows of the
-// fine nodes I of R's row g.
-template <class T>
+// RAW = R (AP): warp per coarse node g; inner rows are AP's rows of the fine
+// nodes I of R's row g.  acc(kg, pos(c)) += sum_ka R((g,kg),(I,ka)) AP((I,ka), c).
+template <class T, int B1>
 __global__ void __launch_bounds__(256) k_rap_rows(i32 nodes, WarpRows w, const i32* __restrict__ first1,
-                                                  const i32* __restrict__ first, int b1, NodeView r,
+                                                  const i32* __restrict__ first, NodeView r,
                                                   const i32* __restrict__ rrow, const T* __restrict__ rval,
                                                   NodeView ap, const i32* __restrict__ aprow,
                                                   const T* __restrict__ apval, NodeView c,
                                                   const i32* __restrict__ crow, T* __restrict__ cval) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* acc;
-  i32 *sl, *soff, *upos;
-  warp_row_setup<T>(w, warps, warp, smem, acc, sl, soff, upos);
+  WarpSmem m;
+  T* acc = warp_setup<T>(w, warps, warp, smem, m);
   for (i32 g = blockIdx.x * warps + warp; g < nodes; g += gridDim.x * warps) {
     const i32 r0 = first1[g], nr = first1[g + 1] - r0;
-    const i32 s0 = c.ptr[g], ns = c.ptr[g + 1] - s0;
+    const int ns = c.ptr[g + 1] - c.ptr[g];
     if (nr == 0 || ns == 0) continue;
     const i32 L = crow[r0 + 1] - crow[r0];
-    for (int q = lane; q < ns; q += 32) {
-      sl[q] = c.nbr[s0 + q];
-      soff[q] = c.off[s0 + q];
-    }
-    for (int q = lane; q < nr * L; q += 32) acc[q] = T(0);
-    __syncwarp();
-    for (i32 t = r.ptr[g]; t < r.ptr[g + 1]; ++t) {
-      const i32 I = r.nbr[t];
-      const i32 ki = first[I], sI = first[I + 1] - ki;
-      const i32 u0 = ap.ptr[I], nu = ap.ptr[I + 1] - u0;
-      if (sI == 0 || nu == 0) continue;
-      for (int u = lane; u < nu; u += 32) upos[u] = soff[lower_slot(sl, ns, ap.nbr[u0 + u])];
-      __syncwarp();
-      const i32 La = aprow[ki + 1] - aprow[ki];
-      const i32 roff = r.off[t];
-      for (int q = lane; q < nr * La; q += 32) {
-        const int kg = q / La, cc = q - kg * La;
-        const int pos = kg * L + inner_pos(cc, b1, ap.off, u0, nu, upos);
-        const T* rv = rval + rrow[r0 + kg] + roff;
-        T v = acc[pos];
-        for (int ka = 0; ka < sI; ++ka) v = xadd(v, xmul(rv[ka], apval[aprow[ki + ka] + cc]));
-        acc[pos] = v;
+    const i32 rbase = rrow[r0], LR = rrow[r0 + 1] - rrow[r0];
+    warp_begin<T>(c, g, nr, L, lane, m, acc);
+    for (i32 t0 = r.ptr[g]; t0 < r.ptr[g + 1]; t0 += kChunk) {
+      const int nt = min(kChunk, r.ptr[g + 1] - t0);
+      warp_chunk(r, t0, nt, first, ap, aprow, ns, lane, m);
+      for (int t = 0; t < nt; ++t) {
+        const int sI = m.msj[t], La = m.mlen[t];
+        if (sI == 0) continue;
+        T rr[6][6];
+        const T* rv = rval + rbase + m.maux[t];
+#pragma unroll
+        for (int kg = 0; kg < 6; ++kg)
+#pragma unroll
+          for (int ka = 0; ka < 6; ++ka) rr[kg][ka] = (kg < nr && ka < sI) ? rv[kg * LR + ka] : T(0);
+        const T* pv = apval + m.mrow[t];
+        for (int cc = lane; cc < La; cc += 32) {
+          T pc[6];
+#pragma unroll
+          for (int ka = 0; ka < 6; ++ka) pc[ka] = ka < sI ? pv[ka * La + cc] : T(0);
+          const int pos = pair_pos<B1>(cc, t, m, ap.off);
+#pragma unroll
+          for (int kg = 0; kg < 6; ++kg) {
+            if (kg < nr) {
+              T v = acc[kg * L + pos];
+#pragma unroll
+              for (int ka = 0; ka < 6; ++ka)
+                if (ka < sI) v = xadd(v, xmul(rr[kg][ka], pc[ka]));
+              acc[kg * L + pos] = v;
+            }
+          }
+        }
+        __syncwarp();
       }
-      __syncwarp();
     }
     for (int kg = 0; kg < nr; ++kg) {
       T* out = cval + crow[r0 + kg];
@@ -158,7 +260,7 @@ __global__ void __launch_bounds__(256) k_rap_rows(i32 nodes, WarpRows w, const i
 
 // P = (I - omega D^-1 A) P-hat (src/fem/Multigrid.cpp:671-716): warp per
 // fine node I; the inner rows are P-hat's rows of I's neighbours J, whose
-// single slot is J's aggregate.
+// single slot is J's aggregate.  Lanes own (ka, j) of one neighbour at a time.
 template <class T>
 __global__ void __launch_bounds__(256) k_prolongator_rows(
     i32 nodes, WarpRows w, const i32* __restrict__ first, const i32* __restrict__ first1,
@@ -167,54 +269,61 @@ __global__ void __launch_bounds__(256) k_prolongator_rows(
     const T* __restrict__ phat, const double* __restrict__ dinv, double omega) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* acc;
-  i32 *sl, *soff, *upos;
-  warp_row_setup<T>(w, warps, warp, smem, acc, sl, soff, upos);
+  WarpSmem m;
+  T* acc = warp_setup<T>(w, warps, warp, smem, m);
   for (i32 I = blockIdx.x * warps + warp; I < nodes; I += gridDim.x * warps) {
     const i32 r0 = first[I], nr = first[I + 1] - r0;
-    const i32 s0 = p.ptr[I], ns = p.ptr[I + 1] - s0;
+    const int ns = p.ptr[I + 1] - p.ptr[I];
     if (nr == 0 || ns == 0) continue;
     const i32 L = prow[r0 + 1] - prow[r0];
-    for (int q = lane; q < ns; q += 32) {
-      sl[q] = p.nbr[s0 + q];
-      soff[q] = p.off[s0 + q];
-    }
-    for (int q = lane; q < nr * L; q += 32) acc[q] = T(0);
-    __syncwarp();
-    for (i32 t = a.ptr[I]; t < a.ptr[I + 1]; ++t) {
-      const i32 J = a.nbr[t];
-      const i32 kj = first[J], sJ = first[J + 1] - kj;
-      const i32 g = agg[J];
-      if (sJ == 0 || g < 0) continue;
-      const i32 rg = first1[g + 1] - first1[g];
-      const int base = soff[lower_slot(sl, ns, g)];
-      const i32 aoff = a.off[t];
-      for (int q = lane; q < nr * rg; q += 32) {
-        const int ka = q / rg, j = q - ka * rg;
-        const int pos = ka * L + base + j;
-        const T* av = aval + arow[r0 + ka] + aoff;
-        T v = acc[pos];
-        for (int kb = 0; kb < sJ; ++kb) v = xadd(v, xmul(av[kb], phat[phat_ptr[kj + kb] + j]));
-        acc[pos] = v;
+    const i32 abase = arow[r0], LA = arow[r0 + 1] - arow[r0];
+    warp_begin<T>(p, I, nr, L, lane, m, acc);
+    for (i32 t0 = a.ptr[I]; t0 < a.ptr[I + 1]; t0 += kChunk) {
+      const int nt = min(kChunk, a.ptr[I + 1] - t0);
+      // per neighbour: its unknowns, its aggregate's position and rank
+      if (lane < nt) {
+        const i32 J = a.nbr[t0 + lane];
+        const i32 kj = first[J], sJ = first[J + 1] - kj;
+        const i32 gJ = agg[J];
+        const bool ok = sJ > 0 && gJ >= 0;
+        m.mj[lane] = kj;
+        m.msj[lane] = ok ? sJ : 0;
+        m.mlen[lane] = ok ? first1[gJ + 1] - first1[gJ] : 0;
+        m.mrow[lane] = ok ? m.soff[lower_slot(m.sl, ns, gJ)] : 0;
+        m.maux[lane] = a.off[t0 + lane];
       }
       __syncwarp();
+      for (int t = 0; t < nt; ++t) {
+        const int sJ = m.msj[t], rg = m.mlen[t];
+        if (sJ == 0) continue;
+        const int base = m.mrow[t], kj = m.mj[t];
+        const T* av = aval + abase + m.maux[t];
+        for (int q = lane; q < nr * rg; q += 32) {
+          const int ka = q / rg, j = q - ka * rg;
+          const int pos = ka * L + base + j;
+          T v = acc[pos];
+          for (int kb = 0; kb < sJ; ++kb) v = xadd(v, xmul(av[ka * LA + kb], phat[phat_ptr[kj + kb] + j]));
+          acc[pos] = v;
+        }
+        __syncwarp();
+      }
     }
     // P(i, :) = P-hat(i, :) - omega dinv_i (A P-hat)(i, :)
     const i32 gi = agg[I];
-    const int own = gi >= 0 ? soff[lower_slot(sl, ns, gi)] : -1;
+    const int own = gi >= 0 ? m.soff[lower_slot(m.sl, ns, gi)] : -1;
+    const int rown = gi >= 0 ? first1[gi + 1] - first1[gi] : 0;
     for (int ka = 0; ka < nr; ++ka) {
       const T scale = static_cast<T>(omega * dinv[r0 + ka]);
       T* out = pval + prow[r0 + ka];
       const T* ph = phat + phat_ptr[r0 + ka];
       for (int q = lane; q < L; q += 32) {
         T v = xmul(acc[ka * L + q], -scale);
-        if (own >= 0 && q >= own && q < own + (first1[gi + 1] - first1[gi])) v = xadd(v, ph[q - own]);
+        if (own >= 0 && q >= own && q < own + rown) v = xadd(v, ph[q - own]);
         out[q] = v;
       }
     }
     __syncwarp();
   }
-  (void)upos;
 }
 
 }  // namespace

@@ -182,8 +182,8 @@ class GpuSimpProblem:
                                                           C.c_void_p(y_device_ptr)))
 
     def time_operator(self, reps: int = 20):
-        """(ms per launch, algorithmic bytes per launch) of the level-0
-        operator application the V-cycle uses, timed with CUDA events."""
+        """(ms per launch, algorithmic bytes per launch) of the FP64 level-0
+        operator application (the CG operator), timed with CUDA events."""
         ms, by = C.c_double(), C.c_double()
         self._check(self._lib.simp_problem_time_operator(self._h, C.c_int32(reps), C.byref(ms),
                                                          C.byref(by)))
