@@ -179,6 +179,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def whole_job_rate(ms_local, steps, world, device=None):
+    """The slowest replica bounds the job: the max over ranks of the timed
+    milliseconds, and the whole-job rate world * steps / that time."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * steps / (ms * 1e-3)
+
+
 def run_own(args):
     import torch
     import torch.distributed as dist
@@ -221,13 +234,8 @@ def run_own(args):
     barrier()
     clocks = sampler.stop()
     launches = lib.simp_kernel_launches() - launches0
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = whole_job_rate(e0.elapsed_time(e1), args.steps, world, dev)
     per_step = ms / args.steps
-    value = world * args.steps / (ms * 1e-3)
 
     # e2e: design from pinned host memory, iterate, design and compliance back
     x_host = torch.empty(prob.ne, dtype=torch.float64, pin_memory=True).numpy()
@@ -242,11 +250,7 @@ def run_own(args):
         _ = r.compliance
     f1.record()
     barrier()
-    e2e_ms = f0.elapsed_time(f1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms, e2e_value = whole_job_rate(f0.elapsed_time(f1), args.steps, world, dev)
 
     # dominant kernel: the FP64 level-0 operator of the CG (both modes), timed
     # alone with CUDA events on the library's stream
@@ -279,16 +283,19 @@ def run_own(args):
                    "amg_levels": st["num_levels"],
                    "operator_complexity": round(st["operator_complexity"], 6),
                    "cg_iterations_per_step": [r.linear_iterations for r in recs],
+                   "oc_bisections_per_step": [r.bisections for r in recs],
                    "compliance_last": recs[-1].compliance,
                    "warmup_seconds_incl_setup": round(t_setup, 3)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_rows_apply<4,3,0,double> (level-0 K_ff operator of the CG, FP64 values; "
-                               "FP64-pipe bound on GB300)",
+                     "kernel": ("k_rows_apply<4,3,0,double> (level-0 K_ff operator of the CG, FP64 values; "
+                                "FP64-pipe bound on GB300)" if args.precision == "fp64" else
+                                "k_rows_apply_df<8,3,0> (level-0 K_ff operator of the CG, double-float "
+                                "values and arithmetic on the FP32 pipes)"),
                      "bytes_per_launch": alg_bytes, "ms_per_launch": kms,
                      "peak_kind": f"{peak_kind} hbm_gbs (burst copy)"},
         "cpu_baseline": cpu,
-        "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "iter/s",
+        "e2e": {"value": e2e_value, "unit": "iter/s",
                 "h2d_bytes_per_step": 8 * prob.ne, "d2h_bytes_per_step": 8 * prob.ne + 8},
         "gpu_launches": int(launches),
         "clocks": clocks,

@@ -181,7 +181,7 @@ MfView mf_view(const MfOp& o) {
 
 template <int MODE>
 void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
-  const dim3 grid((mf.nnx + kTX - 1) / kTX, (mf.nny + kTY - 1) / kTY, (mf.nz + 1 + kTZ - 1) / kTZ);
+  const dim3 grid((mf.nnx + kTX - 1) / kTX, (mf.nny + kTY - 1) / kTY, (mf.nz + 1 + kTZ * kNZ - 1) / (kTZ * kNZ));
   KeF32 ke;
   std::copy(mf.ke_host, mf.ke_host + 24 * 24, ke.k);
   k_mf3_tile<MODE><<<grid, kTX * kTY * kTZ, 0, s>>>(mf_view(mf), a, ke);
@@ -318,13 +318,36 @@ void GpuAmg::make_ops(size_t l) {
   }
 }
 
-void GpuAmg::spmv0(const double* x, double* y) {
+void GpuAmg::op0(const double* x, double* y, const double* rhs, bool split_ready) {
   Level& l0 = *levels.front();
-  nb_apply<0, double, double, double>(l0.opA, l0.a.v64.p, x, y, nullptr, stream);
+  const NbOp& op = l0.opA;
+  if (!mixed()) {
+    if (rhs) nb_apply<1, double, double, double>(op, l0.a.v64.p, x, y, rhs, stream);
+    else nb_apply<0, double, double, double>(op, l0.a.v64.p, x, y, nullptr, stream);
+    return;
+  }
+  xsplit_.alloc(static_cast<size_t>(l0.n));
+  if (!split_ready) {
+    k_split_pairs<<<grid_for(l0.n, 256, 8192), 256, 0, stream>>>(l0.n, x, xsplit_.p);
+    SIMP_CHECK_LAUNCH();
+  }
+  with_shape<float>(op, [&](auto vs, auto blk) {
+    constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
+    if (rhs)
+      k_rows_apply_df<VS, B, 1><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
+                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit_.p, y, rhs,
+                                                                       op.rows);
+    else
+      k_rows_apply_df<VS, B, 0><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
+                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit_.p, y,
+                                                                       nullptr, op.rows);
+  });
+  SIMP_CHECK_LAUNCH();
 }
 
-// CUDA-event time of the FP64 level-0 operator (the CG operator of both
-// precision modes) on this context's stream, and its compulsory bytes.
+// CUDA-event time of the level-0 CG operator (op0: FP64 values in fp64
+// mode, double-float values in mixed mode) on this context's stream, and its
+// compulsory bytes (8 per value either way).
 void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
   if (!ready_) throw Error(kBadInput, "the operator is built by the first setup");
   Level& l0 = *levels.front();
@@ -332,7 +355,7 @@ void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
   DBuf<double> x64(n), y64(n);
   k_fill<double><<<grid_for(n, 256), 256, 0, stream>>>(x64.p, 1.0, n);
   SIMP_CHECK_LAUNCH();
-  auto launch = [&]() { nb_apply<0, double, double, double>(l0.opA, l0.a.v64.p, x64.p, y64.p, nullptr, stream); };
+  auto launch = [&]() { op0(x64.p, y64.p, nullptr); };
   for (int k = 0; k < 3; ++k) launch();
   // the timed launches are the profiler's capture window when one is attached
   cudaProfilerStart();
@@ -361,7 +384,9 @@ void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
 void GpuAmg::refresh_level0_fp32() {
   Level& l0 = *levels.front();
   l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
-  convert(l0.a.v64.p, l0.a.v32.p, l0.a.nnz, stream);
+  l0.a.v32lo.alloc(static_cast<size_t>(l0.a.nnz));
+  k_split_values<<<grid_for(l0.a.nnz, 256, 8192), 256, 0, stream>>>(l0.a.nnz, l0.a.v64.p, l0.a.v32.p, l0.a.v32lo.p);
+  SIMP_CHECK_LAUNCH();
 }
 
 // inverse diagonal and lambda_max(D^-1 A) of one level (Multigrid.cpp:718-747)
@@ -606,7 +631,7 @@ static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t 
   T* raw = f32 ? reinterpret_cast<T*>(lv.raw32.p) : reinterpret_cast<T*>(lv.raw64.p);
   const double omega = g.opt.damping / lv.lambda;
   const int b1 = uniform_block(nv.first);
-  if (!launch_rows<T>(k_prolongator_rows<T>, lv.nnodes, lv.wr_p, stream, lv.d_first.p, nv.d_first.p, lv.d_agg.p,
+  if (!launch_rows<T>(k_prolongator_rows<T, std::is_same<T, double>::value>, lv.nnodes, lv.wr_p, stream, lv.d_first.p, nv.d_first.p, lv.d_agg.p,
                       lv.d_apat.view(), lv.a.ptr.p, A(lv.a), lv.d_ppat.view(), lv.p.ptr.p, A(lv.p),
                       lv.phat_ptr.p, phat, lv.dinv64.p, omega)) {
     const i64 th = static_cast<i64>(lv.n) * 8;
@@ -631,10 +656,15 @@ static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t 
                           lv.r.ptr.p, A(lv.r), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap), nv.d_apat.view(),
                           nv.a.ptr.p, raw);
   };
-  const bool ap_done = b1 == 6   ? ap_rows(k_ap_rows<T, 6>)
-                       : b1 == 3 ? ap_rows(k_ap_rows<T, 3>)
-                       : b1 == 2 ? ap_rows(k_ap_rows<T, 2>)
-                                 : ap_rows(k_ap_rows<T, 0>);
+  // compile-time node widths for the common shapes: 3-D level 0 (3 -> 6),
+  // coarse 3-D (6 -> 6), 2-D level 0 (2 -> 3), coarse 2-D (3 -> 3)
+  constexpr bool X = std::is_same<T, double>::value;
+  const int b0 = uniform_block(lv.first);
+  const bool ap_done = (b0 == 3 && b1 == 6)   ? ap_rows(k_ap_rows<T, X, 3, 6>)
+                       : (b0 == 6 && b1 == 6) ? ap_rows(k_ap_rows<T, X, 6, 6>)
+                       : (b0 == 2 && b1 == 3) ? ap_rows(k_ap_rows<T, X, 2, 3>)
+                       : (b0 == 3 && b1 == 3) ? ap_rows(k_ap_rows<T, X, 3, 3>)
+                                              : ap_rows(k_ap_rows<T, X, 0, 0>);
   if (!ap_done) {
     const i64 th = static_cast<i64>(lv.n) * 32;
     k_product_ap<32, T><<<grid_for(th, 256), 256, 0, stream>>>(
@@ -642,10 +672,11 @@ static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t 
         lv.d_ppat.view(), lv.p.ptr.p, A(lv.p), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap));
     SIMP_CHECK_LAUNCH();
   }
-  const bool rap_done = b1 == 6   ? rap_rows(k_rap_rows<T, 6>)
-                        : b1 == 3 ? rap_rows(k_rap_rows<T, 3>)
-                        : b1 == 2 ? rap_rows(k_rap_rows<T, 2>)
-                                  : rap_rows(k_rap_rows<T, 0>);
+  const bool rap_done = (b1 == 6 && b0 == 3)   ? rap_rows(k_rap_rows<T, X, 6, 3>)
+                        : (b1 == 6 && b0 == 6) ? rap_rows(k_rap_rows<T, X, 6, 6>)
+                        : (b1 == 3 && b0 == 2) ? rap_rows(k_rap_rows<T, X, 3, 2>)
+                        : (b1 == 3 && b0 == 3) ? rap_rows(k_rap_rows<T, X, 3, 3>)
+                                               : rap_rows(k_rap_rows<T, X, 0, 0>);
   if (!rap_done) {
     const i64 th = static_cast<i64>(nv.n) * 32;
     k_product_rap<32, T><<<grid_for(th, 256), 256, 0, stream>>>(
@@ -903,10 +934,14 @@ GpuAmg::PcgResult GpuAmg::pcg(const double* b, double* x, double target, int bud
   PcgResult res;
   PcgScalars* sc = reinterpret_cast<PcgScalars*>(scal.p + 8);
   static_assert(sizeof(PcgScalars) <= 8 * sizeof(double), "scalar block");
-  auto op = [&](const double* in, double* out, const double* rhs) {
-    if (rhs) nb_apply<1, double, double, double>(f.opA, f.a.v64.p, in, out, rhs, stream);
-    else nb_apply<0, double, double, double>(f.opA, f.a.v64.p, in, out, nullptr, stream);
-  };
+  auto op = [&](const double* in, double* out, const double* rhs) { op0(in, out, rhs, false); };
+  // mixed: the direction update also writes p's double-float split
+  float2* psplit = nullptr;
+  if (mixed()) {
+    xsplit_.alloc(static_cast<size_t>(n));
+    psplit = xsplit_.p;
+  }
+  bool p_split = false;
   int total = 0;
   bool rec_conv = false;
   double best = std::numeric_limits<double>::max();
@@ -925,8 +960,9 @@ GpuAmg::PcgResult GpuAmg::pcg(const double* b, double* x, double target, int bud
       SIMP_CUDA(cudaMemcpyAsync(sc, &h, sizeof(h), cudaMemcpyHostToDevice, stream));
     }
     bool conv = false;
+    p_split = false;
     while (total < budget) {
-      op(pp.p, pq.p, nullptr);
+      op0(pp.p, pq.p, nullptr, p_split);
       k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(pp.p, pq.p, n, part.p);
       SIMP_CHECK_LAUNCH();
       k_pcg_alpha<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, sc);
@@ -953,8 +989,9 @@ GpuAmg::PcgResult GpuAmg::pcg(const double* b, double* x, double target, int bud
       SIMP_CHECK_LAUNCH();
       k_pcg_beta<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, sc);
       SIMP_CHECK_LAUNCH();
-      k_pcg_direction<<<grid_for(n, 256), 256, 0, stream>>>(pp.p, pz.p, n, sc);
+      k_pcg_direction<<<grid_for(n, 256), 256, 0, stream>>>(pp.p, pz.p, n, sc, psplit);
       SIMP_CHECK_LAUNCH();
+      p_split = psplit != nullptr;
     }
     if (!restarts) {
       res.converged = conv;

@@ -49,6 +49,7 @@ struct DevCsr {
   DBuf<i32> ptr, col;
   DBuf<double> v64;
   DBuf<float> v32;
+  DBuf<float> v32lo;  // level 0, mixed: v64 - v32 (double-float CG operator)
 };
 
 // A node-chunked matrix as the operator kernels see it (see nbspmv.cuh).
@@ -135,8 +136,10 @@ class GpuAmg {
   cudaStream_t stream = 0;
 
   bool mixed() const { return opt.precision == 1; }
-  // Set by an assembler that wrote level 0's FP32 values itself; otherwise
-  // setup converts them from the FP64 values (mixed mode).
+  // Set by an assembler that wrote level 0's FP32 values (hi in a.v32 and
+  // lo in a.v32lo) itself; otherwise setup splits the FP64 values (mixed
+  // mode).  In mixed mode the CG operator reads hi/lo only, so an assembler
+  // may leave a.v64 stale after the structure-defining first setup.
   bool level0_fp32_fresh = false;
   MfOp mf;
   // Level 0: the caller fills levels[0]->a (device CSR with FP64 values, and
@@ -147,7 +150,7 @@ class GpuAmg {
   // structure); otherwise reuse them when opt.reuse.
   void setup(bool structure_changed);
   bool ready() const { return ready_; }
-  // level-0 FP32 values from the FP64 ones (mixed mode)
+  // level-0 FP32 hi/lo values from the FP64 ones (mixed mode)
   void refresh_level0_fp32();
 
   // z = M^-1 r (FP64 device vectors of level-0 length).
@@ -159,10 +162,13 @@ class GpuAmg {
   };
   // PCG (src/fem/Multigrid.cpp:1152-1237); x holds the guess on entry.
   PcgResult solve(const double* b, double* x);
-  // y = A0 x in FP64
-  void spmv0(const double* x, double* y);
-  // CUDA-event time of the cycle's level-0 operator launch (ms) and its
-  // algorithmic bytes
+  // The CG operator on FP64 vectors: y = A0 x (rhs null) or y = rhs - A0 x.
+  // FP64 values in fp64 mode; double-float values in mixed mode.
+  // split_ready: x's double-float split is already in the split buffer
+  // (written by the PCG direction update).
+  void op0(const double* x, double* y, const double* rhs, bool split_ready = false);
+  void spmv0(const double* x, double* y) { op0(x, y, nullptr); }
+  // CUDA-event time of one op0 launch (ms) and its algorithmic bytes
   void time_operator(int reps, double* ms, double* bytes);
 
   DBuf<double> part, scal;
@@ -173,6 +179,7 @@ class GpuAmg {
   bool ready_ = false;
   i32 nc_ = 0;
   DBuf<double> dense_, inv_t_, piv_, tmp_;
+  DBuf<float2> xsplit_;  // op0's input as (hi, lo) pairs (mixed mode)
 
   void numeric_level(size_t l);
   void build_transfer(size_t l);

@@ -138,9 +138,26 @@ __device__ __forceinline__ int pair_pos(int c, int t, const WarpSmem& m, const i
   }
 }
 
+// One product term: exact (rounded product, rounded add: the reference's
+// order and rounding, FP64 setups) or fused (the FP32 reuse setups).
+template <bool EXACT, class T>
+__device__ __forceinline__ T term(T acc, T a, T b) {
+  if constexpr (EXACT) return xadd(acc, xmul(a, b));
+  else return fma(a, b, acc);
+}
+
+// Compile-time row widths: W > 0 fixes the count at W, W == 0 means "the
+// runtime value n, at most 6".
+template <int W>
+__device__ __forceinline__ constexpr int wmax() { return W > 0 ? W : 6; }
+template <int W>
+__device__ __forceinline__ bool within(int k, int n) { return W > 0 ? true : k < n; }
+
 // AP = A P: warp per fine node I; inner rows are P's rows of I's neighbours J.
 // acc(ka, pos(c)) += sum_kb A((I,ka),(J,kb)) P((J,kb), c), kb ascending.
-template <class T, int B1>
+// NR: unknowns per node of this level (rows of I and of every J), B1: of the
+// next level (0 = not uniform).
+template <class T, bool EXACT, int NR, int B1>
 __global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i32* __restrict__ first,
                                                  NodeView a, const i32* __restrict__ arow,
                                                  const T* __restrict__ aval, NodeView p,
@@ -148,11 +165,12 @@ __global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i3
                                                  NodeView ap, const i32* __restrict__ aprow,
                                                  T* __restrict__ apval) {
   extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int MR = wmax<NR>();
   const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpSmem m;
   T* acc = warp_setup<T>(w, warps, warp, smem, m);
   for (i32 I = blockIdx.x * warps + warp; I < nodes; I += gridDim.x * warps) {
-    const i32 r0 = first[I], nr = first[I + 1] - r0;
+    const i32 r0 = first[I], nr = NR > 0 ? NR : first[I + 1] - r0;
     const int ns = ap.ptr[I + 1] - ap.ptr[I];
     if (nr == 0 || ns == 0) continue;
     const i32 L = aprow[r0 + 1] - aprow[r0];
@@ -162,27 +180,28 @@ __global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i3
       const int nt = min(kChunk, a.ptr[I + 1] - t0);
       warp_chunk(a, t0, nt, first, p, prow, ns, lane, m);
       for (int t = 0; t < nt; ++t) {
-        const int sJ = m.msj[t], Lp = m.mlen[t];
-        if (sJ == 0) continue;
-        T ar[6][6];
+        const int sJ = NR > 0 ? NR : m.msj[t], Lp = m.mlen[t];
+        if (NR == 0 && sJ == 0) continue;
+        T ar[MR][MR];
         const T* av = aval + abase + m.maux[t];
 #pragma unroll
-        for (int ka = 0; ka < 6; ++ka)
+        for (int ka = 0; ka < MR; ++ka)
 #pragma unroll
-          for (int kb = 0; kb < 6; ++kb) ar[ka][kb] = (ka < nr && kb < sJ) ? av[ka * LA + kb] : T(0);
+          for (int kb = 0; kb < MR; ++kb)
+            ar[ka][kb] = (within<NR>(ka, nr) && within<NR>(kb, sJ)) ? av[ka * LA + kb] : T(0);
         const T* pv = pval + m.mrow[t];
         for (int c = lane; c < Lp; c += 32) {
-          T pc[6];
+          T pc[MR];
 #pragma unroll
-          for (int kb = 0; kb < 6; ++kb) pc[kb] = kb < sJ ? pv[kb * Lp + c] : T(0);
+          for (int kb = 0; kb < MR; ++kb) pc[kb] = within<NR>(kb, sJ) ? pv[kb * Lp + c] : T(0);
           const int pos = pair_pos<B1>(c, t, m, p.off);
 #pragma unroll
-          for (int ka = 0; ka < 6; ++ka) {
-            if (ka < nr) {
+          for (int ka = 0; ka < MR; ++ka) {
+            if (within<NR>(ka, nr)) {
               T v = acc[ka * L + pos];
 #pragma unroll
-              for (int kb = 0; kb < 6; ++kb)
-                if (kb < sJ) v = xadd(v, xmul(ar[ka][kb], pc[kb]));
+              for (int kb = 0; kb < MR; ++kb)
+                if (within<NR>(kb, sJ)) v = term<EXACT>(v, ar[ka][kb], pc[kb]);
               acc[ka * L + pos] = v;
             }
           }
@@ -200,7 +219,9 @@ __global__ void __launch_bounds__(256) k_ap_rows(i32 nodes, WarpRows w, const i3
 
 // RAW = R (AP): warp per coarse node g; inner rows are AP's rows of the fine
 // nodes I of R's row g.  acc(kg, pos(c)) += sum_ka R((g,kg),(I,ka)) AP((I,ka), c).
-template <class T, int B1>
+// NC: unknowns per coarse node (rows of g, and the AP column-node width),
+// NF: per fine node (0 = not uniform).
+template <class T, bool EXACT, int NC, int NF>
 __global__ void __launch_bounds__(256) k_rap_rows(i32 nodes, WarpRows w, const i32* __restrict__ first1,
                                                   const i32* __restrict__ first, NodeView r,
                                                   const i32* __restrict__ rrow, const T* __restrict__ rval,
@@ -208,11 +229,12 @@ __global__ void __launch_bounds__(256) k_rap_rows(i32 nodes, WarpRows w, const i
                                                   const T* __restrict__ apval, NodeView c,
                                                   const i32* __restrict__ crow, T* __restrict__ cval) {
   extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int MC = wmax<NC>(), MF = wmax<NF>();
   const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpSmem m;
   T* acc = warp_setup<T>(w, warps, warp, smem, m);
   for (i32 g = blockIdx.x * warps + warp; g < nodes; g += gridDim.x * warps) {
-    const i32 r0 = first1[g], nr = first1[g + 1] - r0;
+    const i32 r0 = first1[g], nr = NC > 0 ? NC : first1[g + 1] - r0;
     const int ns = c.ptr[g + 1] - c.ptr[g];
     if (nr == 0 || ns == 0) continue;
     const i32 L = crow[r0 + 1] - crow[r0];
@@ -222,27 +244,28 @@ __global__ void __launch_bounds__(256) k_rap_rows(i32 nodes, WarpRows w, const i
       const int nt = min(kChunk, r.ptr[g + 1] - t0);
       warp_chunk(r, t0, nt, first, ap, aprow, ns, lane, m);
       for (int t = 0; t < nt; ++t) {
-        const int sI = m.msj[t], La = m.mlen[t];
-        if (sI == 0) continue;
-        T rr[6][6];
+        const int sI = NF > 0 ? NF : m.msj[t], La = m.mlen[t];
+        if (NF == 0 && sI == 0) continue;
+        T rr[MC][MF];
         const T* rv = rval + rbase + m.maux[t];
 #pragma unroll
-        for (int kg = 0; kg < 6; ++kg)
+        for (int kg = 0; kg < MC; ++kg)
 #pragma unroll
-          for (int ka = 0; ka < 6; ++ka) rr[kg][ka] = (kg < nr && ka < sI) ? rv[kg * LR + ka] : T(0);
+          for (int ka = 0; ka < MF; ++ka)
+            rr[kg][ka] = (within<NC>(kg, nr) && within<NF>(ka, sI)) ? rv[kg * LR + ka] : T(0);
         const T* pv = apval + m.mrow[t];
         for (int cc = lane; cc < La; cc += 32) {
-          T pc[6];
+          T pc[MF];
 #pragma unroll
-          for (int ka = 0; ka < 6; ++ka) pc[ka] = ka < sI ? pv[ka * La + cc] : T(0);
-          const int pos = pair_pos<B1>(cc, t, m, ap.off);
+          for (int ka = 0; ka < MF; ++ka) pc[ka] = within<NF>(ka, sI) ? pv[ka * La + cc] : T(0);
+          const int pos = pair_pos<NC>(cc, t, m, ap.off);
 #pragma unroll
-          for (int kg = 0; kg < 6; ++kg) {
-            if (kg < nr) {
+          for (int kg = 0; kg < MC; ++kg) {
+            if (within<NC>(kg, nr)) {
               T v = acc[kg * L + pos];
 #pragma unroll
-              for (int ka = 0; ka < 6; ++ka)
-                if (ka < sI) v = xadd(v, xmul(rr[kg][ka], pc[ka]));
+              for (int ka = 0; ka < MF; ++ka)
+                if (within<NF>(ka, sI)) v = term<EXACT>(v, rr[kg][ka], pc[ka]);
               acc[kg * L + pos] = v;
             }
           }
@@ -261,7 +284,7 @@ __global__ void __launch_bounds__(256) k_rap_rows(i32 nodes, WarpRows w, const i
 // P = (I - omega D^-1 A) P-hat (src/fem/Multigrid.cpp:671-716): warp per
 // fine node I; the inner rows are P-hat's rows of I's neighbours J, whose
 // single slot is J's aggregate.  Lanes own (ka, j) of one neighbour at a time.
-template <class T>
+template <class T, bool EXACT>
 __global__ void __launch_bounds__(256) k_prolongator_rows(
     i32 nodes, WarpRows w, const i32* __restrict__ first, const i32* __restrict__ first1,
     const i32* __restrict__ agg, NodeView a, const i32* __restrict__ arow, const T* __restrict__ aval, NodeView p,
@@ -302,7 +325,7 @@ __global__ void __launch_bounds__(256) k_prolongator_rows(
           const int ka = q / rg, j = q - ka * rg;
           const int pos = ka * L + base + j;
           T v = acc[pos];
-          for (int kb = 0; kb < sJ; ++kb) v = xadd(v, xmul(av[ka * LA + kb], phat[phat_ptr[kj + kb] + j]));
+          for (int kb = 0; kb < sJ; ++kb) v = term<EXACT>(v, av[ka * LA + kb], phat[phat_ptr[kj + kb] + j]);
           acc[pos] = v;
         }
         __syncwarp();
@@ -317,8 +340,14 @@ __global__ void __launch_bounds__(256) k_prolongator_rows(
       T* out = pval + prow[r0 + ka];
       const T* ph = phat + phat_ptr[r0 + ka];
       for (int q = lane; q < L; q += 32) {
-        T v = xmul(acc[ka * L + q], -scale);
-        if (own >= 0 && q >= own && q < own + rown) v = xadd(v, ph[q - own]);
+        const bool mine = own >= 0 && q >= own && q < own + rown;
+        T v;
+        if constexpr (EXACT) {
+          v = xmul(acc[ka * L + q], -scale);
+          if (mine) v = xadd(v, ph[q - own]);
+        } else {
+          v = mine ? fma(acc[ka * L + q], -scale, ph[q - own]) : acc[ka * L + q] * -scale;
+        }
         out[q] = v;
       }
     }

@@ -35,6 +35,49 @@ __device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
 
+// Double-float arithmetic (a value is an unevaluated sum hi + lo of two
+// floats, about 48 significant bits): Knuth's TwoSum and Dekker's product
+// with a fused multiply-add for the exact product error.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (sh, sl) += (ah + al)(bh + bl), dropping al * bl
+__device__ __forceinline__ void df_fma(float ah, float al, float bh, float bl, float& sh, float& sl) {
+  const float p = __fmul_rn(ah, bh);
+  float pe = __fmaf_rn(ah, bh, -p);
+  pe = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, pe));
+  float t, e;
+  two_sum(sh, p, t, e);
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(e, pe));
+}
+
+// hi = fl32(v), lo = fl32(v - hi)
+__device__ __forceinline__ void df_split(double v, float& hi, float& lo) {
+  hi = __double2float_rn(v);
+  lo = __double2float_rn(v - static_cast<double>(hi));
+}
+
+__global__ void k_split_values(i64 n, const double* __restrict__ v, float* __restrict__ hi, float* __restrict__ lo) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    float h, l;
+    df_split(v[i], h, l);
+    if (hi) hi[i] = h;
+    lo[i] = l;
+  }
+}
+
+__global__ void k_split_pairs(i64 n, const double* __restrict__ v, float2* __restrict__ out) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    float h, l;
+    df_split(v[i], h, l);
+    out[i] = make_float2(h, l);
+  }
+}
+
 template <class T>
 __device__ __forceinline__ double todbl(T v) { return static_cast<double>(v); }
 
@@ -153,11 +196,19 @@ __global__ void __launch_bounds__(kRedThreads) k_pcg_update(double* __restrict__
 }
 
 // p = z + beta p
+// p = z + beta p; with ps, also its double-float split (the next operator
+// application's input in mixed precision)
 __global__ void k_pcg_direction(double* __restrict__ p, const double* __restrict__ z, i64 n,
-                                const PcgScalars* __restrict__ sc) {
+                                const PcgScalars* __restrict__ sc, float2* __restrict__ ps) {
   const double beta = sc->beta;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
-    p[i] = z[i] + beta * p[i];
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    const double v = z[i] + beta * p[i];
+    p[i] = v;
+    if (ps) {
+      const float h = __double2float_rn(v);
+      ps[i] = make_float2(h, __double2float_rn(v - static_cast<double>(h)));
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -139,17 +139,18 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 }
 
 // ---------------------------------------------------------------------------
-// Tiled 3-D variant: a block owns a 32 x 4 x 2 tile of grid nodes; the tile's
-// node values plus a one-node halo (one shared array per component) and the
-// scales of the 33 x 5 x 3 cells that touch it are staged in shared memory
-// once.  Each thread loads its 27 neighbour values into registers and sums
+// Tiled 3-D variant: a block of 32 x 4 x 2 threads owns a 32 x 4 x 4 tile of
+// grid nodes (two node layers per thread); the tile's node values plus a
+// one-node halo (one shared array per component) and the scales of the
+// 33 x 5 x 5 cells that touch it are staged in shared memory once.  Each thread loads its 27 neighbour values into registers and sums
 // the 64 (cell, corner) 3 x 3 block products with K_e^0 taken from the kernel
 // parameter (a __grid_constant__ struct indexed by compile-time constants,
 // so its entries are constant-bank operands of the FMAs rather than loads).
 // Modes: 0 y = A x, 1 y = b - A x, 3 Chebyshev step, 4 Chebyshev first step
 // (same epilogues as the other operator kernels).
 // ---------------------------------------------------------------------------
-constexpr int kTX = 32, kTY = 4, kTZ = 2;
+constexpr int kTX = 32, kTY = 4, kTZ = 2;  // threads per block axis
+constexpr int kNZ = 2;                      // node layers per thread
 
 struct KeF32 {
   float k[24 * 24];  // K_e^0, row-major
@@ -169,13 +170,14 @@ struct MfArgs {
 
 template <int MODE>
 __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, const __grid_constant__ KeF32 ke) {
-  __shared__ float xh[3][kTZ + 2][kTY + 2][kTX + 2];
-  __shared__ float sc[kTZ + 1][kTY + 1][kTX + 1];
+  constexpr int NZ = kTZ * kNZ;  // node layers of the tile
+  __shared__ float xh[3][NZ + 2][kTY + 2][kTX + 2];
+  __shared__ float sc[NZ + 1][kTY + 1][kTX + 1];
   const int tid = threadIdx.x;
-  const i32 x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * kTZ;
+  const i32 x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * NZ;
   const i32 nnz = m.nz + 1;
   // node values of the tile and its halo (zero outside the grid / clamped)
-  for (int e = tid; e < (kTZ + 2) * (kTY + 2) * (kTX + 2); e += kTX * kTY * kTZ) {
+  for (int e = tid; e < (NZ + 2) * (kTY + 2) * (kTX + 2); e += kTX * kTY * kTZ) {
     const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
     const i32 gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
     float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
     xh[2][hz][hy][hx] = v2;
   }
   // cell scales (zero outside the grid)
-  for (int e = tid; e < (kTZ + 1) * (kTY + 1) * (kTX + 1); e += kTX * kTY * kTZ) {
+  for (int e = tid; e < (NZ + 1) * (kTY + 1) * (kTX + 1); e += kTX * kTY * kTZ) {
     const int cx = e % (kTX + 1), cy = (e / (kTX + 1)) % (kTY + 1), cz = e / ((kTX + 1) * (kTY + 1));
     const i32 gx = x0 - 1 + cx, gy = y0 - 1 + cy, gz = z0 - 1 + cz;
     float s = 0.0f;
@@ -203,70 +205,67 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
   }
   __syncthreads();
   const int tx = tid % kTX, ty = (tid / kTX) % kTY, tz = tid / (kTX * kTY);
-  const i32 gx = x0 + tx, gy = y0 + ty, gz = z0 + tz;
-  if (gx >= m.nnx || gy >= m.nny || gz >= nnz) return;
-  const i32 I = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
-  if (I < 0) return;
-  // the 27 neighbour values, nb[k][z][y][x] for offsets z, y, x in {0, 1, 2}
-  float nb[3][3][3][3];
+  const i32 gx = x0 + tx, gy = y0 + ty;
+  if (gx >= m.nnx || gy >= m.nny) return;
+  // kNZ consecutive node layers per thread: their neighbourhoods share
+  // layers, so each shared value is loaded once per thread
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
+  for (int q = 0; q < kNZ; ++q) {
+    const int lz = tz * kNZ + q;  // node layer in the tile
+    const i32 gz = z0 + lz;
+    if (gz >= nnz) break;
+    const i32 I = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
+    if (I < 0) continue;
+    float out0 = 0.0f, out1 = 0.0f, out2 = 0.0f;
 #pragma unroll
-    for (int z = 0; z < 3; ++z)
+    for (int dz = -1; dz <= 0; ++dz)
 #pragma unroll
-      for (int y = 0; y < 3; ++y)
+      for (int dy = -1; dy <= 0; ++dy)
 #pragma unroll
-        for (int x = 0; x < 3; ++x) nb[k][z][y][x] = xh[k][tz + z][ty + y][tx + x];
-  float out0 = 0.0f, out1 = 0.0f, out2 = 0.0f;
+        for (int dx = -1; dx <= 0; ++dx) {
+          const float s = sc[lz + dz + 1][ty + dy + 1][tx + dx + 1];
+          const int ox = -dx, oy = -dy, oz = -dz;
+          const int aI = 4 * oz + (oy ? 3 - ox : ox);
+          float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
 #pragma unroll
-  for (int dz = -1; dz <= 0; ++dz)
+          for (int b = 0; b < 8; ++b) {
+            const int bx = (b == 1 || b == 2 || b == 5 || b == 6) ? 1 : 0;
+            const int by = (b == 2 || b == 3 || b == 6 || b == 7) ? 1 : 0;
+            const int bz = b >= 4 ? 1 : 0;
 #pragma unroll
-    for (int dy = -1; dy <= 0; ++dy)
-#pragma unroll
-      for (int dx = -1; dx <= 0; ++dx) {
-        const float s = sc[tz + dz + 1][ty + dy + 1][tx + dx + 1];
-        const int ox = -dx, oy = -dy, oz = -dz;
-        const int aI = 4 * oz + (oy ? 3 - ox : ox);
-        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-#pragma unroll
-        for (int b = 0; b < 8; ++b) {
-          const int bx = (b == 1 || b == 2 || b == 5 || b == 6) ? 1 : 0;
-          const int by = (b == 2 || b == 3 || b == 6 || b == 7) ? 1 : 0;
-          const int bz = b >= 4 ? 1 : 0;
-          const int nz_ = dz + 1 + bz, ny_ = dy + 1 + by, nx_ = dx + 1 + bx;
-#pragma unroll
-          for (int kb = 0; kb < 3; ++kb) {
-            const float xv = nb[kb][nz_][ny_][nx_];
-            a0 = fmaf(ke.k[(3 * aI + 0) * 24 + 3 * b + kb], xv, a0);
-            a1 = fmaf(ke.k[(3 * aI + 1) * 24 + 3 * b + kb], xv, a1);
-            a2 = fmaf(ke.k[(3 * aI + 2) * 24 + 3 * b + kb], xv, a2);
+            for (int kb = 0; kb < 3; ++kb) {
+              const float xv = xh[kb][lz + dz + 1 + bz][ty + dy + 1 + by][tx + dx + 1 + bx];
+              a0 = fmaf(ke.k[(3 * aI + 0) * 24 + 3 * b + kb], xv, a0);
+              a1 = fmaf(ke.k[(3 * aI + 1) * 24 + 3 * b + kb], xv, a1);
+              a2 = fmaf(ke.k[(3 * aI + 2) * 24 + 3 * b + kb], xv, a2);
+            }
           }
+          out0 = fmaf(s, a0, out0);
+          out1 = fmaf(s, a1, out1);
+          out2 = fmaf(s, a2, out2);
         }
-        out0 = fmaf(s, a0, out0);
-        out1 = fmaf(s, a1, out1);
-        out2 = fmaf(s, a2, out2);
-      }
-  const float o[3] = {out0, out1, out2};
+    const float o[3] = {out0, out1, out2};
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const i64 row = static_cast<i64>(I) * 3 + k;
-    if (MODE == 0) {
-      a.y[row] = o[k];
-    } else if (MODE == 1) {
-      a.y[row] = a.b[row] - o[k];
-    } else if (MODE == 3) {
-      const float ri = a.b[row] - o[k];
-      a.r[row] = ri;
-      const float dv = a.x[row];
-      const float di = a.c1 * dv + a.c2 * a.dinv[row] * ri;
-      a.dn[row] = di;
-      float xi = a.xs[row];
-      if (a.add_d) xi = xi + dv;
-      a.xs[row] = xi + di;
-    } else {
-      const float ri = a.b[row] - o[k];
-      a.r[row] = ri;
-      a.dn[row] = a.dinv[row] * ri * a.inv_theta;
+    for (int k = 0; k < 3; ++k) {
+      const i64 row = static_cast<i64>(I) * 3 + k;
+      if (MODE == 0) {
+        a.y[row] = o[k];
+      } else if (MODE == 1) {
+        a.y[row] = a.b[row] - o[k];
+      } else if (MODE == 3) {
+        const float ri = a.b[row] - o[k];
+        a.r[row] = ri;
+        const float dv = a.x[row];
+        const float di = a.c1 * dv + a.c2 * a.dinv[row] * ri;
+        a.dn[row] = di;
+        float xi = a.xs[row];
+        if (a.add_d) xi = xi + dv;
+        a.xs[row] = xi + di;
+      } else {
+        const float ri = a.b[row] - o[k];
+        a.r[row] = ri;
+        a.dn[row] = a.dinv[row] * ri * a.inv_theta;
+      }
     }
   }
 }

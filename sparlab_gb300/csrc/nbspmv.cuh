@@ -19,6 +19,43 @@
 namespace simp {
 namespace {
 
+constexpr int kUnroll = 4;  // row steps whose loads a lane issues before their products
+
+// Column of entry w of a row: column-free decode (B > 0) or the column array.
+template <int B>
+__device__ __forceinline__ i32 row_col(i32 w, i32 s0, const i32* __restrict__ nbr, const i32* __restrict__ cl) {
+  if constexpr (B > 0) {
+    const i32 t = w / B;
+    return B * nbr[s0 + t] + (w - B * t);
+  } else {
+    return cl[w];
+  }
+}
+
+// This lane's partial sum of one row, entries w = lane, lane + VS, ... in
+// ascending order; kUnroll steps' loads are issued before their products so
+// each lane keeps several independent loads in flight.
+template <int VS, int B, class TV, class TX, class TA>
+__device__ __forceinline__ TA lane_dot(i32 len, int lane, i32 s0, const i32* __restrict__ nbr,
+                                       const i32* __restrict__ cl, const TV* __restrict__ v,
+                                       const TX* __restrict__ x) {
+  TA s = TA(0);
+  i32 w = lane;
+  for (; w + (kUnroll - 1) * VS < len; w += kUnroll * VS) {
+    TV vv[kUnroll];
+    TX xx[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      vv[u] = v[w + u * VS];
+      xx[u] = x[row_col<B>(w + u * VS, s0, nbr, cl)];
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) s += static_cast<TA>(vv[u]) * static_cast<TA>(xx[u]);
+  }
+  for (; w < len; w += VS) s += static_cast<TA>(v[w]) * static_cast<TA>(x[row_col<B>(w, s0, nbr, cl)]);
+  return s;
+}
+
 // mode 0: y = A x ; 1: y = b - A x ; 2: y += A x.  TA is the arithmetic
 // type (FP64 rows get VS = 4: GB300's FP64 rate is 1/64 of FP32, and a short
 // reduction keeps the FP64 pipe on the products).
@@ -33,17 +70,8 @@ __global__ void __launch_bounds__(256) k_rows_apply(const i32* __restrict__ node
   TA s = TA(0);
   if (row < rows) {
     const i32 k0 = rowptr[row], len = rowptr[row + 1] - k0;
-    const TV* v = val + k0;
-    if constexpr (B > 0) {
-      const i32 s0 = pat.ptr[node_of[row]];
-      for (i32 w = lane; w < len; w += VS) {
-        const i32 tt = w / B;
-        s += static_cast<TA>(v[w]) * static_cast<TA>(x[B * pat.nbr[s0 + tt] + (w - B * tt)]);
-      }
-    } else {
-      const i32* cl = col + k0;
-      for (i32 w = lane; w < len; w += VS) s += static_cast<TA>(v[w]) * static_cast<TA>(x[cl[w]]);
-    }
+    const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
+    s = lane_dot<VS, B, TV, TX, TA>(len, lane, s0, pat.nbr, col + k0, val + k0, x);
   }
 #pragma unroll
   for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, VS);
@@ -61,17 +89,8 @@ __device__ __forceinline__ TX rows_dot(i32 row, int lane, bool valid, const i32*
   TX s = TX(0);
   if (valid) {
     const i32 k0 = rowptr[row], len = rowptr[row + 1] - k0;
-    const TV* v = val + k0;
-    if constexpr (B > 0) {
-      const i32 s0 = pat.ptr[node_of[row]];
-      for (i32 w = lane; w < len; w += VS) {
-        const i32 tt = w / B;
-        s += static_cast<TX>(v[w]) * x[B * pat.nbr[s0 + tt] + (w - B * tt)];
-      }
-    } else {
-      const i32* cl = col + k0;
-      for (i32 w = lane; w < len; w += VS) s += static_cast<TX>(v[w]) * x[cl[w]];
-    }
+    const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
+    s = lane_dot<VS, B, TV, TX, TX>(len, lane, s0, pat.nbr, col + k0, val + k0, x);
   }
 #pragma unroll
   for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, VS);
@@ -118,6 +137,61 @@ __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __
     const T ri = b[row] - s;
     r[row] = ri;
     d[row] = dinv[row] * ri * inv_theta;
+  }
+}
+
+// Double-float operator (mixed precision's CG operator): values stored as
+// hi + lo float pairs, x as (hi, lo) pairs, products and sums in
+// double-float arithmetic on the FP32 pipes, y in FP64.  About 2^-44 relative
+// to the FP64 product, at FP32 instruction rates: bandwidth bound where the
+// FP64 kernel is bound by GB300's FP64 rate.  mode 0: y = A x ; 1: y = b - A x.
+template <int VS, int B, int MODE>
+__global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ node_of, NodeView pat,
+                                                       const i32* __restrict__ rowptr, const i32* __restrict__ col,
+                                                       const float* __restrict__ vhi, const float* __restrict__ vlo,
+                                                       const float2* __restrict__ x, double* __restrict__ y,
+                                                       const double* __restrict__ b, i32 rows) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  float sh = 0.0f, sl = 0.0f;
+  if (row < rows) {
+    const i32 k0 = rowptr[row], len = rowptr[row + 1] - k0;
+    const float* vh = vhi + k0;
+    const float* vl = vlo + k0;
+    const i32* cl = col + k0;
+    const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
+    i32 w = lane;
+    for (; w + (kUnroll - 1) * VS < len; w += kUnroll * VS) {
+      float h[kUnroll], l[kUnroll];
+      float2 xv[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        h[u] = vh[w + u * VS];
+        l[u] = vl[w + u * VS];
+        xv[u] = x[row_col<B>(w + u * VS, s0, pat.nbr, cl)];
+      }
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) df_fma(h[u], l[u], xv[u].x, xv[u].y, sh, sl);
+    }
+    for (; w < len; w += VS) {
+      const float2 xv = x[row_col<B>(w, s0, pat.nbr, cl)];
+      df_fma(vh[w], vl[w], xv.x, xv.y, sh, sl);
+    }
+  }
+#pragma unroll
+  for (int o = VS / 2; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, sh, o, VS);
+    const float ol = __shfl_xor_sync(0xffffffffu, sl, o, VS);
+    float s, e;
+    two_sum(sh, oh, s, e);
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(ol, e));
+  }
+  if (row < rows && lane == 0) {
+    const double v = static_cast<double>(sh) + static_cast<double>(sl);
+    if (MODE == 0) y[row] = v;
+    else y[row] = b[row] - v;
   }
 }
 

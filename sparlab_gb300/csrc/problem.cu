@@ -438,29 +438,41 @@ void GpuProblem::get_design(double* h) {
 
 void GpuProblem::assemble(const double* scale, bool exact) {
   Level& l0 = *amg.levels.front();
+  if (l0.nnodes == 0) return;
   const GridView g = grid_of(d);
   const int offsets = d.dim == 3 ? 27 : 9;
   const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
   const size_t smem = assemble_smem(d.dim);
-  // FP64 values always (CG operator, aggregation); FP32 values in the same
-  // pass for the mixed-precision preconditioner
-  auto launch = [&](auto kernel, auto* out, double* out64) {
+  auto launch = [&](auto kernel, const float* sh, const float* sl, double* v64, float* hi, float* lo) {
     SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     kernel<<<blocks, offsets * kAsmTile, smem, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p, nmask.p,
-                                                              l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale, out,
-                                                              out64);
+                                                              l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale, sh, sl,
+                                                              v64, hi, lo);
     SIMP_CHECK_LAUNCH();
   };
-  if (l0.nnodes == 0) return;
-  if (amg.mixed()) {
-    l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
-    if (exact) launch(k_assemble_tiles<true, float>, l0.a.v32.p, l0.a.v64.p);
-    else launch(k_assemble_tiles<false, float>, l0.a.v32.p, l0.a.v64.p);
-    amg.level0_fp32_fresh = true;
-  } else {
-    if (exact) launch(k_assemble_tiles<true, double>, l0.a.v64.p, nullptr);
-    else launch(k_assemble_tiles<false, double>, l0.a.v64.p, nullptr);
+  if (!amg.mixed()) {
+    if (exact) launch(k_assemble_tiles<true, false>, nullptr, nullptr, l0.a.v64.p, nullptr, nullptr);
+    else launch(k_assemble_tiles<false, false>, nullptr, nullptr, l0.a.v64.p, nullptr, nullptr);
+    return;
   }
+  // mixed: the double-float split (hi = the FP32 values of the preconditioner,
+  // hi + lo = the CG operator); FP64 values only for the structure-defining
+  // exact assembly
+  l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
+  l0.a.v32lo.alloc(static_cast<size_t>(l0.a.nnz));
+  if (exact) {
+    launch(k_assemble_tiles<true, false>, nullptr, nullptr, l0.a.v64.p, l0.a.v32.p, l0.a.v32lo.p);
+  } else if (!amg.opt.reuse) {
+    // every setup rebuilds the hierarchy from FP64 values
+    launch(k_assemble_tiles<false, false>, nullptr, nullptr, l0.a.v64.p, l0.a.v32.p, l0.a.v32lo.p);
+  } else {
+    scale_hi.alloc(static_cast<size_t>(ne));
+    scale_lo.alloc(static_cast<size_t>(ne));
+    k_split_values<<<grid_for(ne, 256, 8192), 256, 0, amg.stream>>>(ne, scale, scale_hi.p, scale_lo.p);
+    SIMP_CHECK_LAUNCH();
+    launch(k_assemble_tiles<false, true>, scale_hi.p, scale_lo.p, nullptr, l0.a.v32.p, l0.a.v32lo.p);
+  }
+  amg.level0_fp32_fresh = true;
 }
 
 Evaluation GpuProblem::evaluate() {
@@ -537,11 +549,16 @@ OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
   cudaStream_t s = amg.stream;
   const double target = d.vf * domain_volume;
   double* part = opart.p;
+  // per-update factors of the candidate; a trial is one fused pass
+  oc_g.alloc(static_cast<size_t>(ne));
+  oc_lo.alloc(static_cast<size_t>(ne));
+  oc_hi.alloc(static_cast<size_t>(ne));
+  k_oc_prepare<<<grid_for(ne, 256), 256, 0, s>>>(ne, x.p, dc_dx.p, dv_dx.p, d.move, d.damping, oc_g.p, oc_lo.p,
+                                                oc_hi.p);
+  SIMP_CHECK_LAUNCH();
+  auto factor = [&](double lam) { return d.damping == 0.5 ? 1.0 / std::sqrt(lam) : std::pow(lam, -d.damping); };
   auto volume_of = [&](double lam) {
-    k_oc_candidate<<<grid_for(ne, 256), 256, 0, s>>>(ne, x.p, dc_dx.p, dv_dx.p, lam, d.move, d.damping, xnew.p);
-    SIMP_CHECK_LAUNCH();
-    k_filter_forward<<<kRedBlocks, kRedThreads, 0, s>>>(grid_of(d), static_cast<const Stencil*>(stencil_d), hw.p,
-                                                       ne, xnew.p, nullptr, 1, vols.p, part);
+    k_oc_volume<<<kRedBlocks, kRedThreads, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p, dv_dx.p, factor(lam), part);
     SIMP_CHECK_LAUNCH();
     k_reduce_final<<<1, kRedThreads, 0, s>>>(part, kRedBlocks, amg.scal.p + 5, 0);
     SIMP_CHECK_LAUNCH();
@@ -586,10 +603,11 @@ OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
       break;
     }
   }
-  if (st.bisections == 0) {
-    // no bisection ran: the candidate of the lower bracket end
-    volume_of(lo);
-  }
+  // the design of the final multiplier (the lower bracket end when no
+  // bisection ran)
+  k_oc_apply<<<grid_for(ne, 256), 256, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p,
+                                              factor(st.bisections == 0 ? lo : st.lambda), xnew.p);
+  SIMP_CHECK_LAUNCH();
   st.volume = vol;
   // max |x' - x| and the grey level of the evaluated density
   k_change_gray<<<kRedBlocks, kRedThreads, 0, s>>>(ne, xnew.p, x.p, rho.p, part, part + kRedBlocks);

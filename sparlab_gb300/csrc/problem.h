@@ -78,8 +78,10 @@ class GpuProblem {
   DBuf<uint8_t> cmask, ucomp;
   DBuf<uint32_t> nmask;     // per free node: free neighbours by offset
   DBuf<double> opart;
+  DBuf<double> oc_g, oc_lo, oc_hi;  // OC candidate factors of the current update
   // matrix-free level-0 operator (mixed precision, fully free / clamped nodes)
   DBuf<float> ke32, sf32;
+  DBuf<float> scale_hi, scale_lo;  // double-float split of the stiffness factors (mixed assembly)
   DBuf<i32> nindex;
   void* stencil_d = nullptr;
   std::vector<double> last_compliance;

@@ -42,17 +42,33 @@ inline size_t assemble_smem(int dim) {
   return sizeof(double) * (static_cast<size_t>(ed) * ed + static_cast<size_t>(kAsmTile) * rowvals);
 }
 
-template <bool EXACT, class TO>
+// Outputs: val64 (FP64 values), hi and lo (the double-float split, FP32),
+// each optional.  DF: the sums themselves run in double-float arithmetic on
+// the FP32 pipes from the split scales (sh, sl) and the split element matrix
+// (the mixed-precision reuse assemblies, which write hi/lo only); otherwise
+// in FP64 (EXACT: rounded products and sums; else fused multiply-adds).
+template <bool EXACT, bool DF>
 __global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
     GridView g, i32 nodes, const i32* __restrict__ first, const i32* __restrict__ gnode,
     const uint8_t* __restrict__ cmask, const uint32_t* __restrict__ nmask, NodeView a,
     const i32* __restrict__ rowptr, const double* __restrict__ ke, const double* __restrict__ scale,
-    TO* __restrict__ val, double* __restrict__ val64) {
+    const float* __restrict__ scale_hi, const float* __restrict__ scale_lo, double* __restrict__ val64,
+    float* __restrict__ hi, float* __restrict__ lo) {
   extern __shared__ double smem_asm[];
   const int ed = g.dim == 3 ? 24 : 8;
   double* ks = smem_asm;
   double* stage = smem_asm + ed * ed;
-  for (int e = threadIdx.x; e < ed * ed; e += blockDim.x) ks[e] = ke[e];
+  float2* ks2 = reinterpret_cast<float2*>(ks);
+  float2* stage2 = reinterpret_cast<float2*>(stage);
+  for (int e = threadIdx.x; e < ed * ed; e += blockDim.x) {
+    if constexpr (DF) {
+      float h, l;
+      df_split(ke[e], h, l);
+      ks2[e] = make_float2(h, l);
+    } else {
+      ks[e] = ke[e];
+    }
+  }
   const i32 I0 = blockIdx.x * kAsmTile;
   const i32 I1 = min(I0 + kAsmTile, nodes);
   const i32 base = rowptr[first[I0]], end = rowptr[first[I1]];
@@ -69,23 +85,38 @@ __global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
     const i32 J = a.nbr[t];
     const int maskI = cmask[I], maskJ = cmask[J];
     double acc[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    float ah[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+    float al[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
     const i32 z0 = max(max(iz, jz) - 1, 0), z1 = min(min(iz, jz), g.nz - 1);
     const i32 y0 = max(max(iy, jy) - 1, 0), y1 = min(min(iy, jy), g.ny - 1);
     const i32 x0 = max(max(ix, jx) - 1, 0), x1 = min(min(ix, jx), g.nx - 1);
     for (i32 cz = z0; cz <= z1; ++cz)
       for (i32 cy = y0; cy <= y1; ++cy)
         for (i32 cx = x0; cx <= x1; ++cx) {
-          const double s = scale[(static_cast<i64>(cz) * g.ny + cy) * g.nx + cx];
+          const i64 c = (static_cast<i64>(cz) * g.ny + cy) * g.nx + cx;
           const int aI = corner_of(ix - cx, iy - cy, g.dim == 3 ? iz - cz : 0);
           const int aJ = corner_of(jx - cx, jy - cy, g.dim == 3 ? jz - cz : 0);
+          if constexpr (DF) {
+            const float sh = scale_hi[c], sl = scale_lo[c];
 #pragma unroll
-          for (int ka = 0; ka < 3; ++ka)
+            for (int ka = 0; ka < 3; ++ka)
 #pragma unroll
-            for (int kb = 0; kb < 3; ++kb)
-              if (ka < g.dim && kb < g.dim) {
-                const double k = ks[(g.dim * aJ + kb) * ed + g.dim * aI + ka];
-                acc[ka][kb] = EXACT ? xadd(acc[ka][kb], xmul(s, k)) : fma(s, k, acc[ka][kb]);
-              }
+              for (int kb = 0; kb < 3; ++kb)
+                if (ka < g.dim && kb < g.dim) {
+                  const float2 k = ks2[(g.dim * aJ + kb) * ed + g.dim * aI + ka];
+                  df_fma(sh, sl, k.x, k.y, ah[ka][kb], al[ka][kb]);
+                }
+          } else {
+            const double s = scale[c];
+#pragma unroll
+            for (int ka = 0; ka < 3; ++ka)
+#pragma unroll
+              for (int kb = 0; kb < 3; ++kb)
+                if (ka < g.dim && kb < g.dim) {
+                  const double k = ks[(g.dim * aJ + kb) * ed + g.dim * aI + ka];
+                  acc[ka][kb] = EXACT ? xadd(acc[ka][kb], xmul(s, k)) : fma(s, k, acc[ka][kb]);
+                }
+          }
         }
     const i32 r0 = first[I];
     int qa = 0;
@@ -97,7 +128,13 @@ __global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
 #pragma unroll
       for (int kb = 0; kb < 3; ++kb) {
         if (kb >= g.dim || !(maskJ & (1 << kb))) continue;
-        stage[rb + qb] = acc[ka][kb];
+        if constexpr (DF) {
+          float s, e;  // renormalised pair
+          two_sum(ah[ka][kb], al[ka][kb], s, e);
+          stage2[rb + qb] = make_float2(s, e);
+        } else {
+          stage[rb + qb] = acc[ka][kb];
+        }
         ++qb;
       }
       ++qa;
@@ -105,9 +142,22 @@ __global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
   }
   __syncthreads();
   for (i32 k = threadIdx.x; k < end - base; k += blockDim.x) {
-    const double v = stage[k];
-    val[base + k] = static_cast<TO>(v);
-    if (val64) val64[base + k] = v;
+    if constexpr (DF) {
+      const float2 v = stage2[k];
+      hi[base + k] = v.x;
+      lo[base + k] = v.y;
+    } else {
+      const double v = stage[k];
+      if (val64) val64[base + k] = v;
+      if (lo) {
+        float h, l;
+        df_split(v, h, l);
+        hi[base + k] = h;
+        lo[base + k] = l;
+      } else if (hi) {
+        hi[base + k] = __double2float_rn(v);
+      }
+    }
   }
 }
 
@@ -259,6 +309,47 @@ __global__ void k_oc_candidate(i64 ne, const double* __restrict__ x, const doubl
     const double f = damping == 0.5 ? sqrt(b) : pow(b, damping);
     xn[e] = fmin(fmax(xe * f, lo), hi);
   }
+}
+
+// Per OC update (src/topopt/OptimalityCriteria.cpp:14-38 restated for a
+// multiplier search on the GPU): g_e = x_e max(0, -dc_e / dv_e)^eta (0 where
+// dv_e <= 0) and the move-limited box [lo_e, hi_e], so that the candidate of
+// multiplier lam is clamp(g_e lam^-eta, lo_e, hi_e) -- the reference's
+// x (-dc / (lam dv))^eta with the quotient and the power taken once per
+// update instead of once per bisection trial (GB300's FP64 division and
+// square root are long instruction sequences on its 1/64-rate FP64 pipe).
+__global__ void k_oc_prepare(i64 ne, const double* __restrict__ x, const double* __restrict__ dc,
+                             const double* __restrict__ dv, double move, double eta, double* __restrict__ g,
+                             double* __restrict__ lo, double* __restrict__ hi) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x) {
+    const double xe = x[e];
+    lo[e] = fmax(0.0, xe - move);
+    hi[e] = fmin(1.0, xe + move);
+    double q = 0.0;
+    if (dv[e] > 0.0) q = fmax(0.0, -dc[e] / dv[e]);
+    g[e] = xe * (eta == 0.5 ? sqrt(q) : pow(q, eta));
+  }
+}
+
+// Filtered volume of the candidate of multiplier lam (t = lam^-eta): the
+// volume sum_e v_e (H x')_e equals c^T x' with c = H^T v (dv_dx), so a trial
+// needs no filter pass.  Block partials of sum_e c_e clamp(g_e t, lo_e, hi_e).
+__global__ void __launch_bounds__(kRedThreads) k_oc_volume(i64 ne, const double* __restrict__ g,
+                                                           const double* __restrict__ lo,
+                                                           const double* __restrict__ hi,
+                                                           const double* __restrict__ c, double t,
+                                                           double* __restrict__ part) {
+  double s = 0.0;
+  for (i64 e = blockIdx.x * (i64)kRedThreads + threadIdx.x; e < ne; e += (i64)gridDim.x * kRedThreads)
+    s += c[e] * fmin(fmax(g[e] * t, lo[e]), hi[e]);
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void k_oc_apply(i64 ne, const double* __restrict__ g, const double* __restrict__ lo,
+                           const double* __restrict__ hi, double t, double* __restrict__ xn) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x)
+    xn[e] = fmin(fmax(g[e] * t, lo[e]), hi[e]);
 }
 
 // max |a - b| and sum rho (1 - rho) partials

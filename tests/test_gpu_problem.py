@@ -157,3 +157,28 @@ def test_projected_warm_start_matches_oracle(precision):
             assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (mode, k, r.compliance, hist[k, 0])
         its[mode] = sum(r.linear_iterations for r in recs)
     assert its[2] <= its[1], its
+
+
+def test_mixed_cg_operator_matches_fp64_operator():
+    """Mixed precision's CG operator (K_ff values split into float pairs,
+    double-float products and sums) against the FP64 operator on the same
+    design, after the exact first assembly and after a reuse assembly."""
+    import torch
+    spec = small_hex(20, 10, 10)
+    spec.rtol = 1e-8
+    ref = oracle.Problem(spec)
+    rng = P.SplitMix64(17)
+    probs = {p: GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision=p) for p in ("fp64", "mixed")}
+    x = torch.tensor(rng.uniform_array(probs["fp64"].nfree, -1.0, 1.0), dtype=torch.float64, device="cuda")
+    for design_seed in (5, 6):
+        design = P.SplitMix64(design_seed).uniform_array(ref.ne, 0.05, 1.0)
+        ys = {}
+        for name, prob in probs.items():
+            prob.set_design(design)
+            prob.evaluate()
+            y = torch.empty_like(x)
+            prob.apply_operator(x.data_ptr(), y.data_ptr())
+            torch.cuda.synchronize()
+            ys[name] = y.cpu().numpy()
+        scale = np.abs(ys["fp64"]).max()
+        assert np.abs(ys["mixed"] - ys["fp64"]).max() <= 1e-11 * scale, design_seed
