@@ -41,8 +41,11 @@ extern "C" {
 #define SIMP_NONFINITE 5
 #define SIMP_CUDA_ERROR 6
 
-/* Arithmetic of the operator, smoother and transfers.  CG scalars, the
- * true-residual refinement and the coarsest dense Cholesky are FP64 in both. */
+/* FP64: every operator, vector and scalar in FP64.  MIXED: the V-cycle and
+ * the reuse setups in FP32 (level 0 matrix-free on structured grids), the CG
+ * operator in double-float arithmetic (K_ff as float pairs, ~2^-44 relative
+ * to FP64); CG vectors and scalars, the true-residual restarts and the
+ * coarsest dense Cholesky are FP64 in both. */
 #define SIMP_PRECISION_FP64 0
 #define SIMP_PRECISION_MIXED 1
 
@@ -233,10 +236,10 @@ int simp_element_stiffness(int32_t dim, double hx, double hy, double hz, double 
  * stream.  Exposed so a caller can time the dominant kernel in isolation. */
 int simp_problem_apply_operator(simp_problem* p, const double* x_device, double* y_device);
 
-/* Times `reps` launches of the FP64 level-0 operator application (the CG
- * operator of both precision modes) with CUDA events on the library's stream:
- * average milliseconds per launch and its algorithmic bytes (values, the
- * index data the kernel reads, x read and y written once). */
+/* Times `reps` launches of the level-0 CG operator (FP64 values in FP64 mode,
+ * double-float hi + lo values in mixed mode) with CUDA events on the library's
+ * stream: average milliseconds per launch and its algorithmic bytes (8 per
+ * value, the index data the kernel reads, x read and y written once). */
 int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms_per_launch,
                                double* bytes_per_launch);
 

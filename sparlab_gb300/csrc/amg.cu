@@ -421,13 +421,24 @@ void GpuAmg::numeric_level(size_t l) {
     convert(lv.dinv64.p, lv.dinv32.p, n, stream);
   }
   // Lanczos on D^-1/2 A D^-1/2 with the reference's start vector.
-  DBuf<double> v(n), vp(n), w(n), s(n), tmp(n);
+  // Lanczos vectors, kept with the level so reuse setups allocate nothing
+  // (cudaFree synchronises the device)
+  DBuf<double>& v = lv.lz[0];
+  DBuf<double>& vp = lv.lz[1];
+  DBuf<double>& w = lv.lz[2];
+  DBuf<double>& s = lv.lz[3];
+  DBuf<double>& tmp = lv.lz[4];
+  for (auto& b : lv.lz) b.alloc(static_cast<size_t>(n));
   {
-    std::vector<double> h(static_cast<size_t>(n));
-    for (i32 i = 0; i < n; ++i) h[i] = 1.0 + 0.5 * std::sin(1.7 * static_cast<double>(i) + 0.3);
-    v.upload(h, stream);
-    const double nv = std::sqrt(dot(v.p, v.p, n));
-    SIMP_CUDA(cudaMemcpyAsync(scal.p + 1, &nv, sizeof(double), cudaMemcpyHostToDevice, stream));
+    // the reference's start vector depends on n only: made and normed once
+    if (lv.lz_start.n != static_cast<size_t>(n)) {
+      std::vector<double> h(static_cast<size_t>(n));
+      for (i32 i = 0; i < n; ++i) h[i] = 1.0 + 0.5 * std::sin(1.7 * static_cast<double>(i) + 0.3);
+      lv.lz_start.upload(h, stream);
+      lv.lz_norm = std::sqrt(dot(lv.lz_start.p, lv.lz_start.p, n));
+    }
+    SIMP_CUDA(cudaMemcpyAsync(v.p, lv.lz_start.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+    SIMP_CUDA(cudaMemcpyAsync(scal.p + 1, &lv.lz_norm, sizeof(double), cudaMemcpyHostToDevice, stream));
     k_lanczos_start<<<grid_for(n, 256), 256, 0, stream>>>(v.p, scal.p + 1, lv.dinv64.p, s.p, tmp.p, n);
     SIMP_CHECK_LAUNCH();
   }

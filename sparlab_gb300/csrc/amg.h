@@ -103,6 +103,9 @@ struct Level {
   DBuf<float> x32, b32, r32, d32, e32;
   std::vector<double> c1, c2;
   double inv_theta = 0.0;
+  DBuf<double> lz[5];  // Lanczos work vectors
+  DBuf<double> lz_start;  // Lanczos start vector (depends on n only) and its norm
+  double lz_norm = 0.0;
 };
 
 // Matrix-free level-0 operator of a structured grid (see mfree.cuh), used

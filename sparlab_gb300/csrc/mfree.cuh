@@ -139,10 +139,11 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 }
 
 // ---------------------------------------------------------------------------
-// Tiled 3-D variant: a block of 32 x 4 x 2 threads owns a 32 x 4 x 4 tile of
-// grid nodes (two node layers per thread); the tile's node values plus a
-// one-node halo (one shared array per component) and the scales of the
-// 33 x 5 x 5 cells that touch it are staged in shared memory once.  Each thread loads its 27 neighbour values into registers and sums
+// Tiled 3-D variant: a block of 32 x 4 x 2 threads owns a 32 x 4 x (2 kNZ)
+// tile of grid nodes (kNZ node layers per thread; two layers per thread
+// measured slower at 192 x 96 x 96, 109 against 105 us); the tile's node
+// values plus a one-node halo (one shared array per component) and the
+// scales of the cells that touch it are staged in shared memory once.  Each thread loads its 27 neighbour values into registers and sums
 // the 64 (cell, corner) 3 x 3 block products with K_e^0 taken from the kernel
 // parameter (a __grid_constant__ struct indexed by compile-time constants,
 // so its entries are constant-bank operands of the FMAs rather than loads).
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 // (same epilogues as the other operator kernels).
 // ---------------------------------------------------------------------------
 constexpr int kTX = 32, kTY = 4, kTZ = 2;  // threads per block axis
-constexpr int kNZ = 2;                      // node layers per thread
+constexpr int kNZ = 1;                      // node layers per thread
 
 struct KeF32 {
   float k[24 * 24];  // K_e^0, row-major
@@ -176,23 +177,41 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
   const int tid = threadIdx.x;
   const i32 x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * NZ;
   const i32 nnz = m.nz + 1;
-  // node values of the tile and its halo (zero outside the grid / clamped)
-  for (int e = tid; e < (NZ + 2) * (kTY + 2) * (kTX + 2); e += kTX * kTY * kTZ) {
+  // node values of the tile and its halo (zero outside the grid / clamped):
+  // every thread first loads the free-node indices of all its halo entries,
+  // then their values, so the loads of one thread are independent
+  constexpr int kHalo = (NZ + 2) * (kTY + 2) * (kTX + 2);
+  constexpr int kPer = (kHalo + kTX * kTY * kTZ - 1) / (kTX * kTY * kTZ);
+  i32 hj[kPer];
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int e = tid + q * kTX * kTY * kTZ;
     const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
     const i32 gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
-    float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
-    if (gx >= 0 && gx < m.nnx && gy >= 0 && gy < m.nny && gz >= 0 && gz < nnz) {
-      const i32 J = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
-      if (J >= 0) {
-        const float* p = a.x + static_cast<i64>(J) * 3;
-        v0 = p[0];
-        v1 = p[1];
-        v2 = p[2];
-      }
+    hj[q] = -1;
+    if (e < kHalo && gx >= 0 && gx < m.nnx && gy >= 0 && gy < m.nny && gz >= 0 && gz < nnz)
+      hj[q] = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
+  }
+  float hv[kPer][3];
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    hv[q][0] = hv[q][1] = hv[q][2] = 0.0f;
+    if (hj[q] >= 0) {
+      const float* p = a.x + static_cast<i64>(hj[q]) * 3;
+      hv[q][0] = p[0];
+      hv[q][1] = p[1];
+      hv[q][2] = p[2];
     }
-    xh[0][hz][hy][hx] = v0;
-    xh[1][hz][hy][hx] = v1;
-    xh[2][hz][hy][hx] = v2;
+  }
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int e = tid + q * kTX * kTY * kTZ;
+    if (e < kHalo) {
+      const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
+      xh[0][hz][hy][hx] = hv[q][0];
+      xh[1][hz][hy][hx] = hv[q][1];
+      xh[2][hz][hy][hx] = hv[q][2];
+    }
   }
   // cell scales (zero outside the grid)
   for (int e = tid; e < (NZ + 1) * (kTY + 1) * (kTX + 1); e += kTX * kTY * kTZ) {

@@ -296,21 +296,6 @@ __global__ void __launch_bounds__(128) k_sensitivities(GridView g, i64 ne, int n
   }
 }
 
-// OC candidate (src/topopt/OptimalityCriteria.cpp:14-36)
-__global__ void k_oc_candidate(i64 ne, const double* __restrict__ x, const double* __restrict__ dc,
-                               const double* __restrict__ dv, double lam, double move, double damping,
-                               double* __restrict__ xn) {
-  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x) {
-    const double xe = x[e];
-    const double lo = fmax(0.0, xe - move), hi = fmin(1.0, xe + move);
-    const double den = lam * dv[e];
-    double b = 0.0;
-    if (den > 0.0) b = fmax(0.0, -dc[e] / den);
-    const double f = damping == 0.5 ? sqrt(b) : pow(b, damping);
-    xn[e] = fmin(fmax(xe * f, lo), hi);
-  }
-}
-
 // Per OC update (src/topopt/OptimalityCriteria.cpp:14-38 restated for a
 // multiplier search on the GPU): g_e = x_e max(0, -dc_e / dv_e)^eta (0 where
 // dv_e <= 0) and the move-limited box [lo_e, hi_e], so that the candidate of
