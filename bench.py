@@ -48,6 +48,10 @@ WORKLOADS = {
     "q4_600x200": (P.q4_cantilever_600x200, None),
     "q4_120x40": (P.q4_cantilever_120x40, None),
 }
+# 64 independent instances (48 Q4, 16 Hex8, seed 4): a step is one SIMP
+# iteration of every instance; the metric is instance-iterations per second
+BATCHED = "batched_64"
+BATCHED_METRIC = "instance SIMP iter/s, 64 independent Q4/Hex8 instances (seed 4)"
 
 
 def sample_spec(name):
@@ -140,14 +144,51 @@ def cpu_baseline(name, steps=2):
     t = min(times)
     cores = os.cpu_count()
     return {"value": 1.0 / (t * ratio), "unit": "iter/s", "cores": cores, "kind": "port",
-            "sample": f"{spec.nx}x{spec.ny}x{spec.nz} Hex8 cantilever (1/{ratio:.0f} of the cells), "
-                      f"min of {steps} SIMP iterations ({t:.3f} s each) after one setup iteration, "
-                      f"scaled by the cell ratio {ratio:.0f}"}
+            "sample": f"{spec.name}: {spec.nx}x{spec.ny}" + (f"x{spec.nz}" if spec.dim == 3 else "") +
+                      f" cells (1/{ratio:.0f} of the workload's), min of {steps} SIMP iterations "
+                      f"({t:.3f} s each) after one setup iteration, scaled by the cell ratio {ratio:.0f}"}
+
+
+def batched_cpu_baseline(specs, every=8):
+    """Oracle on every `every`-th instance (one setup iteration, one timed
+    iteration each), scaled to the whole batch."""
+    import oracle
+    total = 0.0
+    sample = specs[::every]
+    for spec in sample:
+        pr = oracle.Problem(spec)
+        x = np.full(pr.ne, spec.volume_fraction)
+        ev = pr.evaluate(x)
+        x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
+        t0 = time.perf_counter()
+        ev = pr.evaluate(x)
+        pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
+        total += time.perf_counter() - t0
+    scale = len(specs) / len(sample)
+    return {"value": len(specs) / (total * scale), "unit": "instance-iter/s", "cores": os.cpu_count(),
+            "kind": "port", "sample": f"{len(sample)} of the {len(specs)} instances (every {every}th), "
+                                      f"one timed SIMP iteration each after a setup iteration "
+                                      f"({total:.2f} s), scaled by {scale:.0f}"}
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.config == BATCHED:
+        specs = P.batched_instances(seed=4)
+        base = batched_cpu_baseline(specs)
+        v = base["value"]
+        print(json.dumps({
+            "impl": "reference", "metric": BATCHED_METRIC, "value": v, "unit": "instance-iter/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": len(specs) / v * 1e3, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded instances (no dataset)",
+            "config": {"workload": BATCHED, "instances": len(specs), "precision": "fp64",
+                       "host_threads": os.cpu_count()},
+            "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "instance-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
         return
     import oracle
     spec, ratio = sample_spec(args.config)
@@ -190,6 +231,101 @@ def whole_job_rate(ms_local, steps, world, device=None):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     return ms, world * steps / (ms * 1e-3)
+
+
+def run_own_batched(args):
+    """64 independent instances: each rank takes instances rank, rank + N, ...
+    (no collective on the data path) and drives its share from host threads,
+    one CUDA stream per instance."""
+    import torch
+    import torch.distributed as dist
+    from sparlab_gb300 import _lib
+    from sparlab_gb300.topopt import GpuSimpProblem, run_batched
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    specs = P.batched_instances(seed=4)
+    mine = specs[rank::world]
+    probs = [GpuSimpProblem(s, precision=args.precision, device=local) for s in mine]
+    lib = _lib.load()
+    run_batched(probs, args.warmup)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    barrier()
+    launches0 = lib.simp_kernel_launches()
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    recs = run_batched(probs, args.steps)
+    e1.record()
+    barrier()
+    clocks = sampler.stop()
+    launches = lib.simp_kernel_launches() - launches0
+    ms, _ = whole_job_rate(e0.elapsed_time(e1), args.steps, world, dev)
+    value = len(specs) * args.steps / (ms * 1e-3)
+
+    # e2e: every instance's design from pinned host memory and back, each step
+    hosts = []
+    for p in probs:
+        h = torch.empty(p.ne, dtype=torch.float64, pin_memory=True).numpy()
+        h[:] = p.design()
+        hosts.append(h)
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(args.steps):
+        for p, h in zip(probs, hosts):
+            p.set_design(h)
+        run_batched(probs, 1)
+        for p, h in zip(probs, hosts):
+            h[:] = p.design()
+    f1.record()
+    barrier()
+    e2e_ms, _ = whole_job_rate(f0.elapsed_time(f1), args.steps, world, dev)
+    h2d = sum(8 * p.ne for p in probs)
+
+    big = max(probs, key=lambda p: p.nnz)
+    kms, alg_bytes = big.time_operator(20)
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    if rank != 0:
+        return
+    line = {
+        "metric": BATCHED_METRIC, "value": value, "unit": "instance-iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic seeded instances (no dataset)",
+        "config": {"workload": BATCHED, "instances": len(specs), "precision": args.precision,
+                   "instances_per_rank": len(mine), "host_threads": os.cpu_count(),
+                   "elements_total": sum(s.num_elements for s in specs),
+                   "cg_iterations_per_step": [sum(r[k].linear_iterations for r in recs)
+                                              for k in range(args.steps)],
+                   "l2": "no flush: a step touches every instance's operators once"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "level-0 CG operator of the largest instance (%s)" % big.spec.name,
+                     "bytes_per_launch": alg_bytes, "ms_per_launch": kms,
+                     "peak_kind": f"{peak_kind} hbm_gbs (burst copy)"},
+        "cpu_baseline": batched_cpu_baseline(specs) if world == 1 else None,
+        "e2e": {"value": len(specs) * args.steps / (e2e_ms * 1e-3), "unit": "instance-iter/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
 
 
 def run_own(args):
@@ -266,6 +402,26 @@ def run_own(args):
         if d.get("workload") == spec.name:
             traffic = d.get("traffic_bytes_per_launch")
 
+    # the plain FP64 loop on the same iterations (same start design, same
+    # warm-up), for the metric's plain-vs-mixed ratio and the compliance bar
+    plain = None
+    if args.precision == "mixed" and not args.no_plain and world == 1:
+        ref = GpuSimpProblem(spec, precision="fp64", device=local)
+        for _ in range(args.warmup):
+            ref.iterate()
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record()
+        prec = [ref.iterate() for _ in range(args.steps)]
+        g1.record()
+        torch.cuda.synchronize()
+        pms = g0.elapsed_time(g1)
+        plain = {"value": args.steps / (pms * 1e-3), "unit": "iter/s", "ms_per_step": pms / args.steps,
+                 "cg_iterations_per_step": [r.linear_iterations for r in prec],
+                 "max_rel_compliance_diff": max(abs(a.compliance / b.compliance - 1)
+                                                for a, b in zip(recs, prec))}
+        ref.close()
+
     if rank != 0:
         return
     st = prob.amg_stats()
@@ -285,7 +441,8 @@ def run_own(args):
                    "cg_iterations_per_step": [r.linear_iterations for r in recs],
                    "oc_bisections_per_step": [r.bisections for r in recs],
                    "compliance_last": recs[-1].compliance,
-                   "warmup_seconds_incl_setup": round(t_setup, 3)},
+                   "warmup_seconds_incl_setup": round(t_setup, 3),
+                   "plain_fp64": plain},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": ("k_rows_apply<4,3,0,double> (level-0 K_ff operator of the CG, FP64 values; "
@@ -311,8 +468,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
-    ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS) + [BATCHED])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 comparison run that follows a mixed-precision run")
     ap.add_argument("--warm", default="previous", choices=sorted(WARM),
                     help="PCG initial guess: zero, the previous displacement (the reference's "
                          "warm start) or the energy-optimal combination of the last three")
@@ -321,6 +480,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == BATCHED:
+        run_own_batched(args)
     else:
         run_own(args)
 

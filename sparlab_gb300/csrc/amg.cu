@@ -257,13 +257,23 @@ double seconds_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
+// Each context owns a stream, so contexts driven from different host threads
+// (independent problem instances) run concurrently.  It is a blocking
+// stream: work on the legacy default stream (one-time uploads, a caller's
+// own kernels on device pointers it passes in) stays ordered with it.
 GpuAmg::GpuAmg(const AmgOptions& o) : opt(o) {
+  SIMP_CUDA(cudaStreamCreate(&stream));
   part.alloc(kRedBlocks);
   scal.alloc(16);
   dstatus.alloc(4);
 }
 
-GpuAmg::~GpuAmg() = default;
+GpuAmg::~GpuAmg() {
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+}
 
 Level& GpuAmg::level0() {
   if (levels.empty()) levels.emplace_back(new Level());

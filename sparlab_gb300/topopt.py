@@ -263,3 +263,31 @@ class TopologyOptimizer:
             if self.change_tolerance > 0 and r.max_change <= self.change_tolerance:
                 break
         return history
+
+
+def run_batched(problems: List[GpuSimpProblem], iterations: int, workers: Optional[int] = None):
+    """Iterate independent problem instances concurrently.
+
+    Each problem owns a CUDA stream and the library releases the GIL during
+    a call, so ``workers`` host threads (default: one per host core, at most
+    one per problem) each drive their share of the instances, round robin,
+    and the instances' kernels overlap on the GPU.  Every instance computes
+    exactly what it computes alone.  Returns the per-problem iteration
+    records (lists, in problem order)."""
+    import concurrent.futures as cf
+    import os
+    n = len(problems)
+    workers = max(1, min(workers or os.cpu_count() or 1, n))
+    shares = [list(range(w, n, workers)) for w in range(workers)]
+    out: List[List[_lib.IterationRecord]] = [[] for _ in range(n)]
+
+    def drive(share):
+        for _ in range(iterations):
+            for i in share:
+                out[i].append(problems[i].iterate())
+
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        for f in [ex.submit(drive, sh) for sh in shares]:
+            f.result()
+    return out
+
