@@ -133,8 +133,12 @@ class GpuSimpProblem:
         x = np.ascontiguousarray(x, np.float64)
         self._check(self._lib.simp_set_design(self._h, ptr(x)))
 
-    def design(self) -> np.ndarray:
-        x = np.zeros(self.ne)
+    def design(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """The device design copied to host memory (into ``out`` when given:
+        a contiguous float64 array of ne values, e.g. pinned memory)."""
+        x = np.zeros(self.ne) if out is None else out
+        if x.dtype != np.float64 or x.size != self.ne or not x.flags.c_contiguous:
+            raise ValueError("design(out=...) needs a contiguous float64 array of ne values")
         self._check(self._lib.simp_get_design(self._h, ptr(x)))
         return x
 
