@@ -175,10 +175,15 @@ typedef struct {
   int32_t volume_converged;
 } simp_oc_step;
 
+/* One history row (TopologyIteration, include/sparlab/topopt/
+ * TopologyOptimizer.hpp): volume_converged is the OC step's bisection
+ * convergence, or for MMA V/V* - 1 <= 1e-4 (the default constraint_tolerance). */
 typedef struct {
   double compliance, volume_fraction, max_change, lambda, gray_level;
   int32_t linear_iterations, bisections;
   double seconds;
+  int32_t volume_converged;
+  int32_t reserved;
 } simp_iteration_record;
 
 int simp_problem_create(const simp_problem_desc* desc, const simp_solver_options* opts,

@@ -93,7 +93,7 @@ class IterationRecord(C.Structure):
     _fields_ = [("compliance", C.c_double), ("volume_fraction", C.c_double),
                 ("max_change", C.c_double), ("lam", C.c_double), ("gray_level", C.c_double),
                 ("linear_iterations", C.c_int32), ("bisections", C.c_int32),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("volume_converged", C.c_int32), ("reserved", C.c_int32)]
 
 
 _lock = threading.Lock()

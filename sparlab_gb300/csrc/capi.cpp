@@ -548,6 +548,9 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
       rec->linear_iterations = ev.linear_iterations;
       rec->bisections = st.bisections;
       rec->seconds = ms * 1e-3;
+      rec->volume_converged =
+          g.d.optimizer == 1 ? (ev.volume_fraction / g.d.vf - 1.0 <= 1.0e-4 ? 1 : 0) : (st.converged ? 1 : 0);
+      rec->reserved = 0;
     }
   });
 }

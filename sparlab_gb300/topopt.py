@@ -69,6 +69,7 @@ class TopologyIteration:
     linear_iterations: int
     bisections: int
     seconds: float
+    volume_converged: bool = False
 
 
 class GpuSimpProblem:
@@ -263,7 +264,8 @@ class TopologyOptimizer:
             r = self.problem.iterate()
             history.append(TopologyIteration(it, r.compliance, r.volume_fraction, r.max_change,
                                              r.lam, r.gray_level, r.linear_iterations,
-                                             r.bisections, time.perf_counter() - t0))
+                                             r.bisections, time.perf_counter() - t0,
+                                             bool(r.volume_converged)))
             if self.change_tolerance > 0 and r.max_change <= self.change_tolerance:
                 break
         return history

@@ -204,3 +204,19 @@ def test_batched_instances_match_sequential_and_oracle():
     _, hist = ref.run(iters)
     for k in range(iters):
         assert abs(recs[0][k].compliance / hist[k, 0] - 1) < 1e-6
+
+
+def test_run_writes_reference_history(tmp_path):
+    """A GPU run's history.csv carries the records simp_iterate returned."""
+    import csv
+    from sparlab_gb300.results import OC_COLUMNS, write_results
+    spec = small_q4(30, 12)
+    gpu = GpuSimpProblem(spec)
+    hist = TopologyOptimizer(gpu, max_iterations=4, change_tolerance=0).run()
+    write_results(str(tmp_path), spec, hist, "oc", max_iterations=4, change_tolerance=0.0)
+    rows = list(csv.reader(open(tmp_path / "history.csv")))
+    assert rows[0] == OC_COLUMNS and len(rows) == 5
+    for r, h in zip(rows[1:], hist):
+        assert float(r[OC_COLUMNS.index("compliance[J]")]) == h.compliance
+        assert int(float(r[OC_COLUMNS.index("oc_bisections[-]")])) == h.bisections
+        assert r[OC_COLUMNS.index("volume_converged[-]")] in ("0", "1")
