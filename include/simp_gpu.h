@@ -155,6 +155,13 @@ typedef struct {
                                    optimal combination of the last 3 displacements */
   int32_t block_pcg;            /* 1: all load cases as one block of RHS */
   int32_t optimizer;            /* simp_iterate's update: 0 OC, 1 MMA */
+  /* Heaviside projection of the filtered density with beta continuation
+   * (ProjectionOptions, include/sparlab/topopt/Projection.hpp:69-96,
+   * BetaSchedule, src/topopt/TopologyOptimizer.cpp:17-46); 0 disables */
+  int32_t projection;
+  double eta, beta_start, beta_max, beta_factor;
+  int32_t beta_interval, advance_on_convergence;
+  double change_tolerance;      /* design-change tolerance of the beta advance */
 } simp_problem_desc;
 
 /* ObjectiveEvaluation scalars (Sensitivity.hpp:66-107) and an OC step
@@ -183,7 +190,8 @@ typedef struct {
   int32_t linear_iterations, bisections;
   double seconds;
   int32_t volume_converged;
-  int32_t reserved;
+  int32_t final_stage;          /* 1: no projection, or its last beta stage (convergence may stop) */
+  double beta;                  /* projection sharpness of the iteration (0: none) */
 } simp_iteration_record;
 
 int simp_problem_create(const simp_problem_desc* desc, const simp_solver_options* opts,

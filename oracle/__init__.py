@@ -63,7 +63,10 @@ class ProblemDesc(C.Structure):
                 ("emin_ratio", C.c_double), ("move_limit", C.c_double),
                 ("damping", C.c_double), ("rtol", C.c_double),
                 ("max_cg_iterations", C.c_int32), ("warm_start", C.c_int32),
-                ("amg", AmgOptions)]
+                ("amg", AmgOptions), ("projection", C.c_int32), ("eta", C.c_double),
+                ("beta_start", C.c_double), ("beta_max", C.c_double), ("beta_factor", C.c_double),
+                ("beta_interval", C.c_int32), ("advance_on_convergence", C.c_int32),
+                ("change_tolerance", C.c_double)]
 
 
 def lib():
@@ -232,6 +235,14 @@ class Problem:
         d.rtol, d.max_cg_iterations = spec.rtol, spec.max_cg_iterations
         d.warm_start = int(spec.warm_start)
         d.amg = amg_options(**(amg or spec.amg))
+        d.projection = int(getattr(spec, "projection", False))
+        d.eta = getattr(spec, "eta", 0.5)
+        d.beta_start = getattr(spec, "beta_start", 1.0)
+        d.beta_max = getattr(spec, "beta_max", 32.0)
+        d.beta_factor = getattr(spec, "beta_factor", 2.0)
+        d.beta_interval = getattr(spec, "beta_interval", 50)
+        d.advance_on_convergence = int(getattr(spec, "advance_on_convergence", True))
+        d.change_tolerance = getattr(spec, "change_tolerance", 1e-3)
         self._desc = d
         self._h = C.c_void_p()
         _check(lib().orc_problem_create(C.byref(d), C.byref(self._h)))
@@ -317,8 +328,10 @@ class Problem:
         return x, hist[: done.value]
 
     def run(self, iterations, change_tol=0.0):
+        """run_oc: final design and history rows (compliance, volume
+        fraction, max change, lambda, CG iterations, bisections, beta)."""
         x = np.zeros(self.ne)
-        hist = np.zeros((iterations, 6))
+        hist = np.zeros((iterations, 7))
         done = C.c_int32()
         _check(lib().orc_run(self._h, C.c_int32(iterations), C.c_double(change_tol), _p(x),
                              _p(hist), C.byref(done)))

@@ -1198,6 +1198,12 @@ struct Problem {
   int maxit = 1000;
   bool warm = true;
   AmgOptions amg_opt;
+  // Heaviside projection (src/topopt/Projection.cpp) and its beta schedule
+  bool proj = false;
+  double eta = 0.5, beta_start = 1.0, beta_max = 32.0, beta_factor = 2.0, change_tol = 1e-3;
+  int beta_interval = 50;
+  bool advance = true;
+  double beta = 0.0;
   std::unique_ptr<Amg> amg;
   std::vector<Vec> previous;
   Layout layout;
@@ -1487,6 +1493,36 @@ struct Evaluation {
   std::vector<Vec> u;
 };
 
+// heaviside_project / heaviside_derivative (src/topopt/Projection.cpp:56-69)
+double project(double r, double beta, double eta) {
+  const double a = std::tanh(beta * eta);
+  const double denom = a + std::tanh(beta * (1.0 - eta));
+  return (a + std::tanh(beta * (r - eta))) / denom;
+}
+
+double project_derivative(double r, double beta, double eta) {
+  const double denom = std::tanh(beta * eta) + std::tanh(beta * (1.0 - eta));
+  const double t = std::tanh(beta * (r - eta));
+  return beta * (1.0 - t * t) / denom;
+}
+
+// ProjectionOptions::num_stages / beta_of_stage (src/topopt/Projection.cpp:45-54)
+int beta_stages(const Problem& p) {
+  int stages = 1;
+  double b = p.beta_start;
+  while (b < p.beta_max && stages < 64) {
+    b *= p.beta_factor;
+    ++stages;
+  }
+  return stages;
+}
+
+double beta_of_stage(const Problem& p, int k) {
+  double b = p.beta_start;
+  for (int i = 0; i < k && b < p.beta_max; ++i) b *= p.beta_factor;
+  return std::min(b, p.beta_max);
+}
+
 void evaluate(Problem& p, const double* x, Evaluation& out) {
   const Index ne = p.ne;
   for (Index e = 0; e < ne; ++e) if (!std::isfinite(x[e])) throw Error(kBadInput, "design vector contains NaN or Inf");
@@ -1494,6 +1530,15 @@ void evaluate(Problem& p, const double* x, Evaluation& out) {
   out.rho.resize(static_cast<size_t>(ne));
   filter_forward(p, x, out.rho.data());
   for (auto& r : out.rho) r = std::min(std::max(r, 0.0), 1.0);
+  // physical density: the projected filtered density (Sensitivity.cpp:69-73)
+  Vec dproj;
+  if (p.proj) {
+    dproj.resize(static_cast<size_t>(ne));
+    for (Index e = 0; e < ne; ++e) {
+      dproj[e] = project_derivative(out.rho[e], p.beta, p.eta);
+      out.rho[e] = project(out.rho[e], p.beta, p.eta);
+    }
+  }
   Vec sf(static_cast<size_t>(ne)), df(static_cast<size_t>(ne));
   for (Index e = 0; e < ne; ++e) {
     sf[e] = simp_factor(out.rho[e], p.penalty, p.emin);
@@ -1558,8 +1603,18 @@ void evaluate(Problem& p, const double* x, Evaluation& out) {
   out.volume_fraction = vol / p.domain_volume;
   out.dc_dx.resize(static_cast<size_t>(ne));
   out.dv_dx.resize(static_cast<size_t>(ne));
-  filter_adjoint(p, out.dc_dphys.data(), out.dc_dx.data());
-  filter_adjoint(p, p.volumes.data(), out.dv_dx.data());
+  if (p.proj) {  // chain_to_design (Sensitivity.cpp:100-108)
+    Vec dc(static_cast<size_t>(ne)), dv(static_cast<size_t>(ne));
+    for (Index e = 0; e < ne; ++e) {
+      dc[e] = out.dc_dphys[e] * dproj[e];
+      dv[e] = p.volumes[e] * dproj[e];
+    }
+    filter_adjoint(p, dc.data(), out.dc_dx.data());
+    filter_adjoint(p, dv.data(), out.dv_dx.data());
+  } else {
+    filter_adjoint(p, out.dc_dphys.data(), out.dc_dx.data());
+    filter_adjoint(p, p.volumes.data(), out.dv_dx.data());
+  }
   if (!std::isfinite(out.compliance)) throw Error(kNonFinite, "the compliance objective evaluated to a non-finite value");
 }
 
@@ -1586,7 +1641,11 @@ void oc_candidate(const Problem& p, const double* x, const double* dc, const dou
 double design_volume(const Problem& p, const double* xn, Vec& tmp) {
   filter_forward(p, xn, tmp.data());
   double v = 0.0;
-  for (Index e = 0; e < p.ne; ++e) v += std::min(std::max(tmp[e], 0.0), 1.0) * p.volumes[e];
+  for (Index e = 0; e < p.ne; ++e) {
+    double r = std::min(std::max(tmp[e], 0.0), 1.0);
+    if (p.proj) r = project(r, p.beta, p.eta);
+    v += r * p.volumes[e];
+  }
   return v;
 }
 
@@ -2072,6 +2131,17 @@ int orc_problem_create(const orc_problem_desc* d, orc_problem** out) {
     p.maxit = d->max_cg_iterations > 0 ? d->max_cg_iterations : 1000;
     p.warm = d->warm_start != 0;
     p.amg_opt = convert(&d->amg);
+    p.proj = d->projection != 0;
+    if (p.proj) {
+      p.eta = d->eta;
+      p.beta_start = d->beta_start;
+      p.beta_max = d->beta_max;
+      p.beta_factor = d->beta_factor;
+      p.beta_interval = std::max(1, d->beta_interval);
+      p.advance = d->advance_on_convergence != 0;
+      p.change_tol = d->change_tolerance;
+      p.beta = beta_of_stage(p, 0);
+    }
     p.layout = Layout{p.dim, p.dim, p.coords.data(), p.nn, p.free_dofs.data(),
                       static_cast<Index>(p.free_dofs.size())};
     *out = holder.release();
@@ -2206,21 +2276,33 @@ int orc_run(orc_problem* h, int32_t iterations, double change_tol, double* x, do
     Problem& p = h->p;
     Vec xv(static_cast<size_t>(p.ne), p.x0);
     for (auto& v : xv) v = std::min(std::max(v, 0.0), 1.0);
+    // beta continuation (BetaSchedule, src/topopt/TopologyOptimizer.cpp:17-46)
+    const int stages = p.proj ? beta_stages(p) : 1;
+    int stage = 0, stage_start = 1;
+    if (p.proj) p.beta = beta_of_stage(p, 0);
     int it = 0;
     for (it = 1; it <= iterations; ++it) {
       Evaluation ev;
       evaluate(p, xv.data(), ev);
       const OcStep st = oc_update(p, xv.data(), ev.dc_dx.data(), ev.dv_dx.data());
-      double* row = hist + static_cast<size_t>(it - 1) * 6;
+      double* row = hist + static_cast<size_t>(it - 1) * 7;
       row[0] = ev.compliance;
       row[1] = ev.volume_fraction;
       row[2] = st.max_change;
       row[3] = st.lambda;
       row[4] = ev.linear_iterations;
       row[5] = st.bisections;
+      row[6] = p.proj ? p.beta : 0.0;
       xv = st.x;
       for (auto& v : xv) v = std::min(std::max(v, 0.0), 1.0);
-      if (change_tol > 0.0 && st.max_change <= change_tol) break;
+      const bool at_final = !p.proj || stage + 1 >= stages;
+      if (at_final && change_tol > 0.0 && st.max_change <= change_tol) break;
+      if (!at_final && (it - stage_start + 1 >= p.beta_interval ||
+                        (p.advance && st.max_change <= p.change_tol))) {
+        ++stage;
+        stage_start = it + 1;
+        p.beta = beta_of_stage(p, stage);
+      }
     }
     *performed = std::min(it, iterations);
     std::copy(xv.begin(), xv.end(), x);

@@ -49,6 +49,12 @@ typedef struct {
   int32_t max_cg_iterations;   /* 0 -> 1000 */
   int32_t warm_start;
   orc_amg_options amg;
+  /* Heaviside projection with beta continuation (ProjectionOptions,
+   * include/sparlab/topopt/Projection.hpp:69-96); projection = 0 disables */
+  int32_t projection;
+  double eta, beta_start, beta_max, beta_factor;
+  int32_t beta_interval, advance_on_convergence;
+  double change_tolerance;     /* run_oc's design-change tolerance (beta advance) */
 } orc_problem_desc;
 
 typedef struct orc_problem orc_problem;
@@ -107,9 +113,10 @@ int orc_evaluate(orc_problem* p, const double* x, double* out, double* rho_phys,
  * bisections, volume converged */
 int orc_oc_update(orc_problem* p, const double* x, const double* dc_dx,
                   const double* dv_dx, double* xnew, double* out);
-/* run_oc for `iterations` iterations (no early stop when change_tol <= 0);
- * history: per iteration compliance, volume fraction, max change, lambda,
- * linear iterations, bisections. */
+/* run_oc for `iterations` iterations (no early stop when change_tol <= 0;
+ * with projection only the final beta stage may stop); history: per
+ * iteration compliance, volume fraction, max change, lambda, linear
+ * iterations, bisections, beta (0 without projection). */
 int orc_run(orc_problem* p, int32_t iterations, double change_tol, double* x,
             double* history, int32_t* performed);
 /* run_mma for `iterations` iterations (MMA with the volume constraint); history:

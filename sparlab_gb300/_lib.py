@@ -75,7 +75,10 @@ class ProblemDesc(C.Structure):
                 ("filter_radius", C.c_double), ("volume_fraction", C.c_double),
                 ("initial_density", C.c_double), ("penalty", C.c_double),
                 ("emin_ratio", C.c_double), ("move_limit", C.c_double), ("damping", C.c_double),
-                ("warm_start", C.c_int32), ("block_pcg", C.c_int32), ("optimizer", C.c_int32)]
+                ("warm_start", C.c_int32), ("block_pcg", C.c_int32), ("optimizer", C.c_int32),
+                ("projection", C.c_int32), ("eta", C.c_double), ("beta_start", C.c_double),
+                ("beta_max", C.c_double), ("beta_factor", C.c_double), ("beta_interval", C.c_int32),
+                ("advance_on_convergence", C.c_int32), ("change_tolerance", C.c_double)]
 
 
 class Evaluation(C.Structure):
@@ -93,7 +96,8 @@ class IterationRecord(C.Structure):
     _fields_ = [("compliance", C.c_double), ("volume_fraction", C.c_double),
                 ("max_change", C.c_double), ("lam", C.c_double), ("gray_level", C.c_double),
                 ("linear_iterations", C.c_int32), ("bisections", C.c_int32),
-                ("seconds", C.c_double), ("volume_converged", C.c_int32), ("reserved", C.c_int32)]
+                ("seconds", C.c_double), ("volume_converged", C.c_int32), ("final_stage", C.c_int32),
+                ("beta", C.c_double)]
 
 
 _lock = threading.Lock()

@@ -420,6 +420,30 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     if (dsc->warm_start < 0 || dsc->warm_start > 2) throw Error(kBadInput, "warm_start must be 0, 1 or 2");
     d.warm = dsc->warm_start;
     d.block_pcg = dsc->block_pcg != 0;
+    d.projection = dsc->projection != 0;
+    if (d.projection) {
+      // ProjectionOptions::validate (src/topopt/Projection.cpp:10-43)
+      std::ostringstream os;
+      if (!(dsc->eta > 0.0 && dsc->eta < 1.0)) os << "projection eta must lie in (0, 1), got " << dsc->eta;
+      else if (!(dsc->beta_start > 0.0) || !std::isfinite(dsc->beta_start))
+        os << "projection beta_start must be positive, got " << dsc->beta_start;
+      else if (!(dsc->beta_max >= dsc->beta_start) || !std::isfinite(dsc->beta_max))
+        os << "projection beta_max (" << dsc->beta_max << ") must be at least beta_start (" << dsc->beta_start
+           << ")";
+      else if (dsc->beta_max > 1024.0)
+        os << "projection beta_max = " << dsc->beta_max << " is beyond any useful sharpness";
+      else if (!(dsc->beta_factor > 1.0)) os << "projection beta_factor must exceed 1, got " << dsc->beta_factor;
+      else if (dsc->beta_interval < 1)
+        os << "projection beta_interval must be at least 1, got " << dsc->beta_interval;
+      if (!os.str().empty()) throw Error(kBadInput, os.str());
+      d.eta = dsc->eta;
+      d.beta_start = dsc->beta_start;
+      d.beta_max = dsc->beta_max;
+      d.beta_factor = dsc->beta_factor;
+      d.beta_interval = dsc->beta_interval;
+      d.advance_on_convergence = dsc->advance_on_convergence != 0;
+      d.change_tol = dsc->change_tolerance;
+    }
     if (dsc->optimizer != 0 && dsc->optimizer != 1) throw Error(kBadInput, "unknown optimizer (expected 0 OC, 1 MMA)");
     d.optimizer = dsc->optimizer;
     std::unique_ptr<simp_problem> p(new simp_problem());
@@ -531,6 +555,7 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
     SIMP_CUDA(cudaEventCreate(&e0));
     SIMP_CUDA(cudaEventCreate(&e1));
     SIMP_CUDA(cudaEventRecord(e0, g.amg.stream));
+    ++g.iteration;
     const Evaluation ev = g.evaluate();
     const OcStep st = g.d.optimizer == 1 ? g.mma_update(true, nullptr) : g.oc_update(true, nullptr);
     SIMP_CUDA(cudaEventRecord(e1, g.amg.stream));
@@ -550,8 +575,10 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
       rec->seconds = ms * 1e-3;
       rec->volume_converged =
           g.d.optimizer == 1 ? (ev.volume_fraction / g.d.vf - 1.0 <= 1.0e-4 ? 1 : 0) : (st.converged ? 1 : 0);
-      rec->reserved = 0;
+      rec->final_stage = g.beta_at_final() ? 1 : 0;
+      rec->beta = g.d.projection ? g.beta : 0.0;
     }
+    g.advance_beta(st.max_change);
   });
 }
 

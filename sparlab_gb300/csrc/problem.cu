@@ -409,8 +409,13 @@ void GpuProblem::build() {
     }
   }
   hw.upload(w);
-  // dv/dx = H^T v does not depend on the design
+  // dv/dx = H^T v does not depend on the design (without projection)
   filter_adjoint(vols.p, dv_dx.p);
+  if (d.projection) {
+    rhot.alloc(ne_s);
+    dproj.alloc(ne_s);
+    beta = beta_of_stage(d, 0);
+  }
   // initial design
   std::vector<double> x0(ne_s, std::min(std::max(d.x0, 0.0), 1.0));
   x.upload(x0);
@@ -480,8 +485,13 @@ Evaluation GpuProblem::evaluate() {
   Evaluation ev;
   // physical density, SIMP factors, stiffness (Sensitivity.cpp:121-139)
   k_filter_forward<<<grid_for(ne, kRedThreads), kRedThreads, 0, s>>>(
-      grid_of(d), static_cast<const Stencil*>(stencil_d), hw.p, ne, x.p, rho.p, 1, nullptr, nullptr);
+      grid_of(d), static_cast<const Stencil*>(stencil_d), hw.p, ne, x.p, d.projection ? rhot.p : rho.p, 1,
+      nullptr, nullptr);
   SIMP_CHECK_LAUNCH();
+  if (d.projection) {  // the physical density is the projected one (Sensitivity.cpp:69-73)
+    k_project<<<grid_for(ne, 256), 256, 0, s>>>(ne, rhot.p, beta, d.eta, rho.p, dproj.p);
+    SIMP_CHECK_LAUNCH();
+  }
   k_simp<<<grid_for(ne, 256), 256, 0, s>>>(ne, rho.p, d.penalty, d.emin, sf.p, df.p);
   SIMP_CHECK_LAUNCH();
   if (amg.mf.enabled) {
@@ -527,7 +537,16 @@ Evaluation GpuProblem::evaluate() {
   k_sensitivities<<<grid_for(ne, 128), 128, 0, s>>>(grid_of(d), ne, d.nloads, u.p, nfree, dof_map.p, ke_d.p,
                                                    weights_d.p, sf.p, df.p, dc_dphys.p, se.p);
   SIMP_CHECK_LAUNCH();
-  filter_adjoint(dc_dphys.p, dc_dx.p);
+  if (d.projection) {  // chain_to_design (Sensitivity.cpp:100-108)
+    k_mul<<<grid_for(ne, 256), 256, 0, s>>>(ne, dc_dphys.p, dproj.p, tmp.p);
+    SIMP_CHECK_LAUNCH();
+    filter_adjoint(tmp.p, dc_dx.p);
+    k_mul<<<grid_for(ne, 256), 256, 0, s>>>(ne, vols.p, dproj.p, tmp.p);
+    SIMP_CHECK_LAUNCH();
+    filter_adjoint(tmp.p, dv_dx.p);
+  } else {
+    filter_adjoint(dc_dphys.p, dc_dx.p);
+  }
   // volume of the physical density
   k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, s>>>(rho.p, vols.p, ne, amg.part.p);
   SIMP_CHECK_LAUNCH();
@@ -544,6 +563,36 @@ Evaluation GpuProblem::evaluate() {
 
 // optimality_criteria_update with the filtered candidate volume per trial
 // (src/topopt/OptimalityCriteria.cpp:40-149).
+// ProjectionOptions::num_stages / beta_of_stage (src/topopt/Projection.cpp:45-54)
+int beta_stages(const ProblemDesc& d) {
+  int stages = 1;
+  double b = d.beta_start;
+  while (b < d.beta_max && stages < 64) {
+    b *= d.beta_factor;
+    ++stages;
+  }
+  return stages;
+}
+
+double beta_of_stage(const ProblemDesc& d, int k) {
+  double b = d.beta_start;
+  for (int i = 0; i < k && b < d.beta_max; ++i) b *= d.beta_factor;
+  return std::min(b, d.beta_max);
+}
+
+bool GpuProblem::beta_at_final() const { return !d.projection || beta_stage + 1 >= beta_stages(d); }
+
+// BetaSchedule::advance (src/topopt/TopologyOptimizer.cpp:29-40)
+void GpuProblem::advance_beta(double max_change) {
+  if (beta_at_final()) return;
+  if (iteration - beta_stage_start + 1 >= d.beta_interval ||
+      (d.advance_on_convergence && max_change <= d.change_tol)) {
+    ++beta_stage;
+    beta_stage_start = iteration + 1;
+    beta = beta_of_stage(d, beta_stage);
+  }
+}
+
 OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
   if (!evaluated) throw Error(kBadInput, "oc_update needs gradients: call evaluate first");
   cudaStream_t s = amg.stream;
@@ -558,7 +607,16 @@ OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
   SIMP_CHECK_LAUNCH();
   auto factor = [&](double lam) { return d.damping == 0.5 ? 1.0 / std::sqrt(lam) : std::pow(lam, -d.damping); };
   auto volume_of = [&](double lam) {
-    k_oc_volume<<<kRedBlocks, kRedThreads, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p, dv_dx.p, factor(lam), part);
+    if (d.projection) {
+      // the projected volume is not linear in the design: candidate, then a
+      // filter + projection pass (volume_of_design of run_oc)
+      k_oc_apply<<<grid_for(ne, 256), 256, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p, factor(lam), xnew.p);
+      SIMP_CHECK_LAUNCH();
+      k_filter_volume_projected<<<kRedBlocks, kRedThreads, 0, s>>>(
+          grid_of(d), static_cast<const Stencil*>(stencil_d), hw.p, ne, xnew.p, vols.p, beta, d.eta, part);
+    } else {
+      k_oc_volume<<<kRedBlocks, kRedThreads, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p, dv_dx.p, factor(lam), part);
+    }
     SIMP_CHECK_LAUNCH();
     k_reduce_final<<<1, kRedThreads, 0, s>>>(part, kRedBlocks, amg.scal.p + 5, 0);
     SIMP_CHECK_LAUNCH();

@@ -31,6 +31,11 @@ struct ProblemDesc {
   int warm = 1;  // 0 zero start, 1 previous displacement, 2 projection on the last kHistory
   bool block_pcg = false;
   int optimizer = 0;  // 0 OC, 1 MMA
+  // Heaviside projection (src/topopt/Projection.cpp) with beta continuation
+  bool projection = false;
+  double eta = 0.5, beta_start = 1.0, beta_max = 32.0, beta_factor = 2.0, change_tol = 1e-3;
+  int beta_interval = 50;
+  bool advance_on_convergence = true;
 };
 
 struct Evaluation {
@@ -99,6 +104,13 @@ class GpuProblem {
   std::vector<int> hist_count;
   void projected_start(int l, double* ul);
   void record_history(int l, const double* ul);
+  // projection state: current beta, its stage, the stage's first iteration
+  double beta = 0.0;
+  int beta_stage = 0, beta_stage_start = 1, iteration = 0;
+  DBuf<double> rhot, dproj;  // clamped filtered density and d rho_bar / d rho_tilde
+  bool beta_at_final() const;
+  // BetaSchedule::advance after iteration `iteration` with its design change
+  void advance_beta(double max_change);
   bool evaluated = false;
   int evaluations = 0;
   double gray = 0.0;
@@ -109,6 +121,9 @@ class GpuProblem {
   std::vector<i32> free_dofs_;
   void build();
 };
+
+int beta_stages(const ProblemDesc& d);
+double beta_of_stage(const ProblemDesc& d, int k);
 
 void element_stiffness(int dim, double hx, double hy, double hz, double young, double nu, double thick,
                        double* ke);

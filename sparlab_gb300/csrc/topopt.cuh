@@ -296,6 +296,57 @@ __global__ void __launch_bounds__(128) k_sensitivities(GridView g, i64 ne, int n
   }
 }
 
+// Heaviside projection of the clamped filtered density and its derivative
+// (heaviside_project / heaviside_derivative, src/topopt/Projection.cpp:56-69).
+__device__ __forceinline__ double project_one(double r, double beta, double eta, double& deriv) {
+  const double a = tanh(beta * eta);
+  const double denom = a + tanh(beta * (1.0 - eta));
+  const double t = tanh(beta * (r - eta));
+  deriv = beta * (1.0 - t * t) / denom;
+  return (a + t) / denom;
+}
+
+__global__ void k_project(i64 ne, const double* __restrict__ rt, double beta, double eta, double* __restrict__ rho,
+                          double* __restrict__ dproj) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x) {
+    double dp;
+    rho[e] = project_one(rt[e], beta, eta, dp);
+    if (dproj) dproj[e] = dp;
+  }
+}
+
+__global__ void k_mul(i64 ne, const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out) {
+  for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x)
+    out[e] = a[e] * b[e];
+}
+
+// Projected filtered volume of a candidate design: block partials of
+// sum_e v_e rho_bar(clamp((H x)_e)) (the OC trial volume with projection on).
+__global__ void __launch_bounds__(kRedThreads) k_filter_volume_projected(GridView g, const Stencil* __restrict__ st,
+                                                                         const double* __restrict__ w, i64 ne,
+                                                                         const double* __restrict__ x,
+                                                                         const double* __restrict__ volumes,
+                                                                         double beta, double eta,
+                                                                         double* __restrict__ part) {
+  double vs = 0.0;
+  for (i64 e = blockIdx.x * (i64)kRedThreads + threadIdx.x; e < ne; e += (i64)gridDim.x * kRedThreads) {
+    const i32 ex = static_cast<i32>(e % g.nx), ey = static_cast<i32>((e / g.nx) % g.ny),
+              ez = static_cast<i32>(e / ((i64)g.nx * g.ny));
+    double s = 0.0;
+    for (int k = 0; k < st->count; ++k) {
+      const i32 qx = ex + st->dx[k], qy = ey + st->dy[k], qz = ez + st->dz[k];
+      if (!in_grid(g, qx, qy, qz)) continue;
+      const i64 q = (static_cast<i64>(qz) * g.ny + qy) * g.nx + qx;
+      s = xadd(s, xmul(w[k * ne + e], x[q]));
+    }
+    s = fmin(fmax(s, 0.0), 1.0);
+    double dp;
+    vs += project_one(s, beta, eta, dp) * volumes[e];
+  }
+  vs = block_sum<kRedThreads>(vs);
+  if (threadIdx.x == 0) part[blockIdx.x] = vs;
+}
+
 // Per OC update (src/topopt/OptimalityCriteria.cpp:14-38 restated for a
 // multiplier search on the GPU): g_e = x_e max(0, -dc_e / dv_e)^eta (0 where
 // dv_e <= 0) and the move-limited box [lo_e, hi_e], so that the candidate of

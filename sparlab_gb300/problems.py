@@ -79,6 +79,16 @@ class ProblemSpec:
     rtol: float = 1e-8
     max_cg_iterations: int = 0
     warm_start: int = 1  # 0 zero guess, 1 previous displacement, 2 projection on the last 3
+    # Heaviside projection of the filtered density with beta continuation
+    # (ProjectionOptions, include/sparlab/topopt/Projection.hpp:69-96)
+    projection: bool = False
+    eta: float = 0.5
+    beta_start: float = 1.0
+    beta_max: float = 32.0
+    beta_factor: float = 2.0
+    beta_interval: int = 50
+    advance_on_convergence: bool = True
+    change_tolerance: float = 1e-3  # run_oc's design-change tolerance (beta advance)
     amg: Dict = dataclasses.field(default_factory=dict)
     name: str = ""
 

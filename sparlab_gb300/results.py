@@ -4,9 +4,10 @@ formats, so its plotting package (``python/sparlab_viz``: ``load_csv`` of
 ``summary["optimization_result"]``) reads a GPU run unchanged.
 
 * ``history.csv``: the columns of ``ResultWriter::write_history``
-  (``src/io/ResultWriter.cpp:1428-1460``) for a run without stress, projection,
-  buckling or robust terms, numbers as ``CsvWriter`` prints them
-  (``std::setprecision(17)``, ``src/io/CsvWriter.cpp:58-97``).
+  (``src/io/ResultWriter.cpp:1428-1460``) for a run without stress, buckling
+  or robust terms (``beta[-]`` when the projection is on), numbers as
+  ``CsvWriter`` prints them (``std::setprecision(17)``,
+  ``src/io/CsvWriter.cpp:58-97``).
 * ``summary.json``: the ``optimization_setup`` / ``optimization_result`` /
   ``tolerances`` / ``provenance`` members of ``make_topology_summary``
   (``src/io/ResultWriter.cpp:2546-2883``) that this path determines; mesh,
@@ -41,12 +42,20 @@ def domain_volume(spec: ProblemSpec) -> float:
     return spec.lx * spec.ly * spec.lz
 
 
+def history_columns(method: str = "oc", projected: bool = False) -> List[str]:
+    cols = list(MMA_COLUMNS if method == "mma" else OC_COLUMNS)
+    if projected:
+        cols.append("beta[-]")
+    return cols
+
+
 def write_history_csv(path: str, history: Sequence, spec: ProblemSpec, method: str = "oc") -> None:
     """One row per :class:`~sparlab_gb300.topopt.TopologyIteration`."""
     mma = method == "mma"
     vol = domain_volume(spec)
+    projected = bool(getattr(spec, "projection", False))
     with open(path, "w") as f:
-        f.write(",".join(MMA_COLUMNS if mma else OC_COLUMNS) + "\n")
+        f.write(",".join(history_columns(method, projected)) + "\n")
         for it in history:
             row = [spec.penalty, it.compliance, it.volume_fraction * vol, it.volume_fraction,
                    it.max_change, it.lam, it.gray_level, it.bisections,
@@ -55,6 +64,8 @@ def write_history_csv(path: str, history: Sequence, spec: ProblemSpec, method: s
                 # no stress constraint on this path; the volume constraint's violation
                 row += [0.0, 0.0, max(0.0, it.volume_fraction / spec.volume_fraction - 1.0)]
             row.append(it.linear_iterations)
+            if projected:
+                row.append(it.beta)
             f.write(str(int(it.iteration)) + "," + ",".join(_num(v) for v in row) + "\n")
 
 
@@ -90,7 +101,12 @@ def summary(spec: ProblemSpec, history: Sequence, method: str = "oc", max_iterat
         "move_limit": spec.move_limit, "damping": spec.damping,
         "max_iterations": max_iterations, "change_tolerance": change_tolerance,
         "method": method,
-        "projection": {"enabled": False},
+        "projection": ({"enabled": True, "eta": spec.eta, "beta_start": spec.beta_start,
+                        "beta_max": spec.beta_max, "beta_factor": spec.beta_factor,
+                        "beta_interval": spec.beta_interval,
+                        "advance_on_convergence": bool(spec.advance_on_convergence),
+                        "robust": False}
+                       if getattr(spec, "projection", False) else {"enabled": False}),
     }
     if method == "mma":
         setup["constraint_tolerance"] = 1.0e-4
@@ -113,6 +129,8 @@ def summary(spec: ProblemSpec, history: Sequence, method: str = "oc", max_iterat
         "robust": False,
     }
     result["volume_constraint_satisfied"] = result["volume_constraint_relative_violation"] <= 1.0e-6
+    if getattr(spec, "projection", False) and last:
+        result["projection"] = {"final_beta": last.beta, "eta": spec.eta}
     if history:
         c0 = history[0].compliance
         result["initial_compliance_J"] = c0

@@ -70,6 +70,8 @@ class TopologyIteration:
     bisections: int
     seconds: float
     volume_converged: bool = False
+    beta: float = 0.0          # projection sharpness (0: no projection)
+    final_stage: bool = True   # no projection, or its last beta stage
 
 
 class GpuSimpProblem:
@@ -105,6 +107,11 @@ class GpuSimpProblem:
         d.warm_start = int(spec.warm_start)
         d.block_pcg = int(block_pcg)
         d.optimizer = {"oc": 0, "mma": 1}[optimizer]
+        d.projection = int(spec.projection)
+        d.eta, d.beta_start, d.beta_max = spec.eta, spec.beta_start, spec.beta_max
+        d.beta_factor, d.beta_interval = spec.beta_factor, spec.beta_interval
+        d.advance_on_convergence = int(spec.advance_on_convergence)
+        d.change_tolerance = spec.change_tolerance
         prec = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
         opts = dict(spec.amg)
         opts.update(amg)
@@ -265,8 +272,9 @@ class TopologyOptimizer:
             history.append(TopologyIteration(it, r.compliance, r.volume_fraction, r.max_change,
                                              r.lam, r.gray_level, r.linear_iterations,
                                              r.bisections, time.perf_counter() - t0,
-                                             bool(r.volume_converged)))
-            if self.change_tolerance > 0 and r.max_change <= self.change_tolerance:
+                                             bool(r.volume_converged), r.beta, bool(r.final_stage)))
+            # during beta continuation only the final stage may stop the run
+            if self.change_tolerance > 0 and r.final_stage and r.max_change <= self.change_tolerance:
                 break
         return history
 

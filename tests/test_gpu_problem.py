@@ -220,3 +220,45 @@ def test_run_writes_reference_history(tmp_path):
         assert float(r[OC_COLUMNS.index("compliance[J]")]) == h.compliance
         assert int(float(r[OC_COLUMNS.index("oc_bisections[-]")])) == h.bisections
         assert r[OC_COLUMNS.index("volume_converged[-]")] in ("0", "1")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_projected_run_matches_oracle(precision):
+    """Heaviside projection with beta continuation (Projection.cpp,
+    TopologyOptimizer.cpp:17-46): physical density, chain rule, projected OC
+    volume and the beta schedule against the oracle."""
+    spec = small_q4(40, 20)
+    spec.rtol = 1e-10
+    spec.initial_density = 0.5
+    spec.projection, spec.beta_start, spec.beta_max = True, 1.0, 8.0
+    spec.beta_interval, spec.advance_on_convergence = 2, False
+    ref = oracle.Problem(spec)
+    _, hist = ref.run(8)
+    gpu = GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision=precision)
+    recs = TopologyOptimizer(gpu, max_iterations=8, change_tolerance=0).run()
+    assert [r.beta for r in recs] == list(hist[:, 6])
+    for k, r in enumerate(recs):
+        assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
+        assert abs(r.volume_fraction - hist[k, 1]) < 1e-8
+    assert [r.final_stage for r in recs][-1]
+
+
+def test_projected_evaluate_matches_oracle():
+    spec = small_hex(12, 6, 6)
+    spec.volume_fraction = 0.45
+    spec.projection, spec.beta_start = True, 4.0
+    ref, gpu = pair(spec)
+    rng = P.SplitMix64(9)
+    x = rng.uniform_array(ref.ne, 0.01, 1.0)
+    gpu.set_design(x)
+    ev = gpu.evaluate()
+    er = ref.evaluate(x)
+    assert abs(ev.compliance / er["compliance"] - 1) < 1e-8
+    np.testing.assert_allclose(ev.physical_density, er["rho"], rtol=0, atol=1e-14)
+    scale = np.abs(er["dc_dx"]).max()
+    assert np.abs(ev.dc_dx - er["dc_dx"]).max() <= 1e-7 * scale
+    np.testing.assert_allclose(ev.dv_dx, er["dv_dx"], rtol=1e-12, atol=0)
+    step = gpu.oc_update(apply=False)
+    xr, info = ref.oc_update(x, er["dc_dx"], er["dv_dx"])
+    assert abs(step.lam / info["lam"] - 1) < 1e-6
+    assert abs(step.achieved_volume / info["volume"] - 1) < 1e-9

@@ -246,3 +246,54 @@ def test_oc_meets_volume_and_end_to_end_run_improves():
     x, hist = pr.run(30)
     assert np.all(np.abs(hist[:, 1] - 0.4) < 1e-6)
     assert hist[0, 0] / hist[-1, 0] > 1.5
+
+
+def _projected_q4(nx=12, ny=6, beta=4.0):
+    spec = P.q4_cantilever_120x40()
+    spec.nx, spec.ny, spec.lx, spec.ly = nx, ny, float(nx), float(ny)
+    spec.fixed = P.clamp_left(spec)
+    spec.loads = P.point_load(spec, [spec.node_index(nx, ny // 2)], (0.0, -1.0))[None, :]
+    spec.rtol = 1e-13
+    spec.projection, spec.beta_start, spec.beta_max = True, beta, 64.0
+    return spec
+
+
+def test_projection_matches_the_reference_formula():
+    """rho_bar = (tanh(b e) + tanh(b (rho - e))) / (tanh(b e) + tanh(b (1 - e)))
+    (src/topopt/Projection.cpp:56-60) on the clamped filtered density."""
+    spec = _projected_q4()
+    pr = oracle.Problem(spec, amg=dict(coarse_size=60))
+    x = 0.4 + 0.25 * np.sin(np.arange(pr.ne) * 0.7)
+    rt = np.clip(pr.filter_forward(x), 0.0, 1.0)
+    b, e = 4.0, 0.5
+    want = (np.tanh(b * e) + np.tanh(b * (rt - e))) / (np.tanh(b * e) + np.tanh(b * (1 - e)))
+    np.testing.assert_allclose(pr.evaluate(x)["rho"], want, rtol=0, atol=1e-15)
+
+
+def test_projected_finite_difference_sensitivities():
+    """dc/dx and dv/dx through the projection's chain rule (Sensitivity.cpp:
+    100-108) against central differences."""
+    spec = _projected_q4()
+    pr = oracle.Problem(spec, amg=dict(coarse_size=60))
+    x = 0.4 + 0.25 * np.sin(np.arange(pr.ne) * 0.7)
+    ev = pr.evaluate(x)
+    h = 1e-5
+    for e in (0, 7, 33, 60):
+        xp, xm = x.copy(), x.copy()
+        xp[e] += h
+        xm[e] -= h
+        ep, em = pr.evaluate(xp), pr.evaluate(xm)
+        fd = (ep["compliance"] - em["compliance"]) / (2 * h)
+        assert abs(fd - ev["dc_dx"][e]) <= 1e-5 * abs(ev["compliance"])
+        fv = (ep["volume"] - em["volume"]) / (2 * h)
+        assert abs(fv - ev["dv_dx"][e]) <= 1e-6 * abs(ev["dv_dx"]).max()
+
+
+def test_beta_continuation_schedule():
+    """BetaSchedule (TopologyOptimizer.cpp:17-46): beta_start * factor^k,
+    capped, a stage ends after beta_interval iterations."""
+    spec = _projected_q4(20, 10, beta=1.0)
+    spec.beta_max, spec.beta_interval, spec.advance_on_convergence = 4.0, 2, False
+    spec.volume_fraction = 0.45
+    _, hist = oracle.Problem(spec, amg=dict(coarse_size=100)).run(7)
+    assert list(hist[:, 6]) == [1.0, 1.0, 2.0, 2.0, 4.0, 4.0, 4.0]
