@@ -212,84 +212,10 @@ __global__ void k_pcg_direction(double* __restrict__ p, const double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// CSR operator applications: VS lanes per row, butterfly reduction
+// Chebyshev smoothing (Saad, Alg. 12.1 in D^-1 A; src/fem/Multigrid.cpp:
+// 783-855): the operator steps live with the operator kernels (nbspmv.cuh,
+// mfree.cuh); the zero-guess start needs no operator.
 // ---------------------------------------------------------------------------
-template <int VS, class TV, class TX, class TA>
-__device__ __forceinline__ TA csr_row_dot(const i32* __restrict__ ptr, const i32* __restrict__ col,
-                                          const TV* __restrict__ val, const TX* __restrict__ x,
-                                          i32 row, bool valid, int lane) {
-  TA s = TA(0);
-  if (valid) {
-    const i32 e = ptr[row + 1];
-    for (i32 k = ptr[row] + lane; k < e; k += VS) s += static_cast<TA>(val[k]) * static_cast<TA>(x[col[k]]);
-  }
-#pragma unroll
-  for (int o = VS / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, VS);
-  return s;
-}
-
-// mode 0: y = A x ; 1: y = b - A x ; 2: y += A x
-template <int VS, int MODE, class TV, class TX>
-__global__ void __launch_bounds__(256) k_csr(i32 rows, const i32* __restrict__ ptr,
-                                             const i32* __restrict__ col, const TV* __restrict__ val,
-                                             const TX* __restrict__ x, TX* __restrict__ y,
-                                             const TX* __restrict__ b) {
-  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  const i32 row = static_cast<i32>(t / VS);
-  const int lane = static_cast<int>(t % VS);
-  const bool valid = row < rows;
-  const TX s = csr_row_dot<VS, TV, TX, TX>(ptr, col, val, x, row, valid, lane);
-  if (valid && lane == 0) {
-    if (MODE == 0) y[row] = s;
-    else if (MODE == 1) y[row] = b[row] - s;
-    else y[row] += s;
-  }
-}
-
-// Chebyshev step (Saad, Alg. 12.1 in D^-1 A; src/fem/Multigrid.cpp:828-853):
-//   r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ dprev]) + dn
-template <int VS, class TV, class TX>
-__global__ void __launch_bounds__(256) k_cheb_step(i32 rows, const i32* __restrict__ ptr,
-                                                   const i32* __restrict__ col, const TV* __restrict__ val,
-                                                   const TX* __restrict__ d, const TX* __restrict__ r_in,
-                                                   TX* __restrict__ r, TX* __restrict__ dn,
-                                                   TX* __restrict__ x, const TX* __restrict__ dinv,
-                                                   TX c1, TX c2, int add_d_first) {
-  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  const i32 row = static_cast<i32>(t / VS);
-  const int lane = static_cast<int>(t % VS);
-  const bool valid = row < rows;
-  const TX s = csr_row_dot<VS, TV, TX, TX>(ptr, col, val, d, row, valid, lane);
-  if (valid && lane == 0) {
-    const TX ri = r_in[row] - s;
-    r[row] = ri;
-    const TX di = c1 * d[row] + c2 * dinv[row] * ri;
-    dn[row] = di;
-    TX xi = x[row];
-    if (add_d_first) xi = xi + d[row];
-    x[row] = xi + di;
-  }
-}
-
-// r = b - A x ; d = dinv r / theta   (start of a smoothing from a guess)
-template <int VS, class TV, class TX>
-__global__ void __launch_bounds__(256) k_cheb_first(i32 rows, const i32* __restrict__ ptr,
-                                                    const i32* __restrict__ col, const TV* __restrict__ val,
-                                                    const TX* __restrict__ x, const TX* __restrict__ b,
-                                                    TX* __restrict__ r, TX* __restrict__ d,
-                                                    const TX* __restrict__ dinv, TX inv_theta) {
-  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  const i32 row = static_cast<i32>(t / VS);
-  const int lane = static_cast<int>(t % VS);
-  const bool valid = row < rows;
-  const TX s = csr_row_dot<VS, TV, TX, TX>(ptr, col, val, x, row, valid, lane);
-  if (valid && lane == 0) {
-    const TX ri = b[row] - s;
-    r[row] = ri;
-    d[row] = dinv[row] * ri * inv_theta;
-  }
-}
-
 // zero guess: d = dinv b / theta ; x = d
 template <class TX>
 __global__ void k_cheb_zero(i64 n, const TX* __restrict__ b, const TX* __restrict__ dinv,
@@ -304,26 +230,6 @@ __global__ void k_cheb_zero(i64 n, const TX* __restrict__ b, const TX* __restric
 // ---------------------------------------------------------------------------
 // Lanczos pieces (src/fem/Multigrid.cpp:288-327)
 // ---------------------------------------------------------------------------
-// w = s .* (A (s .* v)) - beta vp   with tmp = s .* v precomputed
-template <int VS, class TV>
-__global__ void __launch_bounds__(256) k_lanczos_apply(i32 rows, const i32* __restrict__ ptr,
-                                                       const i32* __restrict__ col, const TV* __restrict__ val,
-                                                       const double* __restrict__ tmp,
-                                                       const double* __restrict__ s,
-                                                       const double* __restrict__ vp, double beta,
-                                                       double* __restrict__ w) {
-  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-  const i32 row = static_cast<i32>(t / VS);
-  const int lane = static_cast<int>(t % VS);
-  const bool valid = row < rows;
-  const double acc = csr_row_dot<VS, TV, double, double>(ptr, col, val, tmp, row, valid, lane);
-  if (valid && lane == 0) {
-    double wi = acc * s[row];
-    if (vp) wi -= beta * vp[row];
-    w[row] = wi;
-  }
-}
-
 // w -= a v ; partial ||w||^2
 __global__ void __launch_bounds__(kRedThreads) k_axpy_norm(double* __restrict__ w, const double* __restrict__ v,
                                                            const double* __restrict__ a_dev, i64 n,

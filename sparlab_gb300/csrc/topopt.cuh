@@ -416,12 +416,5 @@ __global__ void k_clamp01(i64 ne, double* __restrict__ x) {
     x[e] = fmin(fmax(x[e], 0.0), 1.0);
 }
 
-// gather the free part of full-length load vectors: b[l][i] = f[l][free[i]]
-__global__ void k_gather(i64 n, int nl, const double* __restrict__ f, i64 ldf, const i32* __restrict__ free_dofs,
-                         double* __restrict__ b) {
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
-    for (int l = 0; l < nl; ++l) b[l * n + i] = f[l * ldf + free_dofs[i]];
-}
-
 }  // namespace
 }  // namespace simp
