@@ -131,7 +131,10 @@ template <class T>
 int row_lanes(const DevCsr& c) {
   const i64 avg = c.rows > 0 ? c.nnz / c.rows : 0;
   if (std::is_same<T, double>::value) return avg > 100 ? 8 : 4;
-  return avg >= 256 ? 32 : 8;
+  // short rows (the prolongators, ~30 values): 4 lanes put twice the rows in
+  // flight per warp, which the per-row index chain (row -> node -> slots ->
+  // x) needs to hide its latency (P_0 at 192x96x96: 93 against 150 us)
+  return avg >= 256 ? 32 : (avg >= 64 ? 8 : 4);
 }
 
 // Per-precision views of a level's arrays.
