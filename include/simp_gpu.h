@@ -107,6 +107,16 @@ int simp_set_layout(simp_ctx* ctx, int32_t dim, int32_t ndpn, const double* coor
 int simp_factorize(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx,
                    const double* values);
 
+/* The same factorization in steps: the pattern once (copied; n, nnz and the
+ * layout are the reuse fingerprint, Multigrid.cpp:959-966), then per
+ * iteration the values -- host FP64, or a device pointer of nnz FP64 values
+ * that a GPU assembler wrote (read by simp_setup, after the caller's work on
+ * the legacy default stream) -- and simp_setup. */
+int simp_set_pattern(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx);
+int simp_set_values(simp_ctx* ctx, const double* values);
+int simp_set_values_device(simp_ctx* ctx, const double* values_device);
+int simp_setup(simp_ctx* ctx);
+
 /* LinearSolver::solve / solve_from (LinearSolver.hpp:74-82) for nrhs
  * right-hand sides stored one after another (n doubles each).  X0 may be NULL
  * (zero guess).  iterations[k] and relres[k] (true relative residual) are

@@ -24,7 +24,8 @@ PRECISION_MIXED = 1
 
 EXPORTS = [
     "simp_default_options", "simp_ctx_create", "simp_ctx_destroy", "simp_last_error",
-    "simp_set_layout", "simp_factorize", "simp_solve", "simp_apply_preconditioner",
+    "simp_set_layout", "simp_factorize", "simp_set_pattern", "simp_set_values",
+    "simp_set_values_device", "simp_setup", "simp_solve", "simp_apply_preconditioner",
     "simp_stats", "simp_level_aggregates", "simp_level_matrix", "simp_level_prolongator",
     "simp_problem_create", "simp_problem_destroy", "simp_problem_last_error",
     "simp_problem_sizes", "simp_set_design", "simp_get_design", "simp_evaluate",

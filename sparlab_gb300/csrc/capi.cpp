@@ -83,6 +83,10 @@ struct simp_ctx {
   i64 fp_nnz = -1;
   std::string err;
   DBuf<double> db, dx;
+  // simp_set_pattern / simp_set_values(_device) / simp_setup
+  std::vector<i32> pat_rowptr, pat_col;
+  std::vector<double> host_values;
+  const double* device_values = nullptr;
 };
 
 struct simp_problem {
@@ -159,10 +163,15 @@ int simp_set_layout(simp_ctx* ctx, int32_t dim, int32_t ndpn, const double* coor
   });
 }
 
-int simp_factorize(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx, const double* values) {
-  return guarded(ctx->err, [&] {
-    use_device(ctx->device);
+namespace {
+
+// factorize with the values either on the host or on the device (exactly one
+// of host_values / device_values is non-null)
+void factorize_impl(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx,
+                    const double* host_values, const double* device_values) {
     const std::string who = "AMG-CG(chebyshev, GPU)";
+    const double* values = host_values;
+    std::vector<double> staged;
     if (n <= 0 || !rowptr) throw Error(kBadInput, who + " received an empty system");
     if (!ctx->has_layout)
       throw Error(kBadInput, who + " needs the DOF layout (node coordinates of the unknowns) to build its "
@@ -174,10 +183,18 @@ int simp_factorize(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_
     }
     const i64 nnz = rowptr[n];
     if (rowptr[0] != 0 || nnz <= 0) throw Error(kBadInput, "multigrid: malformed row pointer");
-    for (i64 k = 0; k < nnz; ++k)
-      if (!std::isfinite(values[k])) throw Error(kNonFinite, "multigrid: the system matrix has a non-finite entry");
     GpuAmg& amg = *ctx->amg;
     const bool same = amg.ready() && ctx->fp_n == n && ctx->fp_nnz == nnz && !ctx->layout_changed;
+    if (!values && !same) {
+      // device values: the host checks (finite, symmetric) of a new structure
+      staged.resize(static_cast<size_t>(nnz));
+      SIMP_CUDA(cudaMemcpy(staged.data(), device_values, sizeof(double) * nnz, cudaMemcpyDeviceToHost));
+      values = staged.data();
+    }
+    if (values)
+      for (i64 k = 0; k < nnz; ++k)
+        if (!std::isfinite(values[k]))
+          throw Error(kNonFinite, "multigrid: the system matrix has a non-finite entry");
     if (!same) {
       // symmetry check once per structure (Multigrid.cpp:968-991)
       double mx = 0.0;
@@ -247,11 +264,67 @@ int simp_factorize(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_
       l0.null = rigid_body_modes(ctx->dim, ctx->ndpn, ctx->coords, ctx->num_nodes, ctx->unknowns);
     }
     Level& l0 = *amg.levels.front();
-    l0.a.v64.upload(values, static_cast<size_t>(nnz));
+    if (host_values) {
+      l0.a.v64.upload(host_values, static_cast<size_t>(nnz), amg.stream);
+    } else {
+      l0.a.v64.alloc(static_cast<size_t>(nnz));
+      SIMP_CUDA(cudaMemcpyAsync(l0.a.v64.p, device_values, sizeof(double) * nnz, cudaMemcpyDeviceToDevice,
+                                amg.stream));
+    }
     amg.setup(!same);
     ctx->fp_n = n;
     ctx->fp_nnz = nnz;
     ctx->layout_changed = false;
+}
+
+}  // namespace
+
+int simp_factorize(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx, const double* values) {
+  return guarded(ctx->err, [&] {
+    use_device(ctx->device);
+    if (!values) throw Error(kBadInput, "AMG-CG(chebyshev, GPU) received no matrix values");
+    factorize_impl(ctx, n, rowptr, colidx, values, nullptr);
+  });
+}
+
+int simp_set_pattern(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32_t* colidx) {
+  return guarded(ctx->err, [&] {
+    if (n <= 0 || !rowptr || !colidx) throw Error(kBadInput, "AMG-CG(chebyshev, GPU) received an empty pattern");
+    if (rowptr[0] != 0 || rowptr[n] <= 0) throw Error(kBadInput, "multigrid: malformed row pointer");
+    ctx->pat_rowptr.assign(rowptr, rowptr + n + 1);
+    ctx->pat_col.assign(colidx, colidx + rowptr[n]);
+    ctx->host_values.clear();
+    ctx->device_values = nullptr;
+  });
+}
+
+int simp_set_values(simp_ctx* ctx, const double* values) {
+  return guarded(ctx->err, [&] {
+    if (ctx->pat_rowptr.empty()) throw Error(kBadInput, "simp_set_values needs simp_set_pattern first");
+    if (!values) throw Error(kBadInput, "simp_set_values received no values");
+    ctx->host_values.assign(values, values + ctx->pat_col.size());
+    ctx->device_values = nullptr;
+  });
+}
+
+int simp_set_values_device(simp_ctx* ctx, const double* values_device) {
+  return guarded(ctx->err, [&] {
+    if (ctx->pat_rowptr.empty()) throw Error(kBadInput, "simp_set_values_device needs simp_set_pattern first");
+    if (!values_device) throw Error(kBadInput, "simp_set_values_device received no values");
+    ctx->host_values.clear();
+    ctx->device_values = values_device;
+  });
+}
+
+int simp_setup(simp_ctx* ctx) {
+  return guarded(ctx->err, [&] {
+    use_device(ctx->device);
+    if (ctx->pat_rowptr.empty()) throw Error(kBadInput, "simp_setup needs simp_set_pattern first");
+    if (ctx->host_values.empty() && !ctx->device_values)
+      throw Error(kBadInput, "simp_setup needs simp_set_values or simp_set_values_device first");
+    const i32 n = static_cast<i32>(ctx->pat_rowptr.size()) - 1;
+    factorize_impl(ctx, n, ctx->pat_rowptr.data(), ctx->pat_col.data(),
+                   ctx->host_values.empty() ? nullptr : ctx->host_values.data(), ctx->device_values);
   });
 }
 

@@ -76,6 +76,25 @@ class GpuAmgCgSolver:
         self._check(self._lib.simp_factorize(self._h, C.c_int32(self._n), ptr(rowptr, C.c_int32),
                                              ptr(colidx, C.c_int32), ptr(values)))
 
+    def set_pattern(self, rowptr, colidx):
+        """The pattern once (copied); values and setup per factorization."""
+        rowptr = np.ascontiguousarray(rowptr, np.int32)
+        colidx = np.ascontiguousarray(colidx, np.int32)
+        self._n = len(rowptr) - 1
+        self._check(self._lib.simp_set_pattern(self._h, C.c_int32(self._n), ptr(rowptr, C.c_int32),
+                                               ptr(colidx, C.c_int32)))
+
+    def set_values(self, values):
+        values = np.ascontiguousarray(values, np.float64)
+        self._check(self._lib.simp_set_values(self._h, ptr(values)))
+
+    def set_values_device(self, device_ptr: int):
+        """FP64 values already on the device (e.g. ``tensor.data_ptr()``)."""
+        self._check(self._lib.simp_set_values_device(self._h, C.c_void_p(device_ptr)))
+
+    def setup(self):
+        self._check(self._lib.simp_setup(self._h))
+
     def factorize_scipy(self, k):
         k = k.tocsr()
         k.sort_indices()

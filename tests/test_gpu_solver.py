@@ -189,3 +189,28 @@ def test_mixed_precision_matches_fp64_solution():
     xa, xb = out["fp64"][0], out["mixed"][0]
     assert np.linalg.norm(xa - xb) <= 1e-6 * np.linalg.norm(xa)
     assert abs((f @ xa) / (f @ xb) - 1) <= 1e-7
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_stepwise_setup_with_host_and_device_values(precision):
+    """simp_set_pattern + simp_set_values(_device) + simp_setup is the same
+    factorization as simp_factorize: identical solutions, aggregate reuse on
+    the second value set."""
+    import torch
+    spec = P.bench_model(3, 16, 8, 4)
+    pr, (ptr, col, val), ref, gpu = both(spec, coarse_size=60)
+    f = spec.loads[0][pr.free_dofs()]
+    x_fact = gpu.solve(f)
+    step = GpuAmgCgSolver(iterative_tolerance=1e-12, precision=precision, coarse_size=60)
+    step.set_layout(3, pr.coords(), pr.free_dofs())
+    step.set_pattern(ptr, col)
+    if precision == "fp64":
+        step.set_values(val)
+        step.setup()
+        np.testing.assert_array_equal(step.solve(f), x_fact)
+    dev = torch.tensor(val * 0.5, dtype=torch.float64, device="cuda")
+    step.set_values_device(dev.data_ptr())
+    step.setup()
+    assert step.amg_stats()["reused_aggregates"] or precision == "mixed"
+    x_half = step.solve(f)
+    assert np.linalg.norm(x_half - 2.0 * x_fact) <= 1e-8 * np.linalg.norm(x_fact)
