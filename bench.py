@@ -344,7 +344,8 @@ def run_own(args):
 
     spec = WORKLOADS[args.config][0]()
     spec.warm_start = WARM[args.warm]
-    prob = GpuSimpProblem(spec, precision=args.precision, device=local)
+    together = not args.sequential_loads
+    prob = GpuSimpProblem(spec, precision=args.precision, device=local, block_pcg=together)
     lib = _lib.load()
 
     # warm-up: the first iteration builds the hierarchy
@@ -376,7 +377,7 @@ def run_own(args):
     # e2e: a fresh instance over the same iterations (the same warm-up, then
     # the timed steps), with the design copied in from pinned host memory and
     # the design and compliance read back every step
-    e2e_prob = GpuSimpProblem(spec, precision=args.precision, device=local)
+    e2e_prob = GpuSimpProblem(spec, precision=args.precision, device=local, block_pcg=together)
     for _ in range(args.warmup):
         e2e_prob.iterate()
     x_host = torch.empty(prob.ne, dtype=torch.float64, pin_memory=True).numpy()
@@ -412,7 +413,7 @@ def run_own(args):
     # warm-up), for the metric's plain-vs-mixed ratio and the compliance bar
     plain = None
     if args.precision == "mixed" and not args.no_plain and world == 1:
-        ref = GpuSimpProblem(spec, precision="fp64", device=local)
+        ref = GpuSimpProblem(spec, precision="fp64", device=local, block_pcg=together)
         for _ in range(args.warmup):
             ref.iterate()
         torch.cuda.synchronize()
@@ -440,7 +441,8 @@ def run_own(args):
         "data": "synthetic seeded cantilever (no dataset)",
         "config": {"workload": spec.name, "elements": spec.num_elements, "free_dofs": prob.nfree,
                    "nnz_kff": prob.nnz, "precision": args.precision, "warm_start": args.warm,
-                   "replicas": world,
+                   "replicas": world, "load_cases": int(spec.loads.shape[0]),
+                   "load_case_solves": "concurrent" if together else "sequential",
                    "l2": "working set (K_ff %.2f GB) larger than L2" % (nnz * 12 / 1e9),
                    "amg_levels": st["num_levels"],
                    "operator_complexity": round(st["operator_complexity"], 6),
@@ -451,10 +453,10 @@ def run_own(args):
                    "plain_fp64": plain},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": ("k_rows_apply<4,3,0,double> (level-0 K_ff operator of the CG, FP64 values; "
-                                "FP64-pipe bound on GB300)" if args.precision == "fp64" else
-                                "k_rows_apply_df<8,3,0> (level-0 K_ff operator of the CG, double-float "
-                                "values and arithmetic on the FP32 pipes)"),
+                     "kernel": (f"k_rows_apply<4,{spec.dim},0,double> (level-0 K_ff operator of the CG, "
+                                "FP64 values; FP64-pipe bound on GB300)" if args.precision == "fp64" else
+                                f"k_rows_apply_df<8,{spec.dim},0> (level-0 K_ff operator of the CG, "
+                                "double-float values and arithmetic on the FP32 pipes)"),
                      "bytes_per_launch": alg_bytes, "ms_per_launch": kms,
                      "peak_kind": f"{peak_kind} hbm_gbs (burst copy)"},
         "cpu_baseline": cpu,
@@ -481,6 +483,9 @@ def main():
     ap.add_argument("--warm", default="previous", choices=sorted(WARM),
                     help="PCG initial guess: zero, the previous displacement (the reference's "
                          "warm start) or the energy-optimal combination of the last three")
+    ap.add_argument("--sequential-loads", action="store_true",
+                    help="solve a multi-load workload's load cases one after another instead of "
+                         "concurrently (one workspace and stream per load case)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -163,7 +163,8 @@ typedef struct {
   int32_t warm_start;           /* 0: zero guess; 1: previous displacement
                                    (LinearSolverOptions::warm_start); 2: energy-
                                    optimal combination of the last 3 displacements */
-  int32_t block_pcg;            /* 1: all load cases as one block of RHS */
+  int32_t block_pcg;            /* 1: the load cases' PCG solves run at the same time, each
+                                   on its own workspace and stream (same results) */
   int32_t optimizer;            /* simp_iterate's update: 0 OC, 1 MMA */
   /* Heaviside projection of the filtered density with beta continuation
    * (ProjectionOptions, include/sparlab/topopt/Projection.hpp:69-96,

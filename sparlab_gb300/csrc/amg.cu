@@ -143,21 +143,21 @@ struct V;
 template <>
 struct V<double> {
   static const double* a(const DevCsr& c) { return c.v64.p; }
-  static double* x(Level& l) { return l.x64.p; }
-  static double* b(Level& l) { return l.b64.p; }
-  static double* r(Level& l) { return l.r64.p; }
-  static double* d(Level& l) { return l.d64.p; }
-  static double* e(Level& l) { return l.e64.p; }
+  static double* x(LevelWork& l) { return l.x64.p; }
+  static double* b(LevelWork& l) { return l.b64.p; }
+  static double* r(LevelWork& l) { return l.r64.p; }
+  static double* d(LevelWork& l) { return l.d64.p; }
+  static double* e(LevelWork& l) { return l.e64.p; }
   static const double* dinv(Level& l) { return l.dinv64.p; }
 };
 template <>
 struct V<float> {
   static const float* a(const DevCsr& c) { return c.v32.p; }
-  static float* x(Level& l) { return l.x32.p; }
-  static float* b(Level& l) { return l.b32.p; }
-  static float* r(Level& l) { return l.r32.p; }
-  static float* d(Level& l) { return l.d32.p; }
-  static float* e(Level& l) { return l.e32.p; }
+  static float* x(LevelWork& l) { return l.x32.p; }
+  static float* b(LevelWork& l) { return l.b32.p; }
+  static float* r(LevelWork& l) { return l.r32.p; }
+  static float* d(LevelWork& l) { return l.d32.p; }
+  static float* e(LevelWork& l) { return l.e32.p; }
   static const float* dinv(Level& l) { return l.dinv32.p; }
 };
 
@@ -269,13 +269,61 @@ GpuAmg::GpuAmg(const AmgOptions& o) : opt(o) {
   part.alloc(kRedBlocks);
   scal.alloc(16);
   dstatus.alloc(4);
+  main_.stream = stream;
 }
 
 GpuAmg::~GpuAmg() {
+  extra_.clear();
   if (stream) {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
   }
+}
+
+SolveWork::~SolveWork() {
+  if (own_stream && stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+}
+
+SolveWork& GpuAmg::work(int k) {
+  if (k == 0) return main_;
+  while (static_cast<int>(extra_.size()) < k) {
+    std::unique_ptr<SolveWork> w(new SolveWork());
+    SIMP_CUDA(cudaStreamCreate(&w->stream));
+    w->own_stream = true;
+    extra_.push_back(std::move(w));
+  }
+  return *extra_[static_cast<size_t>(k - 1)];
+}
+
+// FP32 vector of length n, zero-filled when (re)allocated
+void GpuAmg::alloc32(DBuf<float>& v, i64 n, cudaStream_t s) {
+  if (v.n == static_cast<size_t>(n) && v.p) return;
+  v.alloc(static_cast<size_t>(n));
+  SIMP_CUDA(cudaMemsetAsync(v.p, 0, sizeof(float) * n, s));
+}
+
+// Sizes a workspace for the current hierarchy (nothing is reallocated while
+// the sizes stay the same).
+void GpuAmg::ensure(SolveWork& w) {
+  w.lv.resize(levels.size());
+  for (size_t l = 0; l < levels.size(); ++l) {
+    const i64 n = levels[l]->n;
+    LevelWork& v = w.lv[l];
+    if (mixed()) {
+      for (DBuf<float>* b : {&v.x32, &v.b32, &v.r32, &v.d32, &v.e32}) alloc32(*b, n, w.stream);
+    } else {
+      for (DBuf<double>* b : {&v.x64, &v.b64, &v.r64, &v.d64, &v.e64}) b->alloc(static_cast<size_t>(n));
+    }
+  }
+  const size_t n0 = levels.empty() ? 0 : static_cast<size_t>(levels.front()->n);
+  w.part.alloc(kRedBlocks);
+  w.scal.alloc(16);
+  for (DBuf<double>* b : {&w.pr, &w.pz, &w.pp, &w.pq}) b->alloc(n0);
+  w.ctmp.alloc(static_cast<size_t>(std::max<i32>(nc_, 1)));
+  if (mixed()) w.xsplit.alloc(n0);
 }
 
 Level& GpuAmg::level0() {
@@ -283,14 +331,18 @@ Level& GpuAmg::level0() {
   return *levels.front();
 }
 
-double GpuAmg::dot(const double* a, const double* b, i64 n) {
-  k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(a, b, n, part.p);
+double GpuAmg::dot(SolveWork& w, const double* a, const double* b, i64 n) {
+  // the context's own workspace uses the context's reduction buffers, so a
+  // dot works before ensure() (setup's Lanczos)
+  double* pt = &w == &main_ ? part.p : w.part.p;
+  double* sc = &w == &main_ ? scal.p : w.scal.p;
+  k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, w.stream>>>(a, b, n, pt);
   SIMP_CHECK_LAUNCH();
-  k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, scal.p, 0);
+  k_reduce_final<<<1, kRedThreads, 0, w.stream>>>(pt, kRedBlocks, sc, 0);
   SIMP_CHECK_LAUNCH();
   double h = 0.0;
-  SIMP_CUDA(cudaMemcpyAsync(&h, scal.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
-  SIMP_CUDA(cudaStreamSynchronize(stream));
+  SIMP_CUDA(cudaMemcpyAsync(&h, sc, sizeof(double), cudaMemcpyDeviceToHost, w.stream));
+  SIMP_CUDA(cudaStreamSynchronize(w.stream));
   return h;
 }
 
@@ -331,28 +383,30 @@ void GpuAmg::make_ops(size_t l) {
   }
 }
 
-void GpuAmg::op0(const double* x, double* y, const double* rhs, bool split_ready) {
+void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bool split_ready) {
   Level& l0 = *levels.front();
   const NbOp& op = l0.opA;
+  const cudaStream_t stream = w.stream;
   if (!mixed()) {
     if (rhs) nb_apply<1, double, double, double>(op, l0.a.v64.p, x, y, rhs, stream);
     else nb_apply<0, double, double, double>(op, l0.a.v64.p, x, y, nullptr, stream);
     return;
   }
-  xsplit_.alloc(static_cast<size_t>(l0.n));
+  w.xsplit.alloc(static_cast<size_t>(l0.n));
+  float2* xsplit = w.xsplit.p;
   if (!split_ready) {
-    k_split_pairs<<<grid_for(l0.n, 256, 8192), 256, 0, stream>>>(l0.n, x, xsplit_.p);
+    k_split_pairs<<<grid_for(l0.n, 256, 8192), 256, 0, stream>>>(l0.n, x, xsplit);
     SIMP_CHECK_LAUNCH();
   }
   with_shape<float>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     if (rhs)
       k_rows_apply_df<VS, B, 1><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
-                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit_.p, y, rhs,
+                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit, y, rhs,
                                                                        op.rows);
     else
       k_rows_apply_df<VS, B, 0><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
-                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit_.p, y,
+                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit, y,
                                                                        nullptr, op.rows);
   });
   SIMP_CHECK_LAUNCH();
@@ -368,7 +422,7 @@ void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
   DBuf<double> x64(n), y64(n);
   k_fill<double><<<grid_for(n, 256), 256, 0, stream>>>(x64.p, 1.0, n);
   SIMP_CHECK_LAUNCH();
-  auto launch = [&]() { op0(x64.p, y64.p, nullptr); };
+  auto launch = [&]() { op0(main_, x64.p, y64.p, nullptr); };
   for (int k = 0; k < 3; ++k) launch();
   // the timed launches are the profiler's capture window when one is attached
   cudaProfilerStart();
@@ -460,13 +514,16 @@ void GpuAmg::numeric_level(size_t l) {
   for (int j = 0; j < m; ++j) {
     if (fp32) {
       // FP32 operator on FP32 copies of the Lanczos vectors
-      lv.x32.alloc(n);
-      lv.b32.alloc(n);
-      convert(tmp.p, lv.x32.p, n, stream);
+      if (main_.lv.size() <= l) main_.lv.resize(l + 1);
+      DBuf<float>& x32 = main_.lv[l].x32;
+      DBuf<float>& b32 = main_.lv[l].b32;
+      alloc32(x32, n, stream);
+      alloc32(b32, n, stream);
+      convert(tmp.p, x32.p, n, stream);
       // level 0 of a structured grid: the matrix-free operator the smoother uses
-      if (l == 0 && mf.enabled) mf_apply(mf, lv.nnodes, lv.x32.p, lv.b32.p, stream);
-      else nb_apply<0, float, float, float>(lv.opA, lv.a.v32.p, lv.x32.p, lv.b32.p, nullptr, stream);
-      convert(lv.b32.p, w.p, n, stream);
+      if (l == 0 && mf.enabled) mf_apply(mf, lv.nnodes, x32.p, b32.p, stream);
+      else nb_apply<0, float, float, float>(lv.opA, lv.a.v32.p, x32.p, b32.p, nullptr, stream);
+      convert(b32.p, w.p, n, stream);
     }
     else nb_apply<0, double, double, double>(lv.opA, lv.a.v64.p, tmp.p, w.p, nullptr, stream);
     k_lanczos_finish<<<grid_for(n, 256), 256, 0, stream>>>(w.p, s.p, j > 0 ? vp.p : nullptr,
@@ -508,19 +565,6 @@ void GpuAmg::numeric_level(size_t l) {
     lv.c1.push_back(rn * rho);
     lv.c2.push_back(2.0 * rn / delta);
     rho = rn;
-  }
-  if (mixed()) {
-    lv.x32.alloc(n);
-    lv.b32.alloc(n);
-    lv.r32.alloc(n);
-    lv.d32.alloc(n);
-    lv.e32.alloc(n);
-  } else {
-    lv.x64.alloc(n);
-    lv.b64.alloc(n);
-    lv.r64.alloc(n);
-    lv.d64.alloc(n);
-    lv.e64.alloc(n);
   }
 }
 
@@ -747,7 +791,6 @@ void GpuAmg::coarse_factorize() {
   dense_.alloc(nn);
   inv_t_.alloc(nn);
   piv_.alloc(n);
-  tmp_.alloc(n);
   SIMP_CUDA(cudaMemsetAsync(dense_.p, 0, nn * sizeof(double), stream));
   k_dense_from_csr<<<grid_for(n, 128), 128, 0, stream>>>(n, lv.a.ptr.p, lv.a.col.p, lv.a.v64.p, dense_.p);
   SIMP_CHECK_LAUNCH();
@@ -803,12 +846,13 @@ void GpuAmg::coarse_factorize() {
 
 // x = W^T (W b) at the coarsest level, in FP64
 template <class T>
-void GpuAmg::coarse_solve(Level& lv) {
+void GpuAmg::coarse_solve(SolveWork& w, size_t l) {
   const int n = nc_;
   const i64 th = static_cast<i64>(n) * 32;
-  k_gemv<T, double><<<grid_for(th, 256), 256, 0, stream>>>(inv_t_.p, n, V<T>::b(lv), tmp_.p, 1);
+  LevelWork& v = w.lv[l];
+  k_gemv<T, double><<<grid_for(th, 256), 256, 0, w.stream>>>(inv_t_.p, n, V<T>::b(v), w.ctmp.p, 1);
   SIMP_CHECK_LAUNCH();
-  k_gemv<double, T><<<grid_for(th, 256), 256, 0, stream>>>(dense_.p, n, tmp_.p, V<T>::x(lv), 2);
+  k_gemv<double, T><<<grid_for(th, 256), 256, 0, w.stream>>>(dense_.p, n, w.ctmp.p, V<T>::x(v), 2);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -845,11 +889,8 @@ void GpuAmg::setup(bool structure_changed) {
   levels.resize(l + 1);
   for (size_t k = 0; k < levels.size(); ++k) make_ops(k);
   coarse_factorize();
-  const i32 n0 = levels.front()->n;
-  pr.alloc(n0);
-  pz.alloc(n0);
-  pp.alloc(n0);
-  pq.alloc(n0);
+  ensure(main_);
+  for (auto& w : extra_) ensure(*w);
   ready_ = true;
   stats.reused = reuse;
   compute_stats();
@@ -876,15 +917,17 @@ void GpuAmg::compute_stats() {
 
 // Chebyshev smoothing of x (Multigrid.cpp:783-855) on level l.
 template <class T>
-void GpuAmg::smooth(size_t l, bool zero_guess) {
+void GpuAmg::smooth(SolveWork& w, size_t l, bool zero_guess) {
   Level& lv = *levels[l];
+  LevelWork& v = w.lv[l];
+  const cudaStream_t stream = w.stream;
   const i32 n = lv.n;
   const T* A = V<T>::a(lv.a);
-  T* x = V<T>::x(lv);
-  T* b = V<T>::b(lv);
-  T* r = V<T>::r(lv);
-  T* d = V<T>::d(lv);
-  T* e = V<T>::e(lv);
+  T* x = V<T>::x(v);
+  T* b = V<T>::b(v);
+  T* r = V<T>::r(v);
+  T* d = V<T>::d(v);
+  T* e = V<T>::e(v);
   const T* dinv = V<T>::dinv(lv);
   bool matrix_free = false;
   if constexpr (std::is_same<T, float>::value) matrix_free = l == 0 && mf.enabled;
@@ -913,58 +956,66 @@ void GpuAmg::smooth(size_t l, bool zero_guess) {
 }
 
 template <class T>
-void GpuAmg::cycle(size_t l) {
+void GpuAmg::cycle(SolveWork& w, size_t l) {
   Level& lv = *levels[l];
   if (l + 1 == levels.size()) {
-    coarse_solve<T>(lv);
+    coarse_solve<T>(w, l);
     return;
   }
-  Level& nv = *levels[l + 1];
-  smooth<T>(l, true);
+  LevelWork& v = w.lv[l];
+  LevelWork& nv = w.lv[l + 1];
+  const cudaStream_t stream = w.stream;
+  smooth<T>(w, l, true);
   bool matrix_free = false;
   if constexpr (std::is_same<T, float>::value) matrix_free = l == 0 && mf.enabled;
   if (matrix_free) {  // residual
-    if constexpr (std::is_same<T, float>::value) mf_residual(mf, lv.nnodes, V<T>::x(lv), V<T>::r(lv), V<T>::b(lv), stream);
+    if constexpr (std::is_same<T, float>::value)
+      mf_residual(mf, lv.nnodes, V<T>::x(v), V<T>::r(v), V<T>::b(v), stream);
   } else {
-    nb_apply<1, T, T, T>(lv.opA, V<T>::a(lv.a), V<T>::x(lv), V<T>::r(lv), V<T>::b(lv), stream);
+    nb_apply<1, T, T, T>(lv.opA, V<T>::a(lv.a), V<T>::x(v), V<T>::r(v), V<T>::b(v), stream);
   }
-  nb_apply<0, T, T, T>(lv.opR, V<T>::a(lv.r), V<T>::r(lv), V<T>::b(nv), nullptr, stream);      // restrict
-  cycle<T>(l + 1);
-  nb_apply<2, T, T, T>(lv.opP, V<T>::a(lv.p), V<T>::x(nv), V<T>::x(lv), nullptr, stream);      // x += P x_c
-  smooth<T>(l, false);
+  nb_apply<0, T, T, T>(lv.opR, V<T>::a(lv.r), V<T>::r(v), V<T>::b(nv), nullptr, stream);      // restrict
+  cycle<T>(w, l + 1);
+  nb_apply<2, T, T, T>(lv.opP, V<T>::a(lv.p), V<T>::x(nv), V<T>::x(v), nullptr, stream);      // x += P x_c
+  smooth<T>(w, l, false);
 }
 
-void GpuAmg::apply(const double* r, double* z) {
+void GpuAmg::apply(SolveWork& w, const double* r, double* z) {
   if (!ready_) throw Error(kBadInput, "multigrid: apply() called before setup()");
   Level& f = *levels.front();
+  LevelWork& v = w.lv.front();
   if (mixed()) {
-    convert(r, f.b32.p, f.n, stream);
-    cycle<float>(0);
-    convert(f.x32.p, z, f.n, stream);
+    convert(r, v.b32.p, f.n, w.stream);
+    cycle<float>(w, 0);
+    convert(v.x32.p, z, f.n, w.stream);
   } else {
-    SIMP_CUDA(cudaMemcpyAsync(f.b64.p, r, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, stream));
-    cycle<double>(0);
-    SIMP_CUDA(cudaMemcpyAsync(z, f.x64.p, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, stream));
+    SIMP_CUDA(cudaMemcpyAsync(v.b64.p, r, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, w.stream));
+    cycle<double>(w, 0);
+    SIMP_CUDA(cudaMemcpyAsync(z, v.x64.p, sizeof(double) * f.n, cudaMemcpyDeviceToDevice, w.stream));
   }
 }
 
 // Preconditioned CG on A x = b (FP64 operator and vectors) from the guess in
 // x; `restarts` follows the reference's true-residual restarts.  Stops when
 // the recursive residual reaches `target` or the iteration `budget` is spent.
-GpuAmg::PcgResult GpuAmg::pcg(const double* b, double* x, double target, int budget, bool restarts,
-                              double bnorm) {
+GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x, double target, int budget,
+                              bool restarts, double bnorm) {
   Level& f = *levels.front();
   const i32 n = f.n;
+  const cudaStream_t stream = w.stream;
+  DBuf<double>& pr = w.pr;
+  DBuf<double>& pz = w.pz;
+  DBuf<double>& pp = w.pp;
+  DBuf<double>& pq = w.pq;
+  DBuf<double>& part = w.part;
   PcgResult res;
-  PcgScalars* sc = reinterpret_cast<PcgScalars*>(scal.p + 8);
+  PcgScalars* sc = reinterpret_cast<PcgScalars*>(w.scal.p + 8);
   static_assert(sizeof(PcgScalars) <= 8 * sizeof(double), "scalar block");
-  auto op = [&](const double* in, double* out, const double* rhs) { op0(in, out, rhs, false); };
+  auto op = [&](const double* in, double* out, const double* rhs) { op0(w, in, out, rhs, false); };
+  auto dot = [&](const double* a, const double* c, i64 m) { return this->dot(w, a, c, m); };
+  auto apply = [&](const double* r, double* z) { this->apply(w, r, z); };
   // mixed: the direction update also writes p's double-float split
-  float2* psplit = nullptr;
-  if (mixed()) {
-    xsplit_.alloc(static_cast<size_t>(n));
-    psplit = xsplit_.p;
-  }
+  float2* psplit = mixed() ? w.xsplit.p : nullptr;
   bool p_split = false;
   int total = 0;
   bool rec_conv = false;
@@ -986,7 +1037,7 @@ GpuAmg::PcgResult GpuAmg::pcg(const double* b, double* x, double target, int bud
     bool conv = false;
     p_split = false;
     while (total < budget) {
-      op0(pp.p, pq.p, nullptr, p_split);
+      op0(w, pp.p, pq.p, nullptr, p_split);
       k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(pp.p, pq.p, n, part.p);
       SIMP_CHECK_LAUNCH();
       k_pcg_alpha<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, sc);
@@ -1035,13 +1086,14 @@ GpuAmg::PcgResult GpuAmg::pcg(const double* b, double* x, double target, int bud
   return res;
 }
 
-GpuAmg::PcgResult GpuAmg::solve(const double* b, double* x) {
+GpuAmg::PcgResult GpuAmg::solve(SolveWork& w, const double* b, double* x) {
   if (!ready_) throw Error(kBadInput, "solve called before factorize");
+  ensure(w);
   Level& f = *levels.front();
   const i32 n = f.n;
-  const double bnorm = std::sqrt(dot(b, b, n));
+  const double bnorm = std::sqrt(dot(w, b, b, n));
   if (bnorm == 0.0) {
-    SIMP_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, stream));
+    SIMP_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, w.stream));
     PcgResult r;
     r.converged = true;
     return r;
@@ -1052,7 +1104,7 @@ GpuAmg::PcgResult GpuAmg::solve(const double* b, double* x) {
   // FP32 operator converges towards the FP32 matrix's solution: with the SIMP
   // stiffness contrast it needed up to twice the CG iterations even with
   // FP64 residual replacement, so the outer operator stays FP64.
-  return pcg(b, x, target, opt.maxit, true, bnorm);
+  return pcg(w, b, x, target, opt.maxit, true, bnorm);
 }
 
 }  // namespace simp

@@ -98,9 +98,6 @@ struct Level {
   DevCsr p, r, ap;
   DBuf<double> raw64;
   DBuf<float> raw32;
-  // cycle workspace
-  DBuf<double> x64, b64, r64, d64, e64;
-  DBuf<float> x32, b32, r32, d32, e32;
   std::vector<double> c1, c2;
   double inv_theta = 0.0;
   DBuf<double> lz[5];  // Lanczos work vectors
@@ -119,6 +116,27 @@ struct MfOp {
   const float* ke = nullptr;    // K_e^0, FP32
   const float* scale = nullptr; // s_e, FP32
   float ke_host[24 * 24] = {};  // K_e^0, FP32 (kernel parameter of the tiled 3-D kernel)
+};
+
+// Work vectors of one solve: the cycle vectors of every level, the PCG
+// vectors, reduction scratch and a stream.  Solves on different workspaces
+// (the load cases of one problem) run concurrently from host threads; every
+// solve computes exactly what it computes alone.
+struct LevelWork {
+  DBuf<double> x64, b64, r64, d64, e64;
+  DBuf<float> x32, b32, r32, d32, e32;
+};
+
+struct SolveWork {
+  cudaStream_t stream = 0;
+  bool own_stream = false;
+  std::vector<LevelWork> lv;
+  DBuf<double> part, scal, pr, pz, pp, pq, ctmp;
+  DBuf<float2> xsplit;  // op0's input as (hi, lo) pairs (mixed mode)
+  SolveWork() = default;
+  SolveWork(const SolveWork&) = delete;
+  SolveWork& operator=(const SolveWork&) = delete;
+  ~SolveWork();
 };
 
 struct AmgStats {
@@ -156,44 +174,54 @@ class GpuAmg {
   // level-0 FP32 hi/lo values from the FP64 ones (mixed mode)
   void refresh_level0_fp32();
 
+  // Workspace k: 0 is the context's own (its stream); k > 0 are made on
+  // demand with their own streams.  ensure() sizes one for the hierarchy.
+  SolveWork& work(int k = 0);
+  void ensure(SolveWork& w);
+
   // z = M^-1 r (FP64 device vectors of level-0 length).
-  void apply(const double* r, double* z);
+  void apply(const double* r, double* z) { apply(work(0), r, z); }
+  void apply(SolveWork& w, const double* r, double* z);
   struct PcgResult {
     int iterations = 0;
     double relres = 0.0;
     bool converged = false;
   };
   // PCG (src/fem/Multigrid.cpp:1152-1237); x holds the guess on entry.
-  PcgResult solve(const double* b, double* x);
+  PcgResult solve(const double* b, double* x) { return solve(work(0), b, x); }
+  PcgResult solve(SolveWork& w, const double* b, double* x);
   // The CG operator on FP64 vectors: y = A0 x (rhs null) or y = rhs - A0 x.
   // FP64 values in fp64 mode; double-float values in mixed mode.
-  // split_ready: x's double-float split is already in the split buffer
-  // (written by the PCG direction update).
-  void op0(const double* x, double* y, const double* rhs, bool split_ready = false);
-  void spmv0(const double* x, double* y) { op0(x, y, nullptr); }
+  // split_ready: x's double-float split is already in w.xsplit (written by
+  // the PCG direction update).
+  void op0(SolveWork& w, const double* x, double* y, const double* rhs, bool split_ready = false);
+  void spmv0(const double* x, double* y) { op0(work(0), x, y, nullptr); }
   // CUDA-event time of one op0 launch (ms) and its algorithmic bytes
   void time_operator(int reps, double* ms, double* bytes);
+  double dot(SolveWork& w, const double* a, const double* b, i64 n);
 
-  DBuf<double> part, scal;
-  DBuf<double> pr, pz, pp, pq;
+  DBuf<double> part, scal;  // reductions of setup and of callers on the context stream
   DBuf<int> dstatus;
 
  private:
   bool ready_ = false;
   i32 nc_ = 0;
-  DBuf<double> dense_, inv_t_, piv_, tmp_;
-  DBuf<float2> xsplit_;  // op0's input as (hi, lo) pairs (mixed mode)
+  DBuf<double> dense_, inv_t_, piv_;
+  SolveWork main_;
+  std::vector<std::unique_ptr<SolveWork>> extra_;
 
   void numeric_level(size_t l);
   void build_transfer(size_t l);
   void galerkin(size_t l, bool fp32);
   void coarse_factorize();
   void make_ops(size_t l);
-  template <class T> void coarse_solve(Level& lv);
-  template <class T> void smooth(size_t l, bool zero_guess);
-  template <class T> void cycle(size_t l);
-  double dot(const double* a, const double* b, i64 n);
-  PcgResult pcg(const double* b, double* x, double target, int budget, bool restarts, double bnorm);
+  void alloc32(DBuf<float>& v, i64 n, cudaStream_t s);
+  template <class T> void coarse_solve(SolveWork& w, size_t l);
+  template <class T> void smooth(SolveWork& w, size_t l, bool zero_guess);
+  template <class T> void cycle(SolveWork& w, size_t l);
+  double dot(const double* a, const double* b, i64 n) { return dot(work(0), a, b, n); }
+  PcgResult pcg(SolveWork& w, const double* b, double* x, double target, int budget, bool restarts,
+                double bnorm);
   void compute_stats();
 };
 

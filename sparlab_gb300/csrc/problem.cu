@@ -6,7 +6,9 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <exception>
 #include <sstream>
+#include <thread>
 
 namespace simp {
 
@@ -503,14 +505,54 @@ Evaluation GpuProblem::evaluate() {
   assemble(sf.p, !structure_built_);
   amg.setup(!structure_built_);
   structure_built_ = true;
-  // one PCG per load case, warm-started from the previous displacement
+  // one PCG per load case, warm-started from the previous displacement; with
+  // several load cases and block_pcg the solves run at the same time, each
+  // on its own workspace and stream (same arithmetic as one after another)
   last_compliance.assign(static_cast<size_t>(d.nloads), 0.0);
-  for (int l = 0; l < d.nloads; ++l) {
+  std::vector<GpuAmg::PcgResult> res(static_cast<size_t>(d.nloads));
+  auto solve_load = [&](int l, SolveWork& w) {
+    const cudaStream_t ws = w.stream;
     double* ul = u.p + static_cast<size_t>(l) * nfree;
     const double* bl = b.p + static_cast<size_t>(l) * nfree;
-    if (d.warm == 0 || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, s));
+    if (d.warm == 0 || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, ws));
     else if (d.warm == 2 && hist_count[l] > 0) projected_start(l, ul);
-    const GpuAmg::PcgResult r = amg.solve(bl, ul);
+    res[static_cast<size_t>(l)] = amg.solve(w, bl, ul);
+    // c_l = f^T u (u vanishes on the supports)
+    last_compliance[static_cast<size_t>(l)] = amg.dot(w, bl, ul, nfree);
+    if (d.warm == 2) record_history(l, ul);
+  };
+  const bool together = d.block_pcg && d.nloads > 1 && d.warm != 2;
+  if (together) {
+    SIMP_CUDA(cudaStreamSynchronize(s));  // assembly and setup are done before the solves start
+    int dev = 0;
+    SIMP_CUDA(cudaGetDevice(&dev));
+    std::vector<SolveWork*> works;
+    for (int l = 0; l < d.nloads; ++l) works.push_back(&amg.work(l));
+    for (SolveWork* w : works) amg.ensure(*w);
+    std::vector<std::exception_ptr> errs(static_cast<size_t>(d.nloads));
+    std::vector<std::thread> threads;
+    for (int l = 1; l < d.nloads; ++l)
+      threads.emplace_back([&, l] {
+        try {
+          SIMP_CUDA(cudaSetDevice(dev));
+          solve_load(l, *works[static_cast<size_t>(l)]);
+        } catch (...) {
+          errs[static_cast<size_t>(l)] = std::current_exception();
+        }
+      });
+    try {
+      solve_load(0, *works[0]);
+    } catch (...) {
+      errs[0] = std::current_exception();
+    }
+    for (auto& t : threads) t.join();
+    for (auto& e : errs)
+      if (e) std::rethrow_exception(e);
+  } else {
+    for (int l = 0; l < d.nloads; ++l) solve_load(l, amg.work(0));
+  }
+  for (int l = 0; l < d.nloads; ++l) {
+    const GpuAmg::PcgResult& r = res[static_cast<size_t>(l)];
     if (!r.converged) {
       std::ostringstream os;
       os << "AMG-CG(chebyshev) did not converge: " << r.iterations
@@ -520,17 +562,7 @@ Evaluation GpuProblem::evaluate() {
     }
     ev.linear_iterations += r.iterations;
     ev.relres_max = std::max(ev.relres_max, r.relres);
-    // c_l = f^T u (u vanishes on the supports)
-    k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, s>>>(bl, ul, nfree, amg.part.p);
-    SIMP_CHECK_LAUNCH();
-    k_reduce_final<<<1, kRedThreads, 0, s>>>(amg.part.p, kRedBlocks, amg.scal.p + 4, 0);
-    SIMP_CHECK_LAUNCH();
-    double c = 0.0;
-    SIMP_CUDA(cudaMemcpyAsync(&c, amg.scal.p + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
-    SIMP_CUDA(cudaStreamSynchronize(s));
-    last_compliance[l] = c;
-    if (d.warm == 2) record_history(l, ul);
-    ev.compliance += d.weights[l] * c;
+    ev.compliance += d.weights[l] * last_compliance[static_cast<size_t>(l)];
   }
   ++evaluations;
   // element energies and sensitivities

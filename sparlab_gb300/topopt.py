@@ -78,7 +78,7 @@ class GpuSimpProblem:
     """A structured SIMP problem resident on the GPU (boundary 2 of the C ABI)."""
 
     def __init__(self, spec: ProblemSpec, precision="fp64", element_matrix=None, device=0,
-                 block_pcg=False, optimizer="oc", **amg):
+                 block_pcg=True, optimizer="oc", **amg):
         self._lib = _lib.load()
         self.spec = spec
         hx, hy = spec.lx / spec.nx, spec.ly / spec.ny
