@@ -282,6 +282,70 @@ int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms_per_lau
 int simp_filter_volume_noalloc(simp_problem* p, const double* x_device, double* rho_device,
                                double* volume_device);
 
+/* ---- Modal analysis (src/fem/ModalAnalysis.cpp) ---------------------- */
+
+/* ModalAnalysisOptions (include/sparlab/fem/ModalAnalysis.hpp:37-65).  The
+ * shifted systems K - sigma M are solved by the problem's AMG-PCG (its
+ * tolerance, iteration cap and precision), so the shift must be <= 0.  The
+ * reference's `seed` fills the start subspace only when it has more vectors
+ * than the model has DOFs, which never happens on the iterative path, so it
+ * has no field here. */
+typedef struct simp_modal_options {
+  int32_t num_modes;          /* lowest modes requested (6) */
+  int32_t mass_type;          /* 0 consistent, 1 lumped (row sums) */
+  int32_t max_iterations;     /* subspace iteration cap (200) */
+  double tolerance;           /* relative eigenvalue change (1e-10) */
+  double shift_factor;        /* sigma = shift_factor * min k_ii / m_ii (0; <= 0) */
+  double rigid_body_ratio;    /* zero-eigenvalue screen (1e-10) */
+  double residual_tolerance;  /* eigenpair residual bound (1e-6) */
+  int32_t warm_start;         /* start each solve from x_c / (mu_c - sigma) (1) */
+  double density;             /* material density, > 0 (1.0) */
+  const double* element_mass; /* M_e^0 (ed x ed, row-major) or NULL: the cell's consistent mass */
+  int32_t concurrent_solves;  /* subspace columns solved at the same time (4) */
+} simp_modal_options;
+
+/* ModalResult's scalars (include/sparlab/fem/ModalAnalysis.hpp:67-86). */
+typedef struct simp_modal_info {
+  int32_t num_modes;          /* modes returned (num_modes, or the free DOFs if fewer) */
+  int32_t iterations;         /* subspace iterations (0 on the dense path) */
+  int32_t subspace_size;
+  int32_t converged;
+  int64_t linear_iterations;  /* PCG iterations over every subspace solve */
+  double final_change;
+  double total_mass;          /* sum of the assembled mass / dim */
+  int32_t num_warnings;       /* texts: simp_modal_warnings */
+} simp_modal_info;
+
+void simp_default_modal_options(simp_modal_options* o);
+
+/* solve_modal (src/fem/ModalAnalysis.cpp:120-418) on the problem's grid and
+ * supports: the lowest modes of K_ff phi = lambda M_ff phi, with K_ff and
+ * M_ff assembled from the element factors stiffness_scale / mass_scale
+ * (host, num_elements each; NULL: all ones).  Outputs (host, NULL to skip):
+ * eigenvalues, frequencies_hz and residuals (num_modes each), mass_fraction
+ * (num_modes; the kinetic-energy share of cells with mass factor < 0.3, zero
+ * without mass_scale) and mode_shapes (num_modes x num_dofs, a mode per row,
+ * M-orthonormal, zero on the supports; the memory layout of the reference's
+ * num_dofs x num_modes column-major matrix).  Systems with at most 400 free
+ * DOFs take the dense path.  The problem's own hierarchy, design and
+ * displacements are left as they are.  SIMP_MAXITER when the subspace
+ * iteration or a solve does not converge, SIMP_BREAKDOWN for a non-positive
+ * pencil or a massless mode, SIMP_NONFINITE for a non-finite basis. */
+int simp_modal(simp_problem* p, const simp_modal_options* options, const double* stiffness_scale,
+               const double* mass_scale, double* eigenvalues, double* frequencies_hz,
+               double* residuals, double* mass_fraction, double* mode_shapes,
+               simp_modal_info* info);
+
+/* Warning k of the last simp_modal (rigid-body modes, large residuals, fewer
+ * modes than requested), or NULL. */
+const char* simp_modal_warning(simp_problem* p, int32_t k);
+
+/* Consistent mass of a box cell (Quad4Element/Hex8Element::consistent_mass,
+ * src/elements/Quad4.cpp:139-173, src/elements/Hex8.cpp:194-214), 3-point
+ * Gauss per direction. */
+int simp_element_mass(int32_t dim, double hx, double hy, double hz, double density,
+                      double thickness, double* me);
+
 /* Number of kernels this library has launched (for launch accounting). */
 int64_t simp_kernel_launches(void);
 

@@ -1168,6 +1168,79 @@ void element_stiffness(int dim, double hx, double hy, double hz, double young, d
     for (int c = 0; c < 24; ++c) ke[r * 24 + c] = 0.5 * (k[static_cast<size_t>(r) * 24 + c] + k[static_cast<size_t>(c) * 24 + r]);
 }
 
+// Consistent mass of one box cell, 3 x 3 (x 3) Gauss (IntegrationOptions::
+// mass_points), symmetrised: Quad4Element::consistent_mass
+// (src/elements/Quad4.cpp:139-173) and Hex8Element::consistent_mass
+// (src/elements/Hex8.cpp:194-214), M_e = sum_g rho t det(J) w_g N^T N.
+void element_mass(int dim, double hx, double hy, double hz, double density, double thick,
+                  double* me) {
+  const double a3 = std::sqrt(3.0 / 5.0);
+  const double gx[3] = {-a3, 0.0, a3};
+  const double gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+  if (dim == 2) {
+    const double xy[4][2] = {{0, 0}, {hx, 0}, {hx, hy}, {0, hy}};
+    double m[8][8] = {};
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) {
+        const double xi = gx[i], eta = gx[j], w = gw[i] * gw[j];
+        const double n[4] = {0.25 * (1 - xi) * (1 - eta), 0.25 * (1 + xi) * (1 - eta),
+                             0.25 * (1 + xi) * (1 + eta), 0.25 * (1 - xi) * (1 + eta)};
+        const double dn[4][2] = {{-0.25 * (1 - eta), -0.25 * (1 - xi)},
+                                 {0.25 * (1 - eta), -0.25 * (1 + xi)},
+                                 {0.25 * (1 + eta), 0.25 * (1 + xi)},
+                                 {-0.25 * (1 + eta), 0.25 * (1 - xi)}};
+        double J[2][2] = {};
+        for (int a = 0; a < 4; ++a)
+          for (int r = 0; r < 2; ++r)
+            for (int c = 0; c < 2; ++c) J[r][c] += xy[a][r] * dn[a][c];
+        const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const double f = density * thick * det * w;
+        for (int a = 0; a < 4; ++a)
+          for (int b = 0; b < 4; ++b)
+            for (int k = 0; k < 2; ++k) m[2 * a + k][2 * b + k] += f * (n[a] * n[b]);
+      }
+    for (int r = 0; r < 8; ++r)
+      for (int c = 0; c < 8; ++c) me[r * 8 + c] = 0.5 * (m[r][c] + m[c][r]);
+    return;
+  }
+  static const double corner[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                      {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+  double X[8][3];
+  for (int a = 0; a < 8; ++a) {
+    X[a][0] = corner[a][0] > 0 ? hx : 0.0;
+    X[a][1] = corner[a][1] > 0 ? hy : 0.0;
+    X[a][2] = corner[a][2] > 0 ? hz : 0.0;
+  }
+  std::vector<double> m(24 * 24, 0.0);
+  for (int gk = 0; gk < 3; ++gk)
+    for (int gj = 0; gj < 3; ++gj)
+      for (int gi = 0; gi < 3; ++gi) {
+        const double xi = gx[gi], eta = gx[gj], zeta = gx[gk], w = gw[gi] * gw[gj] * gw[gk];
+        double n[8], dn[8][3];
+        for (int a = 0; a < 8; ++a) {
+          const double fx = 1 + xi * corner[a][0], fy = 1 + eta * corner[a][1], fz = 1 + zeta * corner[a][2];
+          n[a] = 0.125 * fx * fy * fz;
+          dn[a][0] = 0.125 * corner[a][0] * fy * fz;
+          dn[a][1] = 0.125 * corner[a][1] * fx * fz;
+          dn[a][2] = 0.125 * corner[a][2] * fx * fy;
+        }
+        double J[3][3] = {};
+        for (int a = 0; a < 8; ++a)
+          for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) J[r][c] += X[a][r] * dn[a][c];
+        const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) +
+                           J[0][1] * (J[1][2] * J[2][0] - J[1][0] * J[2][2]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        const double f = density * det * w;
+        for (int a = 0; a < 8; ++a)
+          for (int b = 0; b < 8; ++b)
+            for (int k = 0; k < 3; ++k) m[static_cast<size_t>(3 * a + k) * 24 + 3 * b + k] += f * (n[a] * n[b]);
+      }
+  for (int r = 0; r < 24; ++r)
+    for (int c = 0; c < 24; ++c)
+      me[r * 24 + c] = 0.5 * (m[static_cast<size_t>(r) * 24 + c] + m[static_cast<size_t>(c) * 24 + r]);
+}
+
 struct Problem {
   int dim = 2, npe = 4;
   Index nx = 0, ny = 0, nz = 1;
@@ -1331,8 +1404,9 @@ void build_pattern(Problem& p) {
   }
 }
 
-// K_ff values for element factors `scale` (Assembler.cpp:182-214, 410-455).
-void assemble_kff(const Problem& p, const double* scale, Vec& full, Vec& kff) {
+// Free-free values of sum_e s_e E (E = K_e^0, or M_e^0 for the mass) for
+// element factors `scale` (Assembler.cpp:182-214, 260-275, 410-455).
+void assemble_ff(const Problem& p, const double* elem, const double* scale, Vec& full, Vec& kff) {
   full.assign(p.inner.size(), 0.0);
   const int npe = p.npe, dim = p.dim, ed = p.edofs;
   for (Index e = 0; e < p.ne; ++e) {
@@ -1345,12 +1419,16 @@ void assemble_kff(const Problem& p, const double* scale, Vec& full, Vec& kff) {
         const Index base = p.outer[nodes[b] * dim + kb];
         for (int a = 0; a < npe; ++a) {
           double* t = full.data() + base + off[a * npe + b];
-          for (int ka = 0; ka < dim; ++ka) t[ka] += s * p.ke[static_cast<size_t>(dim * a + ka) * ed + column];
+          for (int ka = 0; ka < dim; ++ka) t[ka] += s * elem[static_cast<size_t>(dim * a + ka) * ed + column];
         }
       }
   }
   kff.resize(p.ff_src.size());
   for (size_t k = 0; k < p.ff_src.size(); ++k) kff[k] = full[static_cast<size_t>(p.ff_src[k])];
+}
+
+void assemble_kff(const Problem& p, const double* scale, Vec& full, Vec& kff) {
+  assemble_ff(p, p.ke.data(), scale, full, kff);
 }
 
 // Centroid hash of the reference's filter (DensityFilter.cpp:19-74): buckets of
@@ -1974,6 +2052,11 @@ int orc_element_stiffness(int dim, double hx, double hy, double hz, double young
   return guarded([&] { element_stiffness(dim, hx, hy, hz, young, poisson, thickness, ke); });
 }
 
+int orc_element_mass(int dim, double hx, double hy, double hz, double density, double thickness,
+                     double* me) {
+  return guarded([&] { element_mass(dim, hx, hy, hz, density, thickness, me); });
+}
+
 int orc_solver_create(const orc_amg_options* o, double rtol, int32_t maxit, orc_solver** out) {
   return guarded([&] {
     auto* s = new orc_solver();
@@ -2184,6 +2267,21 @@ int orc_problem_kff(orc_problem* h, const double* scale, int32_t* ptr, int32_t* 
       Vec full, kff;
       assemble_kff(p, scale, full, kff);
       std::copy(kff.begin(), kff.end(), val);
+    }
+  });
+}
+
+int orc_problem_assemble(orc_problem* h, const double* elem, const double* scale, double* val,
+                         double* full_sum) {
+  return guarded([&] {
+    Vec full, ff;
+    assemble_ff(h->p, elem, scale, full, ff);
+    std::copy(ff.begin(), ff.end(), val);
+    if (full_sum) {
+      // SparseMatrix::sum(): the stored values in storage order
+      double t = 0.0;
+      for (double v : full) t += v;
+      *full_sum = t;
     }
   });
 }

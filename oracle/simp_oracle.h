@@ -67,6 +67,10 @@ const char* orc_last_error(void);
 int orc_element_stiffness(int dim, double hx, double hy, double hz, double young,
                           double poisson, double thickness, double* ke);
 
+/* Consistent mass of one box cell, 3 x 3 (x 3) Gauss, symmetrised. */
+int orc_element_mass(int dim, double hx, double hy, double hz, double density,
+                     double thickness, double* me);
+
 /* ---- AMG-PCG on a caller's matrix (the LinearSolver boundary) ---- */
 int orc_solver_create(const orc_amg_options* o, double rtol, int32_t max_iterations,
                       orc_solver** out);
@@ -100,6 +104,10 @@ int orc_problem_coords(orc_problem* p, double* coords);
 int orc_problem_kff(orc_problem* p, const double* scale, int32_t* rowptr, int32_t* col,
                     double* val);
 int orc_problem_element_matrix(orc_problem* p, double* ke);
+/* Free-free values (K_ff's pattern) of sum_e s_e E for a caller's element
+ * matrix E (the mass matrix with M_e^0), and the sum of the full matrix. */
+int orc_problem_assemble(orc_problem* p, const double* elem, const double* scale, double* val,
+                         double* full_sum);
 int orc_filter_forward(orc_problem* p, const double* x, double* y);
 int orc_filter_adjoint(orc_problem* p, const double* v, double* g);
 int orc_filter_row_sums(orc_problem* p, double* sums);

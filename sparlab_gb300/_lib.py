@@ -32,7 +32,8 @@ EXPORTS = [
     "simp_oc_update", "simp_mma_update", "simp_iterate", "simp_problem_stats", "simp_filter_forward",
     "simp_filter_adjoint", "simp_problem_kff", "simp_element_stiffness",
     "simp_problem_apply_operator", "simp_problem_time_operator", "simp_filter_volume_noalloc",
-    "simp_kernel_launches",
+    "simp_kernel_launches", "simp_default_modal_options", "simp_modal", "simp_modal_warning",
+    "simp_element_mass",
 ]
 
 
@@ -101,6 +102,21 @@ class IterationRecord(C.Structure):
                 ("beta", C.c_double)]
 
 
+class ModalOptions(C.Structure):
+    _fields_ = [("num_modes", C.c_int32), ("mass_type", C.c_int32), ("max_iterations", C.c_int32),
+                ("tolerance", C.c_double), ("shift_factor", C.c_double),
+                ("rigid_body_ratio", C.c_double), ("residual_tolerance", C.c_double),
+                ("warm_start", C.c_int32), ("density", C.c_double),
+                ("element_mass", C.POINTER(C.c_double)), ("concurrent_solves", C.c_int32)]
+
+
+class ModalInfo(C.Structure):
+    _fields_ = [("num_modes", C.c_int32), ("iterations", C.c_int32), ("subspace_size", C.c_int32),
+                ("converged", C.c_int32), ("linear_iterations", C.c_int64),
+                ("final_change", C.c_double), ("total_mass", C.c_double),
+                ("num_warnings", C.c_int32)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -118,6 +134,7 @@ def load(build_if_missing: bool = True):
             lib.simp_last_error.restype = C.c_char_p
             lib.simp_problem_last_error.restype = C.c_char_p
             lib.simp_kernel_launches.restype = C.c_int64
+            lib.simp_modal_warning.restype = C.c_char_p
             _lib = lib
     return _lib
 

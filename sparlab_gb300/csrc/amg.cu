@@ -412,6 +412,10 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
   SIMP_CHECK_LAUNCH();
 }
 
+void GpuAmg::apply_values0(SolveWork& w, const double* values, const double* x, double* y) {
+  nb_apply<0, double, double, double>(levels.front()->opA, values, x, y, nullptr, w.stream);
+}
+
 // CUDA-event time of the level-0 CG operator (op0: FP64 values in fp64
 // mode, double-float values in mixed mode) on this context's stream, and its
 // compulsory bytes (8 per value either way).

@@ -196,6 +196,9 @@ class GpuAmg {
   // the PCG direction update).
   void op0(SolveWork& w, const double* x, double* y, const double* rhs, bool split_ready = false);
   void spmv0(const double* x, double* y) { op0(work(0), x, y, nullptr); }
+  // y = V x for caller's FP64 values V on level 0's pattern (a matrix of the
+  // same structure: the stiffness or mass of a modal analysis)
+  void apply_values0(SolveWork& w, const double* values, const double* x, double* y);
   // CUDA-event time of one op0 launch (ms) and its algorithmic bytes
   void time_operator(int reps, double* ms, double* bytes);
   double dot(SolveWork& w, const double* a, const double* b, i64 n);

@@ -93,6 +93,7 @@ struct simp_problem {
   std::unique_ptr<GpuProblem> p;
   int device = 0;
   std::string err;
+  std::vector<std::string> modal_warnings;
 };
 
 extern "C" {
@@ -734,6 +735,81 @@ int simp_filter_volume_noalloc(simp_problem* p, const double* x, double* rho, do
   return guarded(p->err, [&] {
     use_device(p->device);
     filter_volume_noalloc(*p->p, x, rho, volume);
+  });
+}
+
+void simp_default_modal_options(simp_modal_options* o) {
+  o->num_modes = 6;
+  o->mass_type = 0;
+  o->max_iterations = 200;
+  o->tolerance = 1.0e-10;
+  o->shift_factor = 0.0;
+  o->rigid_body_ratio = 1.0e-10;
+  o->residual_tolerance = 1.0e-6;
+  o->warm_start = 1;
+  o->density = 1.0;
+  o->element_mass = nullptr;
+  o->concurrent_solves = 4;
+}
+
+int simp_modal(simp_problem* p, const simp_modal_options* options, const double* stiffness_scale,
+               const double* mass_scale, double* eigenvalues, double* frequencies_hz, double* residuals,
+               double* mass_fraction, double* mode_shapes, simp_modal_info* info) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    if (!options) throw Error(kBadInput, "simp_modal needs options");
+    GpuProblem& g = *p->p;
+    ModalOptions o;
+    o.num_modes = options->num_modes;
+    o.mass_type = options->mass_type;
+    o.max_iterations = options->max_iterations;
+    o.tolerance = options->tolerance;
+    o.shift_factor = options->shift_factor;
+    o.rigid_body_ratio = options->rigid_body_ratio;
+    o.residual_tolerance = options->residual_tolerance;
+    o.warm_start = options->warm_start != 0;
+    o.density = options->density;
+    o.concurrent_solves = options->concurrent_solves;
+    if (options->element_mass) {
+      const int ed = g.d.dim == 3 ? 24 : 8;
+      o.element_mass.assign(options->element_mass, options->element_mass + ed * ed);
+    }
+    p->modal_warnings.clear();
+    const ModalResult r = solve_modal(g, o, stiffness_scale, mass_scale, mode_shapes != nullptr);
+    p->modal_warnings = r.warnings;
+    const int m = static_cast<int>(r.eigenvalues.size());
+    constexpr double two_pi = 6.283185307179586476925286766559;
+    for (int i = 0; i < m; ++i) {
+      if (eigenvalues) eigenvalues[i] = r.eigenvalues[i];
+      if (frequencies_hz) frequencies_hz[i] = std::sqrt(std::max(r.eigenvalues[i], 0.0)) / two_pi;
+      if (residuals) residuals[i] = r.residuals[i];
+      if (mass_fraction) mass_fraction[i] = r.mass_fraction[i];
+    }
+    if (mode_shapes) std::copy(r.shapes.begin(), r.shapes.end(), mode_shapes);
+    if (info) {
+      info->num_modes = m;
+      info->iterations = r.iterations;
+      info->subspace_size = r.subspace_size;
+      info->converged = r.converged ? 1 : 0;
+      info->linear_iterations = r.linear_iterations;
+      info->final_change = r.final_change;
+      info->total_mass = r.total_mass;
+      info->num_warnings = static_cast<int32_t>(r.warnings.size());
+    }
+  });
+}
+
+const char* simp_modal_warning(simp_problem* p, int32_t k) {
+  if (!p || k < 0 || k >= static_cast<int32_t>(p->modal_warnings.size())) return nullptr;
+  return p->modal_warnings[static_cast<size_t>(k)].c_str();
+}
+
+int simp_element_mass(int32_t dim, double hx, double hy, double hz, double density, double thickness,
+                      double* me) {
+  return guarded(g_create_error, [&] {
+    if (dim != 2 && dim != 3) throw Error(kBadInput, "dim must be 2 or 3");
+    if (!(density > 0.0)) throw Error(kBadInput, "mass assembly requires a positive density");
+    element_mass(dim, hx, hy, hz, density, thickness, me);
   });
 }
 

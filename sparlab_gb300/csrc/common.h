@@ -94,6 +94,13 @@ struct DBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
+// dst = a device copy of src (same length)
+template <class T>
+void copy_device(DBuf<T>& dst, const DBuf<T>& src, cudaStream_t s = 0) {
+  dst.alloc(src.n);
+  if (src.n) SIMP_CUDA(cudaMemcpyAsync(dst.p, src.p, src.n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+}
+
 // Device view of a node-level pattern (see structure.h).
 struct NodeView {
   const i32* ptr;   // row-node slot pointer

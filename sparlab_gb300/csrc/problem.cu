@@ -443,6 +443,21 @@ void GpuProblem::get_design(double* h) {
   SIMP_CUDA(cudaStreamSynchronize(amg.stream));
 }
 
+void GpuProblem::assemble_into(const double* elem, const double* scale, bool exact, double* v64, float* hi,
+                               float* lo, cudaStream_t stream) {
+  Level& l0 = *amg.levels.front();
+  if (l0.nnodes == 0) return;
+  const int offsets = d.dim == 3 ? 27 : 9;
+  const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
+  const size_t smem = assemble_smem(d.dim);
+  auto kernel = exact ? k_assemble_tiles<true, false> : k_assemble_tiles<false, false>;
+  SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  kernel<<<blocks, offsets * kAsmTile, smem, stream>>>(grid_of(d), l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
+                                                       nmask.p, l0.d_apat.view(), l0.a.ptr.p, elem, scale, nullptr,
+                                                       nullptr, v64, hi, lo);
+  SIMP_CHECK_LAUNCH();
+}
+
 void GpuProblem::assemble(const double* scale, bool exact) {
   Level& l0 = *amg.levels.front();
   if (l0.nnodes == 0) return;

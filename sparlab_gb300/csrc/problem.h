@@ -72,6 +72,12 @@ class GpuProblem {
   // exact: rounded products and sums in element order (the structure-
   // defining first assembly); otherwise fused multiply-adds
   void assemble(const double* scale_device, bool exact);
+  // FP64 sum_e s_e E over level 0's pattern for a device element matrix E
+  // (K_e^0, or M_e^0 for the mass), with the same kernel and order; FP32
+  // (hi) or double-float (hi, lo) copies when those are given
+  void assemble_into(const double* elem, const double* scale_device, bool exact, double* v64, float* hi,
+                     float* lo, cudaStream_t stream);
+  const std::vector<i32>& free_dofs() const { return free_dofs_; }
 
   // device state
   DBuf<double> x, xnew, rho, sf, df, dc_dphys, dc_dx, dv_dx, se, vols, tmp;
@@ -127,6 +133,37 @@ double beta_of_stage(const ProblemDesc& d, int k);
 
 void element_stiffness(int dim, double hx, double hy, double hz, double young, double nu, double thick,
                        double* ke);
+// Consistent mass of a box cell, 3-point Gauss per direction (modal.cu).
+void element_mass(int dim, double hx, double hy, double hz, double density, double thick, double* me);
+
+// Undamped free vibration of the structured model (modal.cu):
+// ModalAnalysisOptions (include/sparlab/fem/ModalAnalysis.hpp:37-65).
+struct ModalOptions {
+  int num_modes = 6;
+  int mass_type = 0;  // 0 consistent, 1 lumped (row sums)
+  int max_iterations = 200;
+  double tolerance = 1.0e-10, shift_factor = 0.0, rigid_body_ratio = 1.0e-10, residual_tolerance = 1.0e-6;
+  bool warm_start = true;
+  double density = 1.0;
+  std::vector<double> element_mass;  // M_e^0 (row-major); empty: the cell's consistent mass
+  int concurrent_solves = 4;
+};
+
+// ModalResult (include/sparlab/fem/ModalAnalysis.hpp:67-86)
+struct ModalResult {
+  std::vector<double> eigenvalues, residuals, mass_fraction;
+  std::vector<double> shapes;  // modes x ndof (a mode per row), M-orthonormal, zero on supports
+  double total_mass = 0.0, final_change = 0.0;
+  int iterations = 0, subspace_size = 0;
+  bool converged = false;
+  i64 linear_iterations = 0;
+  std::vector<std::string> warnings;
+};
+
+// solve_modal (src/fem/ModalAnalysis.cpp:120-418) with the problem's grid,
+// supports and solver options; host element factors (null: ones).
+ModalResult solve_modal(GpuProblem& p, const ModalOptions& o, const double* stiffness_scale,
+                        const double* mass_scale, bool want_shapes);
 
 // rho = clamp(H x, 0, 1) and sum_e v_e rho_e without allocating (noalloc.cu).
 void filter_volume_noalloc(GpuProblem& p, const double* x, double* rho, double* volume);

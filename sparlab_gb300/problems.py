@@ -66,6 +66,7 @@ class ProblemSpec:
     young: float = 1.0
     poisson: float = 0.3
     thickness: float = 1.0
+    density: float = 1.0                    # material density (modal analysis)
     fixed: Optional[np.ndarray] = None      # uint8 per DOF (node * dim + k)
     loads: Optional[np.ndarray] = None      # (L, ndof)
     weights: Optional[np.ndarray] = None    # (L,) raw weights
@@ -182,6 +183,22 @@ def bench_model(dim: int, nx: int, ny: int, nz: int = 0) -> ProblemSpec:
     spec.fixed = clamp_left(spec)
     tip = nearest_node(spec, (spec.lx, 0.0, 0.0))
     spec.loads = point_load(spec, [tip], (0.0, -1000.0, 0.0))[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
+def plane_cantilever(nx: int, ny: int, length: float = 1.0, height: float = 0.1,
+                     thickness: float = 0.01, young: float = 70.0e9, poisson: float = 0.0,
+                     density: float = 2700.0) -> ProblemSpec:
+    """The reference's standard modal / static cantilever (tests/TestSupport.hpp:
+    23-86): plane stress, root x = 0 clamped, a -1000 N tip resultant spread
+    over the tip edge."""
+    spec = ProblemSpec(dim=2, nx=nx, ny=ny, nz=0, lx=length, ly=height, lz=0.0, young=young,
+                       poisson=poisson, thickness=thickness, density=density, filter_radius=0.0,
+                       rtol=1e-12, name=f"cantilever_{nx}x{ny}")
+    spec.fixed = clamp_left(spec)
+    tip = [spec.node_index(nx, j) for j in range(ny + 1)]
+    spec.loads = point_load(spec, tip, (0.0, -1000.0))[None, :]
     spec.weights = np.ones(1)
     return spec
 

@@ -74,6 +74,37 @@ class TopologyIteration:
     final_stage: bool = True   # no projection, or its last beta stage
 
 
+def element_mass(dim, hx, hy, hz, density, thickness=1.0) -> np.ndarray:
+    """Consistent mass of a box cell (Quad4Element / Hex8Element::consistent_mass)."""
+    ed = 8 if dim == 2 else 24
+    me = np.zeros((ed, ed))
+    lib = _lib.load()
+    code = lib.simp_element_mass(C.c_int32(dim), C.c_double(hx), C.c_double(hy), C.c_double(hz),
+                                 C.c_double(density), C.c_double(thickness), ptr(me))
+    if code:
+        _lib.raise_for(code, lib.simp_problem_last_error(None).decode())
+    return me
+
+
+@dataclasses.dataclass
+class ModalResult:
+    """``sparlab::ModalResult`` (include/sparlab/fem/ModalAnalysis.hpp:67-86)."""
+    eigenvalues: np.ndarray
+    angular_frequencies: np.ndarray
+    frequencies_hz: np.ndarray
+    mode_shapes: Optional[np.ndarray]   # num_dofs x num_modes
+    modal_residuals: np.ndarray
+    modal_mass_fraction: np.ndarray
+    total_mass: float
+    iterations: int
+    subspace_size: int
+    converged: bool
+    linear_iterations: int
+    final_change: float
+    warnings: List[str]
+    linear_solver: str = "AMG-CG(chebyshev, GPU)"
+
+
 class GpuSimpProblem:
     """A structured SIMP problem resident on the GPU (boundary 2 of the C ABI)."""
 
@@ -228,6 +259,41 @@ class GpuSimpProblem:
         g = np.zeros(self.ne)
         self._check(self._lib.simp_filter_adjoint(self._h, ptr(v), ptr(g)))
         return g
+
+    def modal(self, num_modes=6, mass_type="consistent", max_iterations=200, tolerance=1e-10,
+              shift_factor=0.0, rigid_body_ratio=1e-10, residual_tolerance=1e-6, warm_start=True,
+              density=None, element_mass=None, stiffness_scale=None, mass_scale=None,
+              mode_shapes=True, concurrent_solves=4) -> ModalResult:
+        """``solve_modal`` (src/fem/ModalAnalysis.cpp:120-418) on this
+        problem's grid and supports, with the problem's AMG-PCG options for
+        the shifted solves.  Scales: per-element stiffness / mass factors
+        (None: ones).  ``density`` defaults to ``spec.density``."""
+        o = _lib.ModalOptions()
+        self._lib.simp_default_modal_options(C.byref(o))
+        o.num_modes, o.max_iterations = num_modes, max_iterations
+        o.mass_type = {"consistent": 0, "lumped": 1}[mass_type]
+        o.tolerance, o.shift_factor = tolerance, shift_factor
+        o.rigid_body_ratio, o.residual_tolerance = rigid_body_ratio, residual_tolerance
+        o.warm_start = int(warm_start)
+        o.density = self.spec.density if density is None else density
+        o.concurrent_solves = concurrent_solves
+        me = None
+        if element_mass is not None:
+            me = np.ascontiguousarray(element_mass, np.float64)
+            o.element_mass = ptr(me)
+        ks = None if stiffness_scale is None else np.ascontiguousarray(stiffness_scale, np.float64)
+        ms = None if mass_scale is None else np.ascontiguousarray(mass_scale, np.float64)
+        m = max(1, min(num_modes, self.nfree))
+        lam, freq, res, frac = (np.zeros(m) for _ in range(4))
+        shapes = np.zeros((m, self.ndof)) if mode_shapes else None
+        info = _lib.ModalInfo()
+        self._check(self._lib.simp_modal(self._h, C.byref(o), ptr(ks), ptr(ms), ptr(lam), ptr(freq),
+                                         ptr(res), ptr(frac), ptr(shapes), C.byref(info)))
+        warnings = [self._lib.simp_modal_warning(self._h, k).decode() for k in range(info.num_warnings)]
+        return ModalResult(lam, np.sqrt(np.maximum(lam, 0.0)), freq,
+                           None if shapes is None else shapes.T.copy(), res, frac, info.total_mass,
+                           info.iterations, info.subspace_size, bool(info.converged),
+                           info.linear_iterations, info.final_change, warnings)
 
     def kff(self, scale=None):
         p = np.zeros(self.nfree + 1, np.int32)
