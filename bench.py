@@ -54,6 +54,41 @@ BATCHED = "batched_64"
 BATCHED_METRIC = "instance SIMP iter/s, 64 independent Q4/Hex8 instances (seed 4)"
 
 
+# Undamped free vibration of the solid Hex8 96 x 48 x 48 cantilever (unit
+# cells, E = 1, nu = 0.3, density 1): a step is one complete modal analysis
+# (6 lowest modes, consistent mass, subspace iteration over its own AMG-PCG
+# hierarchy); the metric is modal analyses per second
+MODAL = "modal_hex8_96x48x48"
+MODAL_METRIC = "modal analyses/s (6 lowest modes, Hex8 96x48x48 solid cantilever)"
+MODAL_MODES = 6
+
+
+def modal_spec(nx=96, ny=48, nz=48):
+    spec = P.hex8_cantilever(nx, ny, nz, 0.2, f"modal_hex8_{nx}x{ny}x{nz}")
+    spec.rtol = 1e-10
+    return spec
+
+
+def modal_cpu_baseline(steps=1):
+    """Oracle modal analysis of the same cantilever with every axis divided
+    by four (1/64 of the cells), scaled by the cell ratio."""
+    import oracle
+    from oracle import modal as OM
+    spec = modal_spec(24, 12, 12)
+    ratio = 64.0
+    times, its = [], 0
+    for _ in range(steps):
+        pr = oracle.Problem(spec)
+        t0 = time.perf_counter()
+        r = OM.solve_modal(pr, spec, num_modes=MODAL_MODES, density=spec.density, rtol=spec.rtol)
+        times.append(time.perf_counter() - t0)
+        its = r.iterations
+    t = min(times)
+    return {"value": 1.0 / (t * ratio), "unit": "analyses/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{spec.name}: 24x12x12 cells (1/64 of the workload's), {its} subspace iterations, "
+                      f"min of {steps} analyses ({t:.2f} s each), scaled by the cell ratio 64"}
+
+
 def sample_spec(name):
     """Bounded CPU sample: the same cantilever with every axis halved twice."""
     make, sub = WORKLOADS[name]
@@ -175,6 +210,19 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if args.config == MODAL:
+        base = modal_cpu_baseline()
+        v = base["value"]
+        print(json.dumps({
+            "impl": "reference", "metric": MODAL_METRIC, "value": v, "unit": "analyses/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic cantilever (no dataset)",
+            "config": {"workload": MODAL, "modes": MODAL_MODES, "host_threads": os.cpu_count()},
+            "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "analyses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
+        return
     if args.config == BATCHED:
         specs = P.batched_instances(seed=4)
         base = batched_cpu_baseline(specs)
@@ -231,6 +279,80 @@ def whole_job_rate(ms_local, steps, world, device=None):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     return ms, world * steps / (ms * 1e-3)
+
+
+def run_own_modal(args):
+    """Modal analyses of the solid cantilever; replicas under torchrun."""
+    import torch
+    import torch.distributed as dist
+    from sparlab_gb300 import _lib
+    from sparlab_gb300.topopt import GpuSimpProblem
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    spec = modal_spec()
+    prob = GpuSimpProblem(spec, precision=args.precision, device=local)
+    lib = _lib.load()
+    for _ in range(args.warmup):
+        r = prob.modal(num_modes=MODAL_MODES, mode_shapes=False)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    barrier()
+    launches0 = lib.simp_kernel_launches()
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    recs = [prob.modal(num_modes=MODAL_MODES, mode_shapes=False) for _ in range(args.steps)]
+    e1.record()
+    barrier()
+    clocks = sampler.stop()
+    launches = lib.simp_kernel_launches() - launches0
+    ms, value = whole_job_rate(e0.elapsed_time(e1), args.steps, world, dev)
+    # e2e: the same analysis through the public API with the mode shapes
+    # copied back to the host every step
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(args.steps):
+        r = prob.modal(num_modes=MODAL_MODES, mode_shapes=True)
+    f1.record()
+    barrier()
+    e2e_ms, e2e_value = whole_job_rate(f0.elapsed_time(f1), args.steps, world, dev)
+    if rank != 0:
+        return
+    line = {
+        "metric": MODAL_METRIC, "value": value, "unit": "analyses/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic cantilever (no dataset)",
+        "config": {"workload": MODAL, "elements": spec.num_elements, "free_dofs": prob.nfree,
+                   "modes": MODAL_MODES, "mass": "consistent", "precision": args.precision,
+                   "subspace_size": recs[-1].subspace_size,
+                   "subspace_iterations": [r.iterations for r in recs],
+                   "pcg_iterations": [r.linear_iterations for r in recs],
+                   "frequencies_hz": [float(f) for f in recs[-1].frequencies_hz],
+                   "l2": "working set (K_ff and M_ff 1.3 GB) larger than L2"},
+        "roofline": None,
+        "cpu_baseline": modal_cpu_baseline() if world == 1 else None,
+        "e2e": {"value": e2e_value, "unit": "analyses/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 8 * MODAL_MODES * prob.ndof},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
 
 
 def run_own_batched(args):
@@ -476,7 +598,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
-    ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS) + [BATCHED])
+    ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS) + [BATCHED, MODAL])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 comparison run that follows a mixed-precision run")
@@ -493,6 +615,8 @@ def main():
         run_reference(args)
     elif args.config == BATCHED:
         run_own_batched(args)
+    elif args.config == MODAL:
+        run_own_modal(args)
     else:
         run_own(args)
 
