@@ -664,6 +664,17 @@ ModalResult solve_modal(GpuProblem& p, const ModalOptions& o, const double* ksca
       }
       SIMP_CHECK_LAUNCH();
     }
+    // mixed precision on a fully-free-or-clamped grid: the V-cycle's level-0
+    // operator is the matrix-free K (FP32), as in the optimisation's solver;
+    // only without a shift, where A = K
+    DBuf<float> ks32;
+    if (p.amg.mf.enabled && sigma == 0.0) {
+      ks32.alloc(static_cast<size_t>(ne));
+      k_convert<double, float><<<grid_for(ne, 256), 256, 0, s>>>(ks.p, ks32.p, ne);
+      SIMP_CHECK_LAUNCH();
+      amg.mf = p.amg.mf;
+      amg.mf.scale = ks32.p;
+    }
     amg.setup(true);
     const int workers = std::max(1, std::min(q, o.concurrent_solves));
     std::vector<SolveWork*> works;
