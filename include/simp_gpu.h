@@ -340,6 +340,62 @@ int simp_modal(simp_problem* p, const simp_modal_options* options, const double*
  * modes than requested), or NULL. */
 const char* simp_modal_warning(simp_problem* p, int32_t k);
 
+/* ---- Linear buckling (src/fem/Buckling.cpp) ---------------------------- */
+
+/* BucklingOptions (include/sparlab/fem/Buckling.hpp:91-109) and the material
+ * constants of the prestress sigma = D B u (the problem holds only K_e^0). */
+typedef struct simp_buckling_options {
+  int32_t num_modes;          /* smallest positive load factors requested (4) */
+  int32_t max_iterations;     /* subspace iteration cap (400) */
+  double tolerance;           /* relative change of the requested load factors (1e-8) */
+  double residual_tolerance;  /* eigenpair residual bound (1e-6) */
+  double young;               /* Young's modulus of the material (required) */
+  double poisson;             /* Poisson ratio (plane stress in 2-D) */
+  int32_t transform;          /* 0 auto; 1 the spectral transformation from the start:
+                                 not available (SIMP_BAD_INPUT), see below */
+  int32_t concurrent_solves;  /* subspace columns solved at the same time (4) */
+} simp_buckling_options;
+
+/* BucklingResult's scalars (include/sparlab/fem/Buckling.hpp:111-140). */
+typedef struct simp_buckling_info {
+  int32_t num_modes;               /* positive load factors returned */
+  int32_t iterations;              /* subspace iterations (0 on the dense path) */
+  int32_t subspace_size;
+  int32_t converged;
+  int32_t no_positive_load_factor; /* the load case only stiffens the structure */
+  int32_t subspace_cols;           /* columns written to `subspace` */
+  int64_t linear_iterations;       /* PCG iterations, the static solve included */
+  double final_change;
+  int32_t num_warnings;            /* texts: simp_buckling_warning */
+} simp_buckling_info;
+
+void simp_default_buckling_options(simp_buckling_options* o);
+
+/* analyse_buckling (src/fem/Buckling.cpp:438-466) of load case `load_case`:
+ * the static solution u of K_ff u = f, K_G(u) on the device, and the smallest
+ * positive load factors lambda of (K_ff + lambda K_G,ff) phi = 0 by subspace
+ * iteration X <- K^-1 (-K_G) X on the problem's AMG-PCG (its tolerance and
+ * precision).  Host inputs, NULL for the defaults: stiffness_scale and
+ * stress_scale (num_elements each; ones), solid_mask (num_elements bytes,
+ * 1 = solid; all solid), start_subspace (nfree x start_cols, column-major:
+ * the `subspace` of a previous analysis).  Outputs (host, NULL to skip):
+ * load_factors, residuals and solid_energy_fraction (num_modes each),
+ * mode_shapes (num_modes x num_dofs, phi^T K phi = 1, zero on the supports),
+ * subspace (nfree x subspace_size, column-major).  Systems with at most 400
+ * free DOFs take the dense path.  Not available: the reference's spectral
+ * transformation, which it uses when reversed-load modes crowd the subspace
+ * (mostly tensile stress states): it places its shift by the inertia of
+ * sparse LDL^T factorisations and this library has none, so those cases
+ * return SIMP_BAD_INPUT with a message saying so. */
+int simp_buckling(simp_problem* p, const simp_buckling_options* options, int32_t load_case,
+                  const double* stiffness_scale, const double* stress_scale,
+                  const uint8_t* solid_mask, const double* start_subspace, int32_t start_cols,
+                  double* load_factors, double* residuals, double* solid_energy_fraction,
+                  double* mode_shapes, double* subspace, simp_buckling_info* info);
+
+/* Warning k of the last simp_buckling, or NULL. */
+const char* simp_buckling_warning(simp_problem* p, int32_t k);
+
 /* Consistent mass of a box cell (Quad4Element/Hex8Element::consistent_mass,
  * src/elements/Quad4.cpp:139-173, src/elements/Hex8.cpp:194-214), 3-point
  * Gauss per direction. */

@@ -33,7 +33,7 @@ EXPORTS = [
     "simp_filter_adjoint", "simp_problem_kff", "simp_element_stiffness",
     "simp_problem_apply_operator", "simp_problem_time_operator", "simp_filter_volume_noalloc",
     "simp_kernel_launches", "simp_default_modal_options", "simp_modal", "simp_modal_warning",
-    "simp_element_mass",
+    "simp_element_mass", "simp_default_buckling_options", "simp_buckling", "simp_buckling_warning",
 ]
 
 
@@ -117,6 +117,19 @@ class ModalInfo(C.Structure):
                 ("num_warnings", C.c_int32)]
 
 
+class BucklingOptions(C.Structure):
+    _fields_ = [("num_modes", C.c_int32), ("max_iterations", C.c_int32), ("tolerance", C.c_double),
+                ("residual_tolerance", C.c_double), ("young", C.c_double), ("poisson", C.c_double),
+                ("transform", C.c_int32), ("concurrent_solves", C.c_int32)]
+
+
+class BucklingInfo(C.Structure):
+    _fields_ = [("num_modes", C.c_int32), ("iterations", C.c_int32), ("subspace_size", C.c_int32),
+                ("converged", C.c_int32), ("no_positive_load_factor", C.c_int32),
+                ("subspace_cols", C.c_int32), ("linear_iterations", C.c_int64),
+                ("final_change", C.c_double), ("num_warnings", C.c_int32)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -135,6 +148,7 @@ def load(build_if_missing: bool = True):
             lib.simp_problem_last_error.restype = C.c_char_p
             lib.simp_kernel_launches.restype = C.c_int64
             lib.simp_modal_warning.restype = C.c_char_p
+            lib.simp_buckling_warning.restype = C.c_char_p
             _lib = lib
     return _lib
 

@@ -93,7 +93,7 @@ struct simp_problem {
   std::unique_ptr<GpuProblem> p;
   int device = 0;
   std::string err;
-  std::vector<std::string> modal_warnings;
+  std::vector<std::string> modal_warnings, buckling_warnings;
 };
 
 extern "C" {
@@ -802,6 +802,64 @@ int simp_modal(simp_problem* p, const simp_modal_options* options, const double*
 const char* simp_modal_warning(simp_problem* p, int32_t k) {
   if (!p || k < 0 || k >= static_cast<int32_t>(p->modal_warnings.size())) return nullptr;
   return p->modal_warnings[static_cast<size_t>(k)].c_str();
+}
+
+void simp_default_buckling_options(simp_buckling_options* o) {
+  o->num_modes = 4;
+  o->max_iterations = 400;
+  o->tolerance = 1.0e-8;
+  o->residual_tolerance = 1.0e-6;
+  o->young = 0.0;
+  o->poisson = 0.0;
+  o->transform = 0;
+  o->concurrent_solves = 4;
+}
+
+int simp_buckling(simp_problem* p, const simp_buckling_options* options, int32_t load_case,
+                  const double* stiffness_scale, const double* stress_scale, const uint8_t* solid_mask,
+                  const double* start_subspace, int32_t start_cols, double* load_factors, double* residuals,
+                  double* solid_energy_fraction, double* mode_shapes, double* subspace, simp_buckling_info* info) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    if (!options) throw Error(kBadInput, "simp_buckling needs options");
+    BucklingOptions o;
+    o.num_modes = options->num_modes;
+    o.max_iterations = options->max_iterations;
+    o.tolerance = options->tolerance;
+    o.residual_tolerance = options->residual_tolerance;
+    o.young = options->young;
+    o.poisson = options->poisson;
+    o.transform = options->transform;
+    o.concurrent_solves = options->concurrent_solves;
+    p->buckling_warnings.clear();
+    const BucklingResult r = solve_buckling(*p->p, o, load_case, stiffness_scale, stress_scale, solid_mask,
+                                            start_subspace, start_cols, mode_shapes != nullptr);
+    p->buckling_warnings = r.warnings;
+    const int m = static_cast<int>(r.load_factors.size());
+    for (int i = 0; i < m; ++i) {
+      if (load_factors) load_factors[i] = r.load_factors[i];
+      if (residuals) residuals[i] = r.residuals[i];
+      if (solid_energy_fraction) solid_energy_fraction[i] = r.solid_fraction[i];
+    }
+    if (mode_shapes) std::copy(r.shapes.begin(), r.shapes.end(), mode_shapes);
+    if (subspace) std::copy(r.subspace.begin(), r.subspace.end(), subspace);
+    if (info) {
+      info->num_modes = m;
+      info->iterations = r.iterations;
+      info->subspace_size = r.subspace_size;
+      info->converged = r.converged ? 1 : 0;
+      info->no_positive_load_factor = r.no_positive ? 1 : 0;
+      info->subspace_cols = r.subspace_cols;
+      info->linear_iterations = r.linear_iterations;
+      info->final_change = r.final_change;
+      info->num_warnings = static_cast<int32_t>(r.warnings.size());
+    }
+  });
+}
+
+const char* simp_buckling_warning(simp_problem* p, int32_t k) {
+  if (!p || k < 0 || k >= static_cast<int32_t>(p->buckling_warnings.size())) return nullptr;
+  return p->buckling_warnings[static_cast<size_t>(k)].c_str();
 }
 
 int simp_element_mass(int32_t dim, double hx, double hy, double hz, double density, double thickness,

@@ -168,4 +168,35 @@ ModalResult solve_modal(GpuProblem& p, const ModalOptions& o, const double* stif
 // rho = clamp(H x, 0, 1) and sum_e v_e rho_e without allocating (noalloc.cu).
 void filter_volume_noalloc(GpuProblem& p, const double* x, double* rho, double* volume);
 
+// BucklingOptions (include/sparlab/fem/Buckling.hpp:91-109) with the
+// material constants the prestress needs (the problem holds only K_e^0).
+struct BucklingOptions {
+  int num_modes = 4;
+  int max_iterations = 400;
+  double tolerance = 1.0e-8, residual_tolerance = 1.0e-6;
+  double young = 0.0, poisson = 0.0;
+  int transform = 0;  // 0 auto (plain iteration), 1 shift-invert from the start (not available)
+  int concurrent_solves = 4;
+};
+
+// BucklingResult (include/sparlab/fem/Buckling.hpp:111-140)
+struct BucklingResult {
+  std::vector<double> load_factors, residuals, solid_fraction;
+  std::vector<double> shapes;    // modes x ndof, phi^T K phi = 1, zero on supports
+  std::vector<double> subspace;  // free DOFs x subspace_cols, column-major
+  int subspace_cols = 0;
+  bool no_positive = false, converged = false;
+  int iterations = 0, subspace_size = 0;
+  double final_change = 0.0;
+  i64 linear_iterations = 0;
+  std::vector<std::string> warnings;
+};
+
+// analyse_buckling (src/fem/Buckling.cpp:438-466) of load case `load_case`
+// with optional element stiffness and stress factors, solid flags and a
+// start subspace (free DOFs x start_cols, column-major), all on the host.
+BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_case, const double* stiffness_scale,
+                              const double* stress_scale, const uint8_t* solid, const double* start,
+                              int start_cols, bool want_shapes);
+
 }  // namespace simp

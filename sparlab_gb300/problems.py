@@ -203,6 +203,37 @@ def plane_cantilever(nx: int, ny: int, length: float = 1.0, height: float = 0.1,
     return spec
 
 
+def column(dim: int, nx: int, ny: int, nz: int = 0, length: float = 1.0, height: float = 0.05,
+           width: float = 0.05, thickness: float = 0.02, force: float = -1.0, young: float = 200.0e9,
+           poisson: float = 0.3, transverse: float = 0.0) -> ProblemSpec:
+    """The reference's buckling column (tests/test_buckling.cpp:41-68): along
+    x, root x = 0 clamped, a uniform traction on the face x = length whose
+    axial resultant is `force` (negative: compression) plus an optional
+    transverse (-y) resultant, as consistent nodal forces of the face cells."""
+    spec = ProblemSpec(dim=dim, nx=nx, ny=ny, nz=nz if dim == 3 else 0, lx=length, ly=height,
+                       lz=width if dim == 3 else 0.0, young=young, poisson=poisson,
+                       thickness=thickness if dim == 2 else 1.0, density=7850.0, filter_radius=0.0,
+                       rtol=1e-12, name=f"column_{nx}x{ny}" + (f"x{nz}" if dim == 3 else ""))
+    spec.fixed = clamp_left(spec)
+    f = np.zeros(spec.num_dofs)
+    if dim == 2:
+        for j in range(ny):
+            for jj in (j, j + 1):
+                node = spec.node_index(nx, jj)
+                f[node * 2] += force / ny / 2.0
+                f[node * 2 + 1] -= transverse / ny / 2.0
+    else:
+        for k in range(nz):
+            for j in range(ny):
+                for jj, kk in ((j, k), (j + 1, k), (j + 1, k + 1), (j, k + 1)):
+                    node = spec.node_index(nx, jj, kk)
+                    f[node * 3] += force / (ny * nz) / 4.0
+                    f[node * 3 + 1] -= transverse / (ny * nz) / 4.0
+    spec.loads = f[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
 # ---------------------------------------------------------------------------
 # The five workload configurations
 # ---------------------------------------------------------------------------

@@ -105,6 +105,25 @@ class ModalResult:
     linear_solver: str = "AMG-CG(chebyshev, GPU)"
 
 
+@dataclasses.dataclass
+class BucklingResult:
+    """``sparlab::BucklingResult`` (include/sparlab/fem/Buckling.hpp:111-140)."""
+    load_factors: np.ndarray
+    mode_shapes: Optional[np.ndarray]   # num_dofs x modes, phi^T K phi = 1
+    residuals: np.ndarray
+    solid_energy_fraction: np.ndarray
+    no_positive_load_factor: bool
+    iterations: int
+    subspace_size: int
+    converged: bool
+    linear_iterations: int
+    final_change: float
+    subspace: Optional[np.ndarray]      # free DOFs x columns
+    warnings: List[str]
+    transformed: bool = False
+    linear_solver: str = "AMG-CG(chebyshev, GPU)"
+
+
 class GpuSimpProblem:
     """A structured SIMP problem resident on the GPU (boundary 2 of the C ABI)."""
 
@@ -294,6 +313,46 @@ class GpuSimpProblem:
                            None if shapes is None else shapes.T.copy(), res, frac, info.total_mass,
                            info.iterations, info.subspace_size, bool(info.converged),
                            info.linear_iterations, info.final_change, warnings)
+
+    def buckling(self, load_case=0, num_modes=4, max_iterations=400, tolerance=1e-8,
+                 residual_tolerance=1e-6, transform="auto", stiffness_scale=None, stress_scale=None,
+                 solid_mask=None, initial_subspace=None, mode_shapes=True,
+                 concurrent_solves=4) -> BucklingResult:
+        """``analyse_buckling`` (src/fem/Buckling.cpp:438-466) of one load case
+        with the problem's AMG-PCG; the material is ``spec.young`` /
+        ``spec.poisson``."""
+        o = _lib.BucklingOptions()
+        self._lib.simp_default_buckling_options(C.byref(o))
+        o.num_modes, o.max_iterations = num_modes, max_iterations
+        o.tolerance, o.residual_tolerance = tolerance, residual_tolerance
+        o.young, o.poisson = self.spec.young, self.spec.poisson
+        o.transform = {"auto": 0, "shift_invert": 1}[transform]
+        o.concurrent_solves = concurrent_solves
+        ks = None if stiffness_scale is None else np.ascontiguousarray(stiffness_scale, np.float64)
+        ss = None if stress_scale is None else np.ascontiguousarray(stress_scale, np.float64)
+        mask = None if solid_mask is None else np.ascontiguousarray(solid_mask, np.uint8)
+        start = None
+        cols = 0
+        if initial_subspace is not None:
+            start = np.asfortranarray(initial_subspace, np.float64)
+            cols = start.shape[1]
+        m = max(1, min(num_modes, self.nfree))
+        q = min(self.nfree, max(2 * m, m + 8))
+        lf, res, frac = (np.zeros(m) for _ in range(3))
+        shapes = np.zeros((m, self.ndof)) if mode_shapes else None
+        sub = np.zeros((q, self.nfree))
+        info = _lib.BucklingInfo()
+        self._check(self._lib.simp_buckling(
+            self._h, C.byref(o), C.c_int32(load_case), ptr(ks), ptr(ss), ptr(mask, C.c_uint8),
+            None if start is None else start.ctypes.data_as(C.POINTER(C.c_double)), C.c_int32(cols),
+            ptr(lf), ptr(res), ptr(frac), ptr(shapes), ptr(sub), C.byref(info)))
+        k = info.num_modes
+        warnings = [self._lib.simp_buckling_warning(self._h, i).decode() for i in range(info.num_warnings)]
+        return BucklingResult(lf[:k].copy(), None if shapes is None else shapes[:k].T.copy(), res[:k].copy(),
+                              frac[:k].copy(), bool(info.no_positive_load_factor), info.iterations,
+                              info.subspace_size, bool(info.converged), info.linear_iterations,
+                              info.final_change,
+                              sub[:info.subspace_cols].T.copy() if info.subspace_cols else None, warnings)
 
     def kff(self, scale=None):
         p = np.zeros(self.nfree + 1, np.int32)
