@@ -443,7 +443,7 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
       Mat sq(static_cast<size_t>(cols_in) * cols_in, 0.0);
       for (int i = 0; i < cols_in; ++i)
         for (int c = 0; c < cols_out; ++c) sq[static_cast<size_t>(i) * cols_in + c] = R[static_cast<size_t>(i) * cols_out + c];
-      rot.upload(sq, s);
+      SIMP_CUDA(cudaMemcpyAsync(rot.p, sq.data(), sizeof(double) * sq.size(), cudaMemcpyHostToDevice, s));
       k_rotate<<<grid_for(n, 256), 256, sizeof(double) * cols_in * cols_in, s>>>(n, cols_in, in, rot.p, Y.p);
       SIMP_CHECK_LAUNCH();
       SIMP_CUDA(cudaMemcpyAsync(out, Y.p, sizeof(double) * n * cols_out, cudaMemcpyDeviceToDevice, s));

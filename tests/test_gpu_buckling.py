@@ -92,13 +92,34 @@ def test_simp_factors_and_solid_fractions_match_oracle():
     gpu.close()
 
 
-def test_crowded_tensile_case_reports_the_missing_transformation():
+def test_tension_has_no_positive_load_factor():
+    """400 free DOFs: the dense path, as in the reference's test."""
     spec = P.column(2, 40, 4, thickness=0.02, force=+1e3)
     _, gpu = pair(spec)
+    b = gpu.buckling(num_modes=2)
+    assert b.no_positive_load_factor and len(b.load_factors) == 0
+    gpu.close()
+
+
+def test_crowded_spectrum_reports_the_missing_transformation():
+    """Large axial tension plus a small transverse load: the reversed-load
+    factors crowd the subspace, where the reference needs its LDL^T-based
+    spectral transformation; without the transverse tension the plain
+    iteration matches the oracle."""
+    plain = P.column(2, 60, 6, height=0.1, thickness=0.002, force=0.0, transverse=1.0e6 * 0.1 * 0.002)
+    ref, gpu = pair(plain)
+    o = OB.analyse_buckling(ref, plain, num_modes=3)
+    b = gpu.buckling(num_modes=3)
+    assert not o.transformed
+    np.testing.assert_allclose(b.load_factors, o.load_factors, rtol=1e-7)
+    gpu.close()
+    spec = P.column(2, 60, 6, height=0.1, thickness=0.002, force=2.0e8 * 0.1 * 0.002,
+                    transverse=1.0e6 * 0.1 * 0.002)
+    _, gpu = pair(spec)
     with pytest.raises(SolverError, match="LDL"):
-        gpu.buckling(num_modes=2)
+        gpu.buckling(num_modes=3)
     with pytest.raises(SolverError, match="LDL"):
-        gpu.buckling(num_modes=2, transform="shift_invert")
+        gpu.buckling(num_modes=3, transform="shift_invert")
     gpu.close()
 
 
