@@ -89,6 +89,36 @@ def modal_cpu_baseline(steps=1):
                       f"min of {steps} analyses ({t:.2f} s each), scaled by the cell ratio 64"}
 
 
+# Linear buckling of the same solid cantilever under its tip edge load: a
+# step is one analysis (static solve, geometric stiffness, 4 smallest
+# positive load factors by subspace iteration)
+BUCKLING = "buckling_hex8_96x48x48"
+BUCKLING_METRIC = "buckling analyses/s (4 load factors, Hex8 96x48x48 cantilever)"
+BUCKLING_MODES = 4
+
+
+def buckling_spec(nx=96, ny=48, nz=48):
+    spec = P.hex8_cantilever(nx, ny, nz, 0.2, f"buckling_hex8_{nx}x{ny}x{nz}")
+    spec.rtol = 1e-10
+    return spec
+
+
+def buckling_cpu_baseline():
+    """Oracle buckling analysis (AMG-PCG solves) of the cantilever with every
+    axis divided by eight, scaled by the cell ratio 512 (an analysis of the
+    24 x 12 x 12 cantilever already takes about five minutes on the host)."""
+    import oracle
+    from oracle import buckling as OB
+    spec = buckling_spec(12, 6, 6)
+    pr = oracle.Problem(spec)
+    t0 = time.perf_counter()
+    r = OB.analyse_buckling(pr, spec, num_modes=BUCKLING_MODES, linear="amg_cg", rtol=spec.rtol)
+    t = time.perf_counter() - t0
+    return {"value": 1.0 / (t * 512.0), "unit": "analyses/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{spec.name}: 12x6x6 cells (1/512 of the workload's), {r.iterations} subspace "
+                      f"iterations, one analysis ({t:.2f} s), scaled by the cell ratio 512"}
+
+
 def sample_spec(name):
     """Bounded CPU sample: the same cantilever with every axis halved twice."""
     make, sub = WORKLOADS[name]
@@ -210,6 +240,19 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if args.config == BUCKLING:
+        base = buckling_cpu_baseline()
+        v = base["value"]
+        print(json.dumps({
+            "impl": "reference", "metric": BUCKLING_METRIC, "value": v, "unit": "analyses/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic cantilever (no dataset)",
+            "config": {"workload": BUCKLING, "modes": BUCKLING_MODES, "host_threads": os.cpu_count()},
+            "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "analyses/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
+        return
     if args.config == MODAL:
         base = modal_cpu_baseline()
         v = base["value"]
@@ -279,6 +322,78 @@ def whole_job_rate(ms_local, steps, world, device=None):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     return ms, world * steps / (ms * 1e-3)
+
+
+def run_own_buckling(args):
+    """Buckling analyses of the solid cantilever; replicas under torchrun."""
+    import torch
+    import torch.distributed as dist
+    from sparlab_gb300 import _lib
+    from sparlab_gb300.topopt import GpuSimpProblem
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    spec = buckling_spec()
+    prob = GpuSimpProblem(spec, precision=args.precision, device=local)
+    lib = _lib.load()
+    for _ in range(args.warmup):
+        prob.buckling(num_modes=BUCKLING_MODES, mode_shapes=False)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    barrier()
+    launches0 = lib.simp_kernel_launches()
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    recs = [prob.buckling(num_modes=BUCKLING_MODES, mode_shapes=False) for _ in range(args.steps)]
+    e1.record()
+    barrier()
+    clocks = sampler.stop()
+    launches = lib.simp_kernel_launches() - launches0
+    ms, value = whole_job_rate(e0.elapsed_time(e1), args.steps, world, dev)
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    for _ in range(args.steps):
+        prob.buckling(num_modes=BUCKLING_MODES, mode_shapes=True)
+    f1.record()
+    barrier()
+    e2e_ms, e2e_value = whole_job_rate(f0.elapsed_time(f1), args.steps, world, dev)
+    if rank != 0:
+        return
+    line = {
+        "metric": BUCKLING_METRIC, "value": value, "unit": "analyses/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic cantilever (no dataset)",
+        "config": {"workload": BUCKLING, "elements": spec.num_elements, "free_dofs": prob.nfree,
+                   "modes": BUCKLING_MODES, "precision": args.precision,
+                   "subspace_size": recs[-1].subspace_size,
+                   "subspace_iterations": [r.iterations for r in recs],
+                   "pcg_iterations": [r.linear_iterations for r in recs],
+                   "load_factors": [float(f) for f in recs[-1].load_factors],
+                   "l2": "working set (K_ff and K_G 1.3 GB) larger than L2"},
+        "roofline": None,
+        "cpu_baseline": buckling_cpu_baseline() if world == 1 else None,
+        "e2e": {"value": e2e_value, "unit": "analyses/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 8 * BUCKLING_MODES * prob.ndof},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
 
 
 def run_own_modal(args):
@@ -598,7 +713,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
-    ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS) + [BATCHED, MODAL])
+    ap.add_argument("--config", default="hex8_192x96x96", choices=sorted(WORKLOADS) + [BATCHED, MODAL, BUCKLING])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 comparison run that follows a mixed-precision run")
@@ -617,6 +732,8 @@ def main():
         run_own_batched(args)
     elif args.config == MODAL:
         run_own_modal(args)
+    elif args.config == BUCKLING:
+        run_own_buckling(args)
     else:
         run_own(args)
 

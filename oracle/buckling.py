@@ -395,15 +395,25 @@ def solve_buckling(prob: Problem, spec, k, g, num_modes=4, max_iterations=400, t
 
 
 def analyse_buckling(prob: Problem, spec, load_case=0, stiffness_scale=None, stress_scale=None,
-                     **options) -> BucklingResult:
+                     linear="direct", rtol=1e-12, **options) -> BucklingResult:
     """``analyse_buckling`` (Buckling.cpp:438-466) with optional SIMP factors:
-    static solve of the load case, K_G of its stress state, solve_buckling."""
+    static solve of the load case, K_G of its stress state, solve_buckling.
+    ``linear``: "direct" (SuperLU) or "amg_cg" (the oracle's AMG-PCG, what
+    the reference's Auto solver picks above 10,000 3-D unknowns)."""
     ptr, col, val = prob.kff(stiffness_scale)
     k = sp.csr_matrix((val, col, ptr), shape=(prob.nfree, prob.nfree))
-    lu = spla.splu(k.tocsc())
+    if linear == "direct":
+        solve = spla.splu(k.tocsc()).solve
+    else:
+        from . import Solver
+        solver = Solver(rtol=rtol)
+        solver.factorize(k.indptr, k.indices, k.data, spec.dim, prob.coords(), prob.free_dofs())
+
+        def solve(b):
+            return solver.solve(b)[0]
     free = prob.free_dofs()
     f = np.atleast_2d(spec.loads)[load_case][free]
     u = np.zeros(prob.ndof)
-    u[free] = lu.solve(f)
+    u[free] = solve(f)
     g = -geometric_stiffness_ff(prob, spec, u, stress_scale)
-    return solve_buckling(prob, spec, k, g, solve=lu.solve, stiffness_scale=stiffness_scale, **options)
+    return solve_buckling(prob, spec, k, g, solve=solve, stiffness_scale=stiffness_scale, **options)
