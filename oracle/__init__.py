@@ -66,7 +66,8 @@ class ProblemDesc(C.Structure):
                 ("amg", AmgOptions), ("projection", C.c_int32), ("eta", C.c_double),
                 ("beta_start", C.c_double), ("beta_max", C.c_double), ("beta_factor", C.c_double),
                 ("beta_interval", C.c_int32), ("advance_on_convergence", C.c_int32),
-                ("change_tolerance", C.c_double)]
+                ("change_tolerance", C.c_double), ("robust", C.c_int32),
+                ("robust_delta", C.c_double), ("robust_volume_interval", C.c_int32)]
 
 
 def lib():
@@ -243,6 +244,9 @@ class Problem:
         d.beta_interval = getattr(spec, "beta_interval", 50)
         d.advance_on_convergence = int(getattr(spec, "advance_on_convergence", True))
         d.change_tolerance = getattr(spec, "change_tolerance", 1e-3)
+        d.robust = int(getattr(spec, "robust", False))
+        d.robust_delta = getattr(spec, "robust_delta", 0.1)
+        d.robust_volume_interval = getattr(spec, "robust_volume_interval", 1)
         self._desc = d
         self._h = C.c_void_p()
         _check(lib().orc_problem_create(C.byref(d), C.byref(self._h)))
@@ -329,9 +333,11 @@ class Problem:
 
     def run(self, iterations, change_tol=0.0):
         """run_oc: final design and history rows (compliance, volume
-        fraction, max change, lambda, CG iterations, bisections, beta)."""
+        fraction (the blueprint's in a robust run), max change, lambda, CG
+        iterations, bisections, beta, and for a robust run the eroded and
+        dilated volume fractions and the dilated target fraction)."""
         x = np.zeros(self.ne)
-        hist = np.zeros((iterations, 7))
+        hist = np.zeros((iterations, 10))
         done = C.c_int32()
         _check(lib().orc_run(self._h, C.c_int32(iterations), C.c_double(change_tol), _p(x),
                              _p(hist), C.byref(done)))

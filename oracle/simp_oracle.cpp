@@ -1277,6 +1277,12 @@ struct Problem {
   int beta_interval = 50;
   bool advance = true;
   double beta = 0.0;
+  // robust formulation (Projection.hpp:44-60)
+  bool robust = false;
+  double robust_delta = 0.1;
+  int robust_interval = 1;
+  // the objective's projection threshold: the eroded design's in a robust run
+  double objective_eta() const { return robust ? eta + robust_delta : eta; }
   std::unique_ptr<Amg> amg;
   std::vector<Vec> previous;
   Layout layout;
@@ -1567,7 +1573,7 @@ double simp_derivative(double rho, double pen, double emin) {
 struct Evaluation {
   double compliance = 0.0, volume = 0.0, volume_fraction = 0.0;
   int linear_iterations = 0;
-  Vec rho, dc_dphys, dc_dx, dv_dx, se;
+  Vec rho, rhot, dc_dphys, dc_dx, dv_dx, se;  // rhot: clamped filtered density
   std::vector<Vec> u;
 };
 
@@ -1608,13 +1614,16 @@ void evaluate(Problem& p, const double* x, Evaluation& out) {
   out.rho.resize(static_cast<size_t>(ne));
   filter_forward(p, x, out.rho.data());
   for (auto& r : out.rho) r = std::min(std::max(r, 0.0), 1.0);
-  // physical density: the projected filtered density (Sensitivity.cpp:69-73)
+  // physical density: the projected filtered density (Sensitivity.cpp:69-73),
+  // at the eroded threshold in a robust run
   Vec dproj;
+  out.rhot = out.rho;
   if (p.proj) {
     dproj.resize(static_cast<size_t>(ne));
+    const double eta = p.objective_eta();
     for (Index e = 0; e < ne; ++e) {
-      dproj[e] = project_derivative(out.rho[e], p.beta, p.eta);
-      out.rho[e] = project(out.rho[e], p.beta, p.eta);
+      dproj[e] = project_derivative(out.rho[e], p.beta, eta);
+      out.rho[e] = project(out.rho[e], p.beta, eta);
     }
   }
   Vec sf(static_cast<size_t>(ne)), df(static_cast<size_t>(ne));
@@ -1716,39 +1725,59 @@ void oc_candidate(const Problem& p, const double* x, const double* dc, const dou
   }
 }
 
-double design_volume(const Problem& p, const double* xn, Vec& tmp) {
+// Volume of the physical density of design xn, projected at threshold eta.
+double design_volume(const Problem& p, const double* xn, Vec& tmp, double eta) {
   filter_forward(p, xn, tmp.data());
   double v = 0.0;
   for (Index e = 0; e < p.ne; ++e) {
     double r = std::min(std::max(tmp[e], 0.0), 1.0);
-    if (p.proj) r = project(r, p.beta, p.eta);
+    if (p.proj) r = project(r, p.beta, eta);
     v += r * p.volumes[e];
   }
   return v;
 }
 
-OcStep oc_update(const Problem& p, const double* x, const double* dc, const double* dv) {
+// optimality_criteria_update (OptimalityCriteria.cpp:40-149): volume_target
+// > 0 replaces the domain's target; step_toward takes the reachable corner
+// when the move-limited box cannot bracket the target (the robust run's
+// moved target) instead of failing.
+OcStep oc_update(const Problem& p, const double* x, const double* dc, const double* dv,
+                 double volume_target = 0.0, bool step_toward = false) {
   for (Index e = 0; e < p.ne; ++e)
     if (!std::isfinite(dc[e]) || !std::isfinite(dv[e])) throw Error(kNonFinite, "optimality criteria received a non-finite gradient");
-  const double target = p.vf * p.domain_volume;
+  const double target = volume_target > 0.0 ? volume_target : p.vf * p.domain_volume;
+  // the volume of a trial: the dilated design's in a robust run
+  const double veta = p.robust ? p.eta - p.robust_delta : p.eta;
   Vec cand(static_cast<size_t>(p.ne)), tmp(static_cast<size_t>(p.ne));
   double lo = 1.0e-12, hi = 1.0e12;
   oc_candidate(p, x, dc, dv, lo, cand.data());
-  double vlo = design_volume(p, cand.data(), tmp);
+  double vlo = design_volume(p, cand.data(), tmp, veta);
   oc_candidate(p, x, dc, dv, hi, cand.data());
-  double vhi = design_volume(p, cand.data(), tmp);
+  double vhi = design_volume(p, cand.data(), tmp, veta);
   int widen = 0;
   while (vlo < target && widen < 60) {
     lo *= 1.0e-3;
     oc_candidate(p, x, dc, dv, lo, cand.data());
-    vlo = design_volume(p, cand.data(), tmp);
+    vlo = design_volume(p, cand.data(), tmp, veta);
     ++widen;
   }
   while (vhi > target && widen < 120) {
     hi *= 1.0e3;
     oc_candidate(p, x, dc, dv, hi, cand.data());
-    vhi = design_volume(p, cand.data(), tmp);
+    vhi = design_volume(p, cand.data(), tmp, veta);
     ++widen;
+  }
+  if ((vlo < target || vhi > target) && step_toward) {
+    OcStep st;
+    const bool too_light = vlo < target;
+    st.lambda = too_light ? lo : hi;
+    oc_candidate(p, x, dc, dv, st.lambda, cand.data());
+    st.volume = too_light ? vlo : vhi;
+    double mc = 0.0;
+    for (Index e = 0; e < p.ne; ++e) mc = std::max(mc, std::abs(cand[e] - x[e]));
+    st.max_change = mc;
+    st.x = std::move(cand);
+    return st;
   }
   if (vlo < target || vhi > target) {
     std::ostringstream os;
@@ -1761,7 +1790,7 @@ OcStep oc_update(const Problem& p, const double* x, const double* dc, const doub
   for (int it = 0; it < 200; ++it) {
     const double mid = std::sqrt(lo * hi);
     oc_candidate(p, x, dc, dv, mid, cand.data());
-    vol = design_volume(p, cand.data(), tmp);
+    vol = design_volume(p, cand.data(), tmp, veta);
     st.bisections = it + 1;
     st.lambda = mid;
     if (std::abs(vol - target) <= 1.0e-10 * target) { st.converged = true; break; }
@@ -2224,6 +2253,11 @@ int orc_problem_create(const orc_problem_desc* d, orc_problem** out) {
       p.advance = d->advance_on_convergence != 0;
       p.change_tol = d->change_tolerance;
       p.beta = beta_of_stage(p, 0);
+      p.robust = d->robust != 0;
+      p.robust_delta = d->robust_delta;
+      p.robust_interval = std::max(1, d->robust_volume_interval);
+      if (p.robust && !(p.eta - p.robust_delta > 0.0 && p.eta + p.robust_delta < 1.0))
+        throw Error(kBadInput, "projection.robust_delta must keep eta +- delta inside (0, 1)");
     }
     p.layout = Layout{p.dim, p.dim, p.coords.data(), p.nn, p.free_dofs.data(),
                       static_cast<Index>(p.free_dofs.size())};
@@ -2379,18 +2413,41 @@ int orc_run(orc_problem* h, int32_t iterations, double change_tol, double* x, do
     int stage = 0, stage_start = 1;
     if (p.proj) p.beta = beta_of_stage(p, 0);
     int it = 0;
+    const bool robust = p.proj && p.robust;
+    double dilated_target = p.vf * p.domain_volume;
     for (it = 1; it <= iterations; ++it) {
       Evaluation ev;
       evaluate(p, xv.data(), ev);
-      const OcStep st = oc_update(p, xv.data(), ev.dc_dx.data(), ev.dv_dx.data());
-      double* row = hist + static_cast<size_t>(it - 1) * 7;
+      // robust volumes (TopologyOptimizer.cpp:61-80, 625-636): the dilated
+      // design's volume and gradient, the blueprint's volume, the moved target
+      double vol_i = 0.0, vol_d = 0.0;
+      Vec dv_dilated;
+      if (robust) {
+        const double eta_d = p.eta - p.robust_delta;
+        Vec w(static_cast<size_t>(p.ne));
+        dv_dilated.resize(static_cast<size_t>(p.ne));
+        for (Index e = 0; e < p.ne; ++e) {
+          vol_d += project(ev.rhot[e], p.beta, eta_d) * p.volumes[e];
+          vol_i += project(ev.rhot[e], p.beta, p.eta) * p.volumes[e];
+          w[e] = p.volumes[e] * project_derivative(ev.rhot[e], p.beta, eta_d);
+        }
+        filter_adjoint(p, w.data(), dv_dilated.data());
+        if ((it - 1) % p.robust_interval == 0 && vol_i > 0.0)
+          dilated_target = p.vf * p.domain_volume * vol_d / vol_i;
+      }
+      const OcStep st = robust ? oc_update(p, xv.data(), ev.dc_dx.data(), dv_dilated.data(), dilated_target, true)
+                               : oc_update(p, xv.data(), ev.dc_dx.data(), ev.dv_dx.data());
+      double* row = hist + static_cast<size_t>(it - 1) * 10;
       row[0] = ev.compliance;
-      row[1] = ev.volume_fraction;
+      row[1] = robust ? vol_i / p.domain_volume : ev.volume_fraction;
       row[2] = st.max_change;
       row[3] = st.lambda;
       row[4] = ev.linear_iterations;
       row[5] = st.bisections;
       row[6] = p.proj ? p.beta : 0.0;
+      row[7] = robust ? ev.volume_fraction : 0.0;
+      row[8] = robust ? vol_d / p.domain_volume : 0.0;
+      row[9] = robust ? dilated_target / p.domain_volume : 0.0;
       xv = st.x;
       for (auto& v : xv) v = std::min(std::max(v, 0.0), 1.0);
       const bool at_final = !p.proj || stage + 1 >= stages;

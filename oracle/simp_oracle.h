@@ -55,6 +55,12 @@ typedef struct {
   double eta, beta_start, beta_max, beta_factor;
   int32_t beta_interval, advance_on_convergence;
   double change_tolerance;     /* run_oc's design-change tolerance (beta advance) */
+  /* Robust formulation (Projection.hpp:44-60): objective on the eroded design
+   * (eta + delta), volume on the dilated one (eta - delta) against a target
+   * rescaled every robust_volume_interval iterations to V* V_d / V_i. */
+  int32_t robust;
+  double robust_delta;
+  int32_t robust_volume_interval;
 } orc_problem_desc;
 
 typedef struct orc_problem orc_problem;

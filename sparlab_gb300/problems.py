@@ -90,6 +90,11 @@ class ProblemSpec:
     beta_interval: int = 50
     advance_on_convergence: bool = True
     change_tolerance: float = 1e-3  # run_oc's design-change tolerance (beta advance)
+    # robust formulation: eroded objective (eta + delta), dilated volume
+    # (eta - delta) against a target rescaled every robust_volume_interval
+    robust: bool = False
+    robust_delta: float = 0.1
+    robust_volume_interval: int = 1
     amg: Dict = dataclasses.field(default_factory=dict)
     name: str = ""
 

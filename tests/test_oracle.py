@@ -297,3 +297,88 @@ def test_beta_continuation_schedule():
     spec.volume_fraction = 0.45
     _, hist = oracle.Problem(spec, amg=dict(coarse_size=100)).run(7)
     assert list(hist[:, 6]) == [1.0, 1.0, 2.0, 2.0, 4.0, 4.0, 4.0]
+
+
+def _block_q4(nx=30, ny=15):
+    """make_block of the reference's manufacturing tests (tests/
+    test_manufacturing.cpp:55-82): 0.6 x 0.3 plate, E = 70e9, nu = 0.3,
+    t = 0.01, root clamped, -1000 N at the node nearest (0.6, 0)."""
+    spec = P.ProblemSpec(dim=2, nx=nx, ny=ny, nz=0, lx=0.6, ly=0.3, lz=0.0, young=70e9, poisson=0.3,
+                         thickness=0.01, filter_radius=2.0 * 0.6 / nx, volume_fraction=0.4,
+                         rtol=1e-12, name="block")
+    spec.fixed = P.clamp_left(spec)
+    spec.loads = P.point_load(spec, [P.nearest_node(spec, (0.6, 0.0, 0.0))], (0.0, -1000.0))[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
+def test_robust_thresholds_order_and_gradients():
+    """test_manufacturing.cpp:246-306 (no overhang filter): eroded <=
+    blueprint <= dilated, the objective on the eroded design, the dilated
+    volume gradient against central differences."""
+    spec = _block_q4(12, 6)
+    spec.filter_radius = 1.5 * 0.05
+    spec.projection, spec.robust, spec.robust_delta = True, True, 0.1
+    spec.beta_start = spec.beta_max = 6.0
+    pr = oracle.Problem(spec, amg=dict(coarse_size=60))
+    x = P.SplitMix64(5).uniform_array(pr.ne, 0.0, 1.0)
+    rt = np.clip(pr.filter_forward(x), 0.0, 1.0)
+
+    def proj(eta):
+        return oracle_project(rt, 6.0, eta)
+
+    eroded, blueprint, dilated = proj(0.6), proj(0.5), proj(0.4)
+    assert np.all(blueprint - eroded >= 0) and np.all(dilated - blueprint >= 0)
+    ev = pr.evaluate(x)
+    assert np.abs(ev["rho"] - eroded).max() <= 1e-15  # the objective's design is the eroded one
+    v = np.full(pr.ne, 0.6 * 0.3 * 0.01 / pr.ne)
+    grad = pr.filter_adjoint(v * oracle_project_derivative(rt, 6.0, 0.4))
+
+    def vol_d(xx):
+        return v @ oracle_project(np.clip(pr.filter_forward(xx), 0.0, 1.0), 6.0, 0.4)
+
+    worst = 0.0
+    for e in range(0, pr.ne, 3):
+        xp, xm = x.copy(), x.copy()
+        xp[e] += 1e-6
+        xm[e] -= 1e-6
+        fd = (vol_d(xp) - vol_d(xm)) / 2e-6
+        worst = max(worst, abs(fd - grad[e]) / max(abs(fd), abs(grad[e]), 1e-3 * np.abs(grad).max()))
+    assert worst < 1e-6
+    c_worst = 0.0
+    for e in range(0, pr.ne, 5):
+        xp, xm = x.copy(), x.copy()
+        xp[e] += 1e-4
+        xm[e] -= 1e-4
+        fd = (pr.evaluate(xp)["compliance"] - pr.evaluate(xm)["compliance"]) / 2e-4
+        g = ev["dc_dx"][e]
+        c_worst = max(c_worst, abs(fd - g) / max(abs(fd), abs(g), 1e-3 * np.abs(ev["dc_dx"]).max()))
+    assert c_worst < 3e-5
+
+
+def oracle_project(r, beta, eta):
+    return (np.tanh(beta * eta) + np.tanh(beta * (r - eta))) / (np.tanh(beta * eta) + np.tanh(beta * (1 - eta)))
+
+
+def oracle_project_derivative(r, beta, eta):
+    return beta * (1 - np.tanh(beta * (r - eta)) ** 2) / (np.tanh(beta * eta) + np.tanh(beta * (1 - eta)))
+
+
+def test_robust_run_reports_the_blueprint():
+    """test_manufacturing.cpp:308-347 (OC, no overhang filter): the blueprint
+    meets the volume fraction up to the target's lag, eroded < blueprint <
+    dilated volumes, and the eroded design is the softest."""
+    spec = _block_q4()
+    spec.projection, spec.robust, spec.robust_delta = True, True, 0.1
+    spec.beta_start, spec.beta_max, spec.beta_interval = 2.0, 8.0, 15
+    pr = oracle.Problem(spec)
+    x, hist = pr.run(60, change_tol=1e-3)
+    last = hist[-1]
+    assert abs(last[1] - 0.4) < 0.02
+    assert last[7] < last[1] < last[8]
+    comp = {}
+    for name, eta in (("eroded", 0.6), ("intermediate", 0.5), ("dilated", 0.4)):
+        s2 = _block_q4()
+        s2.projection, s2.eta, s2.beta_start, s2.beta_max = True, eta, 8.0, 8.0
+        comp[name] = oracle.Problem(s2).evaluate(x)["compliance"]
+    assert comp["eroded"] > comp["intermediate"] > comp["dilated"]
