@@ -173,6 +173,14 @@ typedef struct {
   double eta, beta_start, beta_max, beta_factor;
   int32_t beta_interval, advance_on_convergence;
   double change_tolerance;      /* design-change tolerance of the beta advance */
+  /* Robust formulation (Projection.hpp:44-60, run_oc at
+   * src/topopt/TopologyOptimizer.cpp:567-651): the objective on the eroded
+   * design (eta + robust_delta), the OC volume constraint on the dilated one
+   * (eta - robust_delta) against a target moved to V* V_d / V_i every
+   * robust_volume_interval iterations; needs the projection and OC. */
+  int32_t robust;
+  double robust_delta;
+  int32_t robust_volume_interval;
 } simp_problem_desc;
 
 /* ObjectiveEvaluation scalars (Sensitivity.hpp:66-107) and an OC step
@@ -203,6 +211,9 @@ typedef struct {
   int32_t volume_converged;
   int32_t final_stage;          /* 1: no projection, or its last beta stage (convergence may stop) */
   double beta;                  /* projection sharpness of the iteration (0: none) */
+  /* robust runs: volume_fraction is the blueprint's; these are the eroded and
+   * dilated designs' fractions and the dilated target's (0 otherwise) */
+  double eroded_volume_fraction, dilated_volume_fraction, dilated_target_fraction;
 } simp_iteration_record;
 
 int simp_problem_create(const simp_problem_desc* desc, const simp_solver_options* opts,

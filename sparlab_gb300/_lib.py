@@ -80,7 +80,9 @@ class ProblemDesc(C.Structure):
                 ("warm_start", C.c_int32), ("block_pcg", C.c_int32), ("optimizer", C.c_int32),
                 ("projection", C.c_int32), ("eta", C.c_double), ("beta_start", C.c_double),
                 ("beta_max", C.c_double), ("beta_factor", C.c_double), ("beta_interval", C.c_int32),
-                ("advance_on_convergence", C.c_int32), ("change_tolerance", C.c_double)]
+                ("advance_on_convergence", C.c_int32), ("change_tolerance", C.c_double),
+                ("robust", C.c_int32), ("robust_delta", C.c_double),
+                ("robust_volume_interval", C.c_int32)]
 
 
 class Evaluation(C.Structure):
@@ -99,7 +101,8 @@ class IterationRecord(C.Structure):
                 ("max_change", C.c_double), ("lam", C.c_double), ("gray_level", C.c_double),
                 ("linear_iterations", C.c_int32), ("bisections", C.c_int32),
                 ("seconds", C.c_double), ("volume_converged", C.c_int32), ("final_stage", C.c_int32),
-                ("beta", C.c_double)]
+                ("beta", C.c_double), ("eroded_volume_fraction", C.c_double),
+                ("dilated_volume_fraction", C.c_double), ("dilated_target_fraction", C.c_double)]
 
 
 class ModalOptions(C.Structure):

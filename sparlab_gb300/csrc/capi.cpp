@@ -518,6 +518,17 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
       d.advance_on_convergence = dsc->advance_on_convergence != 0;
       d.change_tol = dsc->change_tolerance;
     }
+    d.robust = dsc->robust != 0;
+    if (d.robust) {
+      if (!d.projection) throw Error(kBadInput, "projection.robust needs the projection enabled");
+      if (dsc->optimizer != 0)
+        throw Error(kBadInput, "projection.robust runs with the OC update on the GPU (the MMA form is not built)");
+      if (!(dsc->eta - dsc->robust_delta > 0.0 && dsc->eta + dsc->robust_delta < 1.0 && dsc->robust_delta > 0.0))
+        throw Error(kBadInput, "projection.robust_delta must keep eta - delta and eta + delta inside (0, 1)");
+      if (dsc->robust_volume_interval < 1) throw Error(kBadInput, "projection.robust_volume_interval must be >= 1");
+      d.robust_delta = dsc->robust_delta;
+      d.robust_interval = dsc->robust_volume_interval;
+    }
     if (dsc->optimizer != 0 && dsc->optimizer != 1) throw Error(kBadInput, "unknown optimizer (expected 0 OC, 1 MMA)");
     d.optimizer = dsc->optimizer;
     std::unique_ptr<simp_problem> p(new simp_problem());
@@ -631,6 +642,7 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
     SIMP_CUDA(cudaEventRecord(e0, g.amg.stream));
     ++g.iteration;
     const Evaluation ev = g.evaluate();
+    g.update_robust_target();
     const OcStep st = g.d.optimizer == 1 ? g.mma_update(true, nullptr) : g.oc_update(true, nullptr);
     SIMP_CUDA(cudaEventRecord(e1, g.amg.stream));
     SIMP_CUDA(cudaEventSynchronize(e1));
@@ -651,6 +663,13 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
           g.d.optimizer == 1 ? (ev.volume_fraction / g.d.vf - 1.0 <= 1.0e-4 ? 1 : 0) : (st.converged ? 1 : 0);
       rec->final_stage = g.beta_at_final() ? 1 : 0;
       rec->beta = g.d.projection ? g.beta : 0.0;
+      rec->eroded_volume_fraction = rec->dilated_volume_fraction = rec->dilated_target_fraction = 0.0;
+      if (g.d.robust) {
+        rec->volume_fraction = ev.volume_intermediate / g.domain_volume;
+        rec->eroded_volume_fraction = ev.volume_fraction;
+        rec->dilated_volume_fraction = ev.volume_dilated / g.domain_volume;
+        rec->dilated_target_fraction = g.dilated_target / g.domain_volume;
+      }
     }
     g.advance_beta(st.max_change);
   });

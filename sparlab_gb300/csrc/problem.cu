@@ -506,7 +506,7 @@ Evaluation GpuProblem::evaluate() {
       nullptr, nullptr);
   SIMP_CHECK_LAUNCH();
   if (d.projection) {  // the physical density is the projected one (Sensitivity.cpp:69-73)
-    k_project<<<grid_for(ne, 256), 256, 0, s>>>(ne, rhot.p, beta, d.eta, rho.p, dproj.p);
+    k_project<<<grid_for(ne, 256), 256, 0, s>>>(ne, rhot.p, beta, d.objective_eta(), rho.p, dproj.p);
     SIMP_CHECK_LAUNCH();
   }
   k_simp<<<grid_for(ne, 256), 256, 0, s>>>(ne, rho.p, d.penalty, d.emin, sf.p, df.p);
@@ -602,6 +602,22 @@ Evaluation GpuProblem::evaluate() {
   SIMP_CUDA(cudaMemcpyAsync(&ev.volume, amg.scal.p + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
   SIMP_CUDA(cudaStreamSynchronize(s));
   ev.volume_fraction = ev.volume / domain_volume;
+  if (d.robust) {
+    // robust_volumes (TopologyOptimizer.cpp:61-80): the blueprint's volume,
+    // and the dilated design's volume and gradient, which the OC update
+    // constrains
+    rtmp.alloc(static_cast<size_t>(ne));
+    k_project<<<grid_for(ne, 256), 256, 0, s>>>(ne, rhot.p, beta, d.eta, tmp.p, nullptr);
+    SIMP_CHECK_LAUNCH();
+    ev.volume_intermediate = amg.dot(amg.work(0), tmp.p, vols.p, ne);
+    k_project<<<grid_for(ne, 256), 256, 0, s>>>(ne, rhot.p, beta, d.volume_eta(), tmp.p, rtmp.p);
+    SIMP_CHECK_LAUNCH();
+    ev.volume_dilated = amg.dot(amg.work(0), tmp.p, vols.p, ne);
+    k_mul<<<grid_for(ne, 256), 256, 0, s>>>(ne, vols.p, rtmp.p, tmp.p);
+    SIMP_CHECK_LAUNCH();
+    dv_dilated.alloc(static_cast<size_t>(ne));
+    filter_adjoint(tmp.p, dv_dilated.p);
+  }
   if (!std::isfinite(ev.compliance)) throw Error(kNonFinite, "the compliance objective evaluated to a non-finite value");
   evaluated = true;
   last_evaluation = ev;
@@ -640,17 +656,30 @@ void GpuProblem::advance_beta(double max_change) {
   }
 }
 
+// The dilated target of a robust run, moved to V* V_d / V_i every
+// robust_interval iterations (TopologyOptimizer.cpp:625-631).
+void GpuProblem::update_robust_target() {
+  if (!d.robust) return;
+  if (dilated_target <= 0.0) dilated_target = d.vf * domain_volume;
+  const Evaluation& ev = last_evaluation;
+  if ((iteration - 1) % std::max(1, d.robust_interval) == 0 && ev.volume_intermediate > 0.0)
+    dilated_target = d.vf * domain_volume * ev.volume_dilated / ev.volume_intermediate;
+}
+
 OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
   if (!evaluated) throw Error(kBadInput, "oc_update needs gradients: call evaluate first");
   cudaStream_t s = amg.stream;
-  const double target = d.vf * domain_volume;
+  // a robust run constrains the dilated design's volume against the moved
+  // target, and steps toward a target the move limit cannot reach
+  if (d.robust && dilated_target <= 0.0) dilated_target = d.vf * domain_volume;
+  const double target = d.robust ? dilated_target : d.vf * domain_volume;
   double* part = opart.p;
   // per-update factors of the candidate; a trial is one fused pass
   oc_g.alloc(static_cast<size_t>(ne));
   oc_lo.alloc(static_cast<size_t>(ne));
   oc_hi.alloc(static_cast<size_t>(ne));
-  k_oc_prepare<<<grid_for(ne, 256), 256, 0, s>>>(ne, x.p, dc_dx.p, dv_dx.p, d.move, d.damping, oc_g.p, oc_lo.p,
-                                                oc_hi.p);
+  k_oc_prepare<<<grid_for(ne, 256), 256, 0, s>>>(ne, x.p, dc_dx.p, d.robust ? dv_dilated.p : dv_dx.p, d.move,
+                                                d.damping, oc_g.p, oc_lo.p, oc_hi.p);
   SIMP_CHECK_LAUNCH();
   auto factor = [&](double lam) { return d.damping == 0.5 ? 1.0 / std::sqrt(lam) : std::pow(lam, -d.damping); };
   auto volume_of = [&](double lam) {
@@ -660,7 +689,7 @@ OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
       k_oc_apply<<<grid_for(ne, 256), 256, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p, factor(lam), xnew.p);
       SIMP_CHECK_LAUNCH();
       k_filter_volume_projected<<<kRedBlocks, kRedThreads, 0, s>>>(
-          grid_of(d), static_cast<const Stencil*>(stencil_d), hw.p, ne, xnew.p, vols.p, beta, d.eta, part);
+          grid_of(d), static_cast<const Stencil*>(stencil_d), hw.p, ne, xnew.p, vols.p, beta, d.volume_eta(), part);
     } else {
       k_oc_volume<<<kRedBlocks, kRedThreads, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p, dv_dx.p, factor(lam), part);
     }
@@ -685,15 +714,23 @@ OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
     vhi = volume_of(hi);
     ++widen;
   }
-  if (vlo < target || vhi > target) {
+  OcStep st;
+  bool corner = false;
+  if ((vlo < target || vhi > target) && d.robust) {
+    // the most-material corner when even it is too light, else the least
+    corner = true;
+    const bool too_light = vlo < target;
+    st.lambda = too_light ? lo : hi;
+    st.volume = too_light ? vlo : vhi;
+    st.converged = false;
+  } else if (vlo < target || vhi > target) {
     std::ostringstream os;
     os << "the optimality-criteria bisection cannot bracket the volume target " << target
        << " m^3: the move-limited box yields volumes in [" << vhi << ", " << vlo << "] m^3";
     throw Error(kMaxIter, os.str());
   }
-  OcStep st;
-  double vol = vlo;
-  for (int it = 0; it < 200; ++it) {
+  double vol = corner ? st.volume : vlo;
+  for (int it = 0; it < 200 && !corner; ++it) {
     const double mid = std::sqrt(lo * hi);
     vol = volume_of(mid);
     st.bisections = it + 1;
@@ -711,7 +748,8 @@ OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
   // the design of the final multiplier (the lower bracket end when no
   // bisection ran)
   k_oc_apply<<<grid_for(ne, 256), 256, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p,
-                                              factor(st.bisections == 0 ? lo : st.lambda), xnew.p);
+                                              factor(corner ? st.lambda : (st.bisections == 0 ? lo : st.lambda)),
+                                              xnew.p);
   SIMP_CHECK_LAUNCH();
   st.volume = vol;
   // max |x' - x| and the grey level of the evaluated density

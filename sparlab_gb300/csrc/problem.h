@@ -36,11 +36,20 @@ struct ProblemDesc {
   double eta = 0.5, beta_start = 1.0, beta_max = 32.0, beta_factor = 2.0, change_tol = 1e-3;
   int beta_interval = 50;
   bool advance_on_convergence = true;
+  // robust formulation (Projection.hpp:44-60): the objective on the eroded
+  // design (eta + delta), the volume on the dilated one (eta - delta)
+  bool robust = false;
+  double robust_delta = 0.1;
+  int robust_interval = 1;
+  double objective_eta() const { return robust ? eta + robust_delta : eta; }
+  double volume_eta() const { return robust ? eta - robust_delta : eta; }
 };
 
 struct Evaluation {
   double compliance = 0, volume = 0, volume_fraction = 0, relres_max = 0;
   int linear_iterations = 0;
+  // robust runs: the blueprint's and the dilated design's volumes
+  double volume_intermediate = 0, volume_dilated = 0;
 };
 
 struct OcStep {
@@ -114,6 +123,11 @@ class GpuProblem {
   double beta = 0.0;
   int beta_stage = 0, beta_stage_start = 1, iteration = 0;
   DBuf<double> rhot, dproj;  // clamped filtered density and d rho_bar / d rho_tilde
+  // robust runs: the dilated design's volume target (moved every
+  // robust_interval iterations to V* V_d / V_i) and scratch
+  double dilated_target = 0.0;
+  DBuf<double> rtmp, dv_dilated;
+  void update_robust_target();
   bool beta_at_final() const;
   // BetaSchedule::advance after iteration `iteration` with its design change
   void advance_beta(double max_change);

@@ -42,10 +42,12 @@ def domain_volume(spec: ProblemSpec) -> float:
     return spec.lx * spec.ly * spec.lz
 
 
-def history_columns(method: str = "oc", projected: bool = False) -> List[str]:
+def history_columns(method: str = "oc", projected: bool = False, robust: bool = False) -> List[str]:
     cols = list(MMA_COLUMNS if method == "mma" else OC_COLUMNS)
     if projected:
         cols.append("beta[-]")
+    if robust:
+        cols += ["eroded_volume_fraction[-]", "dilated_volume_fraction[-]", "dilated_target_fraction[-]"]
     return cols
 
 
@@ -54,8 +56,9 @@ def write_history_csv(path: str, history: Sequence, spec: ProblemSpec, method: s
     mma = method == "mma"
     vol = domain_volume(spec)
     projected = bool(getattr(spec, "projection", False))
+    robust = projected and bool(getattr(spec, "robust", False))
     with open(path, "w") as f:
-        f.write(",".join(history_columns(method, projected)) + "\n")
+        f.write(",".join(history_columns(method, projected, robust)) + "\n")
         for it in history:
             row = [spec.penalty, it.compliance, it.volume_fraction * vol, it.volume_fraction,
                    it.max_change, it.lam, it.gray_level, it.bisections,
@@ -66,6 +69,8 @@ def write_history_csv(path: str, history: Sequence, spec: ProblemSpec, method: s
             row.append(it.linear_iterations)
             if projected:
                 row.append(it.beta)
+            if robust:
+                row += [it.eroded_volume_fraction, it.dilated_volume_fraction, it.dilated_target_fraction]
             f.write(str(int(it.iteration)) + "," + ",".join(_num(v) for v in row) + "\n")
 
 
@@ -105,7 +110,10 @@ def summary(spec: ProblemSpec, history: Sequence, method: str = "oc", max_iterat
                         "beta_max": spec.beta_max, "beta_factor": spec.beta_factor,
                         "beta_interval": spec.beta_interval,
                         "advance_on_convergence": bool(spec.advance_on_convergence),
-                        "robust": False}
+                        "robust": bool(getattr(spec, "robust", False)),
+                        **({"robust_delta": spec.robust_delta,
+                            "robust_volume_interval": spec.robust_volume_interval}
+                           if getattr(spec, "robust", False) else {})}
                        if getattr(spec, "projection", False) else {"enabled": False}),
     }
     if method == "mma":
@@ -126,7 +134,7 @@ def summary(spec: ProblemSpec, history: Sequence, method: str = "oc", max_iterat
         "total_seconds": total_seconds,
         "seconds_per_iteration": total_seconds / len(history) if history else 0.0,
         "warnings": [],
-        "robust": False,
+        "robust": bool(getattr(spec, "projection", False) and getattr(spec, "robust", False)),
     }
     result["volume_constraint_satisfied"] = result["volume_constraint_relative_violation"] <= 1.0e-6
     if getattr(spec, "projection", False) and last:

@@ -72,6 +72,10 @@ class TopologyIteration:
     volume_converged: bool = False
     beta: float = 0.0          # projection sharpness (0: no projection)
     final_stage: bool = True   # no projection, or its last beta stage
+    # robust runs (volume_fraction is then the blueprint's)
+    eroded_volume_fraction: float = 0.0
+    dilated_volume_fraction: float = 0.0
+    dilated_target_fraction: float = 0.0
 
 
 def element_mass(dim, hx, hy, hz, density, thickness=1.0) -> np.ndarray:
@@ -162,6 +166,9 @@ class GpuSimpProblem:
         d.beta_factor, d.beta_interval = spec.beta_factor, spec.beta_interval
         d.advance_on_convergence = int(spec.advance_on_convergence)
         d.change_tolerance = spec.change_tolerance
+        d.robust = int(getattr(spec, "robust", False))
+        d.robust_delta = getattr(spec, "robust_delta", 0.1)
+        d.robust_volume_interval = getattr(spec, "robust_volume_interval", 1)
         prec = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
         opts = dict(spec.amg)
         opts.update(amg)
@@ -397,7 +404,9 @@ class TopologyOptimizer:
             history.append(TopologyIteration(it, r.compliance, r.volume_fraction, r.max_change,
                                              r.lam, r.gray_level, r.linear_iterations,
                                              r.bisections, time.perf_counter() - t0,
-                                             bool(r.volume_converged), r.beta, bool(r.final_stage)))
+                                             bool(r.volume_converged), r.beta, bool(r.final_stage),
+                                             r.eroded_volume_fraction, r.dilated_volume_fraction,
+                                             r.dilated_target_fraction))
             # during beta continuation only the final stage may stop the run
             if self.change_tolerance > 0 and r.final_stage and r.max_change <= self.change_tolerance:
                 break

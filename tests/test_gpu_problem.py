@@ -290,3 +290,29 @@ def test_concurrent_load_cases_match_sequential_and_oracle(precision):
     assert [r.linear_iterations for r in recs[True]] == [r.linear_iterations for r in recs[False]]
     for k, r in enumerate(recs[True]):
         assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_robust_run_matches_oracle(precision):
+    """Robust formulation (Projection.hpp:44-60, run_oc at
+    TopologyOptimizer.cpp:567-651): objective on the eroded design, OC on the
+    dilated volume against the moved target, the blueprint's volume reported;
+    every history column against the oracle."""
+    spec = small_q4(40, 20)
+    spec.rtol = 1e-10
+    spec.initial_density = 0.5
+    spec.projection, spec.beta_start, spec.beta_max = True, 2.0, 8.0
+    spec.beta_interval, spec.advance_on_convergence = 3, False
+    spec.robust, spec.robust_delta, spec.robust_volume_interval = True, 0.1, 2
+    ref = oracle.Problem(spec)
+    _, hist = ref.run(8)
+    gpu = GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision=precision)
+    recs = TopologyOptimizer(gpu, max_iterations=8, change_tolerance=0).run()
+    for k, r in enumerate(recs):
+        assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
+        assert abs(r.volume_fraction - hist[k, 1]) < 1e-8
+        assert abs(r.eroded_volume_fraction - hist[k, 7]) < 1e-8
+        assert abs(r.dilated_volume_fraction - hist[k, 8]) < 1e-8
+        assert abs(r.dilated_target_fraction - hist[k, 9]) < 1e-8
+        assert r.eroded_volume_fraction < r.volume_fraction < r.dilated_volume_fraction
+    gpu.close()

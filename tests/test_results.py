@@ -50,3 +50,24 @@ def test_summary_members_the_plots_read(tmp_path):
     assert res["linear_solver"]["iterative_iterations_total"] == 20 + 21 + 22
     assert "optimizer_volume_tolerance" in s["tolerances"]
     assert s["provenance"]["case"] == spec.name
+
+
+def test_robust_history_columns():
+    """ResultWriter::write_history appends the eroded / dilated / target
+    fractions for a robust run (src/io/ResultWriter.cpp:1445-1448)."""
+    import os
+    import tempfile
+    from sparlab_gb300 import problems as P
+    from sparlab_gb300.results import write_history_csv
+    from sparlab_gb300.topopt import TopologyIteration
+    spec = P.q4_cantilever_120x40()
+    spec.projection, spec.robust = True, True
+    hist = [TopologyIteration(1, 2.0, 0.5, 0.1, 1.0, 0.3, 20, 30, 0.01, True, 2.0, False, 0.45, 0.55, 0.56)]
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "history.csv")
+        write_history_csv(path, hist, spec)
+        head, row = open(path).read().splitlines()
+    cols = head.split(",")
+    assert cols[-4:] == ["beta[-]", "eroded_volume_fraction[-]", "dilated_volume_fraction[-]",
+                         "dilated_target_fraction[-]"]
+    assert [float(v) for v in row.split(",")[-3:]] == [0.45, 0.55, 0.56]
