@@ -325,8 +325,10 @@ class Problem:
                         converged=bool(out[4]))
 
     def run_mma(self, iterations):
+        """run_mma: final design and history rows in run()'s layout (the
+        MMA subproblem iterations in the bisections column)."""
         x = np.zeros(self.ne)
-        hist = np.zeros((iterations, 6))
+        hist = np.zeros((iterations, 10))
         done = C.c_int32()
         _check(lib().orc_run_mma(self._h, C.c_int32(iterations), _p(x), _p(hist), C.byref(done)))
         return x, hist[: done.value]

@@ -2376,26 +2376,57 @@ int orc_run_mma(orc_problem* h, int32_t iterations, double* x, double* hist, int
     st.move = p.move;
     double c_ref = 0.0;
     const double target = p.vf * p.domain_volume;
+    // beta continuation and the robust volume row (run_mma,
+    // src/topopt/TopologyOptimizer.cpp:730-980)
+    const int stages = p.proj ? beta_stages(p) : 1;
+    int stage = 0, stage_start = 1;
+    if (p.proj) p.beta = beta_of_stage(p, 0);
+    const bool robust = p.proj && p.robust;
+    double dilated_target = target;
     int it = 0;
     for (it = 1; it <= iterations; ++it) {
       Evaluation ev;
       evaluate(p, xv.data(), ev);
       if (it == 1) c_ref = ev.compliance;
       Vec df0(static_cast<size_t>(p.ne)), dfdx(static_cast<size_t>(p.ne));
-      for (Index e = 0; e < p.ne; ++e) {
-        df0[e] = ev.dc_dx[e] / c_ref;
-        dfdx[e] = ev.dv_dx[e] / target;
+      double vol_i = 0.0, vol_d = 0.0, fval = 0.0;
+      if (robust) {
+        const double eta_d = p.eta - p.robust_delta;
+        Vec w(static_cast<size_t>(p.ne)), g(static_cast<size_t>(p.ne));
+        for (Index e = 0; e < p.ne; ++e) {
+          vol_d += project(ev.rhot[e], p.beta, eta_d) * p.volumes[e];
+          vol_i += project(ev.rhot[e], p.beta, p.eta) * p.volumes[e];
+          w[e] = p.volumes[e] * project_derivative(ev.rhot[e], p.beta, eta_d);
+        }
+        filter_adjoint(p, w.data(), g.data());
+        if ((it - 1) % p.robust_interval == 0 && vol_i > 0.0) dilated_target = target * vol_d / vol_i;
+        for (Index e = 0; e < p.ne; ++e) dfdx[e] = g[e] / dilated_target;
+        fval = vol_d / dilated_target - 1.0;
+      } else {
+        for (Index e = 0; e < p.ne; ++e) dfdx[e] = ev.dv_dx[e] / target;
+        fval = ev.volume / target - 1.0;
       }
-      const MmaResult r = mma_update(st, xv, df0, ev.volume / target - 1.0, dfdx);
-      double* row = hist + static_cast<size_t>(it - 1) * 6;
+      for (Index e = 0; e < p.ne; ++e) df0[e] = ev.dc_dx[e] / c_ref;
+      const MmaResult r = mma_update(st, xv, df0, fval, dfdx);
+      double* row = hist + static_cast<size_t>(it - 1) * 10;
       row[0] = ev.compliance;
-      row[1] = ev.volume_fraction;
+      row[1] = robust ? vol_i / p.domain_volume : ev.volume_fraction;
       row[2] = r.max_change;
       row[3] = r.lam;
       row[4] = ev.linear_iterations;
       row[5] = r.iterations;
+      row[6] = p.proj ? p.beta : 0.0;
+      row[7] = robust ? ev.volume_fraction : 0.0;
+      row[8] = robust ? vol_d / p.domain_volume : 0.0;
+      row[9] = robust ? dilated_target / p.domain_volume : 0.0;
       xv = r.x;
       for (auto& v : xv) v = std::min(std::max(v, 0.0), 1.0);
+      const bool at_final = !p.proj || stage + 1 >= stages;
+      if (!at_final && (it - stage_start + 1 >= p.beta_interval || (p.advance && r.max_change <= p.change_tol))) {
+        ++stage;
+        stage_start = it + 1;
+        p.beta = beta_of_stage(p, stage);
+      }
     }
     *performed = std::min(it, iterations);
     std::copy(xv.begin(), xv.end(), x);

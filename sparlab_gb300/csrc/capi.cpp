@@ -521,8 +521,6 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     d.robust = dsc->robust != 0;
     if (d.robust) {
       if (!d.projection) throw Error(kBadInput, "projection.robust needs the projection enabled");
-      if (dsc->optimizer != 0)
-        throw Error(kBadInput, "projection.robust runs with the OC update on the GPU (the MMA form is not built)");
       if (!(dsc->eta - dsc->robust_delta > 0.0 && dsc->eta + dsc->robust_delta < 1.0 && dsc->robust_delta > 0.0))
         throw Error(kBadInput, "projection.robust_delta must keep eta - delta and eta + delta inside (0, 1)");
       if (dsc->robust_volume_interval < 1) throw Error(kBadInput, "projection.robust_volume_interval must be >= 1");
@@ -659,8 +657,10 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
       rec->linear_iterations = ev.linear_iterations;
       rec->bisections = st.bisections;
       rec->seconds = ms * 1e-3;
-      rec->volume_converged =
-          g.d.optimizer == 1 ? (ev.volume_fraction / g.d.vf - 1.0 <= 1.0e-4 ? 1 : 0) : (st.converged ? 1 : 0);
+      // MMA: the volume row fval(0) <= constraint_tolerance (1e-4)
+      const double fval0 = g.d.robust ? ev.volume_dilated / g.dilated_target - 1.0
+                                      : ev.volume_fraction / g.d.vf - 1.0;
+      rec->volume_converged = g.d.optimizer == 1 ? (fval0 <= 1.0e-4 ? 1 : 0) : (st.converged ? 1 : 0);
       rec->final_stage = g.beta_at_final() ? 1 : 0;
       rec->beta = g.d.projection ? g.beta : 0.0;
       rec->eroded_volume_fraction = rec->dilated_volume_fraction = rec->dilated_target_fraction = 0.0;

@@ -268,20 +268,24 @@ OcStep GpuProblem::mma_update(bool apply, double* xnew_host) {
   ++mma_iteration;
   if (mma_iteration == 1) c_ref = last_evaluation.compliance;
   if (!(c_ref > 0.0)) throw Error(kBadInput, "the initial compliance is not positive; MMA cannot scale it");
-  const double target = d.vf * domain_volume;
-  const double fval = last_evaluation.volume / target - 1.0;
+  // the volume row: the dilated design against the moved target in a robust
+  // run (TopologyOptimizer.cpp:823-836)
+  if (d.robust && dilated_target <= 0.0) dilated_target = d.vf * domain_volume;
+  const double target = d.robust ? dilated_target : d.vf * domain_volume;
+  const double fval = (d.robust ? last_evaluation.volume_dilated : last_evaluation.volume) / target - 1.0;
+  const double* dv = d.robust ? dv_dilated.p : dv_dx.p;
   const double move = d.move, albefa = 0.1, raa0 = 1.0e-5, a0 = 1.0, cc = 1000.0, dd = 1.0, epsimin = 1.0e-7;
   const int grid = kRedBlocks;
   k_mma_asymptotes<<<grid_for(ne, 256), 256, 0, s>>>(ne, mma_iteration, x.p, m_x1.p, m_x2.p, m_low.p, m_upp.p, 0.5,
                                                      1.2, 0.7);
   SIMP_CHECK_LAUNCH();
   // constraint row scale (Mma.cpp:138-149)
-  k_max_abs<<<grid, kRedThreads, 0, s>>>(ne, dv_dx.p, mpart.p);
+  k_max_abs<<<grid, kRedThreads, 0, s>>>(ne, dv, mpart.p);
   SIMP_CHECK_LAUNCH();
   const double dmax = mma_reduce_max(0) / target;
   const double magnitude = std::max(std::abs(fval), dmax * move);
   const double row_scale = magnitude > 10.0 ? 10.0 / magnitude : 1.0;
-  k_mma_coeffs<<<grid, kRedThreads, 0, s>>>(ne, x.p, m_low.p, m_upp.p, dc_dx.p, 1.0 / c_ref, dv_dx.p,
+  k_mma_coeffs<<<grid, kRedThreads, 0, s>>>(ne, x.p, m_low.p, m_upp.p, dc_dx.p, 1.0 / c_ref, dv,
                                             row_scale / target, move, albefa, raa0, m_alfa.p, m_beta.p, m_p0.p, m_q0.p,
                                             m_p.p, m_q.p, mpart.p);
   SIMP_CHECK_LAUNCH();

@@ -292,8 +292,8 @@ def test_concurrent_load_cases_match_sequential_and_oracle(precision):
         assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_robust_run_matches_oracle(precision):
+@pytest.mark.parametrize("precision,optimizer", [("fp64", "oc"), ("mixed", "oc"), ("fp64", "mma")])
+def test_robust_run_matches_oracle(precision, optimizer):
     """Robust formulation (Projection.hpp:44-60, run_oc at
     TopologyOptimizer.cpp:567-651): objective on the eroded design, OC on the
     dilated volume against the moved target, the blueprint's volume reported;
@@ -305,9 +305,10 @@ def test_robust_run_matches_oracle(precision):
     spec.beta_interval, spec.advance_on_convergence = 3, False
     spec.robust, spec.robust_delta, spec.robust_volume_interval = True, 0.1, 2
     ref = oracle.Problem(spec)
-    _, hist = ref.run(8)
-    gpu = GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision=precision)
+    _, hist = ref.run(8) if optimizer == "oc" else ref.run_mma(8)
+    gpu = GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision=precision, optimizer=optimizer)
     recs = TopologyOptimizer(gpu, max_iterations=8, change_tolerance=0).run()
+    assert [r.beta for r in recs] == list(hist[:, 6])
     for k, r in enumerate(recs):
         assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
         assert abs(r.volume_fraction - hist[k, 1]) < 1e-8

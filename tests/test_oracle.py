@@ -364,15 +364,16 @@ def oracle_project_derivative(r, beta, eta):
     return beta * (1 - np.tanh(beta * (r - eta)) ** 2) / (np.tanh(beta * eta) + np.tanh(beta * (1 - eta)))
 
 
-def test_robust_run_reports_the_blueprint():
-    """test_manufacturing.cpp:308-347 (OC, no overhang filter): the blueprint
-    meets the volume fraction up to the target's lag, eroded < blueprint <
-    dilated volumes, and the eroded design is the softest."""
+@pytest.mark.parametrize("method", ["oc", "mma"])
+def test_robust_run_reports_the_blueprint(method):
+    """test_manufacturing.cpp:308-347 (OC and MMA, no overhang filter): the
+    blueprint meets the volume fraction up to the target's lag, eroded <
+    blueprint < dilated volumes, and the eroded design is the softest."""
     spec = _block_q4()
     spec.projection, spec.robust, spec.robust_delta = True, True, 0.1
     spec.beta_start, spec.beta_max, spec.beta_interval = 2.0, 8.0, 15
     pr = oracle.Problem(spec)
-    x, hist = pr.run(60, change_tol=1e-3)
+    x, hist = pr.run(60, change_tol=1e-3) if method == "oc" else pr.run_mma(60)
     last = hist[-1]
     assert abs(last[1] - 0.4) < 0.02
     assert last[7] < last[1] < last[8]
