@@ -293,6 +293,25 @@ int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms_per_lau
 int simp_filter_volume_noalloc(simp_problem* p, const double* x_device, double* rho_device,
                                double* volume_device);
 
+/* RobustRecord (include/sparlab/topopt/TopologyOptimizer.hpp:153-166): the
+ * current design projected at eta + delta (eroded), eta (blueprint) and
+ * eta - delta (dilated) with the current beta, each evaluated (one solve per
+ * load case): what TopologyOptimizer::finish records for a robust run and for
+ * the erosion check of a projected one (src/topopt/TopologyOptimizer.cpp:
+ * 344-415).  delta <= 0 takes the problem's robust_delta.  The densities
+ * (host, num_elements, NULL to skip) are the eroded and dilated designs'.
+ * The evaluations replace the problem's gradients, so an OC / MMA half-step
+ * needs a new simp_evaluate first (simp_iterate always makes one). */
+typedef struct simp_robust_record {
+  double eta_eroded, eta_intermediate, eta_dilated;
+  double compliance_eroded, compliance_intermediate, compliance_dilated;
+  double volume_fraction_eroded, volume_fraction_intermediate, volume_fraction_dilated;
+  double dilated_target_fraction;  /* robust runs: the last moved target; else 0 */
+} simp_robust_record;
+
+int simp_projection_variants(simp_problem* p, double delta, simp_robust_record* record,
+                             double* eroded_density, double* dilated_density);
+
 /* ---- Modal analysis (src/fem/ModalAnalysis.cpp) ---------------------- */
 
 /* ModalAnalysisOptions (include/sparlab/fem/ModalAnalysis.hpp:37-65).  The

@@ -34,6 +34,7 @@ EXPORTS = [
     "simp_problem_apply_operator", "simp_problem_time_operator", "simp_filter_volume_noalloc",
     "simp_kernel_launches", "simp_default_modal_options", "simp_modal", "simp_modal_warning",
     "simp_element_mass", "simp_default_buckling_options", "simp_buckling", "simp_buckling_warning",
+    "simp_projection_variants",
 ]
 
 
@@ -118,6 +119,16 @@ class ModalInfo(C.Structure):
                 ("converged", C.c_int32), ("linear_iterations", C.c_int64),
                 ("final_change", C.c_double), ("total_mass", C.c_double),
                 ("num_warnings", C.c_int32)]
+
+
+class RobustRecord(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "eta_eroded", "eta_intermediate", "eta_dilated", "compliance_eroded",
+        "compliance_intermediate", "compliance_dilated", "volume_fraction_eroded",
+        "volume_fraction_intermediate", "volume_fraction_dilated", "dilated_target_fraction")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 class BucklingOptions(C.Structure):

@@ -757,6 +757,28 @@ int simp_filter_volume_noalloc(simp_problem* p, const double* x, double* rho, do
   });
 }
 
+int simp_projection_variants(simp_problem* p, double delta, simp_robust_record* record, double* eroded_density,
+                             double* dilated_density) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuProblem& g = *p->p;
+    const double dl = delta > 0.0 ? delta : g.d.robust_delta;
+    const GpuProblem::Variants v = g.projection_variants(dl, eroded_density, dilated_density);
+    if (record) {
+      record->eta_eroded = v.eta[0];
+      record->eta_intermediate = v.eta[1];
+      record->eta_dilated = v.eta[2];
+      record->compliance_eroded = v.compliance[0];
+      record->compliance_intermediate = v.compliance[1];
+      record->compliance_dilated = v.compliance[2];
+      record->volume_fraction_eroded = v.volume_fraction[0];
+      record->volume_fraction_intermediate = v.volume_fraction[1];
+      record->volume_fraction_dilated = v.volume_fraction[2];
+      record->dilated_target_fraction = g.d.robust ? g.dilated_target / g.domain_volume : 0.0;
+    }
+  });
+}
+
 void simp_default_modal_options(simp_modal_options* o) {
   o->num_modes = 6;
   o->mass_type = 0;

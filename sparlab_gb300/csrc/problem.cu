@@ -602,7 +602,7 @@ Evaluation GpuProblem::evaluate() {
   SIMP_CUDA(cudaMemcpyAsync(&ev.volume, amg.scal.p + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
   SIMP_CUDA(cudaStreamSynchronize(s));
   ev.volume_fraction = ev.volume / domain_volume;
-  if (d.robust) {
+  if (d.robust && d.eta_override <= 0.0) {
     // robust_volumes (TopologyOptimizer.cpp:61-80): the blueprint's volume,
     // and the dilated design's volume and gradient, which the OC update
     // constrains
@@ -654,6 +654,37 @@ void GpuProblem::advance_beta(double max_change) {
     beta_stage_start = iteration + 1;
     beta = beta_of_stage(d, beta_stage);
   }
+}
+
+GpuProblem::Variants GpuProblem::projection_variants(double delta, double* eroded_density, double* dilated_density) {
+  if (!d.projection) throw Error(kBadInput, "the eroded and dilated variants need the projection");
+  if (!(delta > 0.0 && d.eta - delta > 0.0 && d.eta + delta < 1.0))
+    throw Error(kBadInput, "projection.robust_delta must keep eta - delta and eta + delta inside (0, 1)");
+  Variants v;
+  const double etas[3] = {d.eta + delta, d.eta, d.eta - delta};
+  double* out[3] = {eroded_density, nullptr, dilated_density};
+  for (int k = 0; k < 3; ++k) {
+    d.eta_override = etas[k];
+    Evaluation ev;
+    try {
+      ev = evaluate();
+    } catch (...) {
+      d.eta_override = -1.0;
+      throw;
+    }
+    d.eta_override = -1.0;
+    v.eta[k] = etas[k];
+    v.compliance[k] = ev.compliance;
+    v.volume_fraction[k] = ev.volume_fraction;
+    if (out[k]) {
+      rho.download(out[k], static_cast<size_t>(ne), amg.stream);
+      SIMP_CUDA(cudaStreamSynchronize(amg.stream));
+    }
+  }
+  // the gradients of these evaluations are not the loop's: the next update
+  // needs a fresh evaluate
+  evaluated = false;
+  return v;
 }
 
 // The dilated target of a robust run, moved to V* V_d / V_i every

@@ -41,7 +41,8 @@ struct ProblemDesc {
   bool robust = false;
   double robust_delta = 0.1;
   int robust_interval = 1;
-  double objective_eta() const { return robust ? eta + robust_delta : eta; }
+  double eta_override = -1.0;  // > 0: the threshold of a one-off evaluation (projection_variants)
+  double objective_eta() const { return eta_override > 0.0 ? eta_override : robust ? eta + robust_delta : eta; }
   double volume_eta() const { return robust ? eta - robust_delta : eta; }
 };
 
@@ -128,6 +129,14 @@ class GpuProblem {
   double dilated_target = 0.0;
   DBuf<double> rtmp, dv_dilated;
   void update_robust_target();
+  // RobustRecord (TopologyOptimizer.hpp:153-166) of the current design: its
+  // compliance and volume fraction projected at eta + delta, eta and
+  // eta - delta with the current beta (TopologyOptimizer.cpp:344-415); the
+  // densities of the eroded and dilated designs when asked for (host).
+  struct Variants {
+    double eta[3], compliance[3], volume_fraction[3];
+  };
+  Variants projection_variants(double delta, double* eroded_density, double* dilated_density);
   bool beta_at_final() const;
   // BetaSchedule::advance after iteration `iteration` with its design change
   void advance_beta(double max_change);

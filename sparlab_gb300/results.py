@@ -77,8 +77,12 @@ def write_history_csv(path: str, history: Sequence, spec: ProblemSpec, method: s
 def summary(spec: ProblemSpec, history: Sequence, method: str = "oc", max_iterations: int = 200,
             change_tolerance: float = 1e-3, stop_reason: Optional[str] = None,
             load_case_compliance: Optional[List[float]] = None, case: Optional[str] = None,
-            solver: str = "gpu_amg_cg") -> dict:
-    """The summary members the plotting and result tables read."""
+            solver: str = "gpu_amg_cg", robust_record: Optional[dict] = None) -> dict:
+    """The summary members the plotting and result tables read.
+    ``robust_record``: ``GpuSimpProblem.projection_variants()`` of the final
+    design, written as the reference's ``robust`` (robust runs) or
+    ``erosion_check`` block (src/io/ResultWriter.cpp:2766-2797); for a robust
+    run the blueprint's compliance and volume fraction are the result's."""
     vol = domain_volume(spec)
     last = history[-1] if history else None
     converged = bool(last and change_tolerance > 0 and last.max_change <= change_tolerance)
@@ -139,6 +143,25 @@ def summary(spec: ProblemSpec, history: Sequence, method: str = "oc", max_iterat
     result["volume_constraint_satisfied"] = result["volume_constraint_relative_violation"] <= 1.0e-6
     if getattr(spec, "projection", False) and last:
         result["projection"] = {"final_beta": last.beta, "eta": spec.eta}
+    if robust_record is not None:
+        rr = robust_record
+        designs = [{"design": name, "eta": rr["eta_" + key], "compliance_J": rr["compliance_" + key],
+                    "volume_fraction": rr["volume_fraction_" + key]}
+                   for name, key in (("eroded", "eroded"), ("intermediate (blueprint)", "intermediate"),
+                                     ("dilated", "dilated"))]
+        if getattr(spec, "robust", False):
+            result["robust"] = {
+                "designs": designs, "dilated_target_fraction": rr["dilated_target_fraction"],
+                "note": "compliance_J and volume_fraction below are the blueprint's; the optimiser "
+                        "minimised the eroded design's compliance"}
+            result["compliance_J"] = rr["compliance_intermediate"]
+            result["volume_fraction"] = rr["volume_fraction_intermediate"]
+            result["volume_m3"] = rr["volume_fraction_intermediate"] * vol
+        else:
+            result["erosion_check"] = {
+                "designs": designs,
+                "note": "a design optimised without the robust formulation, evaluated once at the "
+                        "eroded and dilated thresholds eta +- robust_delta of the final beta"}
     if history:
         c0 = history[0].compliance
         result["initial_compliance_J"] = c0

@@ -321,6 +321,20 @@ class GpuSimpProblem:
                            info.iterations, info.subspace_size, bool(info.converged),
                            info.linear_iterations, info.final_change, warnings)
 
+    def projection_variants(self, delta=0.0, densities=False) -> dict:
+        """``RobustRecord`` of the current design (eroded / blueprint /
+        dilated compliance and volume fraction at the current beta); with
+        ``densities`` also the eroded and dilated physical densities."""
+        rec = _lib.RobustRecord()
+        er = np.zeros(self.ne) if densities else None
+        di = np.zeros(self.ne) if densities else None
+        self._check(self._lib.simp_projection_variants(self._h, C.c_double(delta), C.byref(rec),
+                                                       ptr(er), ptr(di)))
+        out = rec.as_dict()
+        if densities:
+            out["eroded_density"], out["dilated_density"] = er, di
+        return out
+
     def buckling(self, load_case=0, num_modes=4, max_iterations=400, tolerance=1e-8,
                  residual_tolerance=1e-6, transform="auto", stiffness_scale=None, stress_scale=None,
                  solid_mask=None, initial_subspace=None, mode_shapes=True,

@@ -317,3 +317,30 @@ def test_robust_run_matches_oracle(precision, optimizer):
         assert abs(r.dilated_target_fraction - hist[k, 9]) < 1e-8
         assert r.eroded_volume_fraction < r.volume_fraction < r.dilated_volume_fraction
     gpu.close()
+
+
+def test_projection_variants_match_oracle():
+    """RobustRecord / erosion check (TopologyOptimizer.cpp:344-415): the
+    current design's eroded, blueprint and dilated compliance and volume
+    fraction against the oracle's evaluations at eta + delta, eta, eta - delta."""
+    spec = small_q4(40, 20)
+    spec.rtol = 1e-10
+    spec.initial_density = 0.5
+    spec.projection, spec.beta_start, spec.beta_max = True, 4.0, 4.0
+    gpu = GpuSimpProblem(spec, precision="fp64")
+    for _ in range(3):
+        gpu.iterate()
+    x = gpu.design()
+    rec = gpu.projection_variants(0.15, densities=True)
+    for key, eta in (("eroded", 0.65), ("intermediate", 0.5), ("dilated", 0.35)):
+        s2 = small_q4(40, 20)
+        s2.rtol = 1e-10
+        s2.projection, s2.eta, s2.beta_start, s2.beta_max = True, eta, 4.0, 4.0
+        ev = oracle.Problem(s2).evaluate(x)
+        assert rec["eta_" + key] == pytest.approx(eta, abs=1e-15)
+        assert rec["compliance_" + key] == pytest.approx(ev["compliance"], rel=1e-7)
+        assert rec["volume_fraction_" + key] == pytest.approx(ev["volume_fraction"], abs=1e-12)
+        if key != "intermediate":
+            np.testing.assert_allclose(rec[key + "_density"], ev["rho"], atol=1e-14)
+    assert rec["compliance_eroded"] > rec["compliance_intermediate"] > rec["compliance_dilated"]
+    gpu.close()

@@ -71,3 +71,21 @@ def test_robust_history_columns():
     assert cols[-4:] == ["beta[-]", "eroded_volume_fraction[-]", "dilated_volume_fraction[-]",
                          "dilated_target_fraction[-]"]
     assert [float(v) for v in row.split(",")[-3:]] == [0.45, 0.55, 0.56]
+
+
+def test_summary_robust_and_erosion_blocks():
+    from sparlab_gb300 import problems as P
+    from sparlab_gb300.results import summary
+    from sparlab_gb300.topopt import TopologyIteration
+    spec = P.q4_cantilever_120x40()
+    spec.projection = True
+    hist = [TopologyIteration(1, 2.0, 0.5, 0.1, 1.0, 0.3, 20, 30, 0.01, True, 2.0, True)]
+    rr = {"eta_eroded": 0.6, "eta_intermediate": 0.5, "eta_dilated": 0.4, "compliance_eroded": 3.0,
+          "compliance_intermediate": 2.0, "compliance_dilated": 1.5, "volume_fraction_eroded": 0.45,
+          "volume_fraction_intermediate": 0.5, "volume_fraction_dilated": 0.55, "dilated_target_fraction": 0.56}
+    s = summary(spec, hist, robust_record=rr)["optimization_result"]
+    assert [d["design"] for d in s["erosion_check"]["designs"]] == ["eroded", "intermediate (blueprint)", "dilated"]
+    spec.robust = True
+    s = summary(spec, hist, robust_record=rr)["optimization_result"]
+    assert s["robust"]["dilated_target_fraction"] == 0.56
+    assert s["compliance_J"] == 2.0 and s["volume_fraction"] == 0.5
