@@ -313,19 +313,11 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
   }
   amg.setup(true);
   SolveWork& w0 = amg.work(0);
-  auto check_solve = [&](const GpuAmg::PcgResult& r) {
-    res.linear_iterations += r.iterations;
-    if (!r.converged) {
-      std::ostringstream os;
-      os << "AMG-CG(chebyshev) did not converge: " << r.iterations << " iterations left a relative residual of "
-         << r.relres << " against a tolerance of " << amg.opt.rtol;
-      throw Error(kMaxIter, os.str());
-    }
-  };
+
   // the static solution of the load case
   DBuf<double> u(static_cast<size_t>(n)), ufull(static_cast<size_t>(p.ndof));
   SIMP_CUDA(cudaMemsetAsync(u.p, 0, sizeof(double) * n, s));
-  check_solve(amg.solve(w0, p.b.p + static_cast<size_t>(load_case) * n, u.p));
+  count_solve(amg.solve(w0, p.b.p + static_cast<size_t>(load_case) * n, u.p), amg.opt.rtol, res.linear_iterations);
   k_expand_free<<<grid_for(p.ndof, 256), 256, 0, s>>>(p.ndof, p.dof_map.p, u.p, ufull.p);
   SIMP_CHECK_LAUNCH();
   // G = -K_G(u) on K_ff's pattern
@@ -404,12 +396,7 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
     top_cols = m_req;
     res.converged = true;
   } else {
-    const int workers = std::max(1, std::min(q, o.concurrent_solves));
-    std::vector<SolveWork*> works;
-    for (int t = 0; t < workers; ++t) works.push_back(&amg.work(t));
-    for (SolveWork* w : works) amg.ensure(*w);
-    int dev = 0;
-    SIMP_CUDA(cudaGetDevice(&dev));
+    const std::vector<SolveWork*> works = workspaces(amg, std::max(1, std::min(q, o.concurrent_solves)));
     // start: the caller's subspace (all but two columns at most), the rest
     // seeded uniform [-1, 1) columns
     SplitMix64 rng(kStartSeed);
@@ -456,26 +443,8 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
       for (int c = 0; c < q; ++c) apply_g(w0, X.p + static_cast<size_t>(c) * n, Y.p + static_cast<size_t>(c) * n);
       SIMP_CUDA(cudaMemsetAsync(Z.p, 0, sizeof(double) * n * q, s));
       SIMP_CUDA(cudaStreamSynchronize(s));
-      std::vector<GpuAmg::PcgResult> pr(static_cast<size_t>(q));
-      std::vector<std::exception_ptr> errs(static_cast<size_t>(workers));
-      auto run = [&](int t) {
-        try {
-          SIMP_CUDA(cudaSetDevice(dev));
-          for (int c = t; c < q; c += workers)
-            pr[static_cast<size_t>(c)] = amg.solve(*works[static_cast<size_t>(t)], Y.p + static_cast<size_t>(c) * n,
-                                                   Z.p + static_cast<size_t>(c) * n);
-          SIMP_CUDA(cudaStreamSynchronize(works[static_cast<size_t>(t)]->stream));
-        } catch (...) {
-          errs[static_cast<size_t>(t)] = std::current_exception();
-        }
-      };
-      std::vector<std::thread> threads;
-      for (int t = 1; t < workers; ++t) threads.emplace_back(run, t);
-      run(0);
-      for (auto& th : threads) th.join();
-      for (auto& e : errs)
-        if (e) std::rethrow_exception(e);
-      for (const GpuAmg::PcgResult& x : pr) check_solve(x);
+      for (const GpuAmg::PcgResult& x : solve_columns(amg, works, q, n, Y.p, Z.p))
+        count_solve(x, amg.opt.rtol, res.linear_iterations);
       // orthonormal basis B of Z, two passes through the Gram matrix
       Mat wz, T;
       gram_of(q, Z.p, Z.p, wz);

@@ -388,12 +388,7 @@ ModalResult solve_modal(GpuProblem& p, const ModalOptions& o, const double* ksca
       amg.mf.scale = ks32.p;
     }
     amg.setup(true);
-    const int workers = std::max(1, std::min(q, o.concurrent_solves));
-    std::vector<SolveWork*> works;
-    for (int t = 0; t < workers; ++t) works.push_back(&amg.work(t));
-    for (SolveWork* w : works) amg.ensure(*w);
-    int dev = 0;
-    SIMP_CUDA(cudaGetDevice(&dev));
+    const std::vector<SolveWork*> works = workspaces(amg, std::max(1, std::min(q, o.concurrent_solves)));
 
     // Bathe's start: the mass diagonal, then unit vectors at the DOFs of
     // largest m_ii / k_ii in stable order (ModalAnalysis.cpp:55-88)
@@ -437,36 +432,8 @@ ModalResult solve_modal(GpuProblem& p, const ModalOptions& o, const double* ksca
         }
       }
       SIMP_CUDA(cudaStreamSynchronize(s));
-      std::vector<GpuAmg::PcgResult> pr(static_cast<size_t>(q));
-      std::vector<std::exception_ptr> errs(static_cast<size_t>(workers));
-      auto run = [&](int t) {
-        try {
-          SIMP_CUDA(cudaSetDevice(dev));
-          for (int c = t; c < q; c += workers)
-            pr[static_cast<size_t>(c)] =
-                amg.solve(*works[static_cast<size_t>(t)], Y.p + static_cast<size_t>(c) * n,
-                          Xb.p + static_cast<size_t>(c) * n);
-          SIMP_CUDA(cudaStreamSynchronize(works[static_cast<size_t>(t)]->stream));
-        } catch (...) {
-          errs[static_cast<size_t>(t)] = std::current_exception();
-        }
-      };
-      std::vector<std::thread> threads;
-      for (int t = 1; t < workers; ++t) threads.emplace_back(run, t);
-      run(0);
-      for (auto& th : threads) th.join();
-      for (auto& e : errs)
-        if (e) std::rethrow_exception(e);
-      for (const GpuAmg::PcgResult& r : pr) {
-        res.linear_iterations += r.iterations;
-        if (!r.converged) {
-          std::ostringstream os;
-          os << "AMG-CG(chebyshev) did not converge: " << r.iterations
-             << " iterations left a relative residual of " << r.relres << " against a tolerance of "
-             << amg.opt.rtol;
-          throw Error(kMaxIter, os.str());
-        }
-      }
+      for (const GpuAmg::PcgResult& r : solve_columns(amg, works, q, n, Y.p, Xb.p))
+        count_solve(r, amg.opt.rtol, res.linear_iterations);
       // projected pencil: Xbar^T K Xbar and Xbar^T M Xbar
       for (int c = 0; c < q; ++c) apply_k(w0, Xb.p + static_cast<size_t>(c) * n, Y.p + static_cast<size_t>(c) * n);
       for (int c = 0; c < q; ++c) apply_m(w0, Xb.p + static_cast<size_t>(c) * n, Z.p + static_cast<size_t>(c) * n);

@@ -11,7 +11,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <exception>
 #include <numeric>
+#include <sstream>
+#include <thread>
 #include <vector>
 
 namespace simp {
@@ -301,6 +304,57 @@ void copy_level0(const Level& s, Level& t, cudaStream_t st) {
   copy_device(t.a.ptr, s.a.ptr, st);
   copy_device(t.a.col, s.a.col, st);
   t.a.v64.alloc(static_cast<size_t>(s.a.nnz));
+}
+
+// A z_c = y_c for the q columns of column-major n x q blocks y, z (z holds
+// the initial guesses), the columns dealt round-robin to the workspaces, one
+// host thread and stream each; every solve computes what it computes alone.
+// Errors of any thread are rethrown after all have joined.
+std::vector<GpuAmg::PcgResult> solve_columns(GpuAmg& amg, const std::vector<SolveWork*>& works, int q, i32 n,
+                                             const double* y, double* z) {
+  int dev = 0;
+  SIMP_CUDA(cudaGetDevice(&dev));
+  const int workers = static_cast<int>(works.size());
+  std::vector<GpuAmg::PcgResult> pr(static_cast<size_t>(q));
+  std::vector<std::exception_ptr> errs(static_cast<size_t>(workers));
+  auto run = [&](int t) {
+    try {
+      SIMP_CUDA(cudaSetDevice(dev));
+      for (int c = t; c < q; c += workers)
+        pr[static_cast<size_t>(c)] =
+            amg.solve(*works[static_cast<size_t>(t)], y + static_cast<size_t>(c) * n, z + static_cast<size_t>(c) * n);
+      SIMP_CUDA(cudaStreamSynchronize(works[static_cast<size_t>(t)]->stream));
+    } catch (...) {
+      errs[static_cast<size_t>(t)] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> threads;
+  for (int t = 1; t < workers; ++t) threads.emplace_back(run, t);
+  run(0);
+  for (auto& th : threads) th.join();
+  for (auto& e : errs)
+    if (e) std::rethrow_exception(e);
+  return pr;
+}
+
+// Adds a solve's iterations to `total`; AmgCgSolver's ConvergenceError text
+// when it did not converge (src/fem/LinearSolver.cpp:219-290)
+void count_solve(const GpuAmg::PcgResult& r, double rtol, i64& total) {
+  total += r.iterations;
+  if (!r.converged) {
+    std::ostringstream os;
+    os << "AMG-CG(chebyshev) did not converge: " << r.iterations << " iterations left a relative residual of "
+       << r.relres << " against a tolerance of " << rtol;
+    throw Error(kMaxIter, os.str());
+  }
+}
+
+// Workspaces 0 .. count-1 of `amg`, sized for its hierarchy.
+std::vector<SolveWork*> workspaces(GpuAmg& amg, int count) {
+  std::vector<SolveWork*> works;
+  for (int t = 0; t < count; ++t) works.push_back(&amg.work(t));
+  for (SolveWork* w : works) amg.ensure(*w);
+  return works;
 }
 
 }  // namespace
