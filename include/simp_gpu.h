@@ -65,6 +65,9 @@ typedef struct {
   int32_t max_iterations;        /* 0 -> 1000 */
   int32_t precision;             /* SIMP_PRECISION_* */
   int32_t device;                /* CUDA device ordinal */
+  int32_t cuda_graphs;           /* 1: each PCG iteration after the first is one CUDA graph
+                                    launch (captured per workspace after every setup);
+                                    0: the same kernels launched one by one */
 } simp_solver_options;
 
 typedef struct {

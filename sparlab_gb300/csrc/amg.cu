@@ -14,17 +14,30 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <mutex>
 #include <sstream>
 #include <type_traits>
+#include <unordered_map>
 
 namespace simp {
 
 std::atomic<int64_t> g_launches{0};
+thread_local int64_t t_launches = 0;
 
-void DevPattern::upload(const NodePattern& p) {
-  ptr.upload(p.ptr);
-  nbr.upload(p.nbr);
-  off.upload(p.off);
+void raise_dynamic_smem(const void* kernel, size_t bytes) {
+  static std::mutex m;
+  static std::unordered_map<const void*, size_t> limits;
+  std::lock_guard<std::mutex> lock(m);
+  size_t& cur = limits[kernel];
+  if (bytes <= cur) return;
+  SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+  cur = bytes;
+}
+
+void DevPattern::upload(const NodePattern& p, cudaStream_t s) {
+  ptr.upload(p.ptr, s);
+  nbr.upload(p.nbr, s);
+  off.upload(p.off, s);
 }
 
 __global__ void k_expand_columns(i32 n, const i32* __restrict__ node_of, NodeView p,
@@ -91,23 +104,22 @@ void nb_apply(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cu
 
 template <class T>
 void nb_cheb_step(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
-                  double c1, double c2, int add_d, cudaStream_t s) {
+                  const T* c12, int add_d, cudaStream_t s) {
   with_shape<T>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     k_rows_cheb_step<VS, B, T><<<rows_grid(op, VS), 256, 0, s>>>(
-        op.rows, op.node_of, op.pat, op.rowptr, op.col, val, d, rin, r, dn, x, dinv, static_cast<T>(c1),
-        static_cast<T>(c2), add_d);
+        op.rows, op.node_of, op.pat, op.rowptr, op.col, val, d, rin, r, dn, x, dinv, c12, add_d);
   });
   SIMP_CHECK_LAUNCH();
 }
 
 template <class T>
 void nb_cheb_first(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
-                   double inv_theta, cudaStream_t s) {
+                   const T* inv_theta, cudaStream_t s) {
   with_shape<T>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     k_rows_cheb_first<VS, B, T><<<rows_grid(op, VS), 256, 0, s>>>(
-        op.rows, op.node_of, op.pat, op.rowptr, op.col, val, x, b, r, d, dinv, static_cast<T>(inv_theta));
+        op.rows, op.node_of, op.pat, op.rowptr, op.col, val, x, b, r, d, dinv, inv_theta);
   });
   SIMP_CHECK_LAUNCH();
 }
@@ -149,6 +161,7 @@ struct V<double> {
   static double* d(LevelWork& l) { return l.d64.p; }
   static double* e(LevelWork& l) { return l.e64.p; }
   static const double* dinv(Level& l) { return l.dinv64.p; }
+  static const double* cheb(Level& l) { return l.cheb64.p; }
 };
 template <>
 struct V<float> {
@@ -159,6 +172,7 @@ struct V<float> {
   static float* d(LevelWork& l) { return l.d32.p; }
   static float* e(LevelWork& l) { return l.e32.p; }
   static const float* dinv(Level& l) { return l.dinv32.p; }
+  static const float* cheb(Level& l) { return l.cheb32.p; }
 };
 
 template <class A, class B>
@@ -193,7 +207,7 @@ void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
 
 // Matrix-free level-0 pieces of the FP32 cycle (tiled in 3-D).
 void mf_cheb_first(const MfOp& mf, i32 nodes, const float* x, const float* b, float* r, float* d,
-                   const float* dinv, float inv_theta, cudaStream_t s) {
+                   const float* dinv, const float* inv_theta, cudaStream_t s) {
   if (mf.dim == 3) {
     MfArgs a{};
     a.x = x;
@@ -201,7 +215,7 @@ void mf_cheb_first(const MfOp& mf, i32 nodes, const float* x, const float* b, fl
     a.r = r;
     a.dn = d;
     a.dinv = dinv;
-    a.inv_theta = inv_theta;
+    a.coef = inv_theta;
     mf3<4>(mf, a, s);
     return;
   }
@@ -210,7 +224,7 @@ void mf_cheb_first(const MfOp& mf, i32 nodes, const float* x, const float* b, fl
 }
 
 void mf_cheb_step(const MfOp& mf, i32 nodes, const float* d, const float* rin, float* r, float* dn, float* x,
-                  const float* dinv, float c1, float c2, int add_d, cudaStream_t s) {
+                  const float* dinv, const float* c12, int add_d, cudaStream_t s) {
   if (mf.dim == 3) {
     MfArgs a{};
     a.x = d;
@@ -219,13 +233,12 @@ void mf_cheb_step(const MfOp& mf, i32 nodes, const float* d, const float* rin, f
     a.dn = dn;
     a.xs = x;
     a.dinv = dinv;
-    a.c1 = c1;
-    a.c2 = c2;
+    a.coef = c12;
     a.add_d = add_d;
     mf3<3>(mf, a, s);
     return;
   }
-  k_mf_cheb_step<<<grid_for(nodes, 256), 256, 0, s>>>(mf_view(mf), nodes, d, rin, r, dn, x, dinv, c1, c2, add_d);
+  k_mf_cheb_step<<<grid_for(nodes, 256), 256, 0, s>>>(mf_view(mf), nodes, d, rin, r, dn, x, dinv, c12, add_d);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -281,6 +294,7 @@ GpuAmg::~GpuAmg() {
 }
 
 SolveWork::~SolveWork() {
+  if (body) cudaGraphExecDestroy(body);
   if (own_stream && stream) {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
@@ -570,6 +584,18 @@ void GpuAmg::numeric_level(size_t l) {
     lv.c2.push_back(2.0 * rn / delta);
     rho = rn;
   }
+  // the kernels read them from device memory: [1 / theta, c1_0, c2_0, ...,
+  // 0, 0] (the closing pair is the degree-1 step's)
+  std::vector<double> coef{lv.inv_theta};
+  for (size_t k = 0; k < lv.c1.size(); ++k) {
+    coef.push_back(lv.c1[k]);
+    coef.push_back(lv.c2[k]);
+  }
+  coef.push_back(0.0);
+  coef.push_back(0.0);
+  const std::vector<float> coef32(coef.begin(), coef.end());
+  lv.cheb64.upload(coef, stream);
+  lv.cheb32.upload(coef32, stream);
 }
 
 // Aggregates, tentative prolongator and symbolic patterns of level l -> l+1.
@@ -644,10 +670,10 @@ void GpuAmg::build_transfer(size_t l) {
   lv.wr_p = shape(lv.ppat, lv.first, lv.apat, nullptr);
   lv.wr_ap = shape(lv.appat, lv.first, lv.apat, &lv.ppat);
   lv.wr_rap = shape(nv.apat, nv.first, lv.rpat, &lv.appat);
-  lv.d_ppat.upload(lv.ppat);
-  lv.d_rpat.upload(lv.rpat);
-  lv.d_appat.upload(lv.appat);
-  nv.d_apat.upload(nv.apat);
+  lv.d_ppat.upload(lv.ppat, stream);
+  lv.d_rpat.upload(lv.rpat, stream);
+  lv.d_appat.upload(lv.appat, stream);
+  nv.d_apat.upload(nv.apat, stream);
   lv.d_r_to_p.upload(r_to_p, stream);
   lv.d_sym_t.upload(sym_t, stream);
   nv.d_self.upload(pattern_self_slots(nv.apat), stream);
@@ -686,8 +712,7 @@ bool launch_rows(void (*kernel)(i32, WarpRows, KArgs...), i32 nodes, const WarpR
   if (per_warp > 200 * 1024) return false;
   const int warps = static_cast<int>(std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp)));
   const size_t smem = per_warp * warps;
-  if (smem > 48 * 1024)
-    SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  if (smem > 48 * 1024) raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
   const i64 blocks = std::max<i64>(1, std::min<i64>((static_cast<i64>(nodes) + warps - 1) / warps, 152 * 64));
   kernel<<<static_cast<unsigned>(blocks), warps * 32, smem, s>>>(nodes, w, args...);
   SIMP_CHECK_LAUNCH();
@@ -896,6 +921,9 @@ void GpuAmg::setup(bool structure_changed) {
   ensure(main_);
   for (auto& w : extra_) ensure(*w);
   ready_ = true;
+  // captured iteration bodies stay valid across reuse setups: their launches
+  // take only workspace and level pointers, which a reuse setup keeps
+  if (!reuse) ++epoch_;
   stats.reused = reuse;
   compute_stats();
   SIMP_CUDA(cudaStreamSynchronize(stream));
@@ -936,27 +964,26 @@ void GpuAmg::smooth(SolveWork& w, size_t l, bool zero_guess) {
   bool matrix_free = false;
   if constexpr (std::is_same<T, float>::value) matrix_free = l == 0 && mf.enabled;
   if (zero_guess) {
-    k_cheb_zero<T><<<grid_for(n, 256), 256, 0, stream>>>(n, b, dinv, d, x, static_cast<T>(lv.inv_theta));
+    k_cheb_zero<T><<<grid_for(n, 256), 256, 0, stream>>>(n, b, dinv, d, x, V<T>::cheb(lv));
     SIMP_CHECK_LAUNCH();
   } else if (matrix_free) {
     if constexpr (std::is_same<T, float>::value)
-      mf_cheb_first(mf, lv.nnodes, x, b, r, d, dinv, static_cast<float>(lv.inv_theta), stream);
+      mf_cheb_first(mf, lv.nnodes, x, b, r, d, dinv, lv.cheb32.p, stream);
   } else {
-    nb_cheb_first<T>(lv.opA, A, x, b, r, d, dinv, lv.inv_theta, stream);
+    nb_cheb_first<T>(lv.opA, A, x, b, r, d, dinv, V<T>::cheb(lv), stream);
   }
   for (int k = 1; k < opt.degree; ++k) {
     const T* rin = (k == 1 && zero_guess) ? b : r;
     const int add_d = (k == 1 && !zero_guess) ? 1 : 0;
     if (matrix_free) {
       if constexpr (std::is_same<T, float>::value)
-        mf_cheb_step(mf, lv.nnodes, d, rin, r, e, x, dinv, static_cast<float>(lv.c1[k - 1]),
-                     static_cast<float>(lv.c2[k - 1]), add_d, stream);
+        mf_cheb_step(mf, lv.nnodes, d, rin, r, e, x, dinv, lv.cheb32.p + 2 * k - 1, add_d, stream);
     } else {
-      nb_cheb_step<T>(lv.opA, A, d, rin, r, e, x, dinv, lv.c1[k - 1], lv.c2[k - 1], add_d, stream);
+      nb_cheb_step<T>(lv.opA, A, d, rin, r, e, x, dinv, V<T>::cheb(lv) + 2 * k - 1, add_d, stream);
     }
     std::swap(d, e);
   }
-  if (opt.degree == 1 && !zero_guess) nb_cheb_step<T>(lv.opA, A, d, r, r, e, x, dinv, 0.0, 0.0, 1, stream);
+  if (opt.degree == 1 && !zero_guess) nb_cheb_step<T>(lv.opA, A, d, r, r, e, x, dinv, V<T>::cheb(lv) + 1, 1, stream);
 }
 
 template <class T>
@@ -1002,16 +1029,87 @@ void GpuAmg::apply(SolveWork& w, const double* r, double* z) {
 // Preconditioned CG on A x = b (FP64 operator and vectors) from the guess in
 // x; `restarts` follows the reference's true-residual restarts.  Stops when
 // the recursive residual reaches `target` or the iteration `budget` is spent.
-GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x, double target, int budget,
+// PCG iteration k > 1, second half of k - 1 and first half of k: z = M r,
+// beta, p = z + beta p (and p's double-float split), then q = A p, alpha,
+// x += alpha p, r -= alpha q, ||r||^2 -- no host value in between.
+void GpuAmg::pcg_tail(SolveWork& w, float2* psplit) {
+  const i32 n = levels.front()->n;
+  const cudaStream_t stream = w.stream;
+  PcgScalars* sc = reinterpret_cast<PcgScalars*>(w.scal.p + 8);
+  apply(w, w.pr.p, w.pz.p);
+  k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(w.pr.p, w.pz.p, n, w.part.p);
+  SIMP_CHECK_LAUNCH();
+  k_pcg_beta<<<1, kRedThreads, 0, stream>>>(w.part.p, kRedBlocks, sc);
+  SIMP_CHECK_LAUNCH();
+  k_pcg_direction<<<grid_for(n, 256), 256, 0, stream>>>(w.pp.p, w.pz.p, n, sc, psplit);
+  SIMP_CHECK_LAUNCH();
+}
+
+void GpuAmg::pcg_head(SolveWork& w, double* x, bool split_ready) {
+  const i32 n = levels.front()->n;
+  const cudaStream_t stream = w.stream;
+  PcgScalars* sc = reinterpret_cast<PcgScalars*>(w.scal.p + 8);
+  op0(w, w.pp.p, w.pq.p, nullptr, split_ready);
+  k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(w.pp.p, w.pq.p, n, w.part.p);
+  SIMP_CHECK_LAUNCH();
+  k_pcg_alpha<<<1, kRedThreads, 0, stream>>>(w.part.p, kRedBlocks, sc);
+  SIMP_CHECK_LAUNCH();
+  k_pcg_update<<<kRedBlocks, kRedThreads, 0, stream>>>(x, w.pr.p, w.pp.p, w.pq.p, n, sc, w.part.p);
+  SIMP_CHECK_LAUNCH();
+  k_reduce_final<<<1, kRedThreads, 0, stream>>>(w.part.p, kRedBlocks, &sc->rr, 0);
+  SIMP_CHECK_LAUNCH();
+}
+
+// pcg_tail + pcg_head as one graph launch: captured on the first use after a
+// setup (thread-local capture, so other threads' solves go on), then
+// replayed; every pointer is the workspace's, x included (w.px).
+void GpuAmg::pcg_body(SolveWork& w, double* x, float2* psplit) {
+  if (w.body && w.body_epoch == epoch_) {
+    SIMP_CUDA(cudaGraphLaunch(w.body, w.stream));
+    g_launches.fetch_add(w.body_kernels, std::memory_order_relaxed);
+    return;
+  }
+  if (w.body) {
+    SIMP_CUDA(cudaGraphExecDestroy(w.body));
+    w.body = nullptr;
+  }
+  SIMP_CUDA(cudaStreamBeginCapture(w.stream, cudaStreamCaptureModeThreadLocal));
+  const int64_t before = t_launches;
+  cudaGraph_t graph = nullptr;
+  try {
+    pcg_tail(w, psplit);
+    pcg_head(w, x, psplit != nullptr);
+  } catch (...) {
+    cudaStreamEndCapture(w.stream, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  const int64_t kernels = t_launches - before;
+  SIMP_CUDA(cudaStreamEndCapture(w.stream, &graph));
+  const cudaError_t e = cudaGraphInstantiate(&w.body, graph, 0);
+  cudaGraphDestroy(graph);
+  SIMP_CUDA(e);
+  // the captured launches ran nothing: count them when the graph runs
+  g_launches.fetch_sub(kernels, std::memory_order_relaxed);
+  w.body_kernels = kernels;
+  w.body_epoch = epoch_;
+  SIMP_CUDA(cudaGraphLaunch(w.body, w.stream));
+  g_launches.fetch_add(kernels, std::memory_order_relaxed);
+}
+
+GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x_out, double target, int budget,
                               bool restarts, double bnorm) {
   Level& f = *levels.front();
   const i32 n = f.n;
   const cudaStream_t stream = w.stream;
+  // the iterate lives in the workspace while CG runs (a fixed address for
+  // the captured iteration body)
+  w.px.alloc(static_cast<size_t>(n));
+  double* x = w.px.p;
+  SIMP_CUDA(cudaMemcpyAsync(x, x_out, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   DBuf<double>& pr = w.pr;
   DBuf<double>& pz = w.pz;
   DBuf<double>& pp = w.pp;
-  DBuf<double>& pq = w.pq;
-  DBuf<double>& part = w.part;
   PcgResult res;
   PcgScalars* sc = reinterpret_cast<PcgScalars*>(w.scal.p + 8);
   static_assert(sizeof(PcgScalars) <= 8 * sizeof(double), "scalar block");
@@ -1040,16 +1138,17 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x, double t
     }
     bool conv = false;
     p_split = false;
+    bool first = true;
     while (total < budget) {
-      op0(w, pp.p, pq.p, nullptr, p_split);
-      k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(pp.p, pq.p, n, part.p);
-      SIMP_CHECK_LAUNCH();
-      k_pcg_alpha<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, sc);
-      SIMP_CHECK_LAUNCH();
-      k_pcg_update<<<kRedBlocks, kRedThreads, 0, stream>>>(x, pr.p, pp.p, pq.p, n, sc, part.p);
-      SIMP_CHECK_LAUNCH();
-      k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, &sc->rr, 0);
-      SIMP_CHECK_LAUNCH();
+      if (first) {
+        pcg_head(w, x, false);
+        first = false;
+      } else if (opt.graphs) {
+        pcg_body(w, x, psplit);
+      } else {
+        pcg_tail(w, psplit);
+        pcg_head(w, x, p_split);
+      }
       PcgScalars h{};
       SIMP_CUDA(cudaMemcpyAsync(&h, sc, sizeof(h), cudaMemcpyDeviceToHost, stream));
       SIMP_CUDA(cudaStreamSynchronize(stream));
@@ -1063,13 +1162,6 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x, double t
       ++total;
       rnorm = std::sqrt(h.rr);
       if (rnorm <= target) { conv = true; break; }
-      apply(pr.p, pz.p);
-      k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(pr.p, pz.p, n, part.p);
-      SIMP_CHECK_LAUNCH();
-      k_pcg_beta<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, sc);
-      SIMP_CHECK_LAUNCH();
-      k_pcg_direction<<<grid_for(n, 256), 256, 0, stream>>>(pp.p, pz.p, n, sc, psplit);
-      SIMP_CHECK_LAUNCH();
       p_split = psplit != nullptr;
     }
     if (!restarts) {
@@ -1087,6 +1179,7 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x, double t
   }
   if (!res.converged && rec_conv) res.converged = true;
   res.iterations = total;
+  SIMP_CUDA(cudaMemcpyAsync(x_out, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   return res;
 }
 

@@ -35,11 +35,12 @@ struct AmgOptions {
   double rtol = 1.0e-12;
   int maxit = 1000;
   int precision = 0;  // 0 FP64, 1 mixed
+  bool graphs = true; // PCG iterations after the first as one CUDA graph launch
 };
 
 struct DevPattern {
   DBuf<i32> ptr, nbr, off;
-  void upload(const NodePattern& p);
+  void upload(const NodePattern& p, cudaStream_t s = 0);
   NodeView view() const { return {ptr.p, nbr.p, off.p}; }
 };
 
@@ -83,6 +84,8 @@ struct Level {
   NbOp opA, opP, opR;
   DBuf<double> dinv64;
   DBuf<float> dinv32;
+  DBuf<double> cheb64;  // Chebyshev coefficients for the kernels: [1 / theta, c1_0, c2_0, ..., 0, 0]
+  DBuf<float> cheb32;
   double lambda = 0.0;
   std::vector<double> null;  // near-null space, n x m row-major (host)
   // transfer to the next level
@@ -133,6 +136,12 @@ struct SolveWork {
   std::vector<LevelWork> lv;
   DBuf<double> part, scal, pr, pz, pp, pq, ctmp;
   DBuf<float2> xsplit;  // op0's input as (hi, lo) pairs (mixed mode)
+  // PCG iteration body (V-cycle, direction, operator, update) captured as a
+  // CUDA graph on this workspace's buffers; valid for one hierarchy epoch
+  DBuf<double> px;      // the iterate (the caller's x is copied in and out)
+  cudaGraphExec_t body = nullptr;
+  uint64_t body_epoch = 0;
+  int64_t body_kernels = 0;
   SolveWork() = default;
   SolveWork(const SolveWork&) = delete;
   SolveWork& operator=(const SolveWork&) = delete;
@@ -225,6 +234,12 @@ class GpuAmg {
   double dot(const double* a, const double* b, i64 n) { return dot(work(0), a, b, n); }
   PcgResult pcg(SolveWork& w, const double* b, double* x, double target, int budget, bool restarts,
                 double bnorm);
+  // the iterations after the first: [V-cycle, beta, direction, operator,
+  // alpha, update] -- launched one by one, or as w's captured graph
+  void pcg_tail(SolveWork& w, float2* psplit);
+  void pcg_head(SolveWork& w, double* x, bool split_ready);
+  void pcg_body(SolveWork& w, double* x, float2* psplit);
+  uint64_t epoch_ = 1;  // bumped by every setup: captured graphs are stale
   void compute_stats();
 };
 

@@ -328,8 +328,7 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
     for (double& c : C) c = -c;
     cten.upload(C, s);
     const size_t smem = sizeof(double) * C.size();
-    SIMP_CUDA(cudaFuncSetAttribute(k_assemble_geometric, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem)));
+    raise_dynamic_smem(reinterpret_cast<const void*>(k_assemble_geometric), smem);
     k_assemble_geometric<<<grid_for(l0.nnodes, 128), 128, smem, s>>>(g, l0.nnodes, l0.d_first.p, p.gnode.p,
                                                                     p.cmask.p, l0.d_apat.view(), l0.a.ptr.p,
                                                                     cten.p, ufull.p, ss.p, gval.p);

@@ -32,6 +32,7 @@ AmgOptions convert(const simp_solver_options* o) {
   a.rtol = o->iterative_tolerance;
   a.maxit = o->max_iterations > 0 ? o->max_iterations : 1000;
   a.precision = o->precision;
+  a.graphs = o->cuda_graphs != 0;
   return a;
 }
 
@@ -112,6 +113,7 @@ void simp_default_options(simp_solver_options* o) {
   o->max_iterations = 0;
   o->precision = SIMP_PRECISION_FP64;
   o->device = 0;
+  o->cuda_graphs = 1;
 }
 
 int simp_ctx_create(const simp_solver_options* opts, simp_ctx** out) {
@@ -254,14 +256,14 @@ void factorize_impl(simp_ctx* ctx, int32_t n, const int32_t* rowptr, const int32
       l0.nnodes = static_cast<i32>(first.size()) - 1;
       l0.first = first;
       l0.apat = std::move(pat);
-      l0.d_first.upload(l0.first);
-      l0.d_node_of.upload(node_of_unknowns(l0.first));
-      l0.d_apat.upload(l0.apat);
-      l0.d_self.upload(pattern_self_slots(l0.apat));
+      l0.d_first.upload(l0.first, amg.stream);
+      l0.d_node_of.upload(node_of_unknowns(l0.first), amg.stream);
+      l0.d_apat.upload(l0.apat, amg.stream);
+      l0.d_self.upload(pattern_self_slots(l0.apat), amg.stream);
       l0.a.rows = l0.a.cols = n;
       l0.a.nnz = nnz;
-      l0.a.ptr.upload(rowptr, static_cast<size_t>(n) + 1);
-      l0.a.col.upload(colidx, static_cast<size_t>(nnz));
+      l0.a.ptr.upload(rowptr, static_cast<size_t>(n) + 1, amg.stream);
+      l0.a.col.upload(colidx, static_cast<size_t>(nnz), amg.stream);
       l0.null = rigid_body_modes(ctx->dim, ctx->ndpn, ctx->coords, ctx->num_nodes, ctx->unknowns);
     }
     Level& l0 = *amg.levels.front();
@@ -401,10 +403,10 @@ static void copy_level_matrix(GpuAmg& amg, int level, int32_t* rows, int64_t* nn
   const Level& lv = *amg.levels[level];
   if (rows) *rows = lv.n;
   if (nnz) *nnz = lv.a.nnz;
-  if (rowptr) lv.a.ptr.download(rowptr, static_cast<size_t>(lv.n) + 1);
-  if (col) lv.a.col.download(col, static_cast<size_t>(lv.a.nnz));
-  if (val) lv.a.v64.download(val, static_cast<size_t>(lv.a.nnz));
-  SIMP_CUDA(cudaDeviceSynchronize());
+  if (rowptr) lv.a.ptr.download(rowptr, static_cast<size_t>(lv.n) + 1, amg.stream);
+  if (col) lv.a.col.download(col, static_cast<size_t>(lv.a.nnz), amg.stream);
+  if (val) lv.a.v64.download(val, static_cast<size_t>(lv.a.nnz), amg.stream);
+  SIMP_CUDA(cudaStreamSynchronize(amg.stream));
 }
 
 int simp_level_aggregates(simp_ctx* ctx, int32_t level, int32_t* agg, int32_t* count) {
@@ -438,10 +440,10 @@ int simp_level_prolongator(simp_ctx* ctx, int32_t level, int32_t* rows, int32_t*
     if (rows) *rows = lv.p.rows;
     if (cols) *cols = lv.p.cols;
     if (nnz) *nnz = lv.p.nnz;
-    if (rowptr) lv.p.ptr.download(rowptr, static_cast<size_t>(lv.p.rows) + 1);
-    if (col) lv.p.col.download(col, static_cast<size_t>(lv.p.nnz));
-    if (val) lv.p.v64.download(val, static_cast<size_t>(lv.p.nnz));
-    SIMP_CUDA(cudaDeviceSynchronize());
+    if (rowptr) lv.p.ptr.download(rowptr, static_cast<size_t>(lv.p.rows) + 1, amg.stream);
+    if (col) lv.p.col.download(col, static_cast<size_t>(lv.p.nnz), amg.stream);
+    if (val) lv.p.v64.download(val, static_cast<size_t>(lv.p.nnz), amg.stream);
+    SIMP_CUDA(cudaStreamSynchronize(amg.stream));
   });
 }
 
@@ -685,10 +687,10 @@ int simp_filter_forward(simp_problem* p, const double* x, double* y) {
     GpuProblem& g = *p->p;
     const size_t ne = static_cast<size_t>(g.ne);
     DBuf<double> a, b(ne);
-    a.upload(x, ne);
+    a.upload(x, ne, g.amg.stream);
     g.filter_forward(a.p, b.p);
-    b.download(y, ne);
-    SIMP_CUDA(cudaDeviceSynchronize());
+    b.download(y, ne, g.amg.stream);
+    SIMP_CUDA(cudaStreamSynchronize(g.amg.stream));
   });
 }
 
@@ -698,10 +700,10 @@ int simp_filter_adjoint(simp_problem* p, const double* v, double* gout) {
     GpuProblem& g = *p->p;
     const size_t ne = static_cast<size_t>(g.ne);
     DBuf<double> a, b(ne);
-    a.upload(v, ne);
+    a.upload(v, ne, g.amg.stream);
     g.filter_adjoint(a.p, b.p);
-    b.download(gout, ne);
-    SIMP_CUDA(cudaDeviceSynchronize());
+    b.download(gout, ne, g.amg.stream);
+    SIMP_CUDA(cudaStreamSynchronize(g.amg.stream));
   });
 }
 
@@ -713,13 +715,14 @@ int simp_problem_kff(simp_problem* p, const double* scale, int32_t* rowptr, int3
     if (val) {
       if (!scale) throw Error(kBadInput, "simp_problem_kff: values need element factors");
       DBuf<double> s;
-      s.upload(scale, static_cast<size_t>(g.ne));
+      s.upload(scale, static_cast<size_t>(g.ne), g.amg.stream);
       g.assemble(s.p, true);
-      l0.a.v64.download(val, static_cast<size_t>(l0.a.nnz));
+      l0.a.v64.download(val, static_cast<size_t>(l0.a.nnz), g.amg.stream);
+      SIMP_CUDA(cudaStreamSynchronize(g.amg.stream));
     }
-    if (rowptr) l0.a.ptr.download(rowptr, static_cast<size_t>(l0.n) + 1);
-    if (col) l0.a.col.download(col, static_cast<size_t>(l0.a.nnz));
-    SIMP_CUDA(cudaDeviceSynchronize());
+    if (rowptr) l0.a.ptr.download(rowptr, static_cast<size_t>(l0.n) + 1, g.amg.stream);
+    if (col) l0.a.col.download(col, static_cast<size_t>(l0.a.nnz), g.amg.stream);
+    SIMP_CUDA(cudaStreamSynchronize(g.amg.stream));
   });
 }
 

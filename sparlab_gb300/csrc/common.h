@@ -39,9 +39,11 @@ struct Error : std::runtime_error {
       throw ::simp::Error(::simp::kCudaError, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-// Kernel launches are counted (the library's own kernels only).
+// Kernel launches are counted (the library's own kernels only); the
+// per-thread count lets a stream capture tell how many kernels it recorded.
 extern std::atomic<int64_t> g_launches;
-#define SIMP_LAUNCHED() (::simp::g_launches.fetch_add(1, std::memory_order_relaxed))
+extern thread_local int64_t t_launches;
+#define SIMP_LAUNCHED() (++::simp::t_launches, ::simp::g_launches.fetch_add(1, std::memory_order_relaxed))
 #define SIMP_CHECK_LAUNCH()             \
   do {                                  \
     SIMP_LAUNCHED();                    \
@@ -93,6 +95,12 @@ struct DBuf {
   }
   size_t bytes() const { return n * sizeof(T); }
 };
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` and never
+// lowers it: the limit is one value per kernel, shared by every host thread,
+// so a thread that set a smaller value could make another thread's larger
+// launch fail between its set and its launch.
+void raise_dynamic_smem(const void* kernel, size_t bytes);
 
 // dst = a device copy of src (same length)
 template <class T>

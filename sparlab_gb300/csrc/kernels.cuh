@@ -219,9 +219,10 @@ __global__ void k_pcg_direction(double* __restrict__ p, const double* __restrict
 // zero guess: d = dinv b / theta ; x = d
 template <class TX>
 __global__ void k_cheb_zero(i64 n, const TX* __restrict__ b, const TX* __restrict__ dinv,
-                            TX* __restrict__ d, TX* __restrict__ x, TX inv_theta) {
+                            TX* __restrict__ d, TX* __restrict__ x, const TX* __restrict__ inv_theta) {
+  const TX it = *inv_theta;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
-    const TX di = dinv[i] * b[i] * inv_theta;
+    const TX di = dinv[i] * b[i] * it;
     d[i] = di;
     x[i] = di;
   }

@@ -95,8 +95,8 @@ __global__ void __launch_bounds__(256) k_mf_apply(MfView m, i32 nodes, const TX*
 __global__ void __launch_bounds__(256) k_mf_cheb_step(MfView m, i32 nodes, const float* __restrict__ d,
                                                       const float* __restrict__ r_in, float* __restrict__ r,
                                                       float* __restrict__ dn, float* __restrict__ x,
-                                                      const float* __restrict__ dinv, float c1, float c2,
-                                                      int add_d) {
+                                                      const float* __restrict__ dinv,
+                                                      const float* __restrict__ c12, int add_d) {
   __shared__ float ks[24 * 24];
   const int ed = m.dim == 3 ? 24 : 8;
   for (int k = threadIdx.x; k < ed * ed; k += blockDim.x) ks[k] = m.ke[k];
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(256) k_mf_cheb_step(MfView m, i32 nodes, const
     const i64 row = static_cast<i64>(I) * m.dim + k;
     const float ri = r_in[row] - out[k];
     r[row] = ri;
-    const float di = c1 * d[row] + c2 * dinv[row] * ri;
+    const float di = c12[0] * d[row] + c12[1] * dinv[row] * ri;
     dn[row] = di;
     float xi = x[row];
     if (add_d) xi = xi + d[row];
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256) k_mf_cheb_step(MfView m, i32 nodes, const
 __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, const float* __restrict__ x,
                                                        const float* __restrict__ b, float* __restrict__ r,
                                                        float* __restrict__ d, const float* __restrict__ dinv,
-                                                       float inv_theta) {
+                                                       const float* __restrict__ inv_theta) {
   __shared__ float ks[24 * 24];
   const int ed = m.dim == 3 ? 24 : 8;
   for (int k = threadIdx.x; k < ed * ed; k += blockDim.x) ks[k] = m.ke[k];
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
     const i64 row = static_cast<i64>(I) * m.dim + k;
     const float ri = b[row] - out[k];
     r[row] = ri;
-    d[row] = dinv[row] * ri * inv_theta;
+    d[row] = dinv[row] * ri * *inv_theta;
   }
 }
 
@@ -165,7 +165,7 @@ struct MfArgs {
   float* dn;          // mode 3: new direction; mode 4: d out
   float* xs;          // mode 3: smoothed iterate (updated)
   const float* dinv;  // mode 3/4
-  float c1, c2, inv_theta;
+  const float* coef;  // mode 3: (c1, c2); mode 4: 1 / theta (device memory)
   int add_d;
 };
 
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
         const float ri = a.b[row] - o[k];
         a.r[row] = ri;
         const float dv = a.x[row];
-        const float di = a.c1 * dv + a.c2 * a.dinv[row] * ri;
+        const float di = a.coef[0] * dv + a.coef[1] * a.dinv[row] * ri;
         a.dn[row] = di;
         float xi = a.xs[row];
         if (a.add_d) xi = xi + dv;
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
       } else {
         const float ri = a.b[row] - o[k];
         a.r[row] = ri;
-        a.dn[row] = a.dinv[row] * ri * a.inv_theta;
+        a.dn[row] = a.dinv[row] * ri * a.coef[0];
       }
     }
   }

@@ -97,14 +97,17 @@ __device__ __forceinline__ TX rows_dot(i32 row, int lane, bool valid, const i32*
   return s;
 }
 
-// Chebyshev step: r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ d]) + dn
+// Chebyshev step: r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ d]) + dn,
+// (c1, c2) = c12[0..1] in device memory (the level's coefficients change with
+// every setup; a captured launch keeps reading them)
 template <int VS, int B, class T>
 __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __restrict__ node_of, NodeView pat,
                                                         const i32* __restrict__ rowptr, const i32* __restrict__ col,
                                                         const T* __restrict__ val, const T* __restrict__ d,
                                                         const T* __restrict__ r_in, T* __restrict__ r,
                                                         T* __restrict__ dn, T* __restrict__ x,
-                                                        const T* __restrict__ dinv, T c1, T c2, int add_d) {
+                                                        const T* __restrict__ dinv, const T* __restrict__ c12,
+                                                        int add_d) {
   const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
   const i32 row = static_cast<i32>(t / VS);
   const int lane = static_cast<int>(t % VS);
@@ -113,7 +116,7 @@ __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __r
   if (valid && lane == 0) {
     const T ri = r_in[row] - s;
     r[row] = ri;
-    const T di = c1 * d[row] + c2 * dinv[row] * ri;
+    const T di = c12[0] * d[row] + c12[1] * dinv[row] * ri;
     dn[row] = di;
     T xi = x[row];
     if (add_d) xi = xi + d[row];
@@ -121,13 +124,14 @@ __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __r
   }
 }
 
-// r = b - A x ; d = dinv r / theta
+// r = b - A x ; d = dinv r / theta (1 / theta = *inv_theta, device memory)
 template <int VS, int B, class T>
 __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __restrict__ node_of, NodeView pat,
                                                          const i32* __restrict__ rowptr, const i32* __restrict__ col,
                                                          const T* __restrict__ val, const T* __restrict__ x,
                                                          const T* __restrict__ b, T* __restrict__ r,
-                                                         T* __restrict__ d, const T* __restrict__ dinv, T inv_theta) {
+                                                         T* __restrict__ d, const T* __restrict__ dinv,
+                                                         const T* __restrict__ inv_theta) {
   const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
   const i32 row = static_cast<i32>(t / VS);
   const int lane = static_cast<int>(t % VS);
@@ -136,7 +140,7 @@ __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __
   if (valid && lane == 0) {
     const T ri = b[row] - s;
     r[row] = ri;
-    d[row] = dinv[row] * ri * inv_theta;
+    d[row] = dinv[row] * ri * *inv_theta;
   }
 }
 

@@ -451,7 +451,7 @@ void GpuProblem::assemble_into(const double* elem, const double* scale, bool exa
   const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
   const size_t smem = assemble_smem(d.dim);
   auto kernel = exact ? k_assemble_tiles<true, false> : k_assemble_tiles<false, false>;
-  SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
   kernel<<<blocks, offsets * kAsmTile, smem, stream>>>(grid_of(d), l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
                                                        nmask.p, l0.d_apat.view(), l0.a.ptr.p, elem, scale, nullptr,
                                                        nullptr, v64, hi, lo);
@@ -466,7 +466,7 @@ void GpuProblem::assemble(const double* scale, bool exact) {
   const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
   const size_t smem = assemble_smem(d.dim);
   auto launch = [&](auto kernel, const float* sh, const float* sl, double* v64, float* hi, float* lo) {
-    SIMP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
     kernel<<<blocks, offsets * kAsmTile, smem, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p, nmask.p,
                                                               l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale, sh, sl,
                                                               v64, hi, lo);

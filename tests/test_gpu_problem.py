@@ -344,3 +344,25 @@ def test_projection_variants_match_oracle():
             np.testing.assert_allclose(rec[key + "_density"], ev["rho"], atol=1e-14)
     assert rec["compliance_eroded"] > rec["compliance_intermediate"] > rec["compliance_dilated"]
     gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cuda_graph_iterations_match_plain_launches(precision):
+    """The PCG iterations replayed as a captured CUDA graph compute what the
+    same kernels launched one by one compute, across setups (re-capture) and
+    concurrent load cases (one graph per workspace)."""
+    spec = P.q4_cantilever_600x200()
+    spec.nx, spec.ny, spec.lx, spec.ly = 90, 30, 90.0, 30.0
+    spec.fixed = P.clamp_left(spec)
+    loads = []
+    for i, j in enumerate((8, 15, 22)):
+        loads.append(P.point_load(spec, [spec.node_index(90, j)], (0.3 * i, -1.0)))
+    spec.loads = np.stack(loads)
+    spec.rtol = 1e-10
+    recs = {}
+    for graphs in (0, 1):
+        gpu = GpuSimpProblem(spec, precision=precision, cuda_graphs=graphs)
+        recs[graphs] = [(r.compliance, r.linear_iterations) for r in
+                        TopologyOptimizer(gpu, max_iterations=4, change_tolerance=0).run()]
+        gpu.close()
+    assert recs[0] == recs[1]
