@@ -681,7 +681,10 @@ def run_own(args):
                    "nnz_kff": prob.nnz, "precision": args.precision, "warm_start": args.warm,
                    "replicas": world, "load_cases": int(spec.loads.shape[0]),
                    "load_case_solves": "concurrent" if together else "sequential",
-                   "l2": "working set (K_ff %.2f GB) larger than L2" % (nnz * 12 / 1e9),
+                   "l2": ("working set (K_ff %.2f GB) larger than the 129 MB L2" % (nnz * 12 / 1e9)
+                          if nnz * 12 > 129e6 else
+                          "working set (K_ff %.3f GB) fits in the 129 MB L2; not flushed between steps"
+                          % (nnz * 12 / 1e9)),
                    "amg_levels": st["num_levels"],
                    "operator_complexity": round(st["operator_complexity"], 6),
                    "cg_iterations_per_step": [r.linear_iterations for r in recs],
