@@ -98,6 +98,10 @@ struct Level {
   WarpRows wr_p, wr_ap, wr_rap;
   DevPattern d_ppat, d_rpat, d_appat;
   DBuf<i32> d_r_to_p, d_sym_t;
+  // per P slot: its contributors, the A slots of its row whose neighbour is
+  // in its aggregate, as (block offset in the A row, first P-hat value)
+  DBuf<i32> d_pc_ptr;
+  DBuf<int2> d_pc;
   DevCsr p, r, ap;
   DBuf<double> raw64;
   DBuf<float> raw32;

@@ -355,5 +355,54 @@ __global__ void __launch_bounds__(256) k_prolongator_rows(
   }
 }
 
+// The same product by output entry, where every fine node has B0 unknowns
+// and every aggregate B1: entry (ka, c) of fine node I's P row is slot
+// s = c / B1, column j = c % B1; its contributors are the slots t of I's A
+// row whose neighbour J lies in slot s's aggregate, ascending t, each stored
+// as (offset of J's block in the A row, first P-hat value of J's rows) when
+// the pattern is built.  Each entry sums its contributions in the warp
+// kernel's order (t ascending, then kb) with the same arithmetic, so P is
+// that kernel's bit for bit, without its per-neighbour passes and barriers.
+template <class T, bool EXACT, int B0, int B1>
+__global__ void __launch_bounds__(256) k_prolongator_gather(
+    i32 nodes, const i32* __restrict__ agg, const i32* __restrict__ arow, const T* __restrict__ aval, NodeView p,
+    const i32* __restrict__ prow, T* __restrict__ pval, const i32* __restrict__ phat_ptr,
+    const T* __restrict__ phat, const double* __restrict__ dinv, double omega, const i32* __restrict__ pc_ptr,
+    const int2* __restrict__ pc) {
+  const int lane = threadIdx.x & 31;
+  const i64 nwarps = (static_cast<i64>(gridDim.x) * blockDim.x) >> 5;
+  for (i64 I = (blockIdx.x * static_cast<i64>(blockDim.x) + threadIdx.x) >> 5; I < nodes; I += nwarps) {
+    const i32 r0 = B0 * static_cast<i32>(I);
+    const i32 ps = p.ptr[I], ns = p.ptr[I + 1] - ps;
+    if (ns == 0) continue;
+    const i32 L = ns * B1;
+    const i32 gi = agg[I];
+    for (i32 q = lane; q < B0 * L; q += 32) {
+      const i32 ka = q / L, c = q - ka * L;
+      const i32 s = c / B1, j = c - s * B1;
+      const i32 gs = ps + s;
+      const T* ak = aval + arow[r0 + ka];
+      T v = T(0);
+      for (i32 k = pc_ptr[gs]; k < pc_ptr[gs + 1]; ++k) {
+        const int2 e = pc[k];
+        const T* av = ak + e.x;
+        const T* ph = phat + e.y + j;
+#pragma unroll
+        for (int kb = 0; kb < B0; ++kb) v = term<EXACT>(v, av[kb], ph[kb * B1]);
+      }
+      const T scale = static_cast<T>(omega * dinv[r0 + ka]);
+      const bool mine = gi >= 0 && p.nbr[gs] == gi;
+      T out;
+      if constexpr (EXACT) {
+        out = xmul(v, -scale);
+        if (mine) out = xadd(out, phat[phat_ptr[r0 + ka] + j]);
+      } else {
+        out = mine ? fma(v, -scale, phat[phat_ptr[r0 + ka] + j]) : v * -scale;
+      }
+      pval[prow[r0 + ka] + c] = out;
+    }
+  }
+}
+
 }  // namespace
 }  // namespace simp
