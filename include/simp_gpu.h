@@ -45,7 +45,7 @@ extern "C" {
  * the reuse setups in FP32 (level 0 matrix-free on structured grids), the CG
  * operator in double-float arithmetic (K_ff as float pairs, ~2^-44 relative
  * to FP64); CG vectors and scalars, the true-residual restarts and the
- * coarsest dense Cholesky are FP64 in both. */
+ * coarsest dense inverse are FP64 in both. */
 #define SIMP_PRECISION_FP64 0
 #define SIMP_PRECISION_MIXED 1
 

@@ -336,7 +336,6 @@ void GpuAmg::ensure(SolveWork& w) {
   w.part.alloc(kRedBlocks);
   w.scal.alloc(16);
   for (DBuf<double>* b : {&w.pr, &w.pz, &w.pp, &w.pq}) b->alloc(n0);
-  w.ctmp.alloc(static_cast<size_t>(std::max<i32>(nc_, 1)));
   if (mixed()) w.xsplit.alloc(n0);
 }
 
@@ -440,7 +439,11 @@ void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
   DBuf<double> x64(n), y64(n);
   k_fill<double><<<grid_for(n, 256), 256, 0, stream>>>(x64.p, 1.0, n);
   SIMP_CHECK_LAUNCH();
-  auto launch = [&]() { op0(main_, x64.p, y64.p, nullptr); };
+  // In mixed mode the CG writes the operand's hi/lo split inside its
+  // direction update, so the operator kernel runs alone: split once here and
+  // time the operator kernel the same way.
+  op0(main_, x64.p, y64.p, nullptr);
+  auto launch = [&]() { op0(main_, x64.p, y64.p, nullptr, true); };
   for (int k = 0; k < 3; ++k) launch();
   // the timed launches are the profiler's capture window when one is attached
   cudaProfilerStart();
@@ -854,7 +857,8 @@ void GpuAmg::galerkin(size_t l, bool fp32) {
   }
 }
 
-// Dense FP64 Cholesky of the coarsest operator and W = L^-1.
+// Dense FP64 inverse of the coarsest operator by the blocked symmetric sweep
+// (dense.cuh), with the squared Cholesky pivots as the singularity check.
 void GpuAmg::coarse_factorize() {
   Level& lv = *levels.back();
   const i32 n = lv.n;
@@ -867,23 +871,24 @@ void GpuAmg::coarse_factorize() {
   nc_ = n;
   const size_t nn = static_cast<size_t>(n) * n;
   dense_.alloc(nn);
-  inv_t_.alloc(nn);
+  swept_.alloc(nn);
   piv_.alloc(n);
-  SIMP_CUDA(cudaMemsetAsync(dense_.p, 0, nn * sizeof(double), stream));
-  k_dense_from_csr<<<grid_for(n, 128), 128, 0, stream>>>(n, lv.a.ptr.p, lv.a.col.p, lv.a.v64.p, dense_.p);
+  panel_.alloc(2 * static_cast<size_t>(n) * kNB + kNB * kNB);
+  double* pu = panel_.p;
+  double* pv = pu + static_cast<size_t>(n) * kNB;
+  double* pp = pv + static_cast<size_t>(n) * kNB;
+  SIMP_CUDA(cudaMemsetAsync(swept_.p, 0, nn * sizeof(double), stream));
+  k_dense_from_csr<<<grid_for(n, 128), 128, 0, stream>>>(n, lv.a.ptr.p, lv.a.col.p, lv.a.v64.p, swept_.p);
   SIMP_CHECK_LAUNCH();
   SIMP_CUDA(cudaMemsetAsync(dstatus.p, 0, sizeof(int), stream));
+  const int nt = (n + kNB - 1) / kNB;
+  const dim3 tiles(nt, nt);
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int kb = std::min(kNB, n - k0);
-    k_potrf_diag<<<1, 256, 0, stream>>>(dense_.p, n, k0, kb, piv_.p, dstatus.p);
+    k_sweep_pivot<<<(n + kSweepRows - 1) / kSweepRows, 256, 0, stream>>>(swept_.p, n, k0, kb, pu, pv, pp,
+                                                                          piv_.p, dstatus.p);
     SIMP_CHECK_LAUNCH();
-    const int rest = n - k0 - kb;
-    if (rest <= 0) break;
-    k_trsm_panel<<<grid_for(rest, 128), 128, 0, stream>>>(dense_.p, n, k0, kb);
-    SIMP_CHECK_LAUNCH();
-    dim3 grid((rest + 31) / 32, (rest + 31) / 32);
-    k_tile_update<<<grid, 256, 0, stream>>>(dense_.p, n, k0 + kb, k0 + kb, rest, rest, dense_.p, k0,
-                                            dense_.p + k0, 1, n, kb, 1);
+    k_sweep_update<<<tiles, 256, 0, stream>>>(swept_.p, n, k0, kb, pu, pv, pp);
     SIMP_CHECK_LAUNCH();
   }
   int status = 0;
@@ -903,34 +908,17 @@ void GpuAmg::coarse_factorize() {
        << "level, so the model is under-constrained: too few supports, or a part connected to nothing";
     throw Error(kUnderConstrained, os.str());
   }
-  // W = L^-1 into inv_t_ (row-major, lower); W^T into dense_
-  k_identity<<<grid_for(static_cast<i64>(nn), 256), 256, 0, stream>>>(inv_t_.p, n);
-  SIMP_CHECK_LAUNCH();
-  for (int k0 = 0; k0 < n; k0 += kNB) {
-    const int kb = std::min(kNB, n - k0);
-    k_trsm_rows<<<grid_for(k0 + kb, 128), 128, 0, stream>>>(inv_t_.p, dense_.p, n, k0, kb);
-    SIMP_CHECK_LAUNCH();
-    const int rest = n - k0 - kb;
-    if (rest <= 0) break;
-    dim3 grid((k0 + kb + 31) / 32, (rest + 31) / 32);
-    k_tile_update<<<grid, 256, 0, stream>>>(inv_t_.p, n, k0 + kb, 0, rest, k0 + kb, dense_.p, k0,
-                                            inv_t_.p + static_cast<size_t>(k0) * n, n, 1, kb, 0);
-    SIMP_CHECK_LAUNCH();
-  }
-  dim3 tg((n + 31) / 32, (n + 31) / 32), tb(32, 8);
-  k_transpose<<<tg, tb, 0, stream>>>(inv_t_.p, dense_.p, n);
+  k_sweep_finish<<<tiles, 256, 0, stream>>>(swept_.p, dense_.p, n);
   SIMP_CHECK_LAUNCH();
 }
 
-// x = W^T (W b) at the coarsest level, in FP64
+// x = A_c^-1 b at the coarsest level: one GEMV with the FP64 inverse
 template <class T>
 void GpuAmg::coarse_solve(SolveWork& w, size_t l) {
   const int n = nc_;
   const i64 th = static_cast<i64>(n) * 32;
   LevelWork& v = w.lv[l];
-  k_gemv<T, double><<<grid_for(th, 256), 256, 0, w.stream>>>(inv_t_.p, n, V<T>::b(v), w.ctmp.p, 1);
-  SIMP_CHECK_LAUNCH();
-  k_gemv<double, T><<<grid_for(th, 256), 256, 0, w.stream>>>(dense_.p, n, w.ctmp.p, V<T>::x(v), 2);
+  k_gemv<T, T><<<grid_for(th, 256), 256, 0, w.stream>>>(dense_.p, n, V<T>::b(v), V<T>::x(v));
   SIMP_CHECK_LAUNCH();
 }
 

@@ -9,7 +9,7 @@
 // transfers; level 0 matrix-free on structured grids), the Lanczos estimates
 // and the reused-structure Galerkin products in FP32.  CG itself -- its
 // operator, vectors, scalars and the true-residual restarts -- and the
-// coarsest dense Cholesky stay FP64 in both modes, so both stop on the same
+// coarsest dense inverse stay FP64 in both modes, so both stop on the same
 // FP64 residual test.
 #pragma once
 
@@ -138,7 +138,7 @@ struct SolveWork {
   cudaStream_t stream = 0;
   bool own_stream = false;
   std::vector<LevelWork> lv;
-  DBuf<double> part, scal, pr, pz, pp, pq, ctmp;
+  DBuf<double> part, scal, pr, pz, pp, pq;
   DBuf<float2> xsplit;  // op0's input as (hi, lo) pairs (mixed mode)
   // PCG iteration body (V-cycle, direction, operator, update) captured as a
   // CUDA graph on this workspace's buffers; valid for one hierarchy epoch
@@ -222,7 +222,7 @@ class GpuAmg {
  private:
   bool ready_ = false;
   i32 nc_ = 0;
-  DBuf<double> dense_, inv_t_, piv_;
+  DBuf<double> dense_, swept_, piv_, panel_;  // A_c^-1 (full), the sweep's lower triangle, pivots, U/V/P
   SolveWork main_;
   std::vector<std::unique_ptr<SolveWork>> extra_;
 

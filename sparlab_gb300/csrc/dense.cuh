@@ -1,8 +1,18 @@
-// Coarsest-level direct solve in FP64 (src/fem/Multigrid.cpp:749-781, 859-865):
-// blocked right-looking Cholesky A = L L^T, the explicit inverse factor
-// W = L^-1, and the per-cycle solve x = W^T (W b) as two GEMVs, so a V-cycle
-// spends a few microseconds at the coarsest level instead of a sequential
-// triangular sweep.  Row-major n x n storage, lower triangle referenced.
+// Coarsest-level direct solve in FP64 (src/fem/Multigrid.cpp:749-781, 859-865).
+// The reference factors the dense coarse operator (LDL^T) and runs two
+// triangular sweeps per V-cycle.  Here the SPD coarse operator is inverted
+// once per setup by a blocked symmetric sweep (Gauss-Jordan elimination
+// without pivoting, which is stable for SPD matrices because every pivot is a
+// Schur complement's diagonal), and a V-cycle's coarse solve is one GEMV.
+//
+// Sweeping pivot block k of a symmetric M (P = M_kk^-1, U = M_{:,k}, V = U P):
+//   M_ij <- M_ij - V_i U_j^T   (i, j outside k)
+//   M_ik <- V_i,  M_kj <- V_j^T,  M_kk <- -P
+// After all blocks M = -A^-1.  Only the lower triangle is stored and updated
+// (GB300's FP64 rate makes the halved update worth the bookkeeping).  The
+// scalar pivots met inside the pivot blocks are the squared Cholesky pivots
+// (the D of A = L D L^T), recorded for the singularity check.
+// Row-major n x n storage.
 #pragma once
 
 #include "common.h"
@@ -10,153 +20,169 @@
 namespace simp {
 namespace {
 
-constexpr int kNB = 32;  // panel width
+constexpr int kNB = 32;        // pivot block width = update tile width
+constexpr int kSweepRows = 16;  // rows of U and V per block of k_sweep_pivot
 
-// Unblocked Cholesky of the kb x kb diagonal block at (k0, k0).  piv[k0 + j]
-// receives the pivot before its square root; status = 1 on a pivot that is
-// not positive and finite.
-__global__ void __launch_bounds__(256) k_potrf_diag(double* __restrict__ a, int n, int k0, int kb,
-                                                    double* __restrict__ piv, int* __restrict__ status) {
+// One launch per pivot block k0 (width kb <= kNB).  Every block sweeps the
+// pivot block S = M[k0:k0+kb, k0:k0+kb] in shared memory into -S^-1 (the same
+// few dozen microseconds of FP64 latency in every block, in parallel, so the
+// panel needs no second launch), then writes U_i = M[i, k0:k0+kb] and
+// V_i = U_i S^-1 for its rows i outside the block.  Block 0 records the
+// pivots, the status (1 on a pivot that is not positive and finite) and P.
+__global__ void __launch_bounds__(256) k_sweep_pivot(const double* __restrict__ m, int n, int k0, int kb,
+                                                     double* __restrict__ u, double* __restrict__ v,
+                                                     double* __restrict__ pout, double* __restrict__ piv,
+                                                     int* __restrict__ status) {
   __shared__ double s[kNB][kNB + 1];
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    const int i = e / kb, j = e % kb;
-    s[i][j] = a[(size_t)(k0 + i) * n + k0 + j];
+  __shared__ double urow[kNB], trow[kNB];
+  __shared__ double pj;
+  __shared__ double ush[8][kNB];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kNB * kNB; e += blockDim.x) {
+    const int r = e / kNB, c = e % kNB;
+    double val = r == c ? 1.0 : 0.0;
+    if (r < kb && c < kb) val = m[(size_t)(k0 + max(r, c)) * n + k0 + min(r, c)];
+    s[r][c] = val;
   }
   __syncthreads();
   for (int j = 0; j < kb; ++j) {
-    __shared__ double djj;
-    if (threadIdx.x == 0) {
+    if (tid < kNB) {
       const double d = s[j][j];
-      piv[k0 + j] = d;
-      if (!(d > 0.0) || !isfinite(d)) {
-        *status = 1;
-        djj = 1.0;
-      } else {
-        djj = sqrt(d);
+      const bool ok = d > 0.0 && isfinite(d);
+      const double p = ok ? 1.0 / d : 1.0;
+      const double uc = s[j][tid];
+      urow[tid] = uc;
+      trow[tid] = p * uc;
+      if (tid == 0) {
+        pj = p;
+        if (blockIdx.x == 0) {
+          piv[k0 + j] = d;
+          if (!ok) *status = 1;
+        }
       }
-      s[j][j] = djj;
     }
     __syncthreads();
-    for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) s[i][j] /= djj;
-    __syncthreads();
-    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-      const int i = e / kb, c = e % kb;
-      if (c > j && i >= c) s[i][c] -= s[i][j] * s[c][j];
+    for (int e = tid; e < kNB * kNB; e += blockDim.x) {
+      const int r = e / kNB, c = e % kNB;
+      if (r >= kb || c >= kb) continue;
+      if (r != j && c != j) s[r][c] = fma(-urow[r], trow[c], s[r][c]);
+      else if (r != j) s[r][j] = trow[r];
+      else if (c != j) s[j][c] = trow[c];
+      else s[j][j] = -pj;
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    const int i = e / kb, j = e % kb;
-    if (j <= i) a[(size_t)(k0 + i) * n + k0 + j] = s[i][j];
+  // s = -S^-1
+  if (blockIdx.x == 0)
+    for (int e = tid; e < kb * kb; e += blockDim.x) pout[(e / kb) * kNB + e % kb] = -s[e / kb][e % kb];
+  const int warp = tid >> 5, lane = tid & 31;
+  const int i_end = min(n, (blockIdx.x + 1) * kSweepRows);
+  for (int i = blockIdx.x * kSweepRows + warp; i < i_end; i += 8) {
+    if (i >= k0 && i < k0 + kb) continue;
+    double ui = 0.0;
+    if (lane < kb) ui = i >= k0 + kb ? m[(size_t)i * n + k0 + lane] : m[(size_t)(k0 + lane) * n + i];
+    ush[warp][lane] = ui;
+    __syncwarp();
+    double acc = 0.0;
+    for (int d = 0; d < kb; ++d) acc = fma(ush[warp][d], s[d][lane], acc);
+    if (lane < kb) {
+      u[(size_t)i * kNB + lane] = ui;
+      v[(size_t)i * kNB + lane] = -acc;
+    }
+    __syncwarp();
   }
 }
 
-// Panel below the diagonal block: L21 = A21 L11^-T, one thread per row.
-__global__ void __launch_bounds__(128) k_trsm_panel(double* __restrict__ a, int n, int k0, int kb) {
-  __shared__ double l[kNB][kNB + 1];
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    const int i = e / kb, j = e % kb;
-    l[i][j] = j <= i ? a[(size_t)(k0 + i) * n + k0 + j] : 0.0;
+// The update of pivot block k0 over the lower triangle, one 32 x 32 tile
+// (I, J), J <= I, per block: a grid of nt x nt blocks, those above the
+// diagonal return at once.  Reads only U, V, P and its own tile.
+__global__ void __launch_bounds__(256) k_sweep_update(double* __restrict__ m, int n, int k0, int kb,
+                                                      const double* __restrict__ u,
+                                                      const double* __restrict__ v,
+                                                      const double* __restrict__ p) {
+  const int ti = blockIdx.y, tj = blockIdx.x;
+  if (tj > ti) return;
+  const int kt = k0 / kNB;
+  const int r0 = ti * kNB, c0 = tj * kNB;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  __shared__ double vs[kNB][kNB + 1];
+  __shared__ double us[kNB][kNB + 1];
+  if (ti == kt && tj == kt) {
+    for (int q = ty; q < kNB; q += 8)
+      if (q < kb && tx < kb) m[(size_t)(k0 + q) * n + k0 + tx] = -p[q * kNB + tx];
+    return;
+  }
+  if (ti == kt) {  // M_kj <- V_j^T for the columns j of tile J
+    for (int q = ty; q < kNB; q += 8) {
+      const int j = c0 + q;
+      vs[q][tx] = (j < n && tx < kb) ? v[(size_t)j * kNB + tx] : 0.0;
+    }
+    __syncthreads();
+    for (int q = ty; q < kb; q += 8)
+      if (c0 + tx < n) m[(size_t)(k0 + q) * n + c0 + tx] = vs[tx][q];
+    return;
+  }
+  if (tj == kt) {  // M_ik <- V_i for the rows i of tile I
+    for (int q = ty; q < kNB; q += 8) {
+      const int i = r0 + q;
+      if (i < n && tx < kb) m[(size_t)i * n + k0 + tx] = v[(size_t)i * kNB + tx];
+    }
+    return;
+  }
+  for (int q = ty; q < kNB; q += 8) {
+    const int i = r0 + q, j = c0 + q;
+    vs[q][tx] = (i < n && tx < kb) ? v[(size_t)i * kNB + tx] : 0.0;
+    us[q][tx] = (j < n && tx < kb) ? u[(size_t)j * kNB + tx] : 0.0;
   }
   __syncthreads();
-  const int r = k0 + kb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  double x[kNB];
-  double* row = a + (size_t)r * n + k0;
+  const int j = c0 + tx;
+  if (j >= n) return;
 #pragma unroll
-  for (int j = 0; j < kNB; ++j) x[j] = j < kb ? row[j] : 0.0;
+  for (int qq = 0; qq < kNB / 8; ++qq) {
+    const int q = ty + 8 * qq;
+    const int i = r0 + q;
+    if (i >= n || j > i) continue;
+    double acc = 0.0;
 #pragma unroll
-  for (int j = 0; j < kNB; ++j) {
-    if (j < kb) {
-      double v = x[j];
-#pragma unroll
-      for (int c = 0; c < kNB; ++c)
-        if (c < j) v -= x[c] * l[j][c];
-      x[j] = v / l[j][j];
+    for (int d = 0; d < kNB; ++d) acc = fma(vs[q][d], us[tx][d], acc);
+    m[(size_t)i * n + j] -= acc;
+  }
+}
+
+// F = -M mirrored from the lower triangle to full storage: one 32 x 32 tile
+// (I, J), J <= I, per block, written to (I, J) and (J, I).
+__global__ void __launch_bounds__(256) k_sweep_finish(const double* __restrict__ m, double* __restrict__ f,
+                                                      int n) {
+  const int ti = blockIdx.y, tj = blockIdx.x;
+  if (tj > ti) return;
+  const int r0 = ti * kNB, c0 = tj * kNB;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  __shared__ double t[kNB][kNB + 1];
+  for (int q = ty; q < kNB; q += 8) {
+    const int i = r0 + q, j = c0 + tx;
+    t[q][tx] = (i < n && j < n && (ti != tj || j <= i)) ? -m[(size_t)i * n + j] : 0.0;
+  }
+  __syncthreads();
+  for (int q = ty; q < kNB; q += 8) {
+    const int i = r0 + q, j = c0 + tx;
+    if (i < n && j < n) f[(size_t)i * n + j] = ti != tj || tx <= q ? t[q][tx] : t[tx][q];
+    if (ti != tj) {
+      const int i2 = c0 + q, j2 = r0 + tx;
+      if (i2 < n && j2 < n) f[(size_t)i2 * n + j2] = t[tx][q];
     }
   }
-#pragma unroll
-  for (int j = 0; j < kNB; ++j)
-    if (j < kb) row[j] = x[j];
 }
 
-// C[r][c] -= sum_j A[r][j] * B(j, c) over 32 x 32 output tiles, with
-// A(r, j) = a[r * n + ka + j] and B(j, c) = b[j * ldbj + c * ldbc].
-// lower != 0 skips tiles strictly above the diagonal (and entries c > r).
-__global__ void __launch_bounds__(256) k_tile_update(double* __restrict__ cmat, int n, int r0, int c0,
-                                                     int rows, int cols, const double* __restrict__ amat,
-                                                     int ka, const double* __restrict__ bmat, long ldbj,
-                                                     long ldbc, int kb, int lower) {
-  const int tr = blockIdx.y * 32, tc = blockIdx.x * 32;
-  if (tr >= rows || tc >= cols) return;
-  if (lower && r0 + tr + 31 < c0 + tc) return;
-  __shared__ double as[32][kNB + 1];
-  __shared__ double bs[kNB][33];
-  for (int e = threadIdx.x; e < 32 * kNB; e += 256) {
-    const int i = e / kNB, j = e % kNB;
-    const int r = tr + i;
-    as[i][j] = (r < rows && j < kb) ? amat[(size_t)(r0 + r) * n + ka + j] : 0.0;
-    const int jj = e / 32, c = e % 32;
-    bs[jj][c] = (tc + c < cols && jj < kb) ? bmat[(long)jj * ldbj + (long)(c0 + tc + c) * ldbc] : 0.0;
-  }
-  __syncthreads();
-  const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;  // 8 rows of threads x 4 outputs
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int i = ty + 8 * q;
-    const int r = tr + i, c = tc + tx;
-    if (r >= rows || c >= cols) continue;
-    if (lower && r0 + r < c0 + c) continue;
-    double s = 0.0;
-#pragma unroll
-    for (int j = 0; j < kNB; ++j) s += as[i][j] * bs[j][tx];
-    cmat[(size_t)(r0 + r) * n + c0 + c] -= s;
-  }
-}
-
-// Rows [k0, k0+kb) of W = L^-1: forward substitution of the updated right-hand
-// sides with L11, one thread per column c < k0 + kb.
-__global__ void __launch_bounds__(128) k_trsm_rows(double* __restrict__ w, const double* __restrict__ l,
-                                                   int n, int k0, int kb) {
-  __shared__ double lk[kNB][kNB + 1];
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    const int i = e / kb, j = e % kb;
-    lk[i][j] = j <= i ? l[(size_t)(k0 + i) * n + k0 + j] : 0.0;
-  }
-  __syncthreads();
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= k0 + kb) return;
-  double x[kNB];
-#pragma unroll
-  for (int j = 0; j < kNB; ++j) x[j] = j < kb ? w[(size_t)(k0 + j) * n + c] : 0.0;
-#pragma unroll
-  for (int j = 0; j < kNB; ++j) {
-    if (j < kb) {
-      double v = x[j];
-#pragma unroll
-      for (int i = 0; i < kNB; ++i)
-        if (i < j) v -= lk[j][i] * x[i];
-      x[j] = v / lk[j][j];
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < kNB; ++j)
-    if (j < kb) w[(size_t)(k0 + j) * n + c] = x[j];
-}
-
-// y = M x for row-major M: one warp per row; `upper` restricts to c >= r,
-// `lower_only` to c <= r.
+// y = M x for row-major M, one warp per row.
 template <class TX, class TY>
 __global__ void __launch_bounds__(256) k_gemv(const double* __restrict__ m, int n, const TX* __restrict__ x,
-                                              TY* __restrict__ y, int tri) {
+                                              TY* __restrict__ y) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
-  const int lo = tri == 2 ? warp : 0;         // 2: upper triangle (c >= r)
-  const int hi = tri == 1 ? warp + 1 : n;     // 1: lower triangle (c <= r)
   const double* row = m + (size_t)warp * n;
   double s = 0.0;
-  for (int c = lo + lane; c < hi; c += 32) s += row[c] * static_cast<double>(x[c]);
+  for (int c = lane; c < n; c += 32) s += row[c] * static_cast<double>(x[c]);
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) y[warp] = static_cast<TY>(s);
 }
@@ -165,26 +191,6 @@ __global__ void k_dense_from_csr(int n, const i32* __restrict__ ptr, const i32* 
                                  const double* __restrict__ val, double* __restrict__ a) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
     for (i32 k = ptr[r]; k < ptr[r + 1]; ++k) a[(size_t)r * n + col[k]] = val[k];
-}
-
-__global__ void k_identity(double* __restrict__ a, int n) {
-  const size_t total = (size_t)n * n;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
-    a[e] = (e / n == e % n) ? 1.0 : 0.0;
-}
-
-__global__ void k_transpose(const double* __restrict__ a, double* __restrict__ t, int n) {
-  __shared__ double tile[32][33];
-  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
-  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-    const int r = by + j, c = bx + threadIdx.x;
-    tile[j][threadIdx.x] = (r < n && c < n) ? a[(size_t)r * n + c] : 0.0;
-  }
-  __syncthreads();
-  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-    const int r = bx + j, c = by + threadIdx.x;
-    if (r < n && c < n) t[(size_t)r * n + c] = tile[threadIdx.x][j];
-  }
 }
 
 }  // namespace
