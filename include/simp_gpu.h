@@ -68,6 +68,11 @@ typedef struct {
   int32_t cuda_graphs;           /* 1: each PCG iteration after the first is one CUDA graph
                                     launch (captured per workspace after every setup);
                                     0: the same kernels launched one by one */
+  int32_t matrix_free_transfer;  /* MIXED on a 3-D structured grid: 1 applies level 0's
+                                    restriction and prolongation in the V-cycle as
+                                    P^T (I - w A D^-1) and (I - w D^-1 A) P^ with the
+                                    matrix-free operator instead of reading the stored
+                                    R and P; 0 reads them */
 } simp_solver_options;
 
 typedef struct {

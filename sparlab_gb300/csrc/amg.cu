@@ -267,6 +267,43 @@ void mf_residual(const MfOp& mf, i32 nodes, const float* x, float* r, const floa
   SIMP_CHECK_LAUNCH();
 }
 
+// Level-0 transfers of the FP32 cycle without the stored R and P
+// (3-D tiled operator): with P = (I - w D^-1 A) P^ and A, D symmetric,
+//   restriction  b_c = P^T (r - w A D^-1 r)   from x and b (r = b - A x),
+//   prolongation x  += t - w D^-1 A t,  t = P^ x_c.
+// u and t are scratch vectors of the level (n floats).
+void mf_restrict(const MfOp& mf, const Level& lv, const float* x, const float* b, float* r, float* u, float* bc,
+                 cudaStream_t s) {
+  MfArgs a{};
+  a.x = x;
+  a.b = b;
+  a.y = r;
+  a.dn = u;
+  a.dinv = lv.dinv32.p;
+  mf3<6>(mf, a, s);
+  MfArgs c{};
+  c.x = u;
+  c.b = r;
+  c.y = r;
+  c.coef = lv.omega32.p;
+  mf3<7>(mf, c, s);
+  const i64 th = static_cast<i64>(lv.naggs) * 32;
+  k_phat_restrict<6><<<grid_for(th, 256), 256, 0, s>>>(lv.naggs, lv.d_members_ptr.p, lv.d_members.p,
+                                                         lv.phat_ptr.p, lv.phat32.p, r, bc);
+  SIMP_CHECK_LAUNCH();
+}
+
+void mf_prolong(const MfOp& mf, const Level& lv, const float* xc, float* t, float* x, cudaStream_t s) {
+  k_phat_prolong<6><<<grid_for(lv.n, 256), 256, 0, s>>>(lv.n, lv.d_agg.p, lv.phat_ptr.p, lv.phat32.p, xc, t);
+  SIMP_CHECK_LAUNCH();
+  MfArgs a{};
+  a.x = t;
+  a.xs = x;
+  a.dinv = lv.dinv32.p;
+  a.coef = lv.omega32.p;
+  mf3<5>(mf, a, s);
+}
+
 double seconds_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -599,6 +636,8 @@ void GpuAmg::numeric_level(size_t l) {
   const std::vector<float> coef32(coef.begin(), coef.end());
   lv.cheb64.upload(coef, stream);
   lv.cheb32.upload(coef32, stream);
+  const std::vector<float> omega{static_cast<float>(opt.damping / lv.lambda)};
+  lv.omega32.upload(omega, stream);
 }
 
 // Aggregates, tentative prolongator and symbolic patterns of level l -> l+1.
@@ -638,6 +677,23 @@ void GpuAmg::build_transfer(size_t l) {
   if (mixed()) {
     lv.phat32.alloc(t.phat.size());
     convert(lv.phat64.p, lv.phat32.p, static_cast<i64>(t.phat.size()), stream);
+  }
+  lv.mf_transfer = false;
+  if (mixed() && l == 0 && uniform_block(lv.first) == 3 && uniform_block(nv.first) == 6) {
+    std::vector<i32> mptr(static_cast<size_t>(lv.naggs) + 1, 0), members(static_cast<size_t>(lv.nnodes));
+    bool all = true;
+    for (i32 I = 0; I < lv.nnodes; ++I) {
+      if (lv.agg[I] < 0) all = false;
+      else ++mptr[lv.agg[I] + 1];
+    }
+    if (all) {
+      for (i32 g = 0; g < lv.naggs; ++g) mptr[g + 1] += mptr[g];
+      std::vector<i32> fill(mptr.begin(), mptr.end() - 1);
+      for (i32 I = 0; I < lv.nnodes; ++I) members[fill[lv.agg[I]]++] = I;
+      lv.d_members_ptr.upload(mptr, stream);
+      lv.d_members.upload(members, stream);
+      lv.mf_transfer = true;
+    }
   }
   // symbolic patterns
   lv.ppat = pattern_prolongator(lv.apat, lv.agg, lv.naggs);
@@ -1035,7 +1091,18 @@ void GpuAmg::cycle(SolveWork& w, size_t l) {
   const cudaStream_t stream = w.stream;
   smooth<T>(w, l, true);
   bool matrix_free = false;
-  if constexpr (std::is_same<T, float>::value) matrix_free = l == 0 && mf.enabled;
+  if constexpr (std::is_same<T, float>::value) {
+    matrix_free = l == 0 && mf.enabled;
+    if (matrix_free && mf.dim == 3 && lv.mf_transfer && opt.mf_transfer) {
+      // residual, restriction, coarse cycle and prolongation without the
+      // stored R and P (d32 and e32 are free between the smoothing sweeps)
+      mf_restrict(mf, lv, v.x32.p, v.b32.p, v.r32.p, v.d32.p, nv.b32.p, stream);
+      cycle<T>(w, l + 1);
+      mf_prolong(mf, lv, nv.x32.p, v.e32.p, v.x32.p, stream);
+      smooth<T>(w, l, false);
+      return;
+    }
+  }
   if (matrix_free) {  // residual
     if constexpr (std::is_same<T, float>::value)
       mf_residual(mf, lv.nnodes, V<T>::x(v), V<T>::r(v), V<T>::b(v), stream);

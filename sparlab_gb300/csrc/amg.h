@@ -36,6 +36,7 @@ struct AmgOptions {
   int maxit = 1000;
   int precision = 0;  // 0 FP64, 1 mixed
   bool graphs = true; // PCG iterations after the first as one CUDA graph launch
+  bool mf_transfer = true;  // level-0 R and P of the FP32 cycle applied matrix-free
 };
 
 struct DevPattern {
@@ -94,6 +95,12 @@ struct Level {
   DBuf<i32> d_agg, phat_ptr;
   DBuf<double> phat64;
   DBuf<float> phat32;
+  // matrix-free transfers of level 0 (FP32 cycle, 3-D grid, 3 -> 6 unknowns
+  // per node): the aggregates' member nodes (CSR, ascending) and the
+  // prolongator damping w = damping / lambda in device memory
+  bool mf_transfer = false;
+  DBuf<i32> d_members_ptr, d_members;
+  DBuf<float> omega32;
   NodePattern ppat, rpat, appat;
   WarpRows wr_p, wr_ap, wr_rap;
   DevPattern d_ppat, d_rpat, d_appat;

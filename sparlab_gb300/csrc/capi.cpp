@@ -33,6 +33,7 @@ AmgOptions convert(const simp_solver_options* o) {
   a.maxit = o->max_iterations > 0 ? o->max_iterations : 1000;
   a.precision = o->precision;
   a.graphs = o->cuda_graphs != 0;
+  a.mf_transfer = o->matrix_free_transfer != 0;
   return a;
 }
 
@@ -114,6 +115,7 @@ void simp_default_options(simp_solver_options* o) {
   o->precision = SIMP_PRECISION_FP64;
   o->device = 0;
   o->cuda_graphs = 1;
+  o->matrix_free_transfer = 1;
 }
 
 int simp_ctx_create(const simp_solver_options* opts, simp_ctx** out) {

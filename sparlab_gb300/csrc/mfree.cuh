@@ -148,7 +148,11 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 // parameter (a __grid_constant__ struct indexed by compile-time constants,
 // so its entries are constant-bank operands of the FMAs rather than loads).
 // Modes: 0 y = A x, 1 y = b - A x, 3 Chebyshev step, 4 Chebyshev first step
-// (same epilogues as the other operator kernels).
+// (same epilogues as the other operator kernels); and the pieces of the
+// smoothed-prolongator transfers P = (I - w D^-1 A) P^ applied without P:
+// 5 x_s += t - w D^-1 A t (t = P^ x_c, the input), 6 y = b - A x with
+// dn = D^-1 y, 7 y = b - w A x (x = D^-1 r, b = r: the vector P^T maps to
+// the coarse right-hand side).
 // ---------------------------------------------------------------------------
 constexpr int kTX = 32, kTY = 4, kTZ = 2;  // threads per block axis
 constexpr int kNZ = 1;                      // node layers per thread
@@ -164,8 +168,8 @@ struct MfArgs {
   float* r;           // mode 3/4: residual out
   float* dn;          // mode 3: new direction; mode 4: d out
   float* xs;          // mode 3: smoothed iterate (updated)
-  const float* dinv;  // mode 3/4
-  const float* coef;  // mode 3: (c1, c2); mode 4: 1 / theta (device memory)
+  const float* dinv;  // mode 3/4/5/6
+  const float* coef;  // mode 3: (c1, c2); mode 4: 1 / theta; mode 5/7: w (device memory)
   int add_d;
 };
 
@@ -280,12 +284,79 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
         float xi = a.xs[row];
         if (a.add_d) xi = xi + dv;
         a.xs[row] = xi + di;
-      } else {
+      } else if (MODE == 4) {
         const float ri = a.b[row] - o[k];
         a.r[row] = ri;
         a.dn[row] = a.dinv[row] * ri * a.coef[0];
+      } else if (MODE == 5) {
+        const float ti = xh[k][lz + 1][ty + 1][tx + 1];  // this node's t
+        a.xs[row] = a.xs[row] + (ti - a.coef[0] * (a.dinv[row] * o[k]));
+      } else if (MODE == 6) {
+        const float ri = a.b[row] - o[k];
+        a.y[row] = ri;
+        a.dn[row] = a.dinv[row] * ri;
+      } else {
+        a.y[row] = a.b[row] - a.coef[0] * o[k];
       }
     }
+  }
+}
+
+// The tentative prolongator P^ of level 0 (3 unknowns per node, B1 per
+// aggregate; aggregate g owns coarse unknowns g B1 .. g B1 + B1 - 1; the row
+// of fine unknown i is phat[phat_ptr[i] ...], B1 values, empty for a node in
+// no aggregate).  t = P^ x_c, one thread per fine unknown.
+template <int B1>
+__global__ void __launch_bounds__(256) k_phat_prolong(i32 n, const i32* __restrict__ agg,
+                                                      const i32* __restrict__ phat_ptr,
+                                                      const float* __restrict__ phat, const float* __restrict__ xc,
+                                                      float* __restrict__ t) {
+  const i32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const i32 g = agg[i / 3];
+  float s = 0.0f;
+  if (g >= 0) {
+    const float* ph = phat + phat_ptr[i];
+    const float* xg = xc + static_cast<i64>(g) * B1;
+#pragma unroll
+    for (int j = 0; j < B1; ++j) s = fmaf(ph[j], xg[j], s);
+  }
+  t[i] = s;
+}
+
+// b_c = P^T t: one warp per aggregate; lane q takes the aggregate's member
+// unknowns q, q + 32, ... (members ascending, 3 unknowns each) into B1 partial
+// sums, reduced across the warp in a fixed butterfly order.
+template <int B1>
+__global__ void __launch_bounds__(256) k_phat_restrict(i32 naggs, const i32* __restrict__ mptr,
+                                                       const i32* __restrict__ members,
+                                                       const i32* __restrict__ phat_ptr,
+                                                       const float* __restrict__ phat, const float* __restrict__ t,
+                                                       float* __restrict__ bc) {
+  const i32 g = static_cast<i32>((blockIdx.x * static_cast<i64>(blockDim.x) + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (g >= naggs) return;
+  const i32 q0 = mptr[g], cnt = 3 * (mptr[g + 1] - q0);
+  float acc[B1];
+#pragma unroll
+  for (int j = 0; j < B1; ++j) acc[j] = 0.0f;
+  for (i32 q = lane; q < cnt; q += 32) {
+    const i32 i = 3 * members[q0 + q / 3] + q % 3;
+    const float ti = t[i];
+    const float* ph = phat + phat_ptr[i];
+#pragma unroll
+    for (int j = 0; j < B1; ++j) acc[j] = fmaf(ph[j], ti, acc[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < B1; ++j)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+  if (lane < B1) {
+    float v = acc[0];
+#pragma unroll
+    for (int j = 1; j < B1; ++j)
+      if (lane == j) v = acc[j];
+    bc[static_cast<i64>(g) * B1 + lane] = v;
   }
 }
 

@@ -71,3 +71,56 @@ def test_context_creation_reports_cuda_errors_without_a_gpu():
     code = lib.simp_ctx_create(None, C.byref(h))
     assert code == _lib.SIMP_CUDA_ERROR
     assert lib.simp_last_error(None)
+
+
+def header_structs():
+    """{typedef name: [(field, type)]} of the plain-C structs include/simp_gpu.h
+    declares, in declaration order; type is 'double', 'int32_t', 'int64_t',
+    'float', 'ptr', or (element type, length) for an array."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"typedef struct(?: \w+)? \{(.*?)\} (simp_\w+);", text, flags=re.S):
+        fields = []
+        for decl in m.group(1).split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            typ, names = re.match(r"((?:const\s+)?\w+\s*\**)\s*(.*)", decl).groups()
+            for nm in names.split(","):
+                nm = nm.strip()
+                ptr = "*" in typ or nm.startswith("*")
+                arr = re.match(r"(\w+)\[(\d+)\]$", nm.lstrip("*"))
+                base = "ptr" if ptr else typ.strip()
+                if arr:
+                    fields.append((arr.group(1), (base, int(arr.group(2)))))
+                else:
+                    fields.append((nm.lstrip("*"), base))
+        out[m.group(2)] = fields
+    return out
+
+
+MIRRORS = {"simp_solver_options": "SolverOptions", "simp_amg_stats": "AmgStats",
+           "simp_problem_desc": "ProblemDesc", "simp_evaluation": "Evaluation",
+           "simp_oc_step": "OcStep", "simp_iteration_record": "IterationRecord",
+           "simp_robust_record": "RobustRecord", "simp_modal_options": "ModalOptions",
+           "simp_modal_info": "ModalInfo", "simp_buckling_options": "BucklingOptions",
+           "simp_buckling_info": "BucklingInfo"}
+
+
+def test_ctypes_mirrors_follow_the_header():
+    """Every struct of the C ABI has a ctypes mirror with the same fields, in
+    the same order, of the same C types (so the offsets agree)."""
+    structs = header_structs()
+    assert set(structs) == set(MIRRORS)
+    scalar = {"double": C.c_double, "int32_t": C.c_int32, "int64_t": C.c_int64, "float": C.c_float}
+    for cname, pyname in MIRRORS.items():
+        mirror = getattr(_lib, pyname)._fields_
+        python_name = {"lambda": "lam"}  # a Python keyword
+        assert [f for f, _ in mirror] == [python_name.get(f, f) for f, _ in structs[cname]], cname
+        for (f, ctype), (_, htype) in zip(mirror, structs[cname]):
+            if isinstance(htype, tuple):
+                assert ctype._type_ is scalar[htype[0]] and ctype._length_ == htype[1], (cname, f)
+            elif htype == "ptr":
+                assert C.sizeof(ctype) == C.sizeof(C.c_void_p) and ctype not in scalar.values(), (cname, f)
+            else:
+                assert ctype is scalar[htype], (cname, f, ctype, htype)

@@ -366,3 +366,23 @@ def test_cuda_graph_iterations_match_plain_launches(precision):
                         TopologyOptimizer(gpu, max_iterations=4, change_tolerance=0).run()]
         gpu.close()
     assert recs[0] == recs[1]
+
+
+def test_matrix_free_transfers_match_stored_transfers():
+    """Level 0's restriction and prolongation applied matrix-free in the FP32
+    V-cycle, P^T (I - w A D^-1) and (I - w D^-1 A) P^, precondition as the
+    stored R and P do: the same compliances (both solves reach rtol 1e-10) and
+    CG iteration counts within one, across reuse setups."""
+    spec = small_hex(24, 12, 12)
+    side = [spec.node_index(24, j, 12) for j in range(13)]
+    spec.loads = np.stack([spec.loads[0], P.point_load(spec, side, (0.0, 1.0, 0.0))])
+    spec.weights = np.array([0.5, 0.5])
+    recs = {}
+    for mft in (0, 1):
+        gpu = GpuSimpProblem(spec, precision="mixed", matrix_free_transfer=mft)
+        recs[mft] = [(r.compliance, r.linear_iterations) for r in
+                     TopologyOptimizer(gpu, max_iterations=5, change_tolerance=0).run()]
+        gpu.close()
+    for (c0, i0), (c1, i1) in zip(recs[0], recs[1]):
+        assert abs(c1 / c0 - 1) < 1e-9, (c0, c1)
+        assert abs(i1 - i0) <= max(1, i0 // 20), (i0, i1)
