@@ -55,14 +55,22 @@ __global__ void k_expand_columns(i32 n, const i32* __restrict__ node_of, NodeVie
 
 namespace {
 
-// w = s .* w - beta vp
+// w = s .* w - beta vp (beta from device memory); nothing once stopped
 __global__ void k_lanczos_finish(double* __restrict__ w, const double* __restrict__ s,
-                                 const double* __restrict__ vp, double beta, i64 n) {
+                                 const double* __restrict__ vp, const double* __restrict__ beta,
+                                 const double* __restrict__ stop, i64 n) {
+  if (*stop != 0.0) return;
+  const double bj = vp ? *beta : 0.0;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     double wi = w[i] * s[i];
-    if (vp) wi -= beta * vp[i];
+    if (vp) wi -= bj * vp[i];
     w[i] = wi;
   }
+}
+
+// The reference's breakdown test of step j: stop when beta_j <= 1e-12 |alpha_j|
+__global__ void k_lanczos_check(const double* __restrict__ ab, int j, double* __restrict__ stop) {
+  if (threadIdx.x == 0 && blockIdx.x == 0 && !(ab[2 * j + 1] > 1.0e-12 * fabs(ab[2 * j]))) *stop = 1.0;
 }
 
 // Every operator application runs the VS-lanes-per-row kernels of
@@ -531,16 +539,8 @@ void GpuAmg::numeric_level(size_t l) {
                                                              lv.d_apat.view(), lv.a.ptr.p, lv.a.v64.p, lv.dinv64.p,
                                                              dstatus.p);
   SIMP_CHECK_LAUNCH();
-  int bad = 0;
-  SIMP_CUDA(cudaMemcpyAsync(&bad, dstatus.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-  SIMP_CUDA(cudaStreamSynchronize(stream));
-  if (bad != 0x7f7f7f7f) {
-    std::ostringstream os;
-    os << "multigrid level " << l << ": diagonal entry " << bad
-       << " is not positive; a stiffness matrix must have a positive diagonal. The model has an "
-          "unconnected degree of freedom or a non-positive stiffness";
-    throw Error(kBreakdown, os.str());
-  }
+  // the diagonal's status is read with the Lanczos coefficients below (one
+  // host round trip per level); a bad diagonal only makes them garbage
   if (mixed()) {
     lv.dinv32.alloc(n);
     convert(lv.dinv64.p, lv.dinv32.p, n, stream);
@@ -567,8 +567,14 @@ void GpuAmg::numeric_level(size_t l) {
     k_lanczos_start<<<grid_for(n, 256), 256, 0, stream>>>(v.p, scal.p + 1, lv.dinv64.p, s.p, tmp.p, n);
     SIMP_CHECK_LAUNCH();
   }
-  std::vector<double> alpha, beta;
+  // alpha_j, beta_j stay in device memory (lz_ab_[2j], [2j+1]; [2m] = the
+  // stop flag of the breakdown test): the steps after a breakdown change
+  // nothing, and the host reads all coefficients once
   const int m = std::max(1, std::min<int>(opt.lanczos_steps, n));
+  lz_ab_.alloc(static_cast<size_t>(2 * m + 1));
+  double* ab = lz_ab_.p;
+  double* stop = ab + 2 * m;
+  SIMP_CUDA(cudaMemsetAsync(stop, 0, sizeof(double), stream));
   for (int j = 0; j < m; ++j) {
     if (fp32) {
       // FP32 operator on FP32 copies of the Lanczos vectors
@@ -585,22 +591,40 @@ void GpuAmg::numeric_level(size_t l) {
     }
     else nb_apply<0, double, double, double>(lv.opA, lv.a.v64.p, tmp.p, w.p, nullptr, stream);
     k_lanczos_finish<<<grid_for(n, 256), 256, 0, stream>>>(w.p, s.p, j > 0 ? vp.p : nullptr,
-                                                          j > 0 ? beta.back() : 0.0, n);
+                                                          j > 0 ? ab + 2 * j - 1 : nullptr, stop, n);
     SIMP_CHECK_LAUNCH();
-    const double aj = dot(w.p, v.p, n);
+    k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(w.p, v.p, n, part.p);
+    SIMP_CHECK_LAUNCH();
+    k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, ab + 2 * j, 0);
+    SIMP_CHECK_LAUNCH();
+    if (j + 1 == m) break;  // beta of the last step is not used
+    k_axpy_norm<<<kRedBlocks, kRedThreads, 0, stream>>>(w.p, v.p, ab + 2 * j, n, part.p);
+    SIMP_CHECK_LAUNCH();
+    k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, ab + 2 * j + 1, 1);
+    SIMP_CHECK_LAUNCH();
+    k_lanczos_check<<<1, 32, 0, stream>>>(ab, j, stop);
+    SIMP_CHECK_LAUNCH();
+    k_lanczos_shift<<<grid_for(n, 256), 256, 0, stream>>>(v.p, vp.p, w.p, s.p, tmp.p, ab + 2 * j + 1, stop, n);
+    SIMP_CHECK_LAUNCH();
+  }
+  int bad = 0;
+  std::vector<double> hab(static_cast<size_t>(2 * m));
+  SIMP_CUDA(cudaMemcpyAsync(hab.data(), ab, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, stream));
+  SIMP_CUDA(cudaMemcpyAsync(&bad, dstatus.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  SIMP_CUDA(cudaStreamSynchronize(stream));
+  if (bad != 0x7f7f7f7f) {
+    std::ostringstream os;
+    os << "multigrid level " << l << ": diagonal entry " << bad
+       << " is not positive; a stiffness matrix must have a positive diagonal. The model has an "
+          "unconnected degree of freedom or a non-positive stiffness";
+    throw Error(kBreakdown, os.str());
+  }
+  std::vector<double> alpha, beta;
+  for (int j = 0; j < m; ++j) {
+    const double aj = hab[2 * j], bj = hab[2 * j + 1];
     alpha.push_back(aj);
-    SIMP_CUDA(cudaMemcpyAsync(scal.p + 2, &aj, sizeof(double), cudaMemcpyHostToDevice, stream));
-    k_axpy_norm<<<kRedBlocks, kRedThreads, 0, stream>>>(w.p, v.p, scal.p + 2, n, part.p);
-    SIMP_CHECK_LAUNCH();
-    k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, scal.p + 3, 1);
-    SIMP_CHECK_LAUNCH();
-    double bj = 0.0;
-    SIMP_CUDA(cudaMemcpyAsync(&bj, scal.p + 3, sizeof(double), cudaMemcpyDeviceToHost, stream));
-    SIMP_CUDA(cudaStreamSynchronize(stream));
     if (j + 1 == m || !(bj > 1.0e-12 * std::abs(aj))) break;
     beta.push_back(bj);
-    k_lanczos_shift<<<grid_for(n, 256), 256, 0, stream>>>(v.p, vp.p, w.p, s.p, tmp.p, bj, n);
-    SIMP_CHECK_LAUNCH();
   }
   std::vector<double> off(beta.begin(), beta.begin() + static_cast<long>(alpha.size() - 1));
   lv.lambda = tridiagonal_max_eigenvalue(alpha, off);

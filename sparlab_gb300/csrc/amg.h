@@ -229,6 +229,7 @@ class GpuAmg {
  private:
   bool ready_ = false;
   i32 nc_ = 0;
+  DBuf<double> lz_ab_;  // Lanczos coefficients of the level in setup, and its stop flag
   DBuf<double> dense_, swept_, piv_, panel_;  // A_c^-1 (full), the sweep's lower triangle, pivots, U/V/P
   SolveWork main_;
   std::vector<std::unique_ptr<SolveWork>> extra_;

@@ -247,8 +247,12 @@ __global__ void __launch_bounds__(kRedThreads) k_axpy_norm(double* __restrict__ 
 }
 
 // vp = v ; v = w / b ; tmp = s .* v
+// (b from device memory; nothing once the breakdown test has stopped the steps)
 __global__ void k_lanczos_shift(double* __restrict__ v, double* __restrict__ vp, const double* __restrict__ w,
-                                const double* __restrict__ s, double* __restrict__ tmp, double bj, i64 n) {
+                                const double* __restrict__ s, double* __restrict__ tmp,
+                                const double* __restrict__ b, const double* __restrict__ stop, i64 n) {
+  if (*stop != 0.0) return;
+  const double bj = *b;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     vp[i] = v[i];
     const double vi = w[i] / bj;
