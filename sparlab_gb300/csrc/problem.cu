@@ -287,7 +287,8 @@ void GpuProblem::build() {
   dv_dx.alloc(ne_s);
   se.alloc(ne_s);
   tmp.alloc(ne_s);
-  opart.alloc(2 * kRedBlocks);
+  opart.alloc(static_cast<size_t>(std::max(2, kOcSpec)) * kRedBlocks);
+  ovol.alloc(kOcSpec);
   // loads restricted to the free DOFs
   std::vector<double> bh(static_cast<size_t>(nfree) * d.nloads);
   for (int l = 0; l < d.nloads; ++l)
@@ -761,19 +762,63 @@ OcStep GpuProblem::oc_update(bool apply, double* xnew_host) {
     throw Error(kMaxIter, os.str());
   }
   double vol = corner ? st.volume : vlo;
-  for (int it = 0; it < 200 && !corner; ++it) {
-    const double mid = std::sqrt(lo * hi);
-    vol = volume_of(mid);
-    st.bisections = it + 1;
-    st.lambda = mid;
-    if (std::abs(vol - target) <= 1.0e-10 * target) {
-      st.converged = true;
-      break;
+  // The bisection of optimality_criteria_update, evaluated speculatively:
+  // one pass computes the volumes of the bracket's midpoint and of the
+  // midpoints either outcome leads to (a depth-3 tree of 7 multipliers), and
+  // the host walks the tree with the sequential rules, so the multipliers,
+  // volumes and stopping point are the one-by-one loop's.  It saves host
+  // round trips where they dominate; on large grids, where a pass's 7 FP64
+  // candidates cost more than the round trips, the depth is 1 (one midpoint
+  // per pass, the plain loop).
+  const int depth = (d.projection || ne > (1 << 20)) ? 1 : 3;
+  int it = 0;
+  bool done = corner;
+  while (!done && it < 200) {
+    double tl[kOcSpec], th[kOcSpec], mids[kOcSpec], vols[kOcSpec];
+    const int nodes = (1 << depth) - 1;
+    tl[0] = lo;
+    th[0] = hi;
+    for (int k = 0; k < nodes; ++k) {
+      mids[k] = std::sqrt(tl[k] * th[k]);
+      if (2 * k + 2 < nodes) {
+        tl[2 * k + 1] = mids[k];  // vol > target: lo = mid
+        th[2 * k + 1] = th[k];
+        tl[2 * k + 2] = tl[k];    // else: hi = mid
+        th[2 * k + 2] = mids[k];
+      }
     }
-    if (vol > target) lo = mid; else hi = mid;
-    if (hi / lo - 1.0 < 1.0e-15) {
-      st.converged = std::abs(vol - target) <= 1.0e-6 * std::max(target, 1.0e-30);
-      break;
+    if (nodes == 1) {
+      vols[0] = volume_of(mids[0]);
+    } else {
+      OcFactors f{};
+      for (int k = 0; k < nodes; ++k) f.t[k] = factor(mids[k]);
+      k_oc_volume_multi<kOcSpec><<<kRedBlocks, kRedThreads, 0, s>>>(ne, oc_g.p, oc_lo.p, oc_hi.p, dv_dx.p, f,
+                                                                    part);
+      SIMP_CHECK_LAUNCH();
+      k_reduce_rows<<<nodes, kRedThreads, 0, s>>>(part, kRedBlocks, ovol.p);
+      SIMP_CHECK_LAUNCH();
+      SIMP_CUDA(cudaMemcpyAsync(vols, ovol.p, sizeof(double) * nodes, cudaMemcpyDeviceToHost, s));
+      SIMP_CUDA(cudaStreamSynchronize(s));
+    }
+    for (int k = 0; k < nodes && !done;) {
+      const double mid = mids[k];
+      vol = vols[k];
+      st.bisections = ++it;
+      st.lambda = mid;
+      if (std::abs(vol - target) <= 1.0e-10 * target) {
+        st.converged = true;
+        done = true;
+        break;
+      }
+      if (vol > target) lo = mid; else hi = mid;
+      if (hi / lo - 1.0 < 1.0e-15) {
+        st.converged = std::abs(vol - target) <= 1.0e-6 * std::max(target, 1.0e-30);
+        done = true;
+        break;
+      }
+      if (it >= 200) break;
+      k = vol > target ? 2 * k + 1 : 2 * k + 2;
+      if (k >= nodes) break;
     }
   }
   // the design of the final multiplier (the lower bracket end when no

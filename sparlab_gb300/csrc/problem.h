@@ -99,6 +99,7 @@ class GpuProblem {
   DBuf<uint8_t> cmask, ucomp;
   DBuf<uint32_t> nmask;     // per free node: free neighbours by offset
   DBuf<double> opart;
+  DBuf<double> ovol;  // volumes of one speculative bisection pass
   DBuf<double> oc_g, oc_lo, oc_hi;  // OC candidate factors of the current update
   // matrix-free level-0 operator (mixed precision, fully free / clamped nodes)
   DBuf<float> ke32, sf32;

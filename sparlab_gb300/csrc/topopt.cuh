@@ -382,6 +382,46 @@ __global__ void __launch_bounds__(kRedThreads) k_oc_volume(i64 ne, const double*
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// The same block partials for K multipliers in one pass over the element
+// arrays (part[k * gridDim.x + block] for t[k]); each multiplier's sum is
+// formed exactly as k_oc_volume forms it.
+constexpr int kOcSpec = 7;  // multipliers of one speculative bisection pass
+struct OcFactors {
+  double t[kOcSpec];
+};
+
+template <int K>
+__global__ void __launch_bounds__(kRedThreads) k_oc_volume_multi(i64 ne, const double* __restrict__ g,
+                                                                 const double* __restrict__ lo,
+                                                                 const double* __restrict__ hi,
+                                                                 const double* __restrict__ c, OcFactors f,
+                                                                 double* __restrict__ part) {
+  double s[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) s[k] = 0.0;
+  for (i64 e = blockIdx.x * (i64)kRedThreads + threadIdx.x; e < ne; e += (i64)gridDim.x * kRedThreads) {
+    const double ge = g[e], le = lo[e], he = hi[e], ce = c[e];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += ce * fmin(fmax(ge * f.t[k], le), he);
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const double v = block_sum<kRedThreads>(s[k]);
+    if (threadIdx.x == 0) part[k * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+// out[k] = sum of part[k * m .. k * m + m), one block per k, each summed as
+// k_reduce_final sums (no square root)
+__global__ void __launch_bounds__(kRedThreads) k_reduce_rows(const double* __restrict__ part, int m,
+                                                             double* __restrict__ out) {
+  const double* pk = part + static_cast<i64>(blockIdx.x) * m;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < m; i += kRedThreads) s += pk[i];
+  s = block_sum<kRedThreads>(s);
+  if (threadIdx.x == 0) out[blockIdx.x] = s;
+}
+
 __global__ void k_oc_apply(i64 ne, const double* __restrict__ g, const double* __restrict__ lo,
                            const double* __restrict__ hi, double t, double* __restrict__ xn) {
   for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < ne; e += (i64)gridDim.x * blockDim.x)
