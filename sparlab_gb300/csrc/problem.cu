@@ -498,6 +498,30 @@ void GpuProblem::assemble(const double* scale, bool exact) {
   amg.level0_fp32_fresh = true;
 }
 
+// Element energies and compliance sensitivities of the current displacements
+// (k_sensitivities with the upper triangle of K'_e^0 as its parameter).
+void GpuProblem::launch_sensitivities(cudaStream_t s) {
+  auto upper = [&](auto& ku, int ed) {
+    int idx = 0;
+    for (int r = 0; r < ed; ++r)
+      for (int c = r; c < ed; ++c)
+        ku.k[idx++] = c == r ? d.ke[static_cast<size_t>(r) * ed + r]
+                             : d.ke[static_cast<size_t>(r) * ed + c] + d.ke[static_cast<size_t>(c) * ed + r];
+  };
+  if (d.dim == 3) {
+    KeUpper<24> ku;
+    upper(ku, 24);
+    k_sensitivities<3><<<grid_for(ne, 128), 128, 0, s>>>(grid_of(d), ne, d.nloads, u.p, nfree, dof_map.p, ku,
+                                                         weights_d.p, sf.p, df.p, dc_dphys.p, se.p);
+  } else {
+    KeUpper<8> ku;
+    upper(ku, 8);
+    k_sensitivities<2><<<grid_for(ne, 128), 128, 0, s>>>(grid_of(d), ne, d.nloads, u.p, nfree, dof_map.p, ku,
+                                                         weights_d.p, sf.p, df.p, dc_dphys.p, se.p);
+  }
+  SIMP_CHECK_LAUNCH();
+}
+
 Evaluation GpuProblem::evaluate() {
   cudaStream_t s = amg.stream;
   Evaluation ev;
@@ -582,9 +606,7 @@ Evaluation GpuProblem::evaluate() {
   }
   ++evaluations;
   // element energies and sensitivities
-  k_sensitivities<<<grid_for(ne, 128), 128, 0, s>>>(grid_of(d), ne, d.nloads, u.p, nfree, dof_map.p, ke_d.p,
-                                                   weights_d.p, sf.p, df.p, dc_dphys.p, se.p);
-  SIMP_CHECK_LAUNCH();
+  launch_sensitivities(s);
   if (d.projection) {  // chain_to_design (Sensitivity.cpp:100-108)
     k_mul<<<grid_for(ne, 256), 256, 0, s>>>(ne, dc_dphys.p, dproj.p, tmp.p);
     SIMP_CHECK_LAUNCH();

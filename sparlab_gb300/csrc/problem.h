@@ -73,6 +73,7 @@ class GpuProblem {
   void set_design(const double* h);
   void get_design(double* h);
   Evaluation evaluate();
+  void launch_sensitivities(cudaStream_t s);
   OcStep oc_update(bool apply, double* xnew_host);
   // MMA step with the gradients of the last evaluate (mma.cu); lambda is the
   // volume multiplier, `bisections` the subproblem's Newton iterations.
