@@ -56,15 +56,15 @@ __global__ void k_expand_columns(i32 n, const i32* __restrict__ node_of, NodeVie
 namespace {
 
 // w = s .* w - beta vp (beta from device memory); nothing once stopped
-__global__ void k_lanczos_finish(double* __restrict__ w, const double* __restrict__ s,
-                                 const double* __restrict__ vp, const double* __restrict__ beta,
-                                 const double* __restrict__ stop, i64 n) {
+template <class T>
+__global__ void k_lanczos_finish(T* __restrict__ w, const T* __restrict__ s, const T* __restrict__ vp,
+                                 const double* __restrict__ beta, const double* __restrict__ stop, i64 n) {
   if (*stop != 0.0) return;
   const double bj = vp ? *beta : 0.0;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
-    double wi = w[i] * s[i];
-    if (vp) wi -= bj * vp[i];
-    w[i] = wi;
+    double wi = todbl(w[i]) * todbl(s[i]);
+    if (vp) wi -= bj * todbl(vp[i]);
+    w[i] = static_cast<T>(wi);
   }
 }
 
@@ -522,6 +522,65 @@ void GpuAmg::refresh_level0_fp32() {
   SIMP_CHECK_LAUNCH();
 }
 
+template <class T>
+struct LzBufs;
+template <>
+struct LzBufs<double> {
+  static DBuf<double>* get(Level& l) { return l.lz; }
+};
+template <>
+struct LzBufs<float> {
+  static DBuf<float>* get(Level& l) { return l.lz32; }
+};
+
+// The m Lanczos steps of a level (Multigrid.cpp:288-327).  T = double: FP64
+// vectors and operator.  T = float (the FP32 reuse setups): FP32 vectors and
+// the FP32 operator the smoother uses (matrix-free on a structured level 0),
+// with the scalars and the sums of the dot products in FP64.
+template <class T>
+void GpuAmg::lanczos(size_t l, int m, double* ab) {
+  Level& lv = *levels[l];
+  const i32 n = lv.n;
+  double* stop = ab + 2 * m;
+  DBuf<T>* bufs = LzBufs<T>::get(lv);
+  for (int k = 0; k < 5; ++k) bufs[k].alloc(static_cast<size_t>(n));
+  T* v = bufs[0].p;
+  T* vp = bufs[1].p;
+  T* w = bufs[2].p;
+  T* s = bufs[3].p;
+  T* tmp = bufs[4].p;
+  if constexpr (std::is_same<T, double>::value)
+    SIMP_CUDA(cudaMemcpyAsync(v, lv.lz_start.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
+  else
+    convert(lv.lz_start.p, v, n, stream);
+  k_lanczos_start<T><<<grid_for(n, 256), 256, 0, stream>>>(v, scal.p + 1, lv.dinv64.p, s, tmp, n);
+  SIMP_CHECK_LAUNCH();
+  for (int j = 0; j < m; ++j) {
+    if constexpr (std::is_same<T, float>::value) {
+      if (l == 0 && mf.enabled) mf_apply(mf, lv.nnodes, tmp, w, stream);
+      else nb_apply<0, float, float, float>(lv.opA, lv.a.v32.p, tmp, w, nullptr, stream);
+    } else {
+      nb_apply<0, double, double, double>(lv.opA, lv.a.v64.p, tmp, w, nullptr, stream);
+    }
+    k_lanczos_finish<T><<<grid_for(n, 256), 256, 0, stream>>>(w, s, j > 0 ? vp : nullptr,
+                                                             j > 0 ? ab + 2 * j - 1 : nullptr, stop, n);
+    SIMP_CHECK_LAUNCH();
+    k_dot_partial<T, T><<<kRedBlocks, kRedThreads, 0, stream>>>(w, v, n, part.p);
+    SIMP_CHECK_LAUNCH();
+    k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, ab + 2 * j, 0);
+    SIMP_CHECK_LAUNCH();
+    if (j + 1 == m) break;  // beta of the last step is not used
+    k_axpy_norm<T><<<kRedBlocks, kRedThreads, 0, stream>>>(w, v, ab + 2 * j, n, part.p);
+    SIMP_CHECK_LAUNCH();
+    k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, ab + 2 * j + 1, 1);
+    SIMP_CHECK_LAUNCH();
+    k_lanczos_check<<<1, 32, 0, stream>>>(ab, j, stop);
+    SIMP_CHECK_LAUNCH();
+    k_lanczos_shift<T><<<grid_for(n, 256), 256, 0, stream>>>(v, vp, w, s, tmp, ab + 2 * j + 1, stop, n);
+    SIMP_CHECK_LAUNCH();
+  }
+}
+
 // inverse diagonal and lambda_max(D^-1 A) of one level (Multigrid.cpp:718-747)
 void GpuAmg::numeric_level(size_t l) {
   Level& lv = *levels[l];
@@ -545,68 +604,23 @@ void GpuAmg::numeric_level(size_t l) {
     lv.dinv32.alloc(n);
     convert(lv.dinv64.p, lv.dinv32.p, n, stream);
   }
-  // Lanczos on D^-1/2 A D^-1/2 with the reference's start vector.
-  // Lanczos vectors, kept with the level so reuse setups allocate nothing
-  // (cudaFree synchronises the device)
-  DBuf<double>& v = lv.lz[0];
-  DBuf<double>& vp = lv.lz[1];
-  DBuf<double>& w = lv.lz[2];
-  DBuf<double>& s = lv.lz[3];
-  DBuf<double>& tmp = lv.lz[4];
-  for (auto& b : lv.lz) b.alloc(static_cast<size_t>(n));
-  {
-    // the reference's start vector depends on n only: made and normed once
-    if (lv.lz_start.n != static_cast<size_t>(n)) {
-      std::vector<double> h(static_cast<size_t>(n));
-      for (i32 i = 0; i < n; ++i) h[i] = 1.0 + 0.5 * std::sin(1.7 * static_cast<double>(i) + 0.3);
-      lv.lz_start.upload(h, stream);
-      lv.lz_norm = std::sqrt(dot(lv.lz_start.p, lv.lz_start.p, n));
-    }
-    SIMP_CUDA(cudaMemcpyAsync(v.p, lv.lz_start.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
-    SIMP_CUDA(cudaMemcpyAsync(scal.p + 1, &lv.lz_norm, sizeof(double), cudaMemcpyHostToDevice, stream));
-    k_lanczos_start<<<grid_for(n, 256), 256, 0, stream>>>(v.p, scal.p + 1, lv.dinv64.p, s.p, tmp.p, n);
-    SIMP_CHECK_LAUNCH();
+  // Lanczos on D^-1/2 A D^-1/2 with the reference's start vector (its norm
+  // made once per size); alpha_j, beta_j stay in device memory (lz_ab_[2j],
+  // [2j+1]; [2m] = the stop flag of the breakdown test): the steps after a
+  // breakdown change nothing, and the host reads all coefficients once
+  if (lv.lz_start.n != static_cast<size_t>(n)) {
+    std::vector<double> h(static_cast<size_t>(n));
+    for (i32 i = 0; i < n; ++i) h[i] = 1.0 + 0.5 * std::sin(1.7 * static_cast<double>(i) + 0.3);
+    lv.lz_start.upload(h, stream);
+    lv.lz_norm = std::sqrt(dot(lv.lz_start.p, lv.lz_start.p, n));
   }
-  // alpha_j, beta_j stay in device memory (lz_ab_[2j], [2j+1]; [2m] = the
-  // stop flag of the breakdown test): the steps after a breakdown change
-  // nothing, and the host reads all coefficients once
   const int m = std::max(1, std::min<int>(opt.lanczos_steps, n));
   lz_ab_.alloc(static_cast<size_t>(2 * m + 1));
   double* ab = lz_ab_.p;
-  double* stop = ab + 2 * m;
-  SIMP_CUDA(cudaMemsetAsync(stop, 0, sizeof(double), stream));
-  for (int j = 0; j < m; ++j) {
-    if (fp32) {
-      // FP32 operator on FP32 copies of the Lanczos vectors
-      if (main_.lv.size() <= l) main_.lv.resize(l + 1);
-      DBuf<float>& x32 = main_.lv[l].x32;
-      DBuf<float>& b32 = main_.lv[l].b32;
-      alloc32(x32, n, stream);
-      alloc32(b32, n, stream);
-      convert(tmp.p, x32.p, n, stream);
-      // level 0 of a structured grid: the matrix-free operator the smoother uses
-      if (l == 0 && mf.enabled) mf_apply(mf, lv.nnodes, x32.p, b32.p, stream);
-      else nb_apply<0, float, float, float>(lv.opA, lv.a.v32.p, x32.p, b32.p, nullptr, stream);
-      convert(b32.p, w.p, n, stream);
-    }
-    else nb_apply<0, double, double, double>(lv.opA, lv.a.v64.p, tmp.p, w.p, nullptr, stream);
-    k_lanczos_finish<<<grid_for(n, 256), 256, 0, stream>>>(w.p, s.p, j > 0 ? vp.p : nullptr,
-                                                          j > 0 ? ab + 2 * j - 1 : nullptr, stop, n);
-    SIMP_CHECK_LAUNCH();
-    k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(w.p, v.p, n, part.p);
-    SIMP_CHECK_LAUNCH();
-    k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, ab + 2 * j, 0);
-    SIMP_CHECK_LAUNCH();
-    if (j + 1 == m) break;  // beta of the last step is not used
-    k_axpy_norm<<<kRedBlocks, kRedThreads, 0, stream>>>(w.p, v.p, ab + 2 * j, n, part.p);
-    SIMP_CHECK_LAUNCH();
-    k_reduce_final<<<1, kRedThreads, 0, stream>>>(part.p, kRedBlocks, ab + 2 * j + 1, 1);
-    SIMP_CHECK_LAUNCH();
-    k_lanczos_check<<<1, 32, 0, stream>>>(ab, j, stop);
-    SIMP_CHECK_LAUNCH();
-    k_lanczos_shift<<<grid_for(n, 256), 256, 0, stream>>>(v.p, vp.p, w.p, s.p, tmp.p, ab + 2 * j + 1, stop, n);
-    SIMP_CHECK_LAUNCH();
-  }
+  SIMP_CUDA(cudaMemsetAsync(ab + 2 * m, 0, sizeof(double), stream));
+  SIMP_CUDA(cudaMemcpyAsync(scal.p + 1, &lv.lz_norm, sizeof(double), cudaMemcpyHostToDevice, stream));
+  if (fp32) lanczos<float>(l, m, ab);
+  else lanczos<double>(l, m, ab);
   int bad = 0;
   std::vector<double> hab(static_cast<size_t>(2 * m));
   SIMP_CUDA(cudaMemcpyAsync(hab.data(), ab, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, stream));

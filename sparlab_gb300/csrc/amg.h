@@ -114,7 +114,8 @@ struct Level {
   DBuf<float> raw32;
   std::vector<double> c1, c2;
   double inv_theta = 0.0;
-  DBuf<double> lz[5];  // Lanczos work vectors
+  DBuf<double> lz[5];  // Lanczos work vectors (FP64 setups)
+  DBuf<float> lz32[5];  // (FP32 reuse setups)
   DBuf<double> lz_start;  // Lanczos start vector (depends on n only) and its norm
   double lz_norm = 0.0;
 };
@@ -235,6 +236,8 @@ class GpuAmg {
   std::vector<std::unique_ptr<SolveWork>> extra_;
 
   void numeric_level(size_t l);
+  template <class T>
+  void lanczos(size_t l, int m, double* ab);
   void build_transfer(size_t l);
   void galerkin(size_t l, bool fp32);
   void coarse_factorize();

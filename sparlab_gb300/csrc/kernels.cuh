@@ -231,16 +231,19 @@ __global__ void k_cheb_zero(i64 n, const TX* __restrict__ b, const TX* __restric
 // ---------------------------------------------------------------------------
 // Lanczos pieces (src/fem/Multigrid.cpp:288-327)
 // ---------------------------------------------------------------------------
-// w -= a v ; partial ||w||^2
-__global__ void __launch_bounds__(kRedThreads) k_axpy_norm(double* __restrict__ w, const double* __restrict__ v,
+// Lanczos vector kernels (FP64 scalars; vectors in T: FP64, or FP32 in the
+// mixed-precision setups whose operator is FP32 anyway).
+// w -= a v (a from device memory); block partials of ||w||^2
+template <class T>
+__global__ void __launch_bounds__(kRedThreads) k_axpy_norm(T* __restrict__ w, const T* __restrict__ v,
                                                            const double* __restrict__ a_dev, i64 n,
                                                            double* __restrict__ part) {
   const double a = *a_dev;
   double s = 0.0;
   for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads) {
-    const double wi = w[i] - a * v[i];
+    const T wi = static_cast<T>(todbl(w[i]) - a * todbl(v[i]));
     w[i] = wi;
-    s += wi * wi;
+    s += todbl(wi) * todbl(wi);
   }
   s = block_sum<kRedThreads>(s);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
@@ -248,30 +251,32 @@ __global__ void __launch_bounds__(kRedThreads) k_axpy_norm(double* __restrict__ 
 
 // vp = v ; v = w / b ; tmp = s .* v
 // (b from device memory; nothing once the breakdown test has stopped the steps)
-__global__ void k_lanczos_shift(double* __restrict__ v, double* __restrict__ vp, const double* __restrict__ w,
-                                const double* __restrict__ s, double* __restrict__ tmp,
+template <class T>
+__global__ void k_lanczos_shift(T* __restrict__ v, T* __restrict__ vp, const T* __restrict__ w,
+                                const T* __restrict__ s, T* __restrict__ tmp,
                                 const double* __restrict__ b, const double* __restrict__ stop, i64 n) {
   if (*stop != 0.0) return;
   const double bj = *b;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     vp[i] = v[i];
-    const double vi = w[i] / bj;
+    const T vi = static_cast<T>(todbl(w[i]) / bj);
     v[i] = vi;
-    tmp[i] = s[i] * vi;
+    tmp[i] = static_cast<T>(todbl(s[i]) * todbl(vi));
   }
 }
 
 // v = v / nrm ; tmp = s .* v ; s = sqrt(dinv)
-__global__ void k_lanczos_start(double* __restrict__ v, const double* __restrict__ nrm,
-                                const double* __restrict__ dinv, double* __restrict__ s,
-                                double* __restrict__ tmp, i64 n) {
+template <class T>
+__global__ void k_lanczos_start(T* __restrict__ v, const double* __restrict__ nrm,
+                                const double* __restrict__ dinv, T* __restrict__ s,
+                                T* __restrict__ tmp, i64 n) {
   const double inv = *nrm;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     const double si = sqrt(dinv[i]);
-    s[i] = si;
-    const double vi = v[i] / inv;
-    v[i] = vi;
-    tmp[i] = si * vi;
+    s[i] = static_cast<T>(si);
+    const double vi = todbl(v[i]) / inv;
+    v[i] = static_cast<T>(vi);
+    tmp[i] = static_cast<T>(todbl(static_cast<T>(si)) * todbl(static_cast<T>(vi)));
   }
 }
 
