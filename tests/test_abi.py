@@ -62,6 +62,32 @@ def test_element_stiffness_matches_oracle(dim, h):
         assert np.abs(ke @ t).max() <= 1e-12 * np.abs(ke).max()
 
 
+@pytest.mark.parametrize("field,value,words", [
+    ("strength_threshold", 1.5, "strength_threshold"),
+    ("strength_threshold", -0.1, "strength_threshold"),
+    ("max_levels", 0, "max_levels"),
+    ("coarse_size", 0, "coarse_size"),
+    ("smoother_degree", 0, "smoother_degree"),
+    ("chebyshev_ratio", 1.0, "chebyshev_ratio"),
+    ("prolongator_damping", 2.0, "prolongator_damping"),
+    ("lanczos_steps", 1, "lanczos_steps"),
+    ("iterative_tolerance", 0.0, "tolerance"),
+    ("precision", 7, "precision"),
+])
+def test_context_creation_rejects_bad_options_before_touching_the_device(field, value, words):
+    """AmgPreconditioner's option checks (src/fem/Multigrid.cpp:907-925;
+    tests/test_multigrid.cpp:451-453 asserts strength 1.5 is refused): the
+    context is refused with SIMP_BAD_INPUT and the option named, whether or
+    not a GPU is present, because the checks come before any CUDA call."""
+    lib = _lib.load()
+    o = _lib.default_options()
+    setattr(o, field, value)
+    h = C.c_void_p()
+    assert lib.simp_ctx_create(C.byref(o), C.byref(h)) == _lib.SIMP_BAD_INPUT
+    assert not h.value
+    assert words in lib.simp_last_error(None).decode()
+
+
 def test_context_creation_reports_cuda_errors_without_a_gpu():
     import torch
     if torch.cuda.is_available():
