@@ -8,9 +8,10 @@
   normalised to one, and its gradient passes the finite-difference check --
   tests/test_topopt.cpp:487-548;
 * the multigrid solve is bitwise identical for one thread and several --
-  tests/test_multigrid.cpp:379-391.
+  tests/test_multigrid.cpp:379-391;
+* a hierarchy set up with reused aggregates equals a fresh one bit for bit
+  -- tests/test_multigrid.cpp:513-542.
 """
-import hashlib
 import os
 import subprocess
 import sys
@@ -169,3 +170,29 @@ def test_multigrid_solve_is_bitwise_identical_for_any_thread_count():
     parallel = _solve_with_threads(4)
     assert int(serial[0]) > 16384
     assert serial == parallel
+
+
+def test_reused_hierarchy_equals_a_fresh_one_bit_for_bit():
+    """tests/test_multigrid.cpp:513-542: a uniformly scaled matrix (every
+    element factor 2.5) aggregates like the first one, so the hierarchy set up
+    on it with the first matrix's aggregates reused and a fresh hierarchy give
+    the same V-cycle bits (coarse_size 50)."""
+    spec = P.ProblemSpec(dim=3, nx=10, ny=4, nz=4, lx=1.0, ly=0.4, lz=0.4, young=70.0e9,
+                         poisson=0.3, filter_radius=0.0)
+    spec.fixed = P.clamp_left(spec)
+    spec.loads = P.point_load(spec, [P.nearest_node(spec, (1.0, 0.0, 0.0))], (0.0, -1000.0, 0.0))[None, :]
+    spec.weights = np.ones(1)
+    pr = oracle.Problem(spec)
+    first = pr.kff()
+    second = pr.kff(np.full(pr.ne, 2.5))
+    coords, free = pr.coords(), pr.free_dofs()
+    reused = oracle.Solver(coarse_size=50)
+    reused.factorize(*first, 3, coords, free)
+    reused.factorize(*second, 3, coords, free)
+    assert reused.stats()["reused_aggregates"]
+    fresh = oracle.Solver(coarse_size=50)
+    fresh.factorize(*second, 3, coords, free)
+    assert not fresh.stats()["reused_aggregates"]
+    assert reused.num_levels() == fresh.num_levels() > 1
+    x = P.SplitMix64(11).uniform_array(len(free), -1.0, 1.0)
+    np.testing.assert_array_equal(reused.apply(x), fresh.apply(x))
