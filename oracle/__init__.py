@@ -209,6 +209,34 @@ class Solver:
                 "reused_aggregates": bool(re.value)}
 
 
+class Mma:
+    """MmaOptimizer(n, 1, 0, 1): n variables in [0, 1], one constraint row,
+    one update per call with the asymptotes kept between calls."""
+
+    def __init__(self, n):
+        self.n = int(n)
+        self._h = C.c_void_p()
+        _check(lib().orc_mma_create(C.c_int32(self.n), C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.orc_mma_destroy(self._h)
+            self._h = None
+
+    def update(self, x, df0, fval, dfdx):
+        x = np.ascontiguousarray(x, np.float64)
+        df0 = np.ascontiguousarray(df0, np.float64)
+        dfdx = np.ascontiguousarray(dfdx, np.float64)
+        assert x.size == df0.size == dfdx.size == self.n
+        xn = np.zeros(self.n)
+        out = np.zeros(7)
+        _check(lib().orc_mma_update(self._h, _p(x), _p(df0), C.c_double(fval), _p(dfdx), _p(xn),
+                                    _p(out)))
+        return xn, dict(lam=out[0], y=out[1], z=out[2], max_change=out[3],
+                        constraint_scale=out[4], subproblem_iterations=int(out[5]),
+                        iteration=int(out[6]))
+
+
 class Problem:
     """Structured SIMP problem: the ComplianceObjective / OC boundary of the oracle.
 

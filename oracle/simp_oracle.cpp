@@ -1822,7 +1822,7 @@ struct MmaState {
 
 struct MmaResult {
   Vec x;
-  double lam = 0.0, y = 0.0, z = 0.0, max_change = 0.0;
+  double lam = 0.0, y = 0.0, z = 0.0, max_change = 0.0, row_scale = 1.0;
   int iterations = 0;
 };
 
@@ -2001,6 +2001,7 @@ MmaResult mma_update(MmaState& st, const Vec& x, const Vec& df0, double fval, co
   r.lam = lam * row_scale;
   r.y = y / row_scale;
   r.z = z;
+  r.row_scale = row_scale;
   r.iterations = total;
   double mc = 0.0;
   for (size_t j = 0; j < n; ++j) mc = std::max(mc, std::abs(xx[j] - x[j]));
@@ -2361,6 +2362,41 @@ int orc_oc_update(orc_problem* h, const double* x, const double* dc, const doubl
     out[2] = st.max_change;
     out[3] = st.bisections;
     out[4] = st.converged ? 1.0 : 0.0;
+  });
+}
+
+// MmaOptimizer(n, 1, 0, 1) on its own (tests/test_mma.cpp:90-167 drive it
+// with analytic functions): one update per call, the state kept between calls.
+struct orc_mma {
+  MmaState st;
+  int32_t n = 0;
+};
+
+int orc_mma_create(int32_t n, orc_mma** out) {
+  return guarded([&] {
+    if (!out || n < 1) throw Error(kBadInput, "MMA needs at least one design variable");
+    auto* h = new orc_mma();
+    h->n = n;
+    *out = h;
+  });
+}
+
+void orc_mma_destroy(orc_mma* h) { delete h; }
+
+int orc_mma_update(orc_mma* h, const double* x, const double* df0, double fval, const double* dfdx,
+                   double* x_out, double* out) {
+  return guarded([&] {
+    const size_t n = static_cast<size_t>(h->n);
+    const Vec xv(x, x + n), g0(df0, df0 + n), g1(dfdx, dfdx + n);
+    const MmaResult r = mma_update(h->st, xv, g0, fval, g1);
+    std::copy(r.x.begin(), r.x.end(), x_out);
+    out[0] = r.lam;
+    out[1] = r.y;
+    out[2] = r.z;
+    out[3] = r.max_change;
+    out[4] = r.row_scale;
+    out[5] = r.iterations;
+    out[6] = h->st.iteration;
   });
 }
 

@@ -139,6 +139,16 @@ int orc_run(orc_problem* p, int32_t iterations, double change_tol, double* x,
 int orc_run_mma(orc_problem* p, int32_t iterations, double* x, double* history,
                 int32_t* performed);
 
+/* MmaOptimizer(n, 1, 0, 1) on its own: n variables in [0, 1], one
+ * constraint row.  Each update takes x, df0/dx, the constraint value and its
+ * gradient row; out: lambda, y, z, max change, constraint row scale,
+ * subproblem Newton iterations, MMA iteration count. */
+typedef struct orc_mma orc_mma;
+int orc_mma_create(int32_t n, orc_mma** out);
+int orc_mma_update(orc_mma* h, const double* x, const double* df0, double fval, const double* dfdx,
+                   double* x_out, double* out);
+void orc_mma_destroy(orc_mma* h);
+
 #ifdef __cplusplus
 }
 #endif

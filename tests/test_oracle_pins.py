@@ -10,7 +10,11 @@
 * the multigrid solve is bitwise identical for one thread and several --
   tests/test_multigrid.cpp:379-391;
 * a hierarchy set up with reused aggregates equals a fresh one bit for bit
-  -- tests/test_multigrid.cpp:513-542.
+  -- tests/test_multigrid.cpp:513-542;
+* MMA with one constraint row reaches the known optima of the reference's
+  analytic problems -- tests/test_mma.cpp:90-167 (the two-row case of
+  :118-146 needs a second constraint row, which the compliance problem never
+  has).
 """
 import os
 import subprocess
@@ -196,3 +200,36 @@ def test_reused_hierarchy_equals_a_fresh_one_bit_for_bit():
     assert reused.num_levels() == fresh.num_levels() > 1
     x = P.SplitMix64(11).uniform_array(len(free), -1.0, 1.0)
     np.testing.assert_array_equal(reused.apply(x), fresh.apply(x))
+
+
+def test_mma_solves_the_separable_problem_with_a_known_optimum():
+    """tests/test_mma.cpp:90-116: min sum x_i^2 s.t. 1 - sum x_i <= 0 on
+    [0, 1]^12 from x = 0.9: x_i = 1/12, multiplier 2/12, row untouched."""
+    n = 12
+    mma = oracle.Mma(n)
+    x = np.full(n, 0.9)
+    for _ in range(60):
+        x, step = mma.update(x, 2.0 * x, 1.0 - x.sum(), np.full(n, -1.0))
+        assert step["lam"] >= 0.0
+        if step["max_change"] < 1e-9:
+            break
+    assert np.abs(x - 1.0 / n).max() < 1e-6
+    assert abs(x.sum() - 1.0) <= 1e-6
+    assert step["constraint_scale"] == 1.0
+    assert abs(step["lam"] / (2.0 / n) - 1.0) <= 1e-3
+    assert step["iteration"] > 2
+
+
+def test_mma_scales_a_badly_violated_constraint_down():
+    """tests/test_mma.cpp:148-167: min x1 + x2 s.t. 1e5 (1 - x1 - x2) <= 0
+    on [0, 1]^2: the row is scaled down for the subproblem and the answer
+    keeps x1 + x2 = 1 with multiplier 1e-5."""
+    mma = oracle.Mma(2)
+    x = np.full(2, 0.9)
+    for _ in range(80):
+        x, step = mma.update(x, np.ones(2), 1.0e5 * (1.0 - x.sum()), np.full(2, -1.0e5))
+        if step["max_change"] < 1e-10:
+            break
+    assert step["constraint_scale"] < 1.0
+    assert abs(x.sum() - 1.0) <= 1e-6
+    assert abs(step["lam"] / 1.0e-5 - 1.0) <= 0.05
