@@ -166,7 +166,7 @@ typedef struct {
   double filter_radius;         /* physical; <= 0: no filter */
   double volume_fraction;
   double initial_density;       /* < 0: the volume fraction */
-  double penalty, emin_ratio;   /* SimpOptions */
+  double penalty, emin_ratio;   /* SimpOptions: penalty >= 1, emin_ratio in (0, 1) */
   double move_limit, damping;   /* OptimalityCriteriaOptions */
   int32_t warm_start;           /* 0: zero guess; 1: previous displacement
                                    (LinearSolverOptions::warm_start); 2: energy-

@@ -459,7 +459,7 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     const simp_solver_options* o = opts ? opts : &def;
     AmgOptions ao = convert(o);
     validate(ao);
-    use_device(o->device);
+    // the descriptor is checked on the host before the device is touched
     ProblemDesc d;
     d.dim = dsc->dim;
     d.nx = dsc->nx;
@@ -489,6 +489,12 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     if (!(d.vf > 0.0 && d.vf <= 1.0)) throw Error(kBadInput, "volume fraction must lie in (0, 1]");
     d.x0 = dsc->initial_density >= 0.0 ? dsc->initial_density : dsc->volume_fraction;
     d.penalty = dsc->penalty;
+    // SimpOptions::validate (src/topopt/SimpInterpolation.cpp:31-44)
+    if (!(d.penalty >= 1.0)) {
+      std::ostringstream os;
+      os << "SIMP penalty must be >= 1 (got " << d.penalty << ")";
+      throw Error(kBadInput, os.str());
+    }
     d.emin = dsc->emin_ratio;
     if (!(d.emin > 0.0 && d.emin < 1.0)) throw Error(kBadInput, "SIMP emin_ratio must lie in (0, 1)");
     d.move = dsc->move_limit;
@@ -533,6 +539,7 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     }
     if (dsc->optimizer != 0 && dsc->optimizer != 1) throw Error(kBadInput, "unknown optimizer (expected 0 OC, 1 MMA)");
     d.optimizer = dsc->optimizer;
+    use_device(o->device);
     std::unique_ptr<simp_problem> p(new simp_problem());
     p->device = o->device;
     p->p.reset(new GpuProblem(d, ao));

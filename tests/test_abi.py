@@ -88,6 +88,31 @@ def test_context_creation_rejects_bad_options_before_touching_the_device(field, 
     assert words in lib.simp_last_error(None).decode()
 
 
+@pytest.mark.parametrize("field,value,words", [
+    ("penalty", 0.5, "penalty"),
+    ("emin_ratio", 0.0, "emin_ratio"),
+    ("emin_ratio", 1.5, "emin_ratio"),
+    ("volume_fraction", 0.0, "volume fraction"),
+    ("move_limit", 0.0, "move_limit"),
+    ("damping", 1.5, "damping"),
+    ("warm_start", 3, "warm_start"),
+])
+def test_problem_creation_rejects_bad_descriptors_before_touching_the_device(field, value, words):
+    """SimpOptions::validate (src/topopt/SimpInterpolation.cpp:31-44; tests/
+    test_topopt.cpp:146-161 refuses penalty 0.5 and emin_ratio 0 and 1.5) and
+    the optimiser's option checks: simp_problem_create refuses the
+    descriptor with SIMP_BAD_INPUT and names the field, with or without a
+    GPU, because the descriptor is checked before the device is selected."""
+    from sparlab_gb300 import problems as P
+    from sparlab_gb300.topopt import GpuSimpProblem
+    spec = P.hex8_cantilever(4, 2, 2, 0.3, "bad_descriptor")
+    setattr(spec, field, value)
+    with pytest.raises(_lib.SolverError) as e:
+        GpuSimpProblem(spec)
+    assert e.value.code == _lib.SIMP_BAD_INPUT
+    assert words in str(e.value)
+
+
 def test_context_creation_reports_cuda_errors_without_a_gpu():
     import torch
     if torch.cuda.is_available():
