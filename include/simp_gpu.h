@@ -73,6 +73,16 @@ typedef struct {
                                     P^T (I - w A D^-1) and (I - w D^-1 A) P^ with the
                                     matrix-free operator instead of reading the stored
                                     R and P; 0 reads them */
+  int32_t matrix_free;           /* MIXED on a structured grid whose nodes are fully free
+                                    or clamped: 0 level 0 assembled throughout (the FP32
+                                    V-cycle on the assembled FP32 K_ff, the CG operator
+                                    on its double-float values); 1 (default) level 0 of
+                                    the FP32 V-cycle matrix-free (element-by-element
+                                    from K_e^0 and the cell scales), the CG operator
+                                    assembled double-float; 2 (3-D) also the CG operator
+                                    matrix-free: FP32 element products inside CG, with
+                                    the true residual of every restart taken by an FP64
+                                    matrix-free product (iterative refinement) */
 } simp_solver_options;
 
 typedef struct {
@@ -286,9 +296,10 @@ int simp_problem_apply_operator(simp_problem* p, const double* x_device, double*
 int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms_per_launch,
                                double* bytes_per_launch);
 
-/* No counterpart in the reference.  rho = clamp(H x, 0, 1) and the volume
- * sum_e v_e rho_e of the problem's density filter -- the physical density and
- * volume simp_evaluate reports for design x -- on device pointers (x and rho:
+/* No counterpart in the reference.  rho = clamp(H x, 0, 1) -- Heaviside-
+ * projected at the problem's current beta and the objective's threshold when
+ * the projection is on -- and the volume sum_e v_e rho_e: the physical density
+ * and volume simp_evaluate reports for design x, on device pointers (x and rho:
  * num_elements doubles, volume: one double), launched on the library's stream.
  * It allocates no device memory: its partial sums live in a fixed 128 KiB
  * device array of the library, so a caller that must not call cudaMalloc at
@@ -296,8 +307,8 @@ int simp_problem_time_operator(simp_problem* p, int32_t reps, double* ms_per_lau
  * without device synchronisation, an application running under its own
  * memory pool) can use it.  At most 67,108,864 elements (SIMP_BAD_INPUT
  * beyond).  The first call on a device sets the array up and should come
- * before any stream capture; calls that overlap on the GPU share the array
- * and race. */
+ * before any stream capture; a cudaDeviceReset after it is not supported.
+ * Calls that overlap on the GPU share the array and race. */
 int simp_filter_volume_noalloc(simp_problem* p, const double* x_device, double* rho_device,
                                double* volume_device);
 

@@ -205,6 +205,15 @@ MfView mf_view(const MfOp& o) {
 }
 
 template <int MODE>
+void mf3_64(const MfOp& mf, const double* x, double* y, const double* b, cudaStream_t s) {
+  const dim3 grid((mf.nnx + kTX - 1) / kTX, (mf.nny + kTY - 1) / kTY, (mf.nz + 1 + kTZ * kNZ - 1) / (kTZ * kNZ));
+  KeF64 ke;
+  std::copy(mf.ke64_host, mf.ke64_host + 24 * 24, ke.k);
+  k_mf3_tile64<MODE><<<grid, kTX * kTY * kTZ, 0, s>>>(mf_view(mf), mf.scale64, x, y, b, ke);
+  SIMP_CHECK_LAUNCH();
+}
+
+template <int MODE>
 void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
   const dim3 grid((mf.nnx + kTX - 1) / kTX, (mf.nny + kTY - 1) / kTY, (mf.nz + 1 + kTZ * kNZ - 1) / (kTZ * kNZ));
   KeF32 ke;
@@ -445,6 +454,11 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
   Level& l0 = *levels.front();
   const NbOp& op = l0.opA;
   const cudaStream_t stream = w.stream;
+  if (mf_cg()) {  // the FP64 matrix-free product (true residuals)
+    if (rhs) mf3_64<1>(mf, x, y, rhs, stream);
+    else mf3_64<0>(mf, x, y, nullptr, stream);
+    return;
+  }
   if (!mixed()) {
     if (rhs) nb_apply<1, double, double, double>(op, l0.a.v64.p, x, y, rhs, stream);
     else nb_apply<0, double, double, double>(op, l0.a.v64.p, x, y, nullptr, stream);
@@ -468,6 +482,20 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
                                                                        nullptr, op.rows);
   });
   SIMP_CHECK_LAUNCH();
+}
+
+void GpuAmg::cg_op(SolveWork& w, const double* p, double* q, bool p32_ready) {
+  if (!mf_cg()) {
+    op0(w, p, q, nullptr, p32_ready);
+    return;
+  }
+  const i32 n = levels.front()->n;
+  w.p32.alloc(static_cast<size_t>(n));
+  if (!p32_ready) convert(p, w.p32.p, n, w.stream);
+  MfArgs a{};
+  a.x = w.p32.p;
+  a.y64 = q;
+  mf3<8>(mf, a, w.stream);
 }
 
 void GpuAmg::apply_values0(SolveWork& w, const double* values, const double* x, double* y) {
@@ -1183,7 +1211,8 @@ void GpuAmg::pcg_tail(SolveWork& w, float2* psplit) {
   SIMP_CHECK_LAUNCH();
   k_pcg_beta<<<1, kRedThreads, 0, stream>>>(w.part.p, kRedBlocks, sc);
   SIMP_CHECK_LAUNCH();
-  k_pcg_direction<<<grid_for(n, 256), 256, 0, stream>>>(w.pp.p, w.pz.p, n, sc, psplit);
+  k_pcg_direction<<<grid_for(n, 256), 256, 0, stream>>>(w.pp.p, w.pz.p, n, sc, psplit,
+                                                         mf_cg() ? w.p32.p : nullptr);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -1191,7 +1220,7 @@ void GpuAmg::pcg_head(SolveWork& w, double* x, bool split_ready) {
   const i32 n = levels.front()->n;
   const cudaStream_t stream = w.stream;
   PcgScalars* sc = reinterpret_cast<PcgScalars*>(w.scal.p + 8);
-  op0(w, w.pp.p, w.pq.p, nullptr, split_ready);
+  cg_op(w, w.pp.p, w.pq.p, split_ready);
   k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(w.pp.p, w.pq.p, n, w.part.p);
   SIMP_CHECK_LAUNCH();
   k_pcg_alpha<<<1, kRedThreads, 0, stream>>>(w.part.p, kRedBlocks, sc);
@@ -1220,7 +1249,7 @@ void GpuAmg::pcg_body(SolveWork& w, double* x, float2* psplit) {
   cudaGraph_t graph = nullptr;
   try {
     pcg_tail(w, psplit);
-    pcg_head(w, x, psplit != nullptr);
+    pcg_head(w, x, psplit != nullptr || mf_cg());
   } catch (...) {
     cudaStreamEndCapture(w.stream, &graph);
     if (graph) cudaGraphDestroy(graph);
@@ -1258,13 +1287,18 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x_out, doub
   auto op = [&](const double* in, double* out, const double* rhs) { op0(w, in, out, rhs, false); };
   auto dot = [&](const double* a, const double* c, i64 m) { return this->dot(w, a, c, m); };
   auto apply = [&](const double* r, double* z) { this->apply(w, r, z); };
-  // mixed: the direction update also writes p's double-float split
-  float2* psplit = mixed() ? w.xsplit.p : nullptr;
+  // mixed: the direction update also writes p's double-float split (or,
+  // with the matrix-free CG operator, its FP32 copy)
+  float2* psplit = mixed() && !mf_cg() ? w.xsplit.p : nullptr;
+  if (mf_cg()) w.p32.alloc(static_cast<size_t>(n));
+  const bool p_copy = psplit != nullptr || mf_cg();
   bool p_split = false;
   int total = 0;
   bool rec_conv = false;
   double best = std::numeric_limits<double>::max();
-  const int rounds = restarts ? 3 : 1;
+  // the FP32 products of the matrix-free CG operator make each restart a
+  // step of iterative refinement on the FP64 true residual: allow more
+  const int rounds = restarts ? (mf_cg() ? 12 : 3) : 1;
   for (int restart = 0; restart < rounds; ++restart) {
     op(x, pr.p, b);
     double rnorm = std::sqrt(dot(pr.p, pr.p, n));
@@ -1304,7 +1338,7 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x_out, doub
       ++total;
       rnorm = std::sqrt(h.rr);
       if (rnorm <= target) { conv = true; break; }
-      p_split = psplit != nullptr;
+      p_split = p_copy;
     }
     if (!restarts) {
       res.converged = conv;

@@ -37,6 +37,10 @@ struct AmgOptions {
   int precision = 0;  // 0 FP64, 1 mixed
   bool graphs = true; // PCG iterations after the first as one CUDA graph launch
   bool mf_transfer = true;  // level-0 R and P of the FP32 cycle applied matrix-free
+  // mixed precision, structured grids: 0 level 0 assembled throughout; 1 the
+  // FP32 V-cycle's level 0 matrix-free; 2 also the CG operator (FP32 element
+  // products, FP64 matrix-free true residuals at the restarts)
+  int matrix_free = 1;
 };
 
 struct DevPattern {
@@ -131,6 +135,8 @@ struct MfOp {
   const float* ke = nullptr;    // K_e^0, FP32
   const float* scale = nullptr; // s_e, FP32
   float ke_host[24 * 24] = {};  // K_e^0, FP32 (kernel parameter of the tiled 3-D kernel)
+  const double* scale64 = nullptr;  // s_e, FP64 (the matrix-free CG operator's true residuals)
+  double ke64_host[24 * 24] = {};   // K_e^0, FP64
 };
 
 // Work vectors of one solve: the cycle vectors of every level, the PCG
@@ -148,6 +154,7 @@ struct SolveWork {
   std::vector<LevelWork> lv;
   DBuf<double> part, scal, pr, pz, pp, pq;
   DBuf<float2> xsplit;  // op0's input as (hi, lo) pairs (mixed mode)
+  DBuf<float> p32;      // the CG direction in FP32 (matrix-free CG operator)
   // PCG iteration body (V-cycle, direction, operator, update) captured as a
   // CUDA graph on this workspace's buffers; valid for one hierarchy epoch
   DBuf<double> px;      // the iterate (the caller's x is copied in and out)
@@ -178,6 +185,8 @@ class GpuAmg {
   cudaStream_t stream = 0;
 
   bool mixed() const { return opt.precision == 1; }
+  // the CG operator is the FP32 matrix-free product (matrix_free = 2, 3-D)
+  bool mf_cg() const { return mixed() && opt.matrix_free >= 2 && mf.enabled && mf.dim == 3; }
   // Set by an assembler that wrote level 0's FP32 values (hi in a.v32 and
   // lo in a.v32lo) itself; otherwise setup splits the FP64 values (mixed
   // mode).  In mixed mode the CG operator reads hi/lo only, so an assembler
@@ -217,6 +226,9 @@ class GpuAmg {
   // the PCG direction update).
   void op0(SolveWork& w, const double* x, double* y, const double* rhs, bool split_ready = false);
   void spmv0(const double* x, double* y) { op0(work(0), x, y, nullptr); }
+  // q = A p, the CG's own product: op0, or with mf_cg() the FP32 matrix-free
+  // product of p's FP32 copy (p32_ready: already in w.p32)
+  void cg_op(SolveWork& w, const double* p, double* q, bool p32_ready);
   // y = V x for caller's FP64 values V on level 0's pattern (a matrix of the
   // same structure: the stiffness or mass of a modal analysis)
   void apply_values0(SolveWork& w, const double* values, const double* x, double* y);

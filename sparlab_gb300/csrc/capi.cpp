@@ -34,6 +34,7 @@ AmgOptions convert(const simp_solver_options* o) {
   a.precision = o->precision;
   a.graphs = o->cuda_graphs != 0;
   a.mf_transfer = o->matrix_free_transfer != 0;
+  a.matrix_free = o->matrix_free;
   return a;
 }
 
@@ -49,6 +50,7 @@ void validate(const AmgOptions& o) {
   if (!(o.rtol > 0.0)) throw Error(kBadInput, "the iterative tolerance must be positive");
   if (o.precision != SIMP_PRECISION_FP64 && o.precision != SIMP_PRECISION_MIXED)
     throw Error(kBadInput, "unknown precision mode");
+  if (o.matrix_free < 0 || o.matrix_free > 2) throw Error(kBadInput, "matrix_free must be 0, 1 or 2");
 }
 
 template <class F>
@@ -116,6 +118,7 @@ void simp_default_options(simp_solver_options* o) {
   o->device = 0;
   o->cuda_graphs = 1;
   o->matrix_free_transfer = 1;
+  o->matrix_free = 1;
 }
 
 int simp_ctx_create(const simp_solver_options* opts, simp_ctx** out) {

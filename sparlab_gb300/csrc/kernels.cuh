@@ -195,11 +195,12 @@ __global__ void __launch_bounds__(kRedThreads) k_pcg_update(double* __restrict__
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// p = z + beta p
 // p = z + beta p; with ps, also its double-float split (the next operator
-// application's input in mixed precision)
+// application's input in mixed precision); with p32, its FP32 copy (the
+// input of the matrix-free CG operator)
 __global__ void k_pcg_direction(double* __restrict__ p, const double* __restrict__ z, i64 n,
-                                const PcgScalars* __restrict__ sc, float2* __restrict__ ps) {
+                                const PcgScalars* __restrict__ sc, float2* __restrict__ ps,
+                                float* __restrict__ p32) {
   const double beta = sc->beta;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     const double v = z[i] + beta * p[i];
@@ -208,6 +209,7 @@ __global__ void k_pcg_direction(double* __restrict__ p, const double* __restrict
       const float h = __double2float_rn(v);
       ps[i] = make_float2(h, __double2float_rn(v - static_cast<double>(h)));
     }
+    if (p32) p32[i] = __double2float_rn(v);
   }
 }
 

@@ -152,7 +152,8 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 // smoothed-prolongator transfers P = (I - w D^-1 A) P^ applied without P:
 // 5 x_s += t - w D^-1 A t (t = P^ x_c, the input), 6 y = b - A x with
 // dn = D^-1 y, 7 y = b - w A x (x = D^-1 r, b = r: the vector P^T maps to
-// the coarse right-hand side).
+// the coarse right-hand side); 8 y64 = A x in FP64 storage (the FP32 product
+// as the CG operator of the matrix-free variant).
 // ---------------------------------------------------------------------------
 constexpr int kTX = 32, kTY = 4, kTZ = 2;  // threads per block axis
 constexpr int kNZ = 1;                      // node layers per thread
@@ -171,6 +172,7 @@ struct MfArgs {
   const float* dinv;  // mode 3/4/5/6
   const float* coef;  // mode 3: (c1, c2); mode 4: 1 / theta; mode 5/7: w (device memory)
   int add_d;
+  double* y64;        // mode 8: output
 };
 
 template <int MODE>
@@ -295,10 +297,101 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
         const float ri = a.b[row] - o[k];
         a.y[row] = ri;
         a.dn[row] = a.dinv[row] * ri;
+      } else if (MODE == 8) {
+        a.y64[row] = static_cast<double>(o[k]);
       } else {
         a.y[row] = a.b[row] - a.coef[0] * o[k];
       }
     }
+  }
+}
+
+// FP64 variant of the tiled operator (same tile, halo and cell order): y =
+// A x (MODE 0) or y = b - A x (MODE 1) with FP64 values, scales and K_e^0.
+// It gives the matrix-free CG operator's true residuals, whose accuracy the
+// FP32 products inside CG lack; FP64-pipe bound (576 multiply-adds per
+// node), so it runs only at the restarts.
+struct KeF64 {
+  double k[24 * 24];
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile64(MfView m, const double* __restrict__ scale,
+                                                              const double* __restrict__ x, double* __restrict__ y,
+                                                              const double* __restrict__ b,
+                                                              const __grid_constant__ KeF64 ke) {
+  constexpr int NZ = kTZ * kNZ;
+  __shared__ double xh[3][NZ + 2][kTY + 2][kTX + 2];
+  __shared__ double sc[NZ + 1][kTY + 1][kTX + 1];
+  const int tid = threadIdx.x;
+  const i32 x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * NZ;
+  const i32 nnz = m.nz + 1;
+  constexpr int kHalo = (NZ + 2) * (kTY + 2) * (kTX + 2);
+  for (int e = tid; e < kHalo; e += kTX * kTY * kTZ) {
+    const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
+    const i32 gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
+    i32 j = -1;
+    if (gx >= 0 && gx < m.nnx && gy >= 0 && gy < m.nny && gz >= 0 && gz < nnz)
+      j = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    if (j >= 0) {
+      const double* p = x + static_cast<i64>(j) * 3;
+      v0 = p[0];
+      v1 = p[1];
+      v2 = p[2];
+    }
+    xh[0][hz][hy][hx] = v0;
+    xh[1][hz][hy][hx] = v1;
+    xh[2][hz][hy][hx] = v2;
+  }
+  for (int e = tid; e < (NZ + 1) * (kTY + 1) * (kTX + 1); e += kTX * kTY * kTZ) {
+    const int cx = e % (kTX + 1), cy = (e / (kTX + 1)) % (kTY + 1), cz = e / ((kTX + 1) * (kTY + 1));
+    const i32 gx = x0 - 1 + cx, gy = y0 - 1 + cy, gz = z0 - 1 + cz;
+    double s = 0.0;
+    if (gx >= 0 && gx < m.nx && gy >= 0 && gy < m.ny && gz >= 0 && gz < m.nz)
+      s = scale[(static_cast<i64>(gz) * m.ny + gy) * m.nx + gx];
+    sc[cz][cy][cx] = s;
+  }
+  __syncthreads();
+  const int tx = tid % kTX, ty = (tid / kTX) % kTY, tz = tid / (kTX * kTY);
+  const i32 gx = x0 + tx, gy = y0 + ty, gz = z0 + tz;
+  if (gx >= m.nnx || gy >= m.nny || gz >= nnz) return;
+  const i32 I = m.nindex[(static_cast<i64>(gz) * m.nny + gy) * m.nnx + gx];
+  if (I < 0) return;
+  double out0 = 0.0, out1 = 0.0, out2 = 0.0;
+#pragma unroll
+  for (int dz = -1; dz <= 0; ++dz)
+#pragma unroll
+    for (int dy = -1; dy <= 0; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 0; ++dx) {
+        const double s = sc[tz + dz + 1][ty + dy + 1][tx + dx + 1];
+        const int ox = -dx, oy = -dy, oz = -dz;
+        const int aI = 4 * oz + (oy ? 3 - ox : ox);
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+#pragma unroll
+        for (int bb = 0; bb < 8; ++bb) {
+          const int bx = (bb == 1 || bb == 2 || bb == 5 || bb == 6) ? 1 : 0;
+          const int by = (bb == 2 || bb == 3 || bb == 6 || bb == 7) ? 1 : 0;
+          const int bz = bb >= 4 ? 1 : 0;
+#pragma unroll
+          for (int kb = 0; kb < 3; ++kb) {
+            const double xv = xh[kb][tz + dz + 1 + bz][ty + dy + 1 + by][tx + dx + 1 + bx];
+            a0 = fma(ke.k[(3 * aI + 0) * 24 + 3 * bb + kb], xv, a0);
+            a1 = fma(ke.k[(3 * aI + 1) * 24 + 3 * bb + kb], xv, a1);
+            a2 = fma(ke.k[(3 * aI + 2) * 24 + 3 * bb + kb], xv, a2);
+          }
+        }
+        out0 = fma(s, a0, out0);
+        out1 = fma(s, a1, out1);
+        out2 = fma(s, a2, out2);
+      }
+  const double o[3] = {out0, out1, out2};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const i64 row = static_cast<i64>(I) * 3 + k;
+    if (MODE == 0) y[row] = o[k];
+    else y[row] = b[row] - o[k];
   }
 }
 

@@ -1,8 +1,9 @@
 // Filtered design volume with no device allocation.
 //
-// simp_filter_volume_noalloc computes rho = clamp(H x, 0, 1) and the volume
-// sum_e v_e rho_e of a structured problem, as simp_evaluate does for its
-// physical density and volume, but it allocates nothing: the per-chunk partial
+// simp_filter_volume_noalloc computes the physical density of a structured
+// problem -- rho = clamp(H x, 0, 1), Heaviside-projected at the current beta
+// and the objective's threshold when the problem has the projection on -- and
+// its volume sum_e v_e rho_e, as simp_evaluate does, but it allocates nothing: the per-chunk partial
 // sums live in a file-scope device array instead of a buffer from cudaMalloc.
 // It is meant for callers that cannot allocate device memory at the point of
 // the call: an optimiser loop that evaluates the volume of many trial designs
@@ -17,7 +18,8 @@
 //    that loads the library until the process exits;
 //  * the first call on a device looks up the array's device address with that
 //    device current and caches it, so make the first call before any stream
-//    capture on that device;
+//    capture on that device; a cudaDeviceReset after that first call is not
+//    supported (the cached address would be stale);
 //  * every call shares the one array: calls whose kernels overlap on the GPU
 //    (other streams, other threads) race on it.  Each call overwrites every
 //    partial it reads, so nothing has to start at zero.
@@ -61,11 +63,14 @@ double* scratch_address() {
 }
 
 // One block per chunk: rho for the chunk's elements and its volume partial.
+// project != 0: rho is the Heaviside projection of the clamped filtered
+// density at (beta, eta), as simp_evaluate's k_project computes it.
 __global__ void __launch_bounds__(kChunkThreads) k_volume_chunks(GridView g, const Stencil* __restrict__ st,
                                                                  const double* __restrict__ w, i64 ne,
                                                                  const double* __restrict__ x,
                                                                  double* __restrict__ rho,
                                                                  const double* __restrict__ vols,
+                                                                 int project, double beta, double eta,
                                                                  double* __restrict__ partial) {
   const i64 lo = static_cast<i64>(blockIdx.x) * kChunk;
   const i64 hi = lo + kChunk < ne ? lo + kChunk : ne;
@@ -81,6 +86,10 @@ __global__ void __launch_bounds__(kChunkThreads) k_volume_chunks(GridView g, con
       s = xadd(s, xmul(w[k * ne + e], x[q]));
     }
     s = fmin(fmax(s, 0.0), 1.0);
+    if (project) {
+      double deriv;
+      s = project_one(s, beta, eta, deriv);
+    }
     rho[e] = s;
     vs += s * vols[e];
   }
@@ -119,7 +128,8 @@ void filter_volume_noalloc(GpuProblem& p, const double* x, double* rho, double* 
   g.nny = p.d.ny + 1;
   g.nnz = p.d.dim == 3 ? p.d.nz + 1 : 1;
   k_volume_chunks<<<chunks, kChunkThreads, 0, p.amg.stream>>>(g, static_cast<const Stencil*>(p.stencil_d), p.hw.p,
-                                                              p.ne, x, rho, p.vols.p, scratch);
+                                                              p.ne, x, rho, p.vols.p, p.d.projection ? 1 : 0,
+                                                              p.beta, p.d.objective_eta(), scratch);
   SIMP_CHECK_LAUNCH();
   k_sum_chunks<<<1, kChunkThreads, 0, p.amg.stream>>>(scratch, chunks, volume);
   SIMP_CHECK_LAUNCH();

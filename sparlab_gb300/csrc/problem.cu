@@ -251,7 +251,7 @@ void GpuProblem::build() {
     const uint8_t full = static_cast<uint8_t>((1 << dim) - 1);
     bool all_or_nothing = true;
     for (uint8_t m : cmask_h) all_or_nothing = all_or_nothing && m == full;
-    if (amg.mixed() && all_or_nothing) {
+    if (amg.mixed() && all_or_nothing && amg.opt.matrix_free >= 1) {
       std::vector<float> k32(d.ke.begin(), d.ke.end());
       ke32.upload(k32);
       sf32.alloc(static_cast<size_t>(ne));
@@ -268,6 +268,7 @@ void GpuProblem::build() {
       mf.nindex = nindex.p;
       mf.ke = ke32.p;
       std::copy(k32.begin(), k32.end(), mf.ke_host);
+      std::copy(d.ke.begin(), d.ke.end(), mf.ke64_host);
       mf.scale = sf32.p;
     }
   }
@@ -281,6 +282,7 @@ void GpuProblem::build() {
   xnew.alloc(ne_s);
   rho.alloc(ne_s);
   sf.alloc(ne_s);
+  amg.mf.scale64 = sf.p;  // the FP64 SIMP factors (matrix-free CG operator)
   df.alloc(ne_s);
   dc_dphys.alloc(ne_s);
   dc_dx.alloc(ne_s);

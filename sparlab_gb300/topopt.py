@@ -260,7 +260,8 @@ class GpuSimpProblem:
 
     def filter_volume_noalloc(self, x_device_ptr: int, rho_device_ptr: int,
                               volume_device_ptr: int):
-        """Physical density rho = clamp(H x, 0, 1) and its volume, written to
+        """Physical density rho = clamp(H x, 0, 1) (Heaviside-projected at the
+        current beta when the projection is on) and its volume, written to
         device memory, without allocating any device memory.
 
         For callers that cannot call cudaMalloc where they evaluate volumes:
@@ -268,8 +269,9 @@ class GpuSimpProblem:
         the device on allocation, or an application that owns all device
         memory through its own pool.  Partial sums go to a fixed 128 KiB
         array of the library (at most 67,108,864 elements); make the first
-        call on a device before any stream capture, and do not let two calls
-        overlap on the GPU: they share that array."""
+        call on a device before any stream capture (and no cudaDeviceReset
+        after it), and do not let two calls overlap on the GPU: they share
+        that array."""
         self._check(self._lib.simp_filter_volume_noalloc(
             self._h, C.c_void_p(x_device_ptr), C.c_void_p(rho_device_ptr),
             C.c_void_p(volume_device_ptr)))
