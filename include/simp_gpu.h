@@ -180,7 +180,11 @@ typedef struct {
   double move_limit, damping;   /* OptimalityCriteriaOptions */
   int32_t warm_start;           /* 0: zero guess; 1: previous displacement
                                    (LinearSolverOptions::warm_start); 2: energy-
-                                   optimal combination of the last 3 displacements */
+                                   optimal combination of the last 3 displacements;
+                                   3: the same with the displacement surrogate's
+                                   prediction as one more vector (first solve: the
+                                   prediction's optimal multiple); needs
+                                   simp_problem_set_surrogate, else as 2 */
   int32_t block_pcg;            /* 1: the load cases' PCG solves run at the same time, each
                                    on its own workspace and stream (same results) */
   int32_t optimizer;            /* simp_iterate's update: 0 OC, 1 MMA */
@@ -450,6 +454,65 @@ const char* simp_buckling_warning(simp_problem* p, int32_t k);
  * Gauss per direction. */
 int simp_element_mass(int32_t dim, double hx, double hy, double hz, double density,
                       double thickness, double* me);
+
+/* ---- Displacement surrogate (the learned PCG start, warm_start = 3) -----
+ * No counterpart in the reference, whose solves start from the previous
+ * displacement (src/topopt/Sensitivity.cpp:142, 169-176 with
+ * src/fem/StaticAnalysis.cpp:134-143).  A 3-D convolutional encoder-decoder
+ * on the nodal grid (4 levels, 16/32/64/64 channels, 3x3x3 kernels, BF16
+ * weights and activations, FP32 accumulation on the tensor cores) maps the
+ * physical (filtered) density and a load case to a displacement shape; its
+ * prediction joins the energy-optimal PCG start, so the PCG converges to the
+ * unchanged tolerance whatever the prediction's error.  3-D problems only. */
+typedef struct simp_surrogate simp_surrogate;
+
+/* Message of the last failed surrogate or layer call on this thread. */
+const char* simp_surrogate_last_error(void);
+
+/* A network with seeded He-uniform weights on `device`. */
+int simp_surrogate_create(int32_t device, uint64_t seed, simp_surrogate** out);
+void simp_surrogate_destroy(simp_surrogate* s);
+/* FP32 parameters, layer by layer: weights [27][cout][cin] (tap t = 9 (dz+1)
+ * + 3 (dy+1) + (dx+1)) then biases [cout]; in-order layers e0a e0b e1a e1b
+ * e2a e2b e3a e3b d2 d1 d0 head. */
+int simp_surrogate_num_params(simp_surrogate* s, int64_t* n);
+int simp_surrogate_get_params(simp_surrogate* s, float* params);
+int simp_surrogate_set_params(simp_surrogate* s, const float* params);
+/* Adds (the problem's physical density and load case, its displacement of
+ * the last evaluation) to the device-resident training set. */
+int simp_surrogate_add_sample(simp_surrogate* s, simp_problem* p, int32_t load_case);
+int simp_surrogate_num_samples(simp_surrogate* s, int32_t* n);
+/* Adam on the samples (seeded shuffle), `batch` samples per step, learning
+ * rate cosine-decayed from learning_rate to learning_rate / 20; the mean
+ * loss of each epoch goes to epoch_losses (epochs values) when non-NULL. */
+int simp_surrogate_train(simp_surrogate* s, int32_t epochs, double learning_rate, int32_t batch, uint64_t seed,
+                         double* epoch_losses);
+/* Predicted displacement shape of load case `load_case` at the problem's
+ * current physical density: nfree doubles on the device. */
+int simp_surrogate_predict(simp_surrogate* s, simp_problem* p, int32_t load_case, double* u_device);
+/* The network on a caller's input: nx x ny x nz nodes, 16 BF16 channels per
+ * node (channels-last, x fastest) -> 3 FP32 values per node (device). */
+int simp_surrogate_forward(simp_surrogate* s, int32_t nx, int32_t ny, int32_t nz, const void* input_device,
+                           float* output_device);
+/* Attaches the surrogate (not owned; NULL detaches) for warm_start 3. */
+int simp_problem_set_surrogate(simp_problem* p, simp_surrogate* s);
+/* Seconds the problem's solves spent in the surrogate's predictions. */
+int simp_problem_learned_seconds(simp_problem* p, double* seconds);
+
+/* Layers of the surrogate on device pointers (BF16 channels-last tensors,
+ * x fastest).  simp_conv3d_bf16: out = act(sum_t W_t in[. + o_t] + bias) for
+ * the 27 taps o_t of a 3x3x3 stencil with zero padding; `nseg` inputs
+ * concatenated along channels (16, 32 or 64 each), weights [27][n][sum cseg]
+ * BF16, n output columns (16..128, step 16) written to `nout` tensors
+ * (columns split at out_c[0]; BF16, or FP32 where out_f32[k]).  flip != 0
+ * negates the offsets (the data gradient, with transposed weights).
+ * simp_conv3d_wgrad: gw[t][co][ci] += sum_v dy[v][co] in[v + o_t][ci],
+ * gb[co] += sum_v dy[v][co] (FP32, device; dy has cdy channels). */
+int simp_conv3d_bf16(int32_t nx, int32_t ny, int32_t nz, int32_t nseg, const void* const* in, const int32_t* cseg,
+                     const void* weights, int32_t n, const float* bias, int32_t relu, int32_t flip, int32_t nout,
+                     void* const* out, const int32_t* out_c, const int32_t* out_pitch, const int32_t* out_f32);
+int simp_conv3d_wgrad(int32_t nx, int32_t ny, int32_t nz, int32_t nseg, const void* const* in, const int32_t* cseg,
+                      const void* dy, int32_t cdy, int32_t cout, float* gw, float* gb);
 
 /* Number of kernels this library has launched (for launch accounting). */
 int64_t simp_kernel_launches(void);

@@ -34,7 +34,12 @@ EXPORTS = [
     "simp_problem_apply_operator", "simp_problem_time_operator", "simp_filter_volume_noalloc",
     "simp_kernel_launches", "simp_default_modal_options", "simp_modal", "simp_modal_warning",
     "simp_element_mass", "simp_default_buckling_options", "simp_buckling", "simp_buckling_warning",
-    "simp_projection_variants",
+    "simp_projection_variants", "simp_surrogate_last_error", "simp_surrogate_create",
+    "simp_surrogate_destroy", "simp_surrogate_num_params", "simp_surrogate_get_params",
+    "simp_surrogate_set_params", "simp_surrogate_add_sample", "simp_surrogate_num_samples",
+    "simp_surrogate_train", "simp_surrogate_predict", "simp_surrogate_forward",
+    "simp_problem_set_surrogate", "simp_problem_learned_seconds", "simp_conv3d_bf16",
+    "simp_conv3d_wgrad",
 ]
 
 
@@ -165,6 +170,7 @@ def load(build_if_missing: bool = True):
             lib.simp_kernel_launches.restype = C.c_int64
             lib.simp_modal_warning.restype = C.c_char_p
             lib.simp_buckling_warning.restype = C.c_char_p
+            lib.simp_surrogate_last_error.restype = C.c_char_p
             _lib = lib
     return _lib
 

@@ -3,6 +3,7 @@
 
 #include "amg.h"
 #include "problem.h"
+#include "surrogate_net.h"
 
 #include <algorithm>
 #include <cmath>
@@ -504,7 +505,7 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     if (!(d.move > 0.0 && d.move <= 1.0)) throw Error(kBadInput, "optimizer.move_limit must lie in (0, 1]");
     d.damping = dsc->damping;
     if (!(d.damping > 0.0 && d.damping <= 1.0)) throw Error(kBadInput, "optimizer.damping must lie in (0, 1]");
-    if (dsc->warm_start < 0 || dsc->warm_start > 2) throw Error(kBadInput, "warm_start must be 0, 1 or 2");
+    if (dsc->warm_start < 0 || dsc->warm_start > 3) throw Error(kBadInput, "warm_start must be 0, 1, 2 or 3");
     d.warm = dsc->warm_start;
     d.block_pcg = dsc->block_pcg != 0;
     d.projection = dsc->projection != 0;
@@ -928,5 +929,131 @@ int simp_element_mass(int32_t dim, double hx, double hy, double hz, double densi
 }
 
 int64_t simp_kernel_launches(void) { return g_launches.load(); }
+
+}  // extern "C"
+
+// ---- the displacement surrogate (surrogate_net.cu) ---------------------
+struct simp_surrogate {
+  std::unique_ptr<sg::Surrogate> s;
+  int device = 0;
+};
+
+namespace {
+template <class F>
+int sg_guarded(F&& f) {
+  try {
+    f();
+    return kOk;
+  } catch (const Error& e) {
+    sg::last_error() = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    sg::last_error() = "out of host memory";
+    return kBadInput;
+  } catch (const std::exception& e) {
+    sg::last_error() = e.what();
+    return kBadInput;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int simp_surrogate_create(int32_t device, uint64_t seed, simp_surrogate** out) {
+  return sg_guarded([&] {
+    if (!out) throw Error(kBadInput, "simp_surrogate_create: out is NULL");
+    use_device(device);
+    std::unique_ptr<simp_surrogate> h(new simp_surrogate());
+    h->device = device;
+    h->s.reset(new sg::Surrogate(seed));
+    *out = h.release();
+  });
+}
+
+void simp_surrogate_destroy(simp_surrogate* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  delete s;
+}
+
+int simp_surrogate_num_params(simp_surrogate* s, int64_t* n) {
+  return sg_guarded([&] { *n = static_cast<int64_t>(s->s->net.nparams); });
+}
+
+int simp_surrogate_get_params(simp_surrogate* s, float* params) {
+  return sg_guarded([&] {
+    use_device(s->device);
+    s->s->net.get_params(params);
+  });
+}
+
+int simp_surrogate_set_params(simp_surrogate* s, const float* params) {
+  return sg_guarded([&] {
+    use_device(s->device);
+    s->s->net.set_params(params);
+  });
+}
+
+int simp_surrogate_add_sample(simp_surrogate* s, simp_problem* p, int32_t load_case) {
+  return sg_guarded([&] {
+    use_device(s->device);
+    if (load_case < 0 || load_case >= p->p->d.nloads) throw Error(kBadInput, "load case out of range");
+    s->s->add_sample(*p->p, load_case);
+  });
+}
+
+int simp_surrogate_num_samples(simp_surrogate* s, int32_t* n) {
+  return sg_guarded([&] { *n = static_cast<int32_t>(s->s->samples.size()); });
+}
+
+int simp_surrogate_train(simp_surrogate* s, int32_t epochs, double learning_rate, int32_t batch, uint64_t seed,
+                         double* epoch_losses) {
+  return sg_guarded([&] {
+    use_device(s->device);
+    if (epochs < 1 || batch < 1 || !(learning_rate > 0.0)) throw Error(kBadInput, "simp_surrogate_train: bad options");
+    const size_t before = s->s->losses.size();
+    s->s->train(epochs, learning_rate, batch, seed);
+    if (epoch_losses)
+      for (int e = 0; e < epochs; ++e) epoch_losses[e] = s->s->losses[before + static_cast<size_t>(e)];
+  });
+}
+
+int simp_surrogate_predict(simp_surrogate* s, simp_problem* p, int32_t load_case, double* u_device) {
+  return sg_guarded([&] {
+    use_device(s->device);
+    if (load_case < 0 || load_case >= p->p->d.nloads) throw Error(kBadInput, "load case out of range");
+    if (!u_device) throw Error(kBadInput, "simp_surrogate_predict: NULL output");
+    s->s->predict(*p->p, load_case, u_device);
+  });
+}
+
+int simp_surrogate_forward(simp_surrogate* s, int32_t nx, int32_t ny, int32_t nz, const void* input_device,
+                           float* output_device) {
+  return sg_guarded([&] {
+    use_device(s->device);
+    if (nx < 2 || ny < 2 || nz < 2) throw Error(kBadInput, "simp_surrogate_forward: at least 2 nodes per axis");
+    sg::Net& net = s->s->net;
+    net.shape(nx, ny, nz);
+    const size_t nodes = static_cast<size_t>(nx) * ny * nz;
+    SIMP_CUDA(cudaMemcpyAsync(net.in16.p, input_device, nodes * 16 * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice,
+                              net.stream));
+    net.forward();
+    SIMP_CUDA(cudaMemcpyAsync(output_device, net.out.p, nodes * 3 * sizeof(float), cudaMemcpyDeviceToDevice,
+                              net.stream));
+    SIMP_CUDA(cudaStreamSynchronize(net.stream));
+    net.check_status();
+  });
+}
+
+int simp_problem_set_surrogate(simp_problem* p, simp_surrogate* s) {
+  return guarded(p->err, [&] {
+    if (s && s->device != p->device) throw Error(kBadInput, "the surrogate lives on another device");
+    p->p->surrogate = s ? s->s.get() : nullptr;
+  });
+}
+
+int simp_problem_learned_seconds(simp_problem* p, double* seconds) {
+  return guarded(p->err, [&] { *seconds = p->p->learned_seconds; });
+}
 
 }  // extern "C"

@@ -297,10 +297,10 @@ void GpuProblem::build() {
     for (i32 i = 0; i < nfree; ++i) bh[static_cast<size_t>(l) * nfree + i] = d.loads[l * ndof + free_dofs_[i]];
   b.upload(bh);
   u.alloc(static_cast<size_t>(nfree) * d.nloads);
-  if (d.warm == 2) {
-    hist.alloc(static_cast<size_t>(nfree) * d.nloads * kHistory);
-    khist.alloc(static_cast<size_t>(nfree) * kHistory);
-    hpart.alloc(static_cast<size_t>(kRedBlocks) * (kHistory * (kHistory + 1) / 2 + kHistory));
+  if (d.warm >= 2) {
+    hist.alloc(static_cast<size_t>(nfree) * d.nloads * kBasis);
+    khist.alloc(static_cast<size_t>(nfree) * kBasis);
+    hpart.alloc(static_cast<size_t>(kRedBlocks) * (kBasis * (kBasis + 1) / 2 + kBasis));
     hist_count.assign(static_cast<size_t>(d.nloads), 0);
   }
   u.zero();
@@ -556,14 +556,16 @@ Evaluation GpuProblem::evaluate() {
     const cudaStream_t ws = w.stream;
     double* ul = u.p + static_cast<size_t>(l) * nfree;
     const double* bl = b.p + static_cast<size_t>(l) * nfree;
-    if (d.warm == 0 || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, ws));
-    else if (d.warm == 2 && hist_count[l] > 0) projected_start(l, ul);
+    const bool learned = d.warm == 3 && surrogate != nullptr;
+    if (learned) projected_start(l, ul, true);  // also the first solve: the prediction alone
+    else if (d.warm == 0 || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, ws));
+    else if (d.warm >= 2 && hist_count[l] > 0) projected_start(l, ul, false);
     res[static_cast<size_t>(l)] = amg.solve(w, bl, ul);
     // c_l = f^T u (u vanishes on the supports)
     last_compliance[static_cast<size_t>(l)] = amg.dot(w, bl, ul, nfree);
-    if (d.warm == 2) record_history(l, ul);
+    if (d.warm >= 2) record_history(l, ul);
   };
-  const bool together = d.block_pcg && d.nloads > 1 && d.warm != 2;
+  const bool together = d.block_pcg && d.nloads > 1 && d.warm < 2;
   if (together) {
     SIMP_CUDA(cudaStreamSynchronize(s));  // assembly and setup are done before the solves start
     int dev = 0;

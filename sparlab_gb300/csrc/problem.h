@@ -15,7 +15,12 @@
 
 namespace simp {
 
-constexpr int kHistory = 3;  // displacements kept per load case by warm start 2
+constexpr int kHistory = 3;  // displacements kept per load case by warm starts 2 and 3
+constexpr int kBasis = kHistory + 1;  // + the surrogate's prediction (warm start 3)
+
+namespace sg {
+class Surrogate;
+}
 
 struct ProblemDesc {
   int dim = 3;
@@ -28,7 +33,8 @@ struct ProblemDesc {
   std::vector<double> loads;    // nloads x ndof
   std::vector<double> weights;  // normalised
   double radius = 1.5, vf = 0.5, x0 = 0.5, penalty = 3.0, emin = 1e-9, move = 0.2, damping = 0.5;
-  int warm = 1;  // 0 zero start, 1 previous displacement, 2 projection on the last kHistory
+  int warm = 1;  // 0 zero start, 1 previous displacement, 2 projection on the last kHistory,
+                 // 3 projection on the last kHistory and the surrogate's prediction
   bool block_pcg = false;
   int optimizer = 0;  // 0 OC, 1 MMA
   // Heaviside projection (src/topopt/Projection.cpp) with beta continuation
@@ -117,10 +123,13 @@ class GpuProblem {
       m_etao, m_dx, m_dxsi, m_deta, m_delx, m_diagx, m_gg, mpart;
   void mma_reduce(int k, std::vector<double>& out);
   double mma_reduce_max(int which);
-  // warm start 2 (warmstart.cu): newest-first displacement history per load
+  // warm starts 2 and 3 (warmstart.cu): newest-first displacement history
+  // per load (kBasis slots: the last one takes the surrogate's prediction)
   DBuf<double> hist, khist, hpart;
   std::vector<int> hist_count;
-  void projected_start(int l, double* ul);
+  sg::Surrogate* surrogate = nullptr;  // warm start 3 (not owned)
+  double learned_seconds = 0.0;        // time in the surrogate's predictions
+  void projected_start(int l, double* ul, bool learned);
   void record_history(int l, const double* ul);
   // projection state: current beta, its stage, the stage's first iteration
   double beta = 0.0;

@@ -1,4 +1,4 @@
-// Projected initial guess for the per-load PCG (warm_start = 2).
+// Projected initial guess for the per-load PCG (warm_start = 2 and 3).
 //
 // The reference warm-starts each solve from the previous iteration's
 // displacement (StaticAnalysis::solve_load_vector with LinearSolverOptions::
@@ -9,19 +9,27 @@
 //   x0 = U c,  (U^T K U) c = U^T f,
 //
 // which is never worse in the energy norm than x0 = u_1 (c = e_1 lies in the
-// search space).  Nearly dependent history vectors are dropped by a pivoted
-// LDL^T of the k x k Gram matrix.  Cost: k FP64 operator applications and one
-// fused multi-dot pass; the PCG itself is unchanged.
+// search space).  Mode 3 adds the displacement surrogate's prediction for the
+// current density as one more basis vector (after the history, so a
+// prediction that adds nothing is the one dropped); on the first solve, with
+// no history, the start is the prediction's energy-optimal multiple.  A
+// non-finite or zero prediction drops out the same way, which leaves the
+// history's start (or zero).  Nearly dependent vectors are dropped by a
+// pivoted LDL^T of the Gram matrix.  Cost: one FP64 operator application per
+// basis vector, one fused multi-dot pass and (mode 3) one network inference;
+// the PCG itself is unchanged.
 #include "kernels.cuh"
 #include "problem.h"
+#include "surrogate_net.h"
 
+#include <chrono>
 #include <cmath>
 
 namespace simp {
 
 namespace {
 
-constexpr int kDots = kHistory * (kHistory + 1) / 2 + kHistory;
+constexpr int kDots = kBasis * (kBasis + 1) / 2 + kBasis;
 
 // partials of u_i . (K u_j) (i <= j) and u_i . f, per block
 __global__ void __launch_bounds__(kRedThreads) k_history_dots(i64 n, int k, const double* __restrict__ u,
@@ -32,20 +40,20 @@ __global__ void __launch_bounds__(kRedThreads) k_history_dots(i64 n, int k, cons
 #pragma unroll
   for (int q = 0; q < kDots; ++q) acc[q] = 0.0;
   for (i64 e = blockIdx.x * (i64)kRedThreads + threadIdx.x; e < n; e += (i64)gridDim.x * kRedThreads) {
-    double ue[kHistory], ke[kHistory];
+    double ue[kBasis], ke[kBasis];
 #pragma unroll
-    for (int i = 0; i < kHistory; ++i) {
+    for (int i = 0; i < kBasis; ++i) {
       ue[i] = i < k ? u[i * n + e] : 0.0;
       ke[i] = i < k ? ku[i * n + e] : 0.0;
     }
     const double fe = f[e];
     int q = 0;
 #pragma unroll
-    for (int i = 0; i < kHistory; ++i)
+    for (int i = 0; i < kBasis; ++i)
 #pragma unroll
-      for (int j = i; j < kHistory; ++j) acc[q++] += ue[i] * ke[j];
+      for (int j = i; j < kBasis; ++j) acc[q++] += ue[i] * ke[j];
 #pragma unroll
-    for (int i = 0; i < kHistory; ++i) acc[q++] += ue[i] * fe;
+    for (int i = 0; i < kBasis; ++i) acc[q++] += ue[i] * fe;
   }
 #pragma unroll
   for (int q = 0; q < kDots; ++q) {
@@ -55,7 +63,7 @@ __global__ void __launch_bounds__(kRedThreads) k_history_dots(i64 n, int k, cons
 }
 
 struct Coefs {
-  double c[kHistory];
+  double c[kBasis];
 };
 
 __global__ void k_history_combine(i64 n, int k, const double* __restrict__ u, Coefs c, double* __restrict__ x) {
@@ -68,11 +76,21 @@ __global__ void k_history_combine(i64 n, int k, const double* __restrict__ u, Co
 
 }  // namespace
 
-void GpuProblem::projected_start(int l, double* ul) {
+void GpuProblem::projected_start(int l, double* ul, bool learned) {
   cudaStream_t s = amg.stream;
-  const int k = hist_count[l];
+  int k = hist_count[l];
   const i64 n = nfree;
-  const double* U = hist.p + static_cast<size_t>(l) * kHistory * n;
+  double* U = hist.p + static_cast<size_t>(l) * kBasis * n;
+  if (learned) {  // the prediction takes the slot after the history
+    const auto t0 = std::chrono::steady_clock::now();
+    surrogate->predict(*this, l, U + static_cast<size_t>(k) * n);
+    learned_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    ++k;
+  }
+  if (k == 0) {
+    SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * n, s));
+    return;
+  }
   const double* f = b.p + static_cast<size_t>(l) * n;
   for (int i = 0; i < k; ++i) amg.spmv0(U + i * n, khist.p + i * n);
   k_history_dots<<<kRedBlocks, kRedThreads, 0, s>>>(n, k, U, khist.p, f, hpart.p);
@@ -86,18 +104,18 @@ void GpuProblem::projected_start(int l, double* ul) {
     for (int p = 0; p < kRedBlocks; ++p) t += hp[static_cast<size_t>(q) * kRedBlocks + p];
     dots[q] = t;
   }
-  double G[kHistory][kHistory] = {}, g[kHistory] = {};
+  double G[kBasis][kBasis] = {}, g[kBasis] = {};
   int q = 0;
-  for (int i = 0; i < kHistory; ++i)
-    for (int j = i; j < kHistory; ++j) {
+  for (int i = 0; i < kBasis; ++i)
+    for (int j = i; j < kBasis; ++j) {
       G[i][j] = G[j][i] = dots[q];
       ++q;
     }
-  for (int i = 0; i < kHistory; ++i) g[i] = dots[q++];
+  for (int i = 0; i < kBasis; ++i) g[i] = dots[q++];
   // LDL^T in history order (newest first); a pivot below 1e-10 of its
   // diagonal marks a dependent vector, whose coefficient is zero
-  double L[kHistory][kHistory] = {}, D[kHistory] = {};
-  bool keep[kHistory] = {};
+  double L[kBasis][kBasis] = {}, D[kBasis] = {};
+  bool keep[kBasis] = {};
   for (int j = 0; j < k; ++j) {
     double dj = G[j][j];
     for (int p = 0; p < j; ++p)
@@ -112,7 +130,7 @@ void GpuProblem::projected_start(int l, double* ul) {
     }
   }
   Coefs c{};
-  double y[kHistory] = {};
+  double y[kBasis] = {};
   for (int i = 0; i < k; ++i) {
     double v = g[i];
     for (int p = 0; p < i; ++p) v -= L[i][p] * y[p];
@@ -125,14 +143,17 @@ void GpuProblem::projected_start(int l, double* ul) {
   }
   bool finite = true;
   for (int i = 0; i < k; ++i) finite = finite && std::isfinite(c.c[i]);
-  if (!finite) return;  // keep the previous displacement
+  if (!finite) {  // keep the previous displacement (zero on a first solve)
+    if (hist_count[l] == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * n, s));
+    return;
+  }
   k_history_combine<<<grid_for(n, 256, 8192), 256, 0, s>>>(n, k, U, c, ul);
   SIMP_CHECK_LAUNCH();
 }
 
 void GpuProblem::record_history(int l, const double* ul) {
   const i64 n = nfree;
-  double* U = hist.p + static_cast<size_t>(l) * kHistory * n;
+  double* U = hist.p + static_cast<size_t>(l) * kBasis * n;
   // newest first: shift the older vectors down one slot
   const int k = std::min(hist_count[l] + 1, kHistory);
   for (int i = k - 1; i > 0; --i)

@@ -194,6 +194,18 @@ class GpuSimpProblem:
         if code:
             _lib.raise_for(code, self._lib.simp_problem_last_error(self._h).decode())
 
+    def set_surrogate(self, surrogate):
+        """Attaches a displacement surrogate (sparlab_gb300.surrogate) for
+        warm start 3; None detaches.  The problem keeps no ownership."""
+        self._surrogate = surrogate
+        self._check(self._lib.simp_problem_set_surrogate(self._h, surrogate.handle if surrogate else None))
+
+    def learned_seconds(self) -> float:
+        """Seconds this problem's solves spent in surrogate predictions."""
+        v = C.c_double()
+        self._check(self._lib.simp_problem_learned_seconds(self._h, C.byref(v)))
+        return v.value
+
     def set_design(self, x):
         x = np.ascontiguousarray(x, np.float64)
         self._check(self._lib.simp_set_design(self._h, ptr(x)))

@@ -95,7 +95,7 @@ def test_context_creation_rejects_bad_options_before_touching_the_device(field, 
     ("volume_fraction", 0.0, "volume fraction"),
     ("move_limit", 0.0, "move_limit"),
     ("damping", 1.5, "damping"),
-    ("warm_start", 3, "warm_start"),
+    ("warm_start", 4, "warm_start"),
 ])
 def test_problem_creation_rejects_bad_descriptors_before_touching_the_device(field, value, words):
     """SimpOptions::validate (src/topopt/SimpInterpolation.cpp:31-44; tests/
