@@ -10,13 +10,17 @@ API with the design copied from pinned host memory and back every step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl own|reference]
                   [--config NAME] [--precision fp64|mixed]
-                  [--warm zero|previous|projection]
+                  [--warm zero|previous|projection|learned]
+
+`--warm learned` trains the displacement surrogate before the timed region
+(2,000 pairs from plain FP64 SIMP runs of seeded variants) and starts every
+PCG solve from the energy-optimal combination of the previous displacements
+and its prediction.
 
 `--impl reference` times the CPU restatement of the reference's algorithm (the
-reference itself needs Eigen, which is absent) on the host cores, on a bounded
-sample of the workload (a geometrically similar grid with 1/64 of the cells,
-whose iteration time is scaled by the cell ratio: the reference's AMG-CG costs
-grow linearly, docs/benchmarks.md:1455-1458 of the reference).
+reference itself needs Eigen, which is absent) on the host cores, on the full
+workload: W warm-up SIMP iterations (the first builds the hierarchy), then K
+timed iterations, each a complete SIMP iteration of the full grid.
 """
 from __future__ import annotations
 
@@ -38,7 +42,7 @@ import numpy as np  # noqa: E402
 from sparlab_gb300 import problems as P  # noqa: E402
 
 # PCG initial guess per load case (simp_problem_desc.warm_start)
-WARM = {"zero": 0, "previous": 1, "projection": 2}
+WARM = {"zero": 0, "previous": 1, "projection": 2, "learned": 3}
 
 METRIC = "SIMP iter/s at Hex8 1.77M elts, compliance err<=1e-6: plain vs learned+mixed"
 
@@ -120,15 +124,12 @@ def buckling_cpu_baseline():
                       f"iterations, one analysis ({t:.2f} s), scaled by the cell ratio 64"}
 
 
-def sample_spec(name):
-    """Bounded CPU sample: the same cantilever with every axis halved twice."""
-    make, sub = WORKLOADS[name]
-    full = make()
-    if sub is None:
-        return full, 1.0
-    nx, ny, nz = full.nx // 4, full.ny // 4, full.nz // 4
-    spec = P.hex8_cantilever(nx, ny, nz, full.volume_fraction, full.name + "_sample")
-    return spec, full.num_elements / spec.num_elements
+def workload_config(spec):
+    """The static description of a workload, printed identically by both
+    arms (run-specific figures go to the line's "run" object)."""
+    return {"workload": spec.name, "elements": spec.num_elements, "free_dofs": int(len(spec.free_dofs())),
+            "load_cases": int(spec.loads.shape[0]), "volume_fraction": spec.volume_fraction,
+            "filter_radius": spec.filter_radius, "rtol": spec.rtol}
 
 
 class ClockSampler:
@@ -193,26 +194,28 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(name, steps=2):
-    """Oracle SIMP iterations on the bounded sample, all host threads."""
+def cpu_baseline(spec):
+    """The oracle (the reference's algorithms, OpenMP on every host core where
+    the reference uses it) on the full workload: the first SIMP iteration
+    builds the hierarchy, the second is timed.  Also returns the oracle's
+    first two iterations (compliance, CG iterations) for the parity check."""
     import oracle
-    spec, ratio = sample_spec(name)
     pr = oracle.Problem(spec)
-    x = np.full(pr.ne, spec.volume_fraction)
-    ev = pr.evaluate(x)                      # first evaluation builds the hierarchy
+    x = np.full(pr.ne, spec.volume_fraction if spec.initial_density < 0 else spec.initial_density)
+    first = []
+    ev = pr.evaluate(x)
+    first.append((float(ev["compliance"]), int(ev["linear_iterations"])))
     x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
-    times = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        ev = pr.evaluate(x)
-        x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
-        times.append(time.perf_counter() - t0)
-    t = min(times)
-    cores = os.cpu_count()
-    return {"value": 1.0 / (t * ratio), "unit": "iter/s", "cores": cores, "kind": "port",
-            "sample": f"{spec.name}: {spec.nx}x{spec.ny}" + (f"x{spec.nz}" if spec.dim == 3 else "") +
-                      f" cells (1/{ratio:.0f} of the workload's), min of {steps} SIMP iterations "
-                      f"({t:.3f} s each) after one setup iteration, scaled by the cell ratio {ratio:.0f}"}
+    t0 = time.perf_counter()
+    ev = pr.evaluate(x)
+    x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
+    t = time.perf_counter() - t0
+    first.append((float(ev["compliance"]), int(ev["linear_iterations"])))
+    base = {"value": 1.0 / t, "unit": "iter/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{spec.name} at full size: its second SIMP iteration ({t:.2f} s, "
+                      f"{first[1][1]} CG iterations; the first builds the hierarchy); the timed GPU steps "
+                      f"are later iterations, which need more CG iterations"}
+    return base, first
 
 
 def batched_cpu_baseline(specs, every=8):
@@ -283,30 +286,38 @@ def run_reference(args):
         }), flush=True)
         return
     import oracle
-    spec, ratio = sample_spec(args.config)
+    spec = WORKLOADS[args.config][0]()
     pr = oracle.Problem(spec)
-    x = np.full(pr.ne, spec.volume_fraction)
-    for _ in range(max(1, args.warmup)):
+    x = np.full(pr.ne, spec.volume_fraction if spec.initial_density < 0 else spec.initial_density)
+    warm_s = time.perf_counter()
+    for _ in range(max(1, args.warmup)):     # the first iteration builds the hierarchy
         ev = pr.evaluate(x)
         x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
-    t0 = time.perf_counter()
+    warm_s = time.perf_counter() - warm_s
+    times, comp, its = [], [], []
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         ev = pr.evaluate(x)
         x, _ = pr.oc_update(x, ev["dc_dx"], ev["dv_dx"])
-    el = time.perf_counter() - t0
-    per = el / args.steps
-    value = 1.0 / (per * ratio)
-    full = WORKLOADS[args.config][0]()
+        times.append(time.perf_counter() - t0)
+        comp.append(float(ev["compliance"]))
+        its.append(int(ev["linear_iterations"]))
+    per = sum(times) / len(times)
+    value = 1.0 / per
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * ratio * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic seeded cantilever (no dataset)",
-        "config": {"workload": full.name, "elements": full.num_elements,
-                   "precision": "fp64", "host_threads": os.cpu_count()},
+        "config": workload_config(spec),
+        "run": {"implementation": "the oracle: a C++ restatement of the reference's algorithms (the reference "
+                                  "needs Eigen, absent here); OpenMP where the reference uses it",
+                "host_threads": os.cpu_count(), "warmup_seconds": round(warm_s, 2),
+                "step_seconds": [round(t, 3) for t in times],
+                "cg_iterations_per_step": its, "compliance_per_step": comp},
         "cpu_baseline": {"value": value, "unit": "iter/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{spec.nx}x{spec.ny}x{spec.nz} Hex8 (1/{ratio:.0f} of the cells), "
-                                   f"{args.steps} SIMP iterations, scaled by the cell ratio"},
+                         "sample": f"the full {spec.name} workload: {args.steps} SIMP iterations timed after "
+                                   f"{max(1, args.warmup)} warm-up iterations (the first builds the hierarchy)"},
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -566,6 +577,24 @@ def run_own_batched(args):
         dist.destroy_process_group()
 
 
+def train_surrogate(args, device):
+    """The learned start's network, trained before the timed region on
+    (density, displacement) pairs that the plain FP64 solver produces along
+    20-iteration SIMP runs of 100 seeded Hex8 cantilever variants (seeds
+    100-149 on 48 x 24 x 24, 150-199 on 96 x 48 x 48): 2,000 pairs."""
+    from sparlab_gb300.surrogate import Surrogate, generate_samples, training_variants
+    sur = Surrogate(seed=7, device=device)
+    t0 = time.perf_counter()
+    generate_samples(sur, training_variants(range(100, 200)), iterations=20, precision="fp64")
+    t1 = time.perf_counter()
+    losses = sur.train(epochs=args.train_epochs, learning_rate=2e-3, batch=4, seed=11)
+    t2 = time.perf_counter()
+    info = {"pairs": sur.num_samples, "generation_seconds": round(t1 - t0, 1),
+            "training_seconds": round(t2 - t1, 1), "epochs": args.train_epochs,
+            "epoch_losses": [round(v, 6) for v in losses], "parameters": sur.num_params}
+    return sur, info
+
+
 def run_own(args):
     import torch
     import torch.distributed as dist
@@ -581,15 +610,22 @@ def run_own(args):
     dev = torch.device("cuda", local)
 
     spec = WORKLOADS[args.config][0]()
-    spec.warm_start = WARM[args.warm]
+    learned = args.warm == "learned" and spec.dim == 3
+    spec.warm_start = WARM["learned" if learned else ("previous" if args.warm == "learned" else args.warm)]
     together = not args.sequential_loads
-    prob = GpuSimpProblem(spec, precision=args.precision, device=local, block_pcg=together)
     lib = _lib.load()
+    sur, sur_info = (train_surrogate(args, local) if learned else (None, None))
 
+    def make(precision, with_surrogate=True):
+        p = GpuSimpProblem(spec, precision=precision, device=local, block_pcg=together)
+        if with_surrogate and sur is not None:
+            p.set_surrogate(sur)
+        return p
+
+    prob = make(args.precision)
     # warm-up: the first iteration builds the hierarchy
     t_setup = time.perf_counter()
-    for _ in range(args.warmup):
-        prob.iterate()
+    warm_recs = [prob.iterate() for _ in range(args.warmup)]
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t_setup
 
@@ -601,6 +637,7 @@ def run_own(args):
     sampler = ClockSampler(local)
     barrier()
     launches0 = lib.simp_kernel_launches()
+    learned0 = prob.learned_seconds()
     sampler.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -609,13 +646,14 @@ def run_own(args):
     barrier()
     clocks = sampler.stop()
     launches = lib.simp_kernel_launches() - launches0
+    learned_s = prob.learned_seconds() - learned0
     ms, value = whole_job_rate(e0.elapsed_time(e1), args.steps, world, dev)
     per_step = ms / args.steps
 
     # e2e: a fresh instance over the same iterations (the same warm-up, then
     # the timed steps), with the design copied in from pinned host memory and
     # the design and compliance read back every step
-    e2e_prob = GpuSimpProblem(spec, precision=args.precision, device=local, block_pcg=together)
+    e2e_prob = make(args.precision)
     for _ in range(args.warmup):
         e2e_prob.iterate()
     x_host = torch.empty(prob.ne, dtype=torch.float64, pin_memory=True).numpy()
@@ -633,7 +671,7 @@ def run_own(args):
     e2e_prob.close()
     e2e_ms, e2e_value = whole_job_rate(f0.elapsed_time(f1), args.steps, world, dev)
 
-    # dominant kernel: the FP64 level-0 operator of the CG (both modes), timed
+    # dominant kernel: the level-0 operator of the CG (both modes), timed
     # alone with CUDA events on the library's stream
     kms, alg_bytes = prob.time_operator(20)
     nnz = prob.nnz
@@ -647,51 +685,82 @@ def run_own(args):
         if d.get("workload") == spec.name:
             traffic = d.get("traffic_bytes_per_launch")
 
-    # the plain FP64 loop on the same iterations (same start design, same
-    # warm-up), for the metric's plain-vs-mixed ratio and the compliance bar
-    plain = None
-    if args.precision == "mixed" and not args.no_plain and world == 1:
-        ref = GpuSimpProblem(spec, precision="fp64", device=local, block_pcg=together)
-        for _ in range(args.warmup):
-            ref.iterate()
+    def timed_run(precision, with_surrogate):
+        p = make(precision, with_surrogate)
+        first = [p.iterate() for _ in range(args.warmup)]
         torch.cuda.synchronize()
         g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         g0.record()
-        prec = [ref.iterate() for _ in range(args.steps)]
+        rr = [p.iterate() for _ in range(args.steps)]
         g1.record()
         torch.cuda.synchronize()
-        pms = g0.elapsed_time(g1)
+        t = g0.elapsed_time(g1)
+        p.close()
+        return first, rr, t
+
+    # the plain FP64 loop (the reference's warm start) on the same iterations,
+    # for the metric's plain-vs-learned+mixed ratio and the compliance bar;
+    # with the learned start also the mixed loop without it
+    plain = mixed_only = None
+    plain_first = None
+    if args.precision == "mixed" and not args.no_plain and world == 1:
+        if learned:
+            spec.warm_start = WARM["previous"]
+            _, mrec, mms = timed_run("mixed", False)
+            mixed_only = {"value": args.steps / (mms * 1e-3), "unit": "iter/s", "ms_per_step": mms / args.steps,
+                          "cg_iterations_per_step": [r.linear_iterations for r in mrec],
+                          "max_rel_compliance_diff": max(abs(a.compliance / b.compliance - 1)
+                                                         for a, b in zip(recs, mrec))}
+        spec.warm_start = WARM["previous"]
+        plain_first, prec, pms = timed_run("fp64", False)
         plain = {"value": args.steps / (pms * 1e-3), "unit": "iter/s", "ms_per_step": pms / args.steps,
+                 "warm_start": "previous",
                  "cg_iterations_per_step": [r.linear_iterations for r in prec],
+                 "compliance_per_step": [r.compliance for r in prec],
                  "max_rel_compliance_diff": max(abs(a.compliance / b.compliance - 1)
                                                 for a, b in zip(recs, prec))}
-        ref.close()
 
     if rank != 0:
         return
     st = prob.amg_stats()
-    cpu = cpu_baseline(args.config) if world == 1 else None
+    cpu, oracle_check = None, None
+    if world == 1:
+        cpu, first = cpu_baseline(spec)
+        if plain_first is not None and len(plain_first) >= 2:
+            oracle_check = {
+                "iterations": [1, 2],
+                "oracle_compliance": [c for c, _ in first],
+                "gpu_fp64_compliance": [r.compliance for r in plain_first[:2]],
+                "max_rel_compliance_diff": max(abs(r.compliance / c - 1) for r, (c, _) in zip(plain_first, first)),
+                "oracle_cg_iterations": [i for _, i in first],
+                "gpu_fp64_cg_iterations": [r.linear_iterations for r in plain_first[:2]]}
     line = {
         "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic seeded cantilever (no dataset)",
-        "config": {"workload": spec.name, "elements": spec.num_elements, "free_dofs": prob.nfree,
-                   "nnz_kff": prob.nnz, "precision": args.precision, "warm_start": args.warm,
-                   "replicas": world, "load_cases": int(spec.loads.shape[0]),
-                   "load_case_solves": "concurrent" if together else "sequential",
-                   "l2": ("working set (K_ff %.2f GB) larger than the 129 MB L2" % (nnz * 12 / 1e9)
-                          if nnz * 12 > 129e6 else
-                          "working set (K_ff %.3f GB) fits in the 129 MB L2; not flushed between steps"
-                          % (nnz * 12 / 1e9)),
-                   "amg_levels": st["num_levels"],
-                   "operator_complexity": round(st["operator_complexity"], 6),
-                   "cg_iterations_per_step": [r.linear_iterations for r in recs],
-                   "oc_bisections_per_step": [r.bisections for r in recs],
-                   "compliance_last": recs[-1].compliance,
-                   "warmup_seconds_incl_setup": round(t_setup, 3),
-                   "plain_fp64": plain},
+        "config": workload_config(spec),
+        "run": {"precision": args.precision,
+                "warm_start": "learned" if learned else spec_warm_name(spec.warm_start),
+                "nnz_kff": prob.nnz, "replicas": world,
+                "load_case_solves": "concurrent" if together else "sequential",
+                "l2": ("working set (K_ff %.2f GB) larger than the 129 MB L2" % (nnz * 12 / 1e9)
+                       if nnz * 12 > 129e6 else
+                       "working set (K_ff %.3f GB) fits in the 129 MB L2; not flushed between steps"
+                       % (nnz * 12 / 1e9)),
+                "amg_levels": st["num_levels"],
+                "operator_complexity": round(st["operator_complexity"], 6),
+                "cg_iterations_per_step": [r.linear_iterations for r in recs],
+                "cg_iterations_warmup": [r.linear_iterations for r in warm_recs],
+                "oc_bisections_per_step": [r.bisections for r in recs],
+                "compliance_per_step": [r.compliance for r in recs],
+                "warmup_seconds_incl_setup": round(t_setup, 3),
+                "surrogate_seconds_in_timed_steps": round(learned_s, 4) if learned else None,
+                "surrogate": sur_info,
+                "mixed_previous_start": mixed_only,
+                "plain_fp64": plain,
+                "oracle_check": oracle_check},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": (f"k_rows_apply<4,{spec.dim},0,double> (level-0 K_ff operator of the CG, "
@@ -711,6 +780,10 @@ def run_own(args):
         dist.destroy_process_group()
 
 
+def spec_warm_name(w):
+    return {v: k for k, v in WARM.items()}.get(w, str(w))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -723,7 +796,11 @@ def main():
                     help="skip the plain FP64 comparison run that follows a mixed-precision run")
     ap.add_argument("--warm", default="previous", choices=sorted(WARM),
                     help="PCG initial guess: zero, the previous displacement (the reference's "
-                         "warm start) or the energy-optimal combination of the last three")
+                         "warm start), the energy-optimal combination of the last three, or that "
+                         "combination with the displacement surrogate's prediction (learned; 3-D "
+                         "workloads: the network is trained before the timed region)")
+    ap.add_argument("--train-epochs", type=int, default=4,
+                    help="training epochs of the surrogate over its 2,000 pairs (learned start)")
     ap.add_argument("--sequential-loads", action="store_true",
                     help="solve a multi-load workload's load cases one after another instead of "
                          "concurrently (one workspace and stream per load case)")

@@ -494,6 +494,14 @@ int simp_surrogate_predict(simp_surrogate* s, simp_problem* p, int32_t load_case
  * node (channels-last, x fastest) -> 3 FP32 values per node (device). */
 int simp_surrogate_forward(simp_surrogate* s, int32_t nx, int32_t ny, int32_t nz, const void* input_device,
                            float* output_device);
+/* One training example on a caller's tensors: input as for
+ * simp_surrogate_forward, target 3 BF16 values per node, mask one byte per
+ * node (bit k: component k counts); loss = sum over counted components of
+ * (prediction - target)^2 / count, and its parameter gradient (host, FP32,
+ * simp_surrogate_num_params values, the layout of simp_surrogate_get_params). */
+int simp_surrogate_loss_gradient(simp_surrogate* s, int32_t nx, int32_t ny, int32_t nz, const void* input_device,
+                                  const void* target_device, const uint8_t* mask_device, int64_t count, double* loss,
+                                  float* gradient);
 /* Attaches the surrogate (not owned; NULL detaches) for warm_start 3. */
 int simp_problem_set_surrogate(simp_problem* p, simp_surrogate* s);
 /* Seconds the problem's solves spent in the surrogate's predictions. */

@@ -39,6 +39,7 @@ EXPORTS = [
     "simp_surrogate_set_params", "simp_surrogate_add_sample", "simp_surrogate_num_samples",
     "simp_surrogate_train", "simp_surrogate_predict", "simp_surrogate_forward",
     "simp_problem_set_surrogate", "simp_problem_learned_seconds", "simp_conv3d_bf16",
+    "simp_surrogate_loss_gradient",
     "simp_conv3d_wgrad",
 ]
 

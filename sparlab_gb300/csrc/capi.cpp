@@ -1045,6 +1045,28 @@ int simp_surrogate_forward(simp_surrogate* s, int32_t nx, int32_t ny, int32_t nz
   });
 }
 
+int simp_surrogate_loss_gradient(simp_surrogate* s, int32_t nx, int32_t ny, int32_t nz, const void* input_device,
+                                  const void* target_device, const uint8_t* mask_device, int64_t count, double* loss,
+                                  float* gradient) {
+  return sg_guarded([&] {
+    use_device(s->device);
+    if (nx < 2 || ny < 2 || nz < 2 || count < 1) throw Error(kBadInput, "simp_surrogate_loss_gradient: bad sizes");
+    sg::Net& net = s->s->net;
+    net.shape(nx, ny, nz);
+    const size_t nodes = static_cast<size_t>(nx) * ny * nz;
+    SIMP_CUDA(cudaMemcpyAsync(net.in16.p, input_device, nodes * 16 * sizeof(__nv_bfloat16), cudaMemcpyDeviceToDevice,
+                              net.stream));
+    net.grad.zero(net.stream);
+    net.forward();
+    *loss = net.loss(static_cast<const __nv_bfloat16*>(target_device), mask_device, count);
+    net.backward();
+    SIMP_CUDA(cudaMemcpyAsync(gradient, net.grad.p, sizeof(float) * net.nparams, cudaMemcpyDeviceToHost, net.stream));
+    net.grad.zero(net.stream);
+    SIMP_CUDA(cudaStreamSynchronize(net.stream));
+    net.check_status();
+  });
+}
+
 int simp_problem_set_surrogate(simp_problem* p, simp_surrogate* s) {
   return guarded(p->err, [&] {
     if (s && s->device != p->device) throw Error(kBadInput, "the surrogate lives on another device");

@@ -80,6 +80,17 @@ class Surrogate:
             out.append((w, b))
         return out
 
+    def loss_gradient(self, nx: int, ny: int, nz: int, input_device_ptr: int, target_device_ptr: int,
+                      mask_device_ptr: int, count: int):
+        """(loss, parameter gradient) of one example on device tensors."""
+        loss = C.c_double()
+        g = np.zeros(self.num_params, np.float32)
+        _raise(self._lib.simp_surrogate_loss_gradient(
+            self._h, C.c_int32(nx), C.c_int32(ny), C.c_int32(nz), C.c_void_p(input_device_ptr),
+            C.c_void_p(target_device_ptr), C.c_void_p(mask_device_ptr), C.c_int64(count), C.byref(loss),
+            g.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss.value, g
+
     def add_sample(self, problem, load_case: int = 0):
         _raise(self._lib.simp_surrogate_add_sample(self._h, problem._h, C.c_int32(load_case)))
 

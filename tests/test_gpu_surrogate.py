@@ -229,6 +229,84 @@ def test_network_forward_matches_torch():
     assert rel <= 2e-2, rel
 
 
+def test_network_gradient_matches_torch_autograd():
+    """The composed backward pass (data gradients through the decoder, the
+    skip connections and the grid transfers; weight and bias gradients) against
+    torch autograd on the reference network, layer by layer."""
+    torch = torch_mod()
+    from sparlab_gb300.surrogate import LAYER_NAMES, Surrogate
+    dev = torch.device("cuda", 0)
+    sur = Surrogate(seed=4)
+    p = sur.get_params()
+    rng = np.random.default_rng(12)
+    p[:] += rng.standard_normal(p.size).astype(np.float32) * 0.01
+    sur.set_params(p)
+    nx, ny, nz = 33, 17, 9
+    x = np.zeros((nz, ny, nx, 16), np.float32)
+    x[..., :4] = rng.uniform(-1.0, 1.0, (nz, ny, nx, 4))
+    xin = bf16_tensor(x, dev)
+    tgt = bf16_tensor(rng.uniform(-1.0, 1.0, (nz, ny, nx, 3)), dev)
+    mask_np = np.full((nz, ny, nx), 7, np.uint8)
+    mask_np[:, :, 0] = 0                     # a clamped face
+    mask = torch.from_numpy(mask_np).to(dev)
+    count = int(3 * (mask_np > 0).sum())
+    loss, g = sur.loss_gradient(nx, ny, nz, xin.data_ptr(), tgt.data_ptr(), mask.data_ptr(), count)
+    params = [(torch.from_numpy(w.copy()).to(dev).requires_grad_(True),
+               torch.from_numpy(b.copy()).to(dev).requires_grad_(True)) for w, b in sur.layer_params(p)]
+
+    class Holder:
+        pass
+    torch_layers = []
+    for w, b in params:
+        torch_layers.append((w, b))
+
+    import torch.nn.functional as F
+    k1 = torch.tensor([0.5, 1.0, 0.5], device=dev)
+    k3 = k1[:, None, None] * k1[None, :, None] * k1[None, None, :]
+
+    def rb(t):
+        return t.to(torch.bfloat16).float()
+
+    def P(t):
+        c = t.shape[1]
+        return rb(F.conv_transpose3d(t, k3.expand(c, 1, 3, 3, 3), stride=2, padding=1, groups=c))
+
+    def R(t):
+        c = t.shape[1]
+        return rb(F.conv3d(t, k3.expand(c, 1, 3, 3, 3) / 8.0, stride=2, padding=1, groups=c))
+
+    def cv(i, t, relu=True):
+        w, b = torch_layers[i]
+        wb = w.to(torch.bfloat16).float()
+        y = F.conv3d(t, torch_weight(wb), bias=b, padding=1)
+        return rb(torch.relu(y)) if relu else y
+
+    xt = to_ncdhw(xin)
+    s0 = cv(1, cv(0, xt))
+    s1 = cv(3, cv(2, R(s0)))
+    s2 = cv(5, cv(4, R(s1)))
+    b3 = cv(7, cv(6, R(s2)))
+    d2 = cv(8, torch.cat([P(b3), s2], 1))
+    d1 = cv(9, torch.cat([P(d2), s1], 1))
+    d0 = cv(10, torch.cat([P(d1), s0], 1))
+    out = from_ncdhw(cv(11, d0, relu=False))
+    m = torch.stack([(mask >> k) & 1 for k in range(3)], dim=-1).float()
+    ref_loss = (((out - tgt.float()) ** 2) * m).sum() / count
+    ref_loss.backward()
+    assert abs(loss / ref_loss.item() - 1) < 2e-2
+    off = 0
+    for name, (w, b) in zip(LAYER_NAMES, params):
+        gw = g[off: off + w.numel()].reshape(w.shape)
+        off += w.numel()
+        gb = g[off: off + b.numel()]
+        off += b.numel()
+        rw = w.grad.cpu().numpy()
+        rel = np.linalg.norm(gw - rw) / np.linalg.norm(rw)
+        assert rel < 5e-2, (name, rel)
+        rbias = b.grad.cpu().numpy()
+        assert np.linalg.norm(gb - rbias) / np.linalg.norm(rbias) < 5e-2, name
+
+
 def _small_specs():
     specs = []
     for s in range(3):
@@ -244,8 +322,10 @@ def test_training_lowers_the_loss_and_learned_start_keeps_the_answer():
     sur = Surrogate(seed=5)
     generate_samples(sur, _small_specs(), iterations=5)
     assert sur.num_samples == 15
-    losses = sur.train(epochs=6, learning_rate=2e-3, batch=3, seed=1)
-    assert all(np.isfinite(losses)) and losses[-1] < losses[0], losses
+    losses = sur.train(epochs=40, learning_rate=1e-3, batch=1, seed=1)
+    # the first epoch starts from a near-zero prediction (its loss is about
+    # the mean squared target); training must get well below it
+    assert all(np.isfinite(losses)) and losses[-1] < 0.3 * losses[0], losses
     runs = {}
     for warm in (1, 3):
         spec = P.hex8_cantilever(24, 12, 12, 0.25, "sg_run")
