@@ -203,6 +203,9 @@ typedef struct {
   int32_t robust;
   double robust_delta;
   int32_t robust_volume_interval;
+  /* displacements of the history that warm starts 2 and 3 combine (1..3;
+   * 0 takes 3); warm start 3 adds the surrogate's prediction to them */
+  int32_t warm_history;
 } simp_problem_desc;
 
 /* ObjectiveEvaluation scalars (Sensitivity.hpp:66-107) and an OC step

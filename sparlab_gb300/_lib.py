@@ -91,7 +91,7 @@ class ProblemDesc(C.Structure):
                 ("beta_max", C.c_double), ("beta_factor", C.c_double), ("beta_interval", C.c_int32),
                 ("advance_on_convergence", C.c_int32), ("change_tolerance", C.c_double),
                 ("robust", C.c_int32), ("robust_delta", C.c_double),
-                ("robust_volume_interval", C.c_int32)]
+                ("robust_volume_interval", C.c_int32), ("warm_history", C.c_int32)]
 
 
 class Evaluation(C.Structure):

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libsimp_gb300.so")
 SOURCES = ["amg.cu", "problem.cu", "mma.cu", "noalloc.cu", "warmstart.cu", "modal.cu", "buckling.cu", "surrogate.cu",
-           "surrogate_net.cu", "structure.cpp", "capi.cpp"]
+           "surrogate_net.cu", "structure.cpp", "autotune.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -3,6 +3,7 @@
 // follows Impl::cycle (:857-885) and Impl::smooth (:783-855); PCG follows
 // pcg_solve (:1152-1237).
 #include "amg.h"
+#include "autotune.h"
 #include "dense.cuh"
 #include "galerkin.cuh"
 #include "kernels.cuh"
@@ -213,13 +214,27 @@ void mf3_64(const MfOp& mf, const double* x, double* y, const double* b, cudaStr
   SIMP_CHECK_LAUNCH();
 }
 
+template <int MODE, int TX, int TY, int TZ>
+void mf3_shape(const MfOp& mf, const MfArgs& a, const KeF32& ke, cudaStream_t s) {
+  const dim3 grid((mf.nnx + TX - 1) / TX, (mf.nny + TY - 1) / TY, (mf.nz + 1 + TZ - 1) / TZ);
+  k_mf3_tile<MODE, TX, TY, TZ><<<grid, TX * TY * TZ, 0, s>>>(mf_view(mf), a, ke);
+  SIMP_CHECK_LAUNCH();
+}
+
+// The tiled matrix-free kernel in the tile shape the tuner chose (mf.tile
+// indexes kMfTileShape; every shape gives the same values).
 template <int MODE>
 void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
-  const dim3 grid((mf.nnx + kTX - 1) / kTX, (mf.nny + kTY - 1) / kTY, (mf.nz + 1 + kTZ * kNZ - 1) / (kTZ * kNZ));
   KeF32 ke;
   std::copy(mf.ke_host, mf.ke_host + 24 * 24, ke.k);
-  k_mf3_tile<MODE><<<grid, kTX * kTY * kTZ, 0, s>>>(mf_view(mf), a, ke);
-  SIMP_CHECK_LAUNCH();
+  static_assert(kMfTiles == 5, "tile table");
+  switch (mf.tile) {
+    case 1: mf3_shape<MODE, 32, 8, 1>(mf, a, ke, s); break;
+    case 2: mf3_shape<MODE, 32, 2, 4>(mf, a, ke, s); break;
+    case 3: mf3_shape<MODE, 64, 2, 2>(mf, a, ke, s); break;
+    case 4: mf3_shape<MODE, 32, 4, 1>(mf, a, ke, s); break;
+    default: mf3_shape<MODE, 32, 4, 2>(mf, a, ke, s); break;
+  }
 }
 
 // Matrix-free level-0 pieces of the FP32 cycle (tiled in 3-D).
@@ -864,12 +879,23 @@ bool launch_rows(void (*kernel)(i32, WarpRows, KArgs...), i32 nodes, const WarpR
   const size_t per_warp =
       static_cast<size_t>(w.acc) * sizeof(T) + static_cast<size_t>(2 * w.slots + kMetaInts + w.inner) * 4;
   if (per_warp > 200 * 1024) return false;
-  const int warps = static_cast<int>(std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp)));
-  const size_t smem = per_warp * warps;
-  if (smem > 48 * 1024) raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
-  const i64 blocks = std::max<i64>(1, std::min<i64>((static_cast<i64>(nodes) + warps - 1) / warps, 152 * 64));
-  kernel<<<static_cast<unsigned>(blocks), warps * 32, smem, s>>>(nodes, w, args...);
-  SIMP_CHECK_LAUNCH();
+  // variants: at most 8, 4 or 2 warps (row nodes) per block within a 96 KB
+  // (variant 0: the untuned launch) or 192 KB shared-memory budget; a row
+  // node's products run in one warp in the same order in every variant
+  auto launch = [&](int v) {
+    static constexpr int kMaxWarps[4] = {8, 4, 2, 8};
+    const size_t budget = v == 3 ? 192 * 1024 : 96 * 1024;
+    const int warps = static_cast<int>(
+        std::min<size_t>(static_cast<size_t>(kMaxWarps[v]), std::max<size_t>(1, budget / per_warp)));
+    const size_t smem = per_warp * warps;
+    if (smem > 48 * 1024) raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
+    const i64 blocks = std::max<i64>(1, std::min<i64>((static_cast<i64>(nodes) + warps - 1) / warps, 152 * 64));
+    kernel<<<static_cast<unsigned>(blocks), warps * 32, smem, s>>>(nodes, w, args...);
+    SIMP_CHECK_LAUNCH();
+  };
+  std::ostringstream key;
+  key << "rows:" << typeid(kernel).name() << ":" << sizeof(T) << ":" << nodes << ":" << w.acc << ":" << w.slots;
+  launch(tune_pick(key.str(), 4, launch, s, 0));
   return true;
 }
 
@@ -1079,6 +1105,7 @@ void GpuAmg::setup(bool structure_changed) {
   coarse_factorize();
   ensure(main_);
   for (auto& w : extra_) ensure(*w);
+  if (!reuse) tune_level0();
   ready_ = true;
   // captured iteration bodies stay valid across reuse setups: their launches
   // take only workspace and level pointers, which a reuse setup keeps
@@ -1087,6 +1114,30 @@ void GpuAmg::setup(bool structure_changed) {
   compute_stats();
   SIMP_CUDA(cudaStreamSynchronize(stream));
   stats.setup_seconds = seconds_since(t0);
+}
+
+// The matrix-free operator's tile shape for this grid: the fastest of the
+// shapes in kMfTileShape on y = A x with the current cell scales (all give
+// the same values).  Before the first CUDA graph capture of a structure.
+void GpuAmg::tune_level0() {
+  if (!(mf.enabled && mf.dim == 3) || !mf.scale) return;
+  const i32 n = levels.front()->n;
+  DBuf<float> tx(static_cast<size_t>(n)), ty(static_cast<size_t>(n));
+  k_fill<float><<<grid_for(n, 256), 256, 0, stream>>>(tx.p, 1.0f, n);
+  SIMP_CHECK_LAUNCH();
+  std::ostringstream key;
+  key << "mf3:" << mf.nnx << "x" << mf.nny << "x" << (mf.nz + 1);
+  mf.tile = tune_pick(key.str(), kMfTiles,
+                      [&](int v) {
+                        MfOp m = mf;
+                        m.tile = v;
+                        MfArgs a{};
+                        a.x = tx.p;
+                        a.y = ty.p;
+                        mf3<0>(m, a, stream);
+                      },
+                      stream, 0, 5);
+  SIMP_CUDA(cudaStreamSynchronize(stream));
 }
 
 void GpuAmg::compute_stats() {

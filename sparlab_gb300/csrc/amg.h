@@ -135,6 +135,7 @@ struct MfOp {
   const float* ke = nullptr;    // K_e^0, FP32
   const float* scale = nullptr; // s_e, FP32
   float ke_host[24 * 24] = {};  // K_e^0, FP32 (kernel parameter of the tiled 3-D kernel)
+  int tile = 0;                 // tile shape of the tiled 3-D kernel (kMfTileShape, tuned)
   const double* scale64 = nullptr;  // s_e, FP64 (the matrix-free CG operator's true residuals)
   double ke64_host[24 * 24] = {};   // K_e^0, FP64
 };
@@ -268,6 +269,7 @@ class GpuAmg {
   void pcg_body(SolveWork& w, double* x, float2* psplit);
   uint64_t epoch_ = 1;  // bumped by every setup: captured graphs are stale
   void compute_stats();
+  void tune_level0();
 };
 
 }  // namespace simp

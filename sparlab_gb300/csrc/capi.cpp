@@ -543,6 +543,8 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     }
     if (dsc->optimizer != 0 && dsc->optimizer != 1) throw Error(kBadInput, "unknown optimizer (expected 0 OC, 1 MMA)");
     d.optimizer = dsc->optimizer;
+    if (dsc->warm_history < 0 || dsc->warm_history > kHistory) throw Error(kBadInput, "warm_history must be 0 .. 3");
+    d.warm_history = dsc->warm_history > 0 ? dsc->warm_history : kHistory;
     use_device(o->device);
     std::unique_ptr<simp_problem> p(new simp_problem());
     p->device = o->device;

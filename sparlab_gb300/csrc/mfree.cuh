@@ -155,8 +155,13 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 // the coarse right-hand side); 8 y64 = A x in FP64 storage (the FP32 product
 // as the CG operator of the matrix-free variant).
 // ---------------------------------------------------------------------------
-constexpr int kTX = 32, kTY = 4, kTZ = 2;  // threads per block axis
+constexpr int kTX = 32, kTY = 4, kTZ = 2;  // threads per block axis (the default tile)
 constexpr int kNZ = 1;                      // node layers per thread
+// Tile shapes the launch-shape tuner chooses among (TX x TY x TZ threads,
+// one node each): every shape sums each node's cells and corners in the same
+// order, so all give the same values bit for bit.
+constexpr int kMfTiles = 5;
+constexpr int kMfTileShape[kMfTiles][3] = {{32, 4, 2}, {32, 8, 1}, {32, 2, 4}, {64, 2, 2}, {32, 4, 1}};
 
 struct KeF32 {
   float k[24 * 24];  // K_e^0, row-major
@@ -175,24 +180,24 @@ struct MfArgs {
   double* y64;        // mode 8: output
 };
 
-template <int MODE>
-__global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, const __grid_constant__ KeF32 ke) {
-  constexpr int NZ = kTZ * kNZ;  // node layers of the tile
-  __shared__ float xh[3][NZ + 2][kTY + 2][kTX + 2];
-  __shared__ float sc[NZ + 1][kTY + 1][kTX + 1];
+template <int MODE, int TX = kTX, int TY = kTY, int TZ = kTZ>
+__global__ void __launch_bounds__(TX* TY* TZ) k_mf3_tile(MfView m, MfArgs a, const __grid_constant__ KeF32 ke) {
+  constexpr int NZ = TZ * kNZ;  // node layers of the tile
+  __shared__ float xh[3][NZ + 2][TY + 2][TX + 2];
+  __shared__ float sc[NZ + 1][TY + 1][TX + 1];
   const int tid = threadIdx.x;
-  const i32 x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY, z0 = blockIdx.z * NZ;
+  const i32 x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * NZ;
   const i32 nnz = m.nz + 1;
   // node values of the tile and its halo (zero outside the grid / clamped):
   // every thread first loads the free-node indices of all its halo entries,
   // then their values, so the loads of one thread are independent
-  constexpr int kHalo = (NZ + 2) * (kTY + 2) * (kTX + 2);
-  constexpr int kPer = (kHalo + kTX * kTY * kTZ - 1) / (kTX * kTY * kTZ);
+  constexpr int kHalo = (NZ + 2) * (TY + 2) * (TX + 2);
+  constexpr int kPer = (kHalo + TX * TY * TZ - 1) / (TX * TY * TZ);
   i32 hj[kPer];
 #pragma unroll
   for (int q = 0; q < kPer; ++q) {
-    const int e = tid + q * kTX * kTY * kTZ;
-    const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
+    const int e = tid + q * TX * TY * TZ;
+    const int hx = e % (TX + 2), hy = (e / (TX + 2)) % (TY + 2), hz = e / ((TX + 2) * (TY + 2));
     const i32 gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
     hj[q] = -1;
     if (e < kHalo && gx >= 0 && gx < m.nnx && gy >= 0 && gy < m.nny && gz >= 0 && gz < nnz)
@@ -211,17 +216,17 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
   }
 #pragma unroll
   for (int q = 0; q < kPer; ++q) {
-    const int e = tid + q * kTX * kTY * kTZ;
+    const int e = tid + q * TX * TY * TZ;
     if (e < kHalo) {
-      const int hx = e % (kTX + 2), hy = (e / (kTX + 2)) % (kTY + 2), hz = e / ((kTX + 2) * (kTY + 2));
+      const int hx = e % (TX + 2), hy = (e / (TX + 2)) % (TY + 2), hz = e / ((TX + 2) * (TY + 2));
       xh[0][hz][hy][hx] = hv[q][0];
       xh[1][hz][hy][hx] = hv[q][1];
       xh[2][hz][hy][hx] = hv[q][2];
     }
   }
   // cell scales (zero outside the grid)
-  for (int e = tid; e < (NZ + 1) * (kTY + 1) * (kTX + 1); e += kTX * kTY * kTZ) {
-    const int cx = e % (kTX + 1), cy = (e / (kTX + 1)) % (kTY + 1), cz = e / ((kTX + 1) * (kTY + 1));
+  for (int e = tid; e < (NZ + 1) * (TY + 1) * (TX + 1); e += TX * TY * TZ) {
+    const int cx = e % (TX + 1), cy = (e / (TX + 1)) % (TY + 1), cz = e / ((TX + 1) * (TY + 1));
     const i32 gx = x0 - 1 + cx, gy = y0 - 1 + cy, gz = z0 - 1 + cz;
     float s = 0.0f;
     if (gx >= 0 && gx < m.nx && gy >= 0 && gy < m.ny && gz >= 0 && gz < m.nz)
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(kTX* kTY* kTZ) k_mf3_tile(MfView m, MfArgs a, 
     sc[cz][cy][cx] = s;
   }
   __syncthreads();
-  const int tx = tid % kTX, ty = (tid / kTX) % kTY, tz = tid / (kTX * kTY);
+  const int tx = tid % TX, ty = (tid / TX) % TY, tz = tid / (TX * TY);
   const i32 gx = x0 + tx, gy = y0 + ty;
   if (gx >= m.nnx || gy >= m.nny) return;
   // kNZ consecutive node layers per thread: their neighbourhoods share

@@ -33,8 +33,9 @@ struct ProblemDesc {
   std::vector<double> loads;    // nloads x ndof
   std::vector<double> weights;  // normalised
   double radius = 1.5, vf = 0.5, x0 = 0.5, penalty = 3.0, emin = 1e-9, move = 0.2, damping = 0.5;
-  int warm = 1;  // 0 zero start, 1 previous displacement, 2 projection on the last kHistory,
-                 // 3 projection on the last kHistory and the surrogate's prediction
+  int warm = 1;  // 0 zero start, 1 previous displacement, 2 projection on the last warm_history,
+                 // 3 projection on the last warm_history and the surrogate's prediction
+  int warm_history = kHistory;
   bool block_pcg = false;
   int optimizer = 0;  // 0 OC, 1 MMA
   // Heaviside projection (src/topopt/Projection.cpp) with beta continuation

@@ -78,7 +78,7 @@ __global__ void k_history_combine(i64 n, int k, const double* __restrict__ u, Co
 
 void GpuProblem::projected_start(int l, double* ul, bool learned) {
   cudaStream_t s = amg.stream;
-  int k = hist_count[l];
+  int k = std::min(hist_count[l], d.warm_history);
   const i64 n = nfree;
   double* U = hist.p + static_cast<size_t>(l) * kBasis * n;
   if (learned) {  // the prediction takes the slot after the history

@@ -79,7 +79,9 @@ class ProblemSpec:
     damping: float = 0.5
     rtol: float = 1e-8
     max_cg_iterations: int = 0
-    warm_start: int = 1  # 0 zero guess, 1 previous displacement, 2 projection on the last 3
+    warm_start: int = 1  # 0 zero guess, 1 previous displacement, 2 projection on the last 3,
+    #                      3 that projection with the surrogate's prediction added
+    warm_history: int = 0  # displacements the projected starts combine (1..3; 0: 3)
     # Heaviside projection of the filtered density with beta continuation
     # (ProjectionOptions, include/sparlab/topopt/Projection.hpp:69-96)
     projection: bool = False

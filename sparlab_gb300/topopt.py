@@ -169,6 +169,7 @@ class GpuSimpProblem:
         d.robust = int(getattr(spec, "robust", False))
         d.robust_delta = getattr(spec, "robust_delta", 0.1)
         d.robust_volume_interval = getattr(spec, "robust_volume_interval", 1)
+        d.warm_history = int(getattr(spec, "warm_history", 0))
         prec = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
         opts = dict(spec.amg)
         opts.update(amg)

@@ -165,6 +165,67 @@ def test_errors_are_reported_and_context_survives():
     gpu2.solve(spec.loads[0][pr.free_dofs()])
 
 
+def _entry(ptr, col, i, j):
+    return [k for k in range(ptr[i], ptr[i + 1]) if col[k] == j][0]
+
+
+def test_zero_stiffness_node_is_reported_as_the_reference_does():
+    """A node whose rows and columns are zero (an unconnected node) fails the
+    positive-diagonal check of the setup (src/fem/Multigrid.cpp:727-733) in
+    the oracle and on the GPU, with the same diagnosis and the entry's index;
+    the context stays usable."""
+    spec = P.bench_model(3, 16, 8, 4)
+    pr, ptr, col, val = system(spec)
+    z = val.copy()
+    node = {90, 91, 92}
+    rows = np.repeat(np.arange(len(ptr) - 1), np.diff(ptr))
+    z[np.isin(rows, list(node)) | np.isin(col, list(node))] = 0.0
+    ref = oracle.Solver(rtol=1e-10, coarse_size=60)
+    with pytest.raises(oracle.OracleError) as eo:
+        ref.factorize(ptr, col, z, 3, pr.coords(), pr.free_dofs())
+    gpu = GpuAmgCgSolver(iterative_tolerance=1e-10, coarse_size=60)
+    gpu.set_layout(3, pr.coords(), pr.free_dofs())
+    with pytest.raises(SolverError) as eg:
+        gpu.factorize(ptr, col, z)
+    for msg in (str(eo.value), str(eg.value)):
+        assert "diagonal entry 90" in msg and "positive diagonal" in msg
+    gpu.factorize(ptr, col, val)
+    x = gpu.solve(spec.loads[0][pr.free_dofs()])
+    assert np.all(np.isfinite(x))
+
+
+def test_pcg_breakdown_is_reported_as_the_reference_does():
+    """p^T A p <= 0 (src/fem/Multigrid.cpp:1187-1193): the x-y coupling of one
+    node raised 2 % above sqrt(d_xx d_yy) makes the stiffness indefinite in a
+    mode the coarse level does not see; the oracle's PCG breaks down at its
+    first iteration and so does the GPU's, with SIMP_BREAKDOWN and the
+    reference's wording; the context stays usable."""
+    from sparlab_gb300._lib import SIMP_BREAKDOWN
+    spec = P.bench_model(3, 16, 8, 4)
+    pr, ptr, col, val = system(spec)
+    b = val.copy()
+    i, j = 3 * 50, 3 * 50 + 1
+    c = 1.02 * np.sqrt(val[_entry(ptr, col, i, i)] * val[_entry(ptr, col, j, j)])
+    b[_entry(ptr, col, i, j)] = c
+    b[_entry(ptr, col, j, i)] = c
+    f = spec.loads[0][pr.free_dofs()]
+    ref = oracle.Solver(rtol=1e-10)
+    ref.factorize(ptr, col, b, 3, pr.coords(), pr.free_dofs())
+    with pytest.raises(oracle.OracleError) as eo:
+        ref.solve(f)
+    assert "broke down at iteration 1" in str(eo.value)
+    gpu = GpuAmgCgSolver(iterative_tolerance=1e-10)
+    gpu.set_layout(3, pr.coords(), pr.free_dofs())
+    gpu.factorize(ptr, col, b)
+    with pytest.raises(SolverError) as eg:
+        gpu.solve(f)
+    assert eg.value.code == SIMP_BREAKDOWN
+    assert "broke down at iteration 1" in str(eg.value)
+    gpu.factorize(ptr, col, val)
+    x = gpu.solve(f)
+    assert np.all(np.isfinite(x))
+
+
 def test_mixed_precision_matches_fp64_solution():
     """FP32 operator / V-cycle with FP64 refinement reaches the same
     tolerance on the FP64 residual: solution within 1e-6 of the FP64 one."""

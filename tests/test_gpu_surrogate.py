@@ -232,8 +232,11 @@ def test_network_forward_matches_torch():
 def test_network_gradient_matches_torch_autograd():
     """The composed backward pass (data gradients through the decoder, the
     skip connections and the grid transfers; weight and bias gradients) against
-    torch autograd on the reference network, layer by layer."""
+    torch autograd on the reference network, layer by layer.  The reference
+    rounds activations and their gradients to BF16 where the network stores
+    them (tensor hooks), so the comparison sees the summation order only."""
     torch = torch_mod()
+    import torch.nn.functional as F
     from sparlab_gb300.surrogate import LAYER_NAMES, Surrogate
     dev = torch.device("cuda", 0)
     sur = Surrogate(seed=4)
@@ -241,7 +244,7 @@ def test_network_gradient_matches_torch_autograd():
     rng = np.random.default_rng(12)
     p[:] += rng.standard_normal(p.size).astype(np.float32) * 0.01
     sur.set_params(p)
-    nx, ny, nz = 33, 17, 9
+    nx, ny, nz = 49, 25, 17     # level 3: 7 x 4 x 3 nodes
     x = np.zeros((nz, ny, nx, 16), np.float32)
     x[..., :4] = rng.uniform(-1.0, 1.0, (nz, ny, nx, 4))
     xin = bf16_tensor(x, dev)
@@ -253,19 +256,15 @@ def test_network_gradient_matches_torch_autograd():
     loss, g = sur.loss_gradient(nx, ny, nz, xin.data_ptr(), tgt.data_ptr(), mask.data_ptr(), count)
     params = [(torch.from_numpy(w.copy()).to(dev).requires_grad_(True),
                torch.from_numpy(b.copy()).to(dev).requires_grad_(True)) for w, b in sur.layer_params(p)]
-
-    class Holder:
-        pass
-    torch_layers = []
-    for w, b in params:
-        torch_layers.append((w, b))
-
-    import torch.nn.functional as F
     k1 = torch.tensor([0.5, 1.0, 0.5], device=dev)
     k3 = k1[:, None, None] * k1[None, :, None] * k1[None, None, :]
 
     def rb(t):
-        return t.to(torch.bfloat16).float()
+        """BF16 storage of an activation and of its gradient"""
+        t = t.to(torch.bfloat16).float()
+        if t.requires_grad:
+            t.register_hook(lambda gr: gr.to(torch.bfloat16).float())
+        return t
 
     def P(t):
         c = t.shape[1]
@@ -276,9 +275,8 @@ def test_network_gradient_matches_torch_autograd():
         return rb(F.conv3d(t, k3.expand(c, 1, 3, 3, 3) / 8.0, stride=2, padding=1, groups=c))
 
     def cv(i, t, relu=True):
-        w, b = torch_layers[i]
-        wb = w.to(torch.bfloat16).float()
-        y = F.conv3d(t, torch_weight(wb), bias=b, padding=1)
+        w, b = params[i]
+        y = F.conv3d(t, torch_weight(w.to(torch.bfloat16).float()), bias=b, padding=1)
         return rb(torch.relu(y)) if relu else y
 
     xt = to_ncdhw(xin)
@@ -289,11 +287,13 @@ def test_network_gradient_matches_torch_autograd():
     d2 = cv(8, torch.cat([P(b3), s2], 1))
     d1 = cv(9, torch.cat([P(d2), s1], 1))
     d0 = cv(10, torch.cat([P(d1), s0], 1))
-    out = from_ncdhw(cv(11, d0, relu=False))
+    head = cv(11, d0, relu=False)
+    head.register_hook(lambda gr: gr.to(torch.bfloat16).float())
+    out = from_ncdhw(head)
     m = torch.stack([(mask >> k) & 1 for k in range(3)], dim=-1).float()
     ref_loss = (((out - tgt.float()) ** 2) * m).sum() / count
     ref_loss.backward()
-    assert abs(loss / ref_loss.item() - 1) < 2e-2
+    assert abs(loss / ref_loss.item() - 1) < 1e-2
     off = 0
     for name, (w, b) in zip(LAYER_NAMES, params):
         gw = g[off: off + w.numel()].reshape(w.shape)
@@ -302,9 +302,9 @@ def test_network_gradient_matches_torch_autograd():
         off += b.numel()
         rw = w.grad.cpu().numpy()
         rel = np.linalg.norm(gw - rw) / np.linalg.norm(rw)
-        assert rel < 5e-2, (name, rel)
+        assert rel < 3e-2, (name, rel)
         rbias = b.grad.cpu().numpy()
-        assert np.linalg.norm(gb - rbias) / np.linalg.norm(rbias) < 5e-2, name
+        assert np.linalg.norm(gb - rbias) / np.linalg.norm(rbias) < 3e-2, name
 
 
 def _small_specs():
