@@ -502,7 +502,9 @@ def run_own_batched(args):
     mine = specs[rank::world]
     probs = [GpuSimpProblem(s, precision=args.precision, device=local) for s in mine]
     lib = _lib.load()
-    run_batched(probs, args.warmup)
+    schedule = {}
+    run_batched(probs, args.warmup, tune=True, report=schedule)   # warm-up iterations pick the host workers
+    workers = schedule.get("workers")
 
     def barrier():
         if world > 1:
@@ -515,7 +517,7 @@ def run_own_batched(args):
     sampler.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    recs = run_batched(probs, args.steps)
+    recs = run_batched(probs, args.steps, workers=workers)
     e1.record()
     barrier()
     clocks = sampler.stop()
@@ -535,7 +537,7 @@ def run_own_batched(args):
     for _ in range(args.steps):
         for p, h in zip(probs, hosts):
             p.set_design(h)
-        run_batched(probs, 1)
+        run_batched(probs, 1, workers=workers)
         for p, h in zip(probs, hosts):
             p.design(out=h)
     f1.record()
@@ -560,6 +562,8 @@ def run_own_batched(args):
                    "elements_total": sum(s.num_elements for s in specs),
                    "cg_iterations_per_step": [sum(r[k].linear_iterations for r in recs)
                                               for k in range(args.steps)],
+                   "schedule": schedule,
+                   "autotune": {k: v[0] for k, v in _lib.autotune_report().items()},
                    "l2": "no flush: a step touches every instance's operators once"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
@@ -759,6 +763,8 @@ def run_own(args):
                 "surrogate_seconds_in_timed_steps": round(learned_s, 4) if learned else None,
                 "surrogate": sur_info,
                 "mixed_previous_start": mixed_only,
+                "autotune": {k: {"chosen": v[0], "ms": [round(t, 4) for t in v[1]]}
+                             for k, v in _lib.autotune_report().items()},
                 "plain_fp64": plain,
                 "oracle_check": oracle_check},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -525,6 +525,20 @@ int simp_conv3d_bf16(int32_t nx, int32_t ny, int32_t nz, int32_t nseg, const voi
 int simp_conv3d_wgrad(int32_t nx, int32_t ny, int32_t nz, int32_t nseg, const void* const* in, const int32_t* cseg,
                       const void* dy, int32_t cdy, int32_t cout, float* gw, float* gb);
 
+/* Launch-shape autotuner (no counterpart in the reference).  Kernels with
+ * several launch shapes that compute the same values bit for bit (the tile
+ * shape of the matrix-free operator, the warps per block of the Galerkin row
+ * products) are timed on the problem's own data the first time a shape key is
+ * seen and the fastest shape is kept (environment SIMP_TUNE_CACHE: a file the
+ * choices are read from and appended to).  simp_autotune_enable(0) keeps the
+ * default shapes.  simp_autotune_report writes one line per key, "key chosen
+ * ms_0 ms_1 ...", into buf (NUL-terminated, truncated to size) and the bytes
+ * the full report needs into *needed. */
+void simp_autotune_enable(int32_t on);
+/* Pins the choice for a key (as it appears in the report). */
+int simp_autotune_set(const char* key, int32_t variant);
+int simp_autotune_report(char* buf, int64_t size, int64_t* needed);
+
 /* Number of kernels this library has launched (for launch accounting). */
 int64_t simp_kernel_launches(void);
 

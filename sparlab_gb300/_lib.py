@@ -39,7 +39,8 @@ EXPORTS = [
     "simp_surrogate_set_params", "simp_surrogate_add_sample", "simp_surrogate_num_samples",
     "simp_surrogate_train", "simp_surrogate_predict", "simp_surrogate_forward",
     "simp_problem_set_surrogate", "simp_problem_learned_seconds", "simp_conv3d_bf16",
-    "simp_surrogate_loss_gradient",
+    "simp_surrogate_loss_gradient", "simp_autotune_enable", "simp_autotune_report",
+    "simp_autotune_set",
     "simp_conv3d_wgrad",
 ]
 
@@ -204,6 +205,21 @@ def default_options(**kw) -> SolverOptions:
             raise TypeError(f"unknown solver option {k!r}")
         setattr(o, k, v)
     return o
+
+
+def autotune_report():
+    """The launch-shape tuner's choices: {key: (chosen variant, [ms per variant])}."""
+    lib = load()
+    need = C.c_int64()
+    lib.simp_autotune_report(None, C.c_int64(0), C.byref(need))
+    buf = C.create_string_buffer(max(1, need.value))
+    lib.simp_autotune_report(buf, C.c_int64(len(buf)), C.byref(need))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        parts = line.split()
+        if len(parts) >= 2:
+            out[parts[0]] = (int(parts[1]), [float(v) for v in parts[2:]])
+    return out
 
 
 def ptr(a, ctype=C.c_double):

@@ -48,6 +48,15 @@ void append_file(const std::string& key, int v) {
 }  // namespace
 
 void tune_set_enabled(bool on) { g_enabled = on; }
+
+void tune_set(const std::string& key, int variant) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  read_file_locked();
+  TuneRecord r;
+  r.key = key;
+  r.chosen = variant;
+  g_table[key] = r;
+}
 bool tune_enabled() { return g_enabled; }
 
 std::vector<TuneRecord> tune_records() {

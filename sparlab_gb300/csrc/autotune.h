@@ -36,6 +36,8 @@ struct TuneRecord {
 int tune_pick(const std::string& key, int count, const std::function<void(int)>& run, cudaStream_t stream,
               int fallback, int reps = 3);
 
+// Records `variant` as the choice for `key` (replacing a tuned one).
+void tune_set(const std::string& key, int variant);
 void tune_set_enabled(bool on);
 bool tune_enabled();
 std::vector<TuneRecord> tune_records();

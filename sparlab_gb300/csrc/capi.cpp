@@ -2,6 +2,7 @@
 #include "../../include/simp_gpu.h"
 
 #include "amg.h"
+#include "autotune.h"
 #include "problem.h"
 #include "surrogate_net.h"
 
@@ -1078,6 +1079,35 @@ int simp_problem_set_surrogate(simp_problem* p, simp_surrogate* s) {
 
 int simp_problem_learned_seconds(simp_problem* p, double* seconds) {
   return guarded(p->err, [&] { *seconds = p->p->learned_seconds; });
+}
+
+}  // extern "C"
+
+extern "C" {
+
+void simp_autotune_enable(int32_t on) { tune_set_enabled(on != 0); }
+
+int simp_autotune_set(const char* key, int32_t variant) {
+  if (!key || variant < 0) return kBadInput;
+  tune_set(key, variant);
+  return kOk;
+}
+
+int simp_autotune_report(char* buf, int64_t size, int64_t* needed) {
+  std::ostringstream os;
+  for (const TuneRecord& r : tune_records()) {
+    os << r.key << ' ' << r.chosen;
+    for (double ms : r.ms) os << ' ' << ms;
+    os << '\n';
+  }
+  const std::string text = os.str();
+  if (needed) *needed = static_cast<int64_t>(text.size()) + 1;
+  if (buf && size > 0) {
+    const size_t n = std::min(static_cast<size_t>(size - 1), text.size());
+    std::memcpy(buf, text.data(), n);
+    buf[n] = '\0';
+  }
+  return kOk;
 }
 
 }  // extern "C"

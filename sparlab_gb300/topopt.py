@@ -442,29 +442,60 @@ class TopologyOptimizer:
         return history
 
 
-def run_batched(problems: List[GpuSimpProblem], iterations: int, workers: Optional[int] = None):
+def run_batched(problems: List[GpuSimpProblem], iterations: int, workers: Optional[int] = None,
+                tune: bool = False, report: Optional[dict] = None):
     """Iterate independent problem instances concurrently.
 
     Each problem owns a CUDA stream and the library releases the GIL during
     a call, so ``workers`` host threads (default: one per host core, at most
-    one per problem) each drive their share of the instances, round robin,
-    and the instances' kernels overlap on the GPU.  Every instance computes
-    exactly what it computes alone.  Returns the per-problem iteration
-    records (lists, in problem order)."""
+    one per problem) each drive their share of the instances, round robin
+    (largest instance first), and the instances' kernels overlap on the GPU.
+    Every instance computes exactly what it computes alone, whatever the
+    worker count.  With ``tune`` the first iterations try worker counts n,
+    n/2, n/4, ... (one iteration each, timed on the host) and the rest use
+    the fastest; ``report`` (a dict) receives the counts tried, their
+    seconds and the choice.  Returns the per-problem iteration records
+    (lists, in problem order)."""
     import concurrent.futures as cf
     import os
     n = len(problems)
-    workers = max(1, min(workers or os.cpu_count() or 1, n))
-    shares = [list(range(w, n, workers)) for w in range(workers)]
+    order = sorted(range(n), key=lambda i: -problems[i].nnz)
     out: List[List[_lib.IterationRecord]] = [[] for _ in range(n)]
 
-    def drive(share):
-        for _ in range(iterations):
-            for i in share:
-                out[i].append(problems[i].iterate())
+    def step(count, its):
+        count = max(1, min(count, n))
+        shares = [order[w::count] for w in range(count)]
 
-    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
-        for f in [ex.submit(drive, sh) for sh in shares]:
-            f.result()
+        def drive(share):
+            for _ in range(its):
+                for i in share:
+                    out[i].append(problems[i].iterate())
+
+        with cf.ThreadPoolExecutor(max_workers=count) as ex:
+            for f in [ex.submit(drive, sh) for sh in shares]:
+                f.result()
+
+    chosen = max(1, min(workers or os.cpu_count() or 1, n))
+    done = 0
+    if tune:
+        cands, c = [], chosen
+        while c >= 1 and len(cands) < 4:
+            cands.append(c)
+            c //= 2
+        tried = []
+        for c in cands:
+            if done >= iterations:
+                break
+            t0 = time.perf_counter()
+            step(c, 1)
+            tried.append((c, time.perf_counter() - t0))
+            done += 1
+        if tried:
+            chosen = min(tried, key=lambda t: t[1])[0]
+        if report is not None:
+            report["workers_tried"] = [c for c, _ in tried]
+            report["seconds"] = [round(t, 4) for _, t in tried]
+            report["workers"] = chosen
+    if iterations > done:
+        step(chosen, iterations - done)
     return out
-
