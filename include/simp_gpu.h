@@ -185,8 +185,12 @@ typedef struct {
                                    prediction as one more vector (first solve: the
                                    prediction's optimal multiple); needs
                                    simp_problem_set_surrogate, else as 2 */
-  int32_t block_pcg;            /* 1: the load cases' PCG solves run at the same time, each
-                                   on its own workspace and stream (same results) */
+  int32_t block_pcg;            /* several load cases: 0 solved one after another; 1 at the
+                                   same time, each on its own workspace and stream from its
+                                   own host thread; 2 advanced together, one CUDA graph
+                                   launch running one PCG iteration of every load case
+                                   still iterating (a conditional node per load case);
+                                   all three compute the same values */
   int32_t optimizer;            /* simp_iterate's update: 0 OC, 1 MMA */
   /* Heaviside projection of the filtered density with beta continuation
    * (ProjectionOptions, include/sparlab/topopt/Projection.hpp:69-96,
@@ -272,6 +276,17 @@ int simp_mma_update(simp_problem* p, int32_t apply, simp_oc_step* out, double* x
 /* One run_oc (or run_mma, per desc->optimizer) iteration: evaluate + update +
  * clamp, device-resident. */
 int simp_iterate(simp_problem* p, simp_iteration_record* rec);
+
+/* One SIMP iteration (simp_iterate) of each of n independent problems, their
+ * linear solves advanced together: every problem's filter, assembly and
+ * AMG setup (host threads, one stream per problem), then the PCG of every
+ * load case of every problem in lock step -- one CUDA graph launch runs one
+ * iteration of each solve still iterating, each under a conditional node set
+ * by its own convergence test -- then every problem's sensitivities and
+ * update.  Each problem computes what simp_iterate computes alone, bit for
+ * bit.  records: n entries.  The first failing problem's status is returned
+ * (its message in simp_problem_last_error); the others still iterate. */
+int simp_iterate_batch(simp_problem* const* problems, int32_t n, simp_iteration_record* records);
 
 /* AMG statistics of the problem's solver. */
 int simp_problem_stats(simp_problem* p, simp_amg_stats* stats);

@@ -40,7 +40,7 @@ EXPORTS = [
     "simp_surrogate_train", "simp_surrogate_predict", "simp_surrogate_forward",
     "simp_problem_set_surrogate", "simp_problem_learned_seconds", "simp_conv3d_bf16",
     "simp_surrogate_loss_gradient", "simp_autotune_enable", "simp_autotune_report",
-    "simp_autotune_set",
+    "simp_autotune_set", "simp_iterate_batch",
     "simp_conv3d_wgrad",
 ]
 

@@ -355,6 +355,7 @@ GpuAmg::GpuAmg(const AmgOptions& o) : opt(o) {
 }
 
 GpuAmg::~GpuAmg() {
+  together_forget(this);
   extra_.clear();
   if (stream) {
     cudaStreamSynchronize(stream);
@@ -489,11 +490,11 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     if (rhs)
       k_rows_apply_df<VS, B, 1><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
-                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit, y, rhs,
+                                                                       l0.a.v2.p, xsplit, y, rhs,
                                                                        op.rows);
     else
       k_rows_apply_df<VS, B, 0><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
-                                                                       l0.a.v32.p, l0.a.v32lo.p, xsplit, y,
+                                                                       l0.a.v2.p, xsplit, y,
                                                                        nullptr, op.rows);
   });
   SIMP_CHECK_LAUNCH();
@@ -560,8 +561,9 @@ void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
 void GpuAmg::refresh_level0_fp32() {
   Level& l0 = *levels.front();
   l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
-  l0.a.v32lo.alloc(static_cast<size_t>(l0.a.nnz));
-  k_split_values<<<grid_for(l0.a.nnz, 256, 8192), 256, 0, stream>>>(l0.a.nnz, l0.a.v64.p, l0.a.v32.p, l0.a.v32lo.p);
+  l0.a.v2.alloc(static_cast<size_t>(l0.a.nnz));
+  k_split_values_pairs<<<grid_for(l0.a.nnz, 256, 8192), 256, 0, stream>>>(l0.a.nnz, l0.a.v64.p, l0.a.v32.p,
+                                                                           l0.a.v2.p);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -874,8 +876,8 @@ void GpuAmg::build_transfer(size_t l) {
 // Launches a warp-per-row-node product with its shared-memory shape; false
 // (nothing launched) when one warp's accumulator would not fit.
 template <class T, class... KArgs, class... Args>
-bool launch_rows(void (*kernel)(i32, WarpRows, KArgs...), i32 nodes, const WarpRows& w, cudaStream_t s,
-                 Args... args) {
+bool launch_rows(const char* name, void (*kernel)(i32, WarpRows, KArgs...), i32 nodes, const WarpRows& w,
+                 cudaStream_t s, Args... args) {
   const size_t per_warp =
       static_cast<size_t>(w.acc) * sizeof(T) + static_cast<size_t>(2 * w.slots + kMetaInts + w.inner) * 4;
   if (per_warp > 200 * 1024) return false;
@@ -894,7 +896,7 @@ bool launch_rows(void (*kernel)(i32, WarpRows, KArgs...), i32 nodes, const WarpR
     SIMP_CHECK_LAUNCH();
   };
   std::ostringstream key;
-  key << "rows:" << typeid(kernel).name() << ":" << sizeof(T) << ":" << nodes << ":" << w.acc << ":" << w.slots;
+  key << name << (sizeof(T) == 4 ? "32:" : "64:") << nodes << "x" << w.acc << "x" << w.slots;
   launch(tune_pick(key.str(), 4, launch, s, 0));
   return true;
 }
@@ -928,7 +930,8 @@ static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t 
     gather(k_prolongator_gather<T, kExact, 6, 6>);
   } else if (!kExact && bf == 3 && b1 == 3) {
     gather(k_prolongator_gather<T, kExact, 3, 3>);
-  } else if (!launch_rows<T>(k_prolongator_rows<T, kExact>, lv.nnodes, lv.wr_p, stream, lv.d_first.p, nv.d_first.p,
+  } else if (!launch_rows<T>("prolongator_rows", k_prolongator_rows<T, kExact>, lv.nnodes, lv.wr_p, stream,
+                             lv.d_first.p, nv.d_first.p,
                              lv.d_agg.p, lv.d_apat.view(), lv.a.ptr.p, A(lv.a), lv.d_ppat.view(), lv.p.ptr.p,
                              A(lv.p), lv.phat_ptr.p, phat, lv.dinv64.p, omega)) {
     const i64 th = static_cast<i64>(lv.n) * 8;
@@ -945,11 +948,13 @@ static void galerkin_t(GpuAmg& g, Level& lv, Level& nv, bool last, cudaStream_t 
     SIMP_CHECK_LAUNCH();
   }
   auto ap_rows = [&](auto kernel) {
-    return launch_rows<T>(kernel, lv.nnodes, lv.wr_ap, stream, lv.d_first.p, lv.d_apat.view(), lv.a.ptr.p, A(lv.a),
+    return launch_rows<T>("ap_rows", kernel, lv.nnodes, lv.wr_ap, stream, lv.d_first.p, lv.d_apat.view(), lv.a.ptr.p,
+                          A(lv.a),
                           lv.d_ppat.view(), lv.p.ptr.p, A(lv.p), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap));
   };
   auto rap_rows = [&](auto kernel) {
-    return launch_rows<T>(kernel, nv.nnodes, lv.wr_rap, stream, nv.d_first.p, lv.d_first.p, lv.d_rpat.view(),
+    return launch_rows<T>("rap_rows", kernel, nv.nnodes, lv.wr_rap, stream, nv.d_first.p, lv.d_first.p,
+                          lv.d_rpat.view(),
                           lv.r.ptr.p, A(lv.r), lv.d_appat.view(), lv.ap.ptr.p, A(lv.ap), nv.d_apat.view(),
                           nv.a.ptr.p, raw);
   };
@@ -1408,6 +1413,340 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x_out, doub
   res.iterations = total;
   SIMP_CUDA(cudaMemcpyAsync(x_out, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   return res;
+}
+
+// ---------------------------------------------------------------------------
+// Several PCG solves advanced together (solve_together).
+// ---------------------------------------------------------------------------
+namespace {
+
+// Sets a system's conditional from its loop flag (first node of its branch).
+__global__ void k_arm(cudaGraphConditionalHandle h, const int* __restrict__ loop) {
+  cudaGraphSetConditional(h, loop[0] != 0 ? 1u : 0u);
+}
+
+// After an iteration body: count the iteration and apply GpuAmg::pcg's test
+// (no breakdown, sqrt(||r||^2) above the stopping norm, budget left); the
+// flag is the host's view of whether the system iterates on.
+__global__ void k_loop_test(const PcgScalars* __restrict__ sc, int* __restrict__ loop,
+                            const double* __restrict__ target, int* __restrict__ flag) {
+  const int total = loop[1] + 1;
+  loop[1] = total;
+  const bool go = sc->status == 0 && !(sqrt(sc->rr) <= target[0]) && total < loop[2];
+  loop[0] = go ? 1 : 0;
+  *flag = go ? 1 : 0;
+}
+
+}  // namespace
+
+// One graph over a set of (hierarchy, workspace) pairs: per pair an arm
+// kernel and a conditional node whose body is the pair's PCG iteration
+// (pcg_tail + pcg_head, as pcg_body captures it) and its loop test.
+struct TogetherGraph {
+  std::vector<std::pair<GpuAmg*, SolveWork*>> members;
+  std::vector<uint64_t> epochs;
+  std::vector<int64_t> kernels;  // kernels of each member's body
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t stream = nullptr;
+  DBuf<int> flags;
+  TogetherGraph() = default;
+  TogetherGraph(const TogetherGraph&) = delete;
+  TogetherGraph& operator=(const TogetherGraph&) = delete;
+  ~TogetherGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  bool matches(const std::vector<std::pair<GpuAmg*, SolveWork*>>& m) const {
+    if (m != members) return false;
+    for (size_t i = 0; i < m.size(); ++i)
+      if (m[i].first->epoch_ != epochs[i]) return false;
+    return true;
+  }
+
+  void build() {
+    const size_t n = members.size();
+    if (!stream) SIMP_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    flags.alloc(n);
+    kernels.assign(n, 0);
+    epochs.clear();
+    cudaGraph_t g = nullptr;
+    SIMP_CUDA(cudaGraphCreate(&g, 0));
+    try {
+      for (size_t i = 0; i < n; ++i) {
+        GpuAmg& a = *members[i].first;
+        SolveWork& w = *members[i].second;
+        epochs.push_back(a.epoch_);
+        cudaGraphConditionalHandle h;
+        SIMP_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+        const int* loop = w.loop.p;
+        void* args[] = {&h, &loop};
+        cudaGraphNodeParams kp = {};
+        kp.type = cudaGraphNodeTypeKernel;
+        kp.kernel.func = reinterpret_cast<void*>(k_arm);
+        kp.kernel.gridDim = dim3(1);
+        kp.kernel.blockDim = dim3(1);
+        kp.kernel.sharedMemBytes = 0;
+        kp.kernel.kernelParams = args;
+        kp.kernel.extra = nullptr;
+        cudaGraphNode_t arm = nullptr;
+        SIMP_CUDA(cudaGraphAddNode(&arm, g, nullptr, nullptr, 0, &kp));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cond = nullptr;
+        SIMP_CUDA(cudaGraphAddNode(&cond, g, &arm, nullptr, 1, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        SIMP_CUDA(cudaStreamBeginCaptureToGraph(w.stream, body, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+        const int64_t before = t_launches;
+        try {
+          float2* ps = a.psplit_of(w);
+          a.pcg_tail(w, ps);
+          a.pcg_head(w, w.px.p, ps != nullptr || a.mf_cg());
+          k_loop_test<<<1, 1, 0, w.stream>>>(reinterpret_cast<const PcgScalars*>(w.scal.p + 8), w.loop.p,
+                                             w.loopd.p, flags.p + i);
+          SIMP_CHECK_LAUNCH();
+        } catch (...) {
+          cudaGraph_t tmp = nullptr;
+          cudaStreamEndCapture(w.stream, &tmp);
+          throw;
+        }
+        kernels[i] = t_launches - before;
+        cudaGraph_t tmp = nullptr;
+        SIMP_CUDA(cudaStreamEndCapture(w.stream, &tmp));
+        // captured launches ran nothing: counted when the graph runs
+        g_launches.fetch_sub(kernels[i], std::memory_order_relaxed);
+      }
+      if (exec) {
+        cudaGraphExecDestroy(exec);
+        exec = nullptr;
+      }
+      SIMP_CUDA(cudaGraphInstantiate(&exec, g, 0));
+    } catch (...) {
+      cudaGraphDestroy(g);
+      throw;
+    }
+    cudaGraphDestroy(g);
+  }
+};
+
+namespace {
+std::mutex g_together_mu;
+std::vector<std::unique_ptr<TogetherGraph>> g_together;  // most recent last
+
+// The graph of a member set (built or rebuilt on demand); the caller holds
+// g_together_mu.
+TogetherGraph& together_graph(const std::vector<std::pair<GpuAmg*, SolveWork*>>& m) {
+  for (auto& t : g_together)
+    if (t->members == m) {
+      if (!t->matches(m)) t->build();
+      return *t;
+    }
+  if (g_together.size() >= 8) g_together.erase(g_together.begin());
+  g_together.emplace_back(new TogetherGraph());
+  g_together.back()->members = m;
+  g_together.back()->build();
+  return *g_together.back();
+}
+}  // namespace
+
+// drops the cached graphs that hold a hierarchy about to be destroyed
+void together_forget(const GpuAmg* a) {
+  std::lock_guard<std::mutex> lock(g_together_mu);
+  for (size_t i = 0; i < g_together.size();) {
+    bool hit = false;
+    for (auto& m : g_together[i]->members) hit = hit || m.first == a;
+    if (hit) g_together.erase(g_together.begin() + static_cast<long>(i));
+    else ++i;
+  }
+}
+
+std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& tasks) {
+  struct St {
+    double bnorm = 0, target = 0, best = std::numeric_limits<double>::max();
+    int total = 0, round = 0, rounds = 3;
+    bool done = false, rec_conv = false, conv = false, looping = false, ran = false;
+  };
+  const size_t n = tasks.size();
+  std::vector<TaskResult> out(n);
+  std::vector<St> st(n);
+  auto fail = [&](size_t i, const Error& e) {
+    out[i].error_code = e.code;
+    out[i].error = e.what();
+    st[i].done = true;
+  };
+  auto finish = [&](size_t i) {
+    GpuAmg& a = *tasks[i].amg;
+    SolveWork& w = *tasks[i].w;
+    if (!out[i].r.converged && st[i].rec_conv) out[i].r.converged = true;
+    out[i].r.iterations = st[i].total;
+    const i32 nn = a.levels.front()->n;
+    SIMP_CUDA(cudaMemcpyAsync(tasks[i].x, w.px.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, w.stream));
+    st[i].done = true;
+  };
+  auto breakdown = [&](size_t i, const PcgScalars& h) {
+    std::ostringstream os;
+    os << "preconditioned CG broke down at iteration " << st[i].total + 1 << " (p^T A p = " << h.pq
+       << "): the stiffness matrix or the multigrid preconditioner is not positive definite. "
+          "Check the supports, or use a direct solver to confirm";
+    fail(i, Error(kBreakdown, os.str()));
+  };
+  // set-up: as solve() does
+  for (size_t i = 0; i < n; ++i) {
+    GpuAmg& a = *tasks[i].amg;
+    SolveWork& w = *tasks[i].w;
+    if (!a.ready_) throw Error(kBadInput, "solve called before factorize");
+    a.ensure(w);
+    w.loop.alloc(4);
+    w.loopd.alloc(2);
+    const i32 nn = a.levels.front()->n;
+    st[i].bnorm = std::sqrt(a.dot(w, tasks[i].b, tasks[i].b, nn));
+    if (st[i].bnorm == 0.0) {
+      SIMP_CUDA(cudaMemsetAsync(tasks[i].x, 0, sizeof(double) * nn, w.stream));
+      out[i].r.converged = true;
+      st[i].done = true;
+      continue;
+    }
+    st[i].target = a.opt.rtol * st[i].bnorm;
+    st[i].rounds = a.mf_cg() ? 12 : 3;
+    w.px.alloc(static_cast<size_t>(nn));
+    if (a.mf_cg()) w.p32.alloc(static_cast<size_t>(nn));
+    SIMP_CUDA(cudaMemcpyAsync(w.px.p, tasks[i].x, sizeof(double) * nn, cudaMemcpyDeviceToDevice, w.stream));
+  }
+  while (true) {
+    bool any = false;
+    // round start and each round's first iteration, per system
+    for (size_t i = 0; i < n; ++i) {
+      St& s = st[i];
+      s.ran = false;
+      s.looping = false;
+      if (s.done) continue;
+      any = true;
+      GpuAmg& a = *tasks[i].amg;
+      SolveWork& w = *tasks[i].w;
+      const i32 nn = a.levels.front()->n;
+      try {
+        a.op0(w, w.px.p, w.pr.p, tasks[i].b, false);
+        const double rnorm = std::sqrt(a.dot(w, w.pr.p, w.pr.p, nn));
+        out[i].r.relres = rnorm / s.bnorm;
+        if (rnorm <= s.target) {
+          out[i].r.converged = true;
+          finish(i);
+          continue;
+        }
+        a.apply(w, w.pr.p, w.pz.p);
+        SIMP_CUDA(cudaMemcpyAsync(w.pp.p, w.pz.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, w.stream));
+        const double rz = a.dot(w, w.pr.p, w.pz.p, nn);
+        PcgScalars* sc = reinterpret_cast<PcgScalars*>(w.scal.p + 8);
+        PcgScalars h{};
+        h.rz = rz;
+        SIMP_CUDA(cudaMemcpyAsync(sc, &h, sizeof(h), cudaMemcpyHostToDevice, w.stream));
+        s.conv = false;
+        s.ran = true;
+        if (s.total < a.opt.maxit) {
+          a.pcg_head(w, w.px.p, false);
+          SIMP_CUDA(cudaMemcpyAsync(&h, sc, sizeof(h), cudaMemcpyDeviceToHost, w.stream));
+          SIMP_CUDA(cudaStreamSynchronize(w.stream));
+          if (h.status != 0) {
+            breakdown(i, h);
+            continue;
+          }
+          ++s.total;
+          if (std::sqrt(h.rr) <= s.target) s.conv = true;
+          else if (s.total < a.opt.maxit) s.looping = true;
+        }
+        if (s.looping) {
+          const int hl[4] = {1, s.total, a.opt.maxit, 0};
+          const double ht[2] = {s.target, 0.0};
+          SIMP_CUDA(cudaMemcpyAsync(w.loop.p, hl, sizeof(hl), cudaMemcpyHostToDevice, w.stream));
+          SIMP_CUDA(cudaMemcpyAsync(w.loopd.p, ht, sizeof(ht), cudaMemcpyHostToDevice, w.stream));
+          SIMP_CUDA(cudaStreamSynchronize(w.stream));
+        }
+      } catch (const Error& e) {
+        fail(i, e);
+      }
+    }
+    if (!any) break;
+    // the later iterations of the round: all looping systems together
+    std::vector<size_t> idx;
+    for (size_t i = 0; i < n; ++i)
+      if (st[i].looping) idx.push_back(i);
+    if (!idx.empty()) {
+      std::vector<std::pair<GpuAmg*, SolveWork*>> members;
+      for (size_t i : idx) members.emplace_back(tasks[i].amg, tasks[i].w);
+      std::lock_guard<std::mutex> lock(g_together_mu);
+      TogetherGraph& tg = together_graph(members);
+      std::vector<int> hf(idx.size(), 1);
+      std::vector<int> active(idx.size(), 1);
+      size_t alive = idx.size();
+      while (alive > 0) {
+        int64_t launched = 0;
+        for (size_t k = 0; k < idx.size(); ++k)
+          if (active[k]) launched += tg.kernels[k];
+        SIMP_CUDA(cudaGraphLaunch(tg.exec, tg.stream));
+        g_launches.fetch_add(launched + static_cast<int64_t>(idx.size()), std::memory_order_relaxed);
+        SIMP_CUDA(cudaMemcpyAsync(hf.data(), tg.flags.p, sizeof(int) * idx.size(), cudaMemcpyDeviceToHost,
+                                  tg.stream));
+        SIMP_CUDA(cudaStreamSynchronize(tg.stream));
+        alive = 0;
+        for (size_t k = 0; k < idx.size(); ++k) {
+          active[k] = active[k] && hf[k];
+          alive += active[k] ? 1 : 0;
+        }
+      }
+      for (size_t k = 0; k < idx.size(); ++k) {
+        const size_t i = idx[k];
+        SolveWork& w = *tasks[i].w;
+        PcgScalars h{};
+        int hl[4] = {0, 0, 0, 0};
+        SIMP_CUDA(cudaMemcpyAsync(&h, w.scal.p + 8, sizeof(h), cudaMemcpyDeviceToHost, w.stream));
+        SIMP_CUDA(cudaMemcpyAsync(hl, w.loop.p, sizeof(hl), cudaMemcpyDeviceToHost, w.stream));
+        SIMP_CUDA(cudaStreamSynchronize(w.stream));
+        if (h.status != 0) {
+          st[i].total = hl[1] - 1;  // the iteration that broke down is not counted
+          breakdown(i, h);
+          continue;
+        }
+        st[i].total = hl[1];
+        st[i].conv = std::sqrt(h.rr) <= st[i].target;
+      }
+    }
+    // round end, per system: true residual and the restart decision
+    for (size_t i = 0; i < n; ++i) {
+      St& s = st[i];
+      if (s.done || !s.ran) continue;
+      GpuAmg& a = *tasks[i].amg;
+      SolveWork& w = *tasks[i].w;
+      const i32 nn = a.levels.front()->n;
+      try {
+        a.op0(w, w.px.p, w.pr.p, tasks[i].b, false);
+        out[i].r.relres = std::sqrt(a.dot(w, w.pr.p, w.pr.p, nn)) / s.bnorm;
+        if (out[i].r.relres * s.bnorm <= s.target) {
+          out[i].r.converged = true;
+          finish(i);
+          continue;
+        }
+        if (!s.conv) {
+          finish(i);
+          continue;
+        }
+        s.rec_conv = true;
+        if (!(out[i].r.relres < 0.5 * s.best)) {
+          finish(i);
+          continue;
+        }
+        s.best = out[i].r.relres;
+        if (++s.round >= s.rounds) finish(i);
+      } catch (const Error& e) {
+        fail(i, e);
+      }
+    }
+  }
+  for (size_t i = 0; i < n; ++i) SIMP_CUDA(cudaStreamSynchronize(tasks[i].w->stream));
+  return out;
 }
 
 GpuAmg::PcgResult GpuAmg::solve(SolveWork& w, const double* b, double* x) {

@@ -55,7 +55,7 @@ struct DevCsr {
   DBuf<i32> ptr, col;
   DBuf<double> v64;
   DBuf<float> v32;
-  DBuf<float> v32lo;  // level 0, mixed: v64 - v32 (double-float CG operator)
+  DBuf<float2> v2;    // level 0, mixed: (v32, v64 - v32) pairs, interleaved (the double-float CG operator)
 };
 
 // A node-chunked matrix as the operator kernels see it (see nbspmv.cuh).
@@ -159,6 +159,10 @@ struct SolveWork {
   // PCG iteration body (V-cycle, direction, operator, update) captured as a
   // CUDA graph on this workspace's buffers; valid for one hierarchy epoch
   DBuf<double> px;      // the iterate (the caller's x is copied in and out)
+  // solves advanced together (solve_together): [0] iterating, [1] iterations
+  // done, [2] budget; loopd[0] the stopping residual norm
+  DBuf<int> loop;
+  DBuf<double> loopd;
   cudaGraphExec_t body = nullptr;
   uint64_t body_epoch = 0;
   int64_t body_kernels = 0;
@@ -175,6 +179,20 @@ struct AmgStats {
   i64 storage = 0;
 };
 
+class GpuAmg;
+
+// drops cached solve_together graphs that hold this hierarchy
+void together_forget(const GpuAmg* a);
+
+// One linear solve of solve_together: the hierarchy, a workspace of it, the
+// right-hand side and the guess / solution (device, level-0 length).
+struct SolveTask {
+  GpuAmg* amg = nullptr;
+  SolveWork* w = nullptr;
+  const double* b = nullptr;
+  double* x = nullptr;
+};
+
 class GpuAmg {
  public:
   explicit GpuAmg(const AmgOptions& o);
@@ -189,7 +207,7 @@ class GpuAmg {
   // the CG operator is the FP32 matrix-free product (matrix_free = 2, 3-D)
   bool mf_cg() const { return mixed() && opt.matrix_free >= 2 && mf.enabled && mf.dim == 3; }
   // Set by an assembler that wrote level 0's FP32 values (hi in a.v32 and
-  // lo in a.v32lo) itself; otherwise setup splits the FP64 values (mixed
+  // (hi, lo) pairs in a.v2) itself; otherwise setup splits the FP64 values (mixed
   // mode).  In mixed mode the CG operator reads hi/lo only, so an assembler
   // may leave a.v64 stale after the structure-defining first setup.
   bool level0_fp32_fresh = false;
@@ -235,6 +253,20 @@ class GpuAmg {
   void apply_values0(SolveWork& w, const double* values, const double* x, double* y);
   // CUDA-event time of one op0 launch (ms) and its algorithmic bytes
   void time_operator(int reps, double* ms, double* bytes);
+  // The PCG of solve() for several systems at once (load cases of one
+  // problem on their own workspaces, or independent problems): the same
+  // iterations, restarts and stopping tests per system, with every round's
+  // iterations after the first advanced together -- one CUDA graph launch
+  // runs one PCG iteration of each system still iterating, each under a
+  // conditional node its own convergence test sets.  Results and iteration
+  // counts equal solve()'s bit for bit.  Errors (breakdown, no convergence)
+  // are thrown after every task has stopped, the first task's first.
+  struct TaskResult {
+    PcgResult r;
+    int error_code = 0;
+    std::string error;
+  };
+  static std::vector<TaskResult> solve_together(std::vector<SolveTask>& tasks);
   double dot(SolveWork& w, const double* a, const double* b, i64 n);
 
   DBuf<double> part, scal;  // reductions of setup and of callers on the context stream
@@ -267,6 +299,8 @@ class GpuAmg {
   void pcg_tail(SolveWork& w, float2* psplit);
   void pcg_head(SolveWork& w, double* x, bool split_ready);
   void pcg_body(SolveWork& w, double* x, float2* psplit);
+  float2* psplit_of(SolveWork& w) { return mixed() && !mf_cg() ? w.xsplit.p : nullptr; }
+  friend struct TogetherGraph;
   uint64_t epoch_ = 1;  // bumped by every setup: captured graphs are stale
   void compute_stats();
   void tune_level0();

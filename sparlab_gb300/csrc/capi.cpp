@@ -7,7 +7,10 @@
 #include "surrogate_net.h"
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
+#include <thread>
 #include <cstring>
 #include <memory>
 #include <sstream>
@@ -73,6 +76,31 @@ int guarded(std::string& err, F&& f) {
 }
 
 void use_device(int dev) { SIMP_CUDA(cudaSetDevice(dev)); }
+
+// One history row (TopologyIteration) from an evaluation and an update.
+void fill_record(const GpuProblem& g, const Evaluation& ev, const OcStep& st, double seconds,
+                 simp_iteration_record* rec) {
+  rec->compliance = ev.compliance;
+  rec->volume_fraction = ev.volume_fraction;
+  rec->max_change = st.max_change;
+  rec->lambda = st.lambda;
+  rec->gray_level = g.gray;
+  rec->linear_iterations = ev.linear_iterations;
+  rec->bisections = st.bisections;
+  rec->seconds = seconds;
+  // MMA: the volume row fval(0) <= constraint_tolerance (1e-4)
+  const double fval0 = g.d.robust ? ev.volume_dilated / g.dilated_target - 1.0 : ev.volume_fraction / g.d.vf - 1.0;
+  rec->volume_converged = g.d.optimizer == 1 ? (fval0 <= 1.0e-4 ? 1 : 0) : (st.converged ? 1 : 0);
+  rec->final_stage = g.beta_at_final() ? 1 : 0;
+  rec->beta = g.d.projection ? g.beta : 0.0;
+  rec->eroded_volume_fraction = rec->dilated_volume_fraction = rec->dilated_target_fraction = 0.0;
+  if (g.d.robust) {
+    rec->volume_fraction = ev.volume_intermediate / g.domain_volume;
+    rec->eroded_volume_fraction = ev.volume_fraction;
+    rec->dilated_volume_fraction = ev.volume_dilated / g.domain_volume;
+    rec->dilated_target_fraction = g.dilated_target / g.domain_volume;
+  }
+}
 
 }  // namespace
 
@@ -508,7 +536,8 @@ int simp_problem_create(const simp_problem_desc* dsc, const simp_solver_options*
     if (!(d.damping > 0.0 && d.damping <= 1.0)) throw Error(kBadInput, "optimizer.damping must lie in (0, 1]");
     if (dsc->warm_start < 0 || dsc->warm_start > 3) throw Error(kBadInput, "warm_start must be 0, 1, 2 or 3");
     d.warm = dsc->warm_start;
-    d.block_pcg = dsc->block_pcg != 0;
+    if (dsc->block_pcg < 0 || dsc->block_pcg > 2) throw Error(kBadInput, "block_pcg must be 0, 1 or 2");
+    d.block_pcg = dsc->block_pcg;
     d.projection = dsc->projection != 0;
     if (d.projection) {
       // ProjectionOptions::validate (src/topopt/Projection.cpp:10-43)
@@ -666,31 +695,102 @@ int simp_iterate(simp_problem* p, simp_iteration_record* rec) {
     SIMP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (rec) {
-      rec->compliance = ev.compliance;
-      rec->volume_fraction = ev.volume_fraction;
-      rec->max_change = st.max_change;
-      rec->lambda = st.lambda;
-      rec->gray_level = g.gray;
-      rec->linear_iterations = ev.linear_iterations;
-      rec->bisections = st.bisections;
-      rec->seconds = ms * 1e-3;
-      // MMA: the volume row fval(0) <= constraint_tolerance (1e-4)
-      const double fval0 = g.d.robust ? ev.volume_dilated / g.dilated_target - 1.0
-                                      : ev.volume_fraction / g.d.vf - 1.0;
-      rec->volume_converged = g.d.optimizer == 1 ? (fval0 <= 1.0e-4 ? 1 : 0) : (st.converged ? 1 : 0);
-      rec->final_stage = g.beta_at_final() ? 1 : 0;
-      rec->beta = g.d.projection ? g.beta : 0.0;
-      rec->eroded_volume_fraction = rec->dilated_volume_fraction = rec->dilated_target_fraction = 0.0;
-      if (g.d.robust) {
-        rec->volume_fraction = ev.volume_intermediate / g.domain_volume;
-        rec->eroded_volume_fraction = ev.volume_fraction;
-        rec->dilated_volume_fraction = ev.volume_dilated / g.domain_volume;
-        rec->dilated_target_fraction = g.dilated_target / g.domain_volume;
-      }
-    }
+    if (rec) fill_record(g, ev, st, ms * 1e-3, rec);
     g.advance_beta(st.max_change);
   });
+}
+
+int simp_iterate_batch(simp_problem* const* problems, int32_t n, simp_iteration_record* records) {
+  if (!problems || n < 1) {
+    g_create_error = "simp_iterate_batch: no problems";
+    return kBadInput;
+  }
+  const int dev = problems[0]->device;
+  for (int i = 0; i < n; ++i)
+    if (!problems[i] || problems[i]->device != dev) {
+      g_create_error = "simp_iterate_batch: the problems must live on one device";
+      return kBadInput;
+    }
+  for (int i = 0; i < n; ++i) problems[i]->err.clear();
+  std::vector<int> codes(static_cast<size_t>(n), 0);
+  auto record_error = [&](int i, int code, const std::string& msg) {
+    problems[i]->err = msg;
+    codes[static_cast<size_t>(i)] = code;
+  };
+  // fn(i) for every problem without an error, from a pool of host threads
+  auto each = [&](auto&& fn) {
+    const int workers = std::max(1, std::min<int>(n, static_cast<int>(std::thread::hardware_concurrency())));
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int k = 0; k < workers; ++k)
+      pool.emplace_back([&] {
+        cudaSetDevice(dev);
+        for (int i = next++; i < n; i = next++) {
+          if (codes[static_cast<size_t>(i)]) continue;
+          try {
+            fn(i);
+          } catch (const Error& e) {
+            record_error(i, e.code, e.what());
+          } catch (const std::exception& e) {
+            record_error(i, kBadInput, e.what());
+          }
+        }
+      });
+    for (auto& t : pool) t.join();
+  };
+  const auto t0 = std::chrono::steady_clock::now();
+  each([&](int i) {
+    GpuProblem& g = *problems[i]->p;
+    ++g.iteration;
+    g.evaluate_prepare();
+    for (int l = 0; l < g.d.nloads; ++l) {
+      SolveWork& w = g.amg.work(l);
+      g.amg.ensure(w);
+      g.start_load(l, w);
+    }
+    SIMP_CUDA(cudaStreamSynchronize(g.amg.stream));
+  });
+  std::vector<SolveTask> tasks;
+  std::vector<std::pair<int, int>> owner;
+  for (int i = 0; i < n; ++i) {
+    if (codes[static_cast<size_t>(i)]) continue;
+    GpuProblem& g = *problems[i]->p;
+    for (int l = 0; l < g.d.nloads; ++l) {
+      tasks.push_back(g.load_task(l, g.amg.work(l)));
+      owner.emplace_back(i, l);
+    }
+  }
+  std::vector<std::vector<GpuAmg::PcgResult>> res(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) res[static_cast<size_t>(i)].resize(static_cast<size_t>(problems[i]->p->d.nloads));
+  try {
+    use_device(dev);
+    const std::vector<GpuAmg::TaskResult> tr = GpuAmg::solve_together(tasks);
+    for (size_t k = 0; k < tr.size(); ++k) {
+      const int i = owner[k].first, l = owner[k].second;
+      if (tr[k].error_code) {
+        if (!codes[static_cast<size_t>(i)]) record_error(i, tr[k].error_code, tr[k].error);
+      } else {
+        res[static_cast<size_t>(i)][static_cast<size_t>(l)] = tr[k].r;
+      }
+    }
+  } catch (const Error& e) {
+    for (int i = 0; i < n; ++i)
+      if (!codes[static_cast<size_t>(i)]) record_error(i, e.code, e.what());
+  }
+  each([&](int i) {
+    GpuProblem& g = *problems[i]->p;
+    for (int l = 0; l < g.d.nloads; ++l) g.end_load(l, g.amg.work(l));
+    const Evaluation ev = g.evaluate_finish(res[static_cast<size_t>(i)]);
+    g.update_robust_target();
+    const OcStep st = g.d.optimizer == 1 ? g.mma_update(true, nullptr) : g.oc_update(true, nullptr);
+    SIMP_CUDA(cudaStreamSynchronize(g.amg.stream));
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (records) fill_record(g, ev, st, sec, &records[i]);
+    g.advance_beta(st.max_change);
+  });
+  for (int i = 0; i < n; ++i)
+    if (codes[static_cast<size_t>(i)]) return codes[static_cast<size_t>(i)];
+  return kOk;
 }
 
 int simp_problem_stats(simp_problem* p, simp_amg_stats* s) {

@@ -70,6 +70,17 @@ __global__ void k_split_values(i64 n, const double* __restrict__ v, float* __res
   }
 }
 
+// hi = float(v) and the interleaved (hi, lo) pairs of the double-float operator
+__global__ void k_split_values_pairs(i64 n, const double* __restrict__ v, float* __restrict__ hi,
+                                     float2* __restrict__ pair) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+    float h, l;
+    df_split(v[i], h, l);
+    hi[i] = h;
+    pair[i] = make_float2(h, l);
+  }
+}
+
 __global__ void k_split_pairs(i64 n, const double* __restrict__ v, float2* __restrict__ out) {
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     float h, l;

@@ -152,8 +152,8 @@ __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __
 template <int VS, int B, int MODE>
 __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ node_of, NodeView pat,
                                                        const i32* __restrict__ rowptr, const i32* __restrict__ col,
-                                                       const float* __restrict__ vhi, const float* __restrict__ vlo,
-                                                       const float2* __restrict__ x, double* __restrict__ y,
+                                                       const float2* __restrict__ v, const float2* __restrict__ x,
+                                                       double* __restrict__ y,
                                                        const double* __restrict__ b, i32 rows) {
   const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
   const i32 row = static_cast<i32>(t / VS);
@@ -161,26 +161,25 @@ __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ n
   float sh = 0.0f, sl = 0.0f;
   if (row < rows) {
     const i32 k0 = rowptr[row], len = rowptr[row + 1] - k0;
-    const float* vh = vhi + k0;
-    const float* vl = vlo + k0;
+    const float2* vp = v + k0;  // (hi, lo) pairs: one 8-byte load per value
     const i32* cl = col + k0;
     const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
     i32 w = lane;
     for (; w + (kUnroll - 1) * VS < len; w += kUnroll * VS) {
-      float h[kUnroll], l[kUnroll];
+      float2 hv[kUnroll];
       float2 xv[kUnroll];
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
-        h[u] = vh[w + u * VS];
-        l[u] = vl[w + u * VS];
+        hv[u] = vp[w + u * VS];
         xv[u] = x[row_col<B>(w + u * VS, s0, pat.nbr, cl)];
       }
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) df_fma(h[u], l[u], xv[u].x, xv[u].y, sh, sl);
+      for (int u = 0; u < kUnroll; ++u) df_fma(hv[u].x, hv[u].y, xv[u].x, xv[u].y, sh, sl);
     }
     for (; w < len; w += VS) {
       const float2 xv = x[row_col<B>(w, s0, pat.nbr, cl)];
-      df_fma(vh[w], vl[w], xv.x, xv.y, sh, sl);
+      const float2 hv = vp[w];
+      df_fma(hv.x, hv.y, xv.x, xv.y, sh, sl);
     }
   }
 #pragma unroll

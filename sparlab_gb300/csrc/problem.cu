@@ -447,7 +447,7 @@ void GpuProblem::get_design(double* h) {
 }
 
 void GpuProblem::assemble_into(const double* elem, const double* scale, bool exact, double* v64, float* hi,
-                               float* lo, cudaStream_t stream) {
+                               float2* pair, cudaStream_t stream) {
   Level& l0 = *amg.levels.front();
   if (l0.nnodes == 0) return;
   const int offsets = d.dim == 3 ? 27 : 9;
@@ -457,7 +457,7 @@ void GpuProblem::assemble_into(const double* elem, const double* scale, bool exa
   raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
   kernel<<<blocks, offsets * kAsmTile, smem, stream>>>(grid_of(d), l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
                                                        nmask.p, l0.d_apat.view(), l0.a.ptr.p, elem, scale, nullptr,
-                                                       nullptr, v64, hi, lo);
+                                                       nullptr, v64, hi, pair);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -468,11 +468,11 @@ void GpuProblem::assemble(const double* scale, bool exact) {
   const int offsets = d.dim == 3 ? 27 : 9;
   const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
   const size_t smem = assemble_smem(d.dim);
-  auto launch = [&](auto kernel, const float* sh, const float* sl, double* v64, float* hi, float* lo) {
+  auto launch = [&](auto kernel, const float* sh, const float* sl, double* v64, float* hi, float2* pair) {
     raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
     kernel<<<blocks, offsets * kAsmTile, smem, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p, nmask.p,
                                                               l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale, sh, sl,
-                                                              v64, hi, lo);
+                                                              v64, hi, pair);
     SIMP_CHECK_LAUNCH();
   };
   if (!amg.mixed()) {
@@ -484,18 +484,18 @@ void GpuProblem::assemble(const double* scale, bool exact) {
   // hi + lo = the CG operator); FP64 values only for the structure-defining
   // exact assembly
   l0.a.v32.alloc(static_cast<size_t>(l0.a.nnz));
-  l0.a.v32lo.alloc(static_cast<size_t>(l0.a.nnz));
+  l0.a.v2.alloc(static_cast<size_t>(l0.a.nnz));
   if (exact) {
-    launch(k_assemble_tiles<true, false>, nullptr, nullptr, l0.a.v64.p, l0.a.v32.p, l0.a.v32lo.p);
+    launch(k_assemble_tiles<true, false>, nullptr, nullptr, l0.a.v64.p, l0.a.v32.p, l0.a.v2.p);
   } else if (!amg.opt.reuse) {
     // every setup rebuilds the hierarchy from FP64 values
-    launch(k_assemble_tiles<false, false>, nullptr, nullptr, l0.a.v64.p, l0.a.v32.p, l0.a.v32lo.p);
+    launch(k_assemble_tiles<false, false>, nullptr, nullptr, l0.a.v64.p, l0.a.v32.p, l0.a.v2.p);
   } else {
     scale_hi.alloc(static_cast<size_t>(ne));
     scale_lo.alloc(static_cast<size_t>(ne));
     k_split_values<<<grid_for(ne, 256, 8192), 256, 0, amg.stream>>>(ne, scale, scale_hi.p, scale_lo.p);
     SIMP_CHECK_LAUNCH();
-    launch(k_assemble_tiles<false, true>, scale_hi.p, scale_lo.p, nullptr, l0.a.v32.p, l0.a.v32lo.p);
+    launch(k_assemble_tiles<false, true>, scale_hi.p, scale_lo.p, nullptr, l0.a.v32.p, l0.a.v2.p);
   }
   amg.level0_fp32_fresh = true;
 }
@@ -524,10 +524,10 @@ void GpuProblem::launch_sensitivities(cudaStream_t s) {
   SIMP_CHECK_LAUNCH();
 }
 
-Evaluation GpuProblem::evaluate() {
+// Filter, projection, SIMP law, assembly and AMG setup of an evaluation
+// (Sensitivity.cpp:121-139): everything before the load cases' solves.
+void GpuProblem::evaluate_prepare() {
   cudaStream_t s = amg.stream;
-  Evaluation ev;
-  // physical density, SIMP factors, stiffness (Sensitivity.cpp:121-139)
   k_filter_forward<<<grid_for(ne, kRedThreads), kRedThreads, 0, s>>>(
       grid_of(d), static_cast<const Stencil*>(stencil_d), hw.p, ne, x.p, d.projection ? rhot.p : rho.p, 1,
       nullptr, nullptr);
@@ -547,26 +547,69 @@ Evaluation GpuProblem::evaluate() {
   assemble(sf.p, !structure_built_);
   amg.setup(!structure_built_);
   structure_built_ = true;
-  // one PCG per load case, warm-started from the previous displacement; with
-  // several load cases and block_pcg the solves run at the same time, each
-  // on its own workspace and stream (same arithmetic as one after another)
   last_compliance.assign(static_cast<size_t>(d.nloads), 0.0);
+}
+
+// The start of load case l's solve: zero, the previous displacement (in
+// place), or the projected / learned start.
+void GpuProblem::start_load(int l, SolveWork& w) {
+  double* ul = u.p + static_cast<size_t>(l) * nfree;
+  const bool learned = d.warm == 3 && surrogate != nullptr;
+  if (learned) projected_start(l, ul, true);  // also the first solve: the prediction alone
+  else if (d.warm == 0 || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, w.stream));
+  else if (d.warm >= 2 && hist_count[l] > 0) projected_start(l, ul, false);
+}
+
+// After load case l's solve: c_l = f^T u (u vanishes on the supports) and
+// the displacement history.
+void GpuProblem::end_load(int l, SolveWork& w) {
+  double* ul = u.p + static_cast<size_t>(l) * nfree;
+  const double* bl = b.p + static_cast<size_t>(l) * nfree;
+  last_compliance[static_cast<size_t>(l)] = amg.dot(w, bl, ul, nfree);
+  if (d.warm >= 2) record_history(l, ul);
+}
+
+SolveTask GpuProblem::load_task(int l, SolveWork& w) {
+  SolveTask t;
+  t.amg = &amg;
+  t.w = &w;
+  t.b = b.p + static_cast<size_t>(l) * nfree;
+  t.x = u.p + static_cast<size_t>(l) * nfree;
+  return t;
+}
+
+Evaluation GpuProblem::evaluate() {
+  evaluate_prepare();
+  cudaStream_t s = amg.stream;
+  // one PCG per load case, warm-started from the previous displacement; with
+  // several load cases, block_pcg 1 runs the solves at the same time, each on
+  // its own workspace and stream from its own host thread, and block_pcg 2
+  // advances them together in one CUDA graph (solve_together); both compute
+  // what the solves compute one after another
   std::vector<GpuAmg::PcgResult> res(static_cast<size_t>(d.nloads));
   auto solve_load = [&](int l, SolveWork& w) {
-    const cudaStream_t ws = w.stream;
-    double* ul = u.p + static_cast<size_t>(l) * nfree;
-    const double* bl = b.p + static_cast<size_t>(l) * nfree;
-    const bool learned = d.warm == 3 && surrogate != nullptr;
-    if (learned) projected_start(l, ul, true);  // also the first solve: the prediction alone
-    else if (d.warm == 0 || evaluations == 0) SIMP_CUDA(cudaMemsetAsync(ul, 0, sizeof(double) * nfree, ws));
-    else if (d.warm >= 2 && hist_count[l] > 0) projected_start(l, ul, false);
-    res[static_cast<size_t>(l)] = amg.solve(w, bl, ul);
-    // c_l = f^T u (u vanishes on the supports)
-    last_compliance[static_cast<size_t>(l)] = amg.dot(w, bl, ul, nfree);
-    if (d.warm >= 2) record_history(l, ul);
+    start_load(l, w);
+    res[static_cast<size_t>(l)] = amg.solve(w, b.p + static_cast<size_t>(l) * nfree, u.p + static_cast<size_t>(l) * nfree);
+    end_load(l, w);
   };
-  const bool together = d.block_pcg && d.nloads > 1 && d.warm < 2;
-  if (together) {
+  const bool together = d.block_pcg == 1 && d.nloads > 1 && d.warm < 2;
+  if (d.block_pcg == 2 && d.nloads > 1) {
+    std::vector<SolveTask> tasks;
+    for (int l = 0; l < d.nloads; ++l) {
+      SolveWork& w = amg.work(l);
+      amg.ensure(w);
+      start_load(l, w);
+      tasks.push_back(load_task(l, w));
+    }
+    SIMP_CUDA(cudaStreamSynchronize(s));
+    const std::vector<GpuAmg::TaskResult> tr = GpuAmg::solve_together(tasks);
+    for (int l = 0; l < d.nloads; ++l)
+      if (tr[static_cast<size_t>(l)].error_code) throw Error(tr[static_cast<size_t>(l)].error_code, tr[static_cast<size_t>(l)].error);
+    for (int l = 0; l < d.nloads; ++l) {
+      res[static_cast<size_t>(l)] = tr[static_cast<size_t>(l)].r;
+      end_load(l, amg.work(l));
+    }
+  } else if (together) {
     SIMP_CUDA(cudaStreamSynchronize(s));  // assembly and setup are done before the solves start
     int dev = 0;
     SIMP_CUDA(cudaGetDevice(&dev));
@@ -595,6 +638,14 @@ Evaluation GpuProblem::evaluate() {
   } else {
     for (int l = 0; l < d.nloads; ++l) solve_load(l, amg.work(0));
   }
+  return evaluate_finish(res);
+}
+
+// Compliance, sensitivities, filter pull-back and volumes of an evaluation
+// whose solves returned `res` (Sensitivity.cpp:177-237).
+Evaluation GpuProblem::evaluate_finish(const std::vector<GpuAmg::PcgResult>& res) {
+  cudaStream_t s = amg.stream;
+  Evaluation ev;
   for (int l = 0; l < d.nloads; ++l) {
     const GpuAmg::PcgResult& r = res[static_cast<size_t>(l)];
     if (!r.converged) {

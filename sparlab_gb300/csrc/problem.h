@@ -36,7 +36,7 @@ struct ProblemDesc {
   int warm = 1;  // 0 zero start, 1 previous displacement, 2 projection on the last warm_history,
                  // 3 projection on the last warm_history and the surrogate's prediction
   int warm_history = kHistory;
-  bool block_pcg = false;
+  int block_pcg = 0;  // load cases: 0 one after another, 1 concurrent threads, 2 one graph
   int optimizer = 0;  // 0 OC, 1 MMA
   // Heaviside projection (src/topopt/Projection.cpp) with beta continuation
   bool projection = false;
@@ -80,6 +80,15 @@ class GpuProblem {
   void set_design(const double* h);
   void get_design(double* h);
   Evaluation evaluate();
+  // evaluate() in phases, for solves advanced together across problems
+  // (simp_iterate_batch): prepare (filter .. AMG setup), per load case its
+  // start, a SolveTask, and after the solve its compliance and history, then
+  // finish (sensitivities, pull-back, volumes) with the solves' results
+  void evaluate_prepare();
+  void start_load(int l, SolveWork& w);
+  SolveTask load_task(int l, SolveWork& w);
+  void end_load(int l, SolveWork& w);
+  Evaluation evaluate_finish(const std::vector<GpuAmg::PcgResult>& res);
   void launch_sensitivities(cudaStream_t s);
   OcStep oc_update(bool apply, double* xnew_host);
   // MMA step with the gradients of the last evaluate (mma.cu); lambda is the
@@ -92,9 +101,9 @@ class GpuProblem {
   void assemble(const double* scale_device, bool exact);
   // FP64 sum_e s_e E over level 0's pattern for a device element matrix E
   // (K_e^0, or M_e^0 for the mass), with the same kernel and order; FP32
-  // (hi) or double-float (hi, lo) copies when those are given
+  // (hi) and interleaved double-float (hi, lo) copies when those are given
   void assemble_into(const double* elem, const double* scale_device, bool exact, double* v64, float* hi,
-                     float* lo, cudaStream_t stream);
+                     float2* pair, cudaStream_t stream);
   const std::vector<i32>& free_dofs() const { return free_dofs_; }
 
   // device state

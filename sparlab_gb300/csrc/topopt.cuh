@@ -42,8 +42,8 @@ inline size_t assemble_smem(int dim) {
   return sizeof(double) * (static_cast<size_t>(ed) * ed + static_cast<size_t>(kAsmTile) * rowvals);
 }
 
-// Outputs: val64 (FP64 values), hi and lo (the double-float split, FP32),
-// each optional.  DF: the sums themselves run in double-float arithmetic on
+// Outputs: val64 (FP64 values), hi (FP32) and pair (the double-float split
+// (hi, lo), interleaved), each optional.  DF: the sums themselves run in double-float arithmetic on
 // the FP32 pipes from the split scales (sh, sl) and the split element matrix
 // (the mixed-precision reuse assemblies, which write hi/lo only); otherwise
 // in FP64 (EXACT: rounded products and sums; else fused multiply-adds).
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
     const uint8_t* __restrict__ cmask, const uint32_t* __restrict__ nmask, NodeView a,
     const i32* __restrict__ rowptr, const double* __restrict__ ke, const double* __restrict__ scale,
     const float* __restrict__ scale_hi, const float* __restrict__ scale_lo, double* __restrict__ val64,
-    float* __restrict__ hi, float* __restrict__ lo) {
+    float* __restrict__ hi, float2* __restrict__ pair) {
   extern __shared__ double smem_asm[];
   const int ed = g.dim == 3 ? 24 : 8;
   double* ks = smem_asm;
@@ -145,15 +145,15 @@ __global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
     if constexpr (DF) {
       const float2 v = stage2[k];
       hi[base + k] = v.x;
-      lo[base + k] = v.y;
+      pair[base + k] = v;
     } else {
       const double v = stage[k];
       if (val64) val64[base + k] = v;
-      if (lo) {
+      if (pair) {
         float h, l;
         df_split(v, h, l);
         hi[base + k] = h;
-        lo[base + k] = l;
+        pair[base + k] = make_float2(h, l);
       } else if (hi) {
         hi[base + k] = __double2float_rn(v);
       }

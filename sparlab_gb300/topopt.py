@@ -159,7 +159,9 @@ class GpuSimpProblem:
         d.penalty, d.emin_ratio = spec.penalty, spec.emin_ratio
         d.move_limit, d.damping = spec.move_limit, spec.damping
         d.warm_start = int(spec.warm_start)
-        d.block_pcg = int(block_pcg)
+        # load cases: False / 0 one after another, True / 1 concurrent host
+        # threads, "graph" / 2 advanced together in one CUDA graph
+        d.block_pcg = 2 if block_pcg == "graph" else int(block_pcg)
         d.optimizer = {"oc": 0, "mma": 1}[optimizer]
         d.projection = int(spec.projection)
         d.eta, d.beta_start, d.beta_max = spec.eta, spec.beta_start, spec.beta_max
@@ -442,8 +444,27 @@ class TopologyOptimizer:
         return history
 
 
+def iterate_batch(problems: List[GpuSimpProblem]) -> List[_lib.IterationRecord]:
+    """One SIMP iteration of every problem with their linear solves advanced
+    together (``simp_iterate_batch``): one CUDA graph launch runs one PCG
+    iteration of every load case of every problem still iterating.  Each
+    problem computes what ``iterate()`` computes alone."""
+    lib = _lib.load()
+    n = len(problems)
+    handles = (C.c_void_p * n)(*[p._h.value for p in problems])
+    recs = (_lib.IterationRecord * n)()
+    code = lib.simp_iterate_batch(handles, C.c_int32(n), recs)
+    if code:
+        for p in problems:
+            msg = lib.simp_problem_last_error(p._h).decode()
+            if msg:
+                _lib.raise_for(code, msg)
+        _lib.raise_for(code, lib.simp_problem_last_error(None).decode())
+    return list(recs)
+
+
 def run_batched(problems: List[GpuSimpProblem], iterations: int, workers: Optional[int] = None,
-                tune: bool = False, report: Optional[dict] = None):
+                tune: bool = False, report: Optional[dict] = None, together: bool = False):
     """Iterate independent problem instances concurrently.
 
     Each problem owns a CUDA stream and the library releases the GIL during
@@ -454,13 +475,19 @@ def run_batched(problems: List[GpuSimpProblem], iterations: int, workers: Option
     worker count.  With ``tune`` the first iterations try worker counts n,
     n/2, n/4, ... (one iteration each, timed on the host) and the rest use
     the fastest; ``report`` (a dict) receives the counts tried, their
-    seconds and the choice.  Returns the per-problem iteration records
-    (lists, in problem order)."""
+    seconds and the choice.  With ``together`` every iteration is one
+    :func:`iterate_batch` over all problems instead.  Returns the
+    per-problem iteration records (lists, in problem order)."""
     import concurrent.futures as cf
     import os
     n = len(problems)
     order = sorted(range(n), key=lambda i: -problems[i].nnz)
     out: List[List[_lib.IterationRecord]] = [[] for _ in range(n)]
+    if together:
+        for _ in range(iterations):
+            for i, r in enumerate(iterate_batch(problems)):
+                out[i].append(r)
+        return out
 
     def step(count, its):
         count = max(1, min(count, n))
