@@ -800,7 +800,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 comparison run that follows a mixed-precision run")
-    ap.add_argument("--warm", default="previous", choices=sorted(WARM),
+    ap.add_argument("--warm", default="learned", choices=sorted(WARM),
                     help="PCG initial guess: zero, the previous displacement (the reference's "
                          "warm start), the energy-optimal combination of the last three, or that "
                          "combination with the displacement surrogate's prediction (learned; 3-D "

@@ -13,7 +13,9 @@
 #include <cuda_profiler_api.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <thread>
 #include <cmath>
 #include <mutex>
 #include <sstream>
@@ -498,6 +500,23 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
                                                                        nullptr, op.rows);
   });
   SIMP_CHECK_LAUNCH();
+}
+
+void GpuAmg::spmv0_fast(const double* x, double* y) {
+  Level& l0 = *levels.front();
+  if (!mixed()) {
+    op0(work(0), x, y, nullptr);
+    return;
+  }
+  const i32 n = l0.n;
+  LevelWork& v = work(0).lv.front();  // the cycle's level-0 vectors are free between solves
+  convert(x, v.d32.p, n, stream);
+  if (mf.enabled) {
+    mf_apply(mf, l0.nnodes, v.d32.p, v.e32.p, stream);
+  } else {
+    nb_apply<0, float, float, float>(l0.opA, l0.a.v32.p, v.d32.p, v.e32.p, nullptr, stream);
+  }
+  convert(v.e32.p, y, n, stream);
 }
 
 void GpuAmg::cg_op(SolveWork& w, const double* p, double* q, bool p32_ready) {
@@ -1564,6 +1583,27 @@ void together_forget(const GpuAmg* a) {
   }
 }
 
+// fn(i) for i in [0, n) from a pool of host threads (each on the caller's
+// device); every task's work goes to its own stream
+template <class F>
+void each_task(size_t n, F&& fn) {
+  const size_t workers = std::max<size_t>(1, std::min<size_t>(n, std::thread::hardware_concurrency()));
+  if (workers <= 1) {
+    for (size_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  int dev = 0;
+  SIMP_CUDA(cudaGetDevice(&dev));
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (size_t k = 0; k < workers; ++k)
+    pool.emplace_back([&] {
+      cudaSetDevice(dev);
+      for (size_t i = next++; i < n; i = next++) fn(i);
+    });
+  for (auto& t : pool) t.join();
+}
+
 std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& tasks) {
   struct St {
     double bnorm = 0, target = 0, best = std::numeric_limits<double>::max();
@@ -1618,13 +1658,15 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
   }
   while (true) {
     bool any = false;
-    // round start and each round's first iteration, per system
-    for (size_t i = 0; i < n; ++i) {
+    for (size_t i = 0; i < n; ++i) any = any || !st[i].done;
+    if (!any) break;
+    // round start and each round's first iteration, per system (host
+    // threads: each system's host round trips overlap the others')
+    each_task(n, [&](size_t i) {
       St& s = st[i];
       s.ran = false;
       s.looping = false;
-      if (s.done) continue;
-      any = true;
+      if (s.done) return;
       GpuAmg& a = *tasks[i].amg;
       SolveWork& w = *tasks[i].w;
       const i32 nn = a.levels.front()->n;
@@ -1635,7 +1677,7 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
         if (rnorm <= s.target) {
           out[i].r.converged = true;
           finish(i);
-          continue;
+          return;
         }
         a.apply(w, w.pr.p, w.pz.p);
         SIMP_CUDA(cudaMemcpyAsync(w.pp.p, w.pz.p, sizeof(double) * nn, cudaMemcpyDeviceToDevice, w.stream));
@@ -1652,7 +1694,7 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
           SIMP_CUDA(cudaStreamSynchronize(w.stream));
           if (h.status != 0) {
             breakdown(i, h);
-            continue;
+            return;
           }
           ++s.total;
           if (std::sqrt(h.rr) <= s.target) s.conv = true;
@@ -1668,8 +1710,7 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
       } catch (const Error& e) {
         fail(i, e);
       }
-    }
-    if (!any) break;
+    });
     // the later iterations of the round: all looping systems together
     std::vector<size_t> idx;
     for (size_t i = 0; i < n; ++i)
@@ -1715,9 +1756,9 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
       }
     }
     // round end, per system: true residual and the restart decision
-    for (size_t i = 0; i < n; ++i) {
+    each_task(n, [&](size_t i) {
       St& s = st[i];
-      if (s.done || !s.ran) continue;
+      if (s.done || !s.ran) return;
       GpuAmg& a = *tasks[i].amg;
       SolveWork& w = *tasks[i].w;
       const i32 nn = a.levels.front()->n;
@@ -1727,23 +1768,23 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
         if (out[i].r.relres * s.bnorm <= s.target) {
           out[i].r.converged = true;
           finish(i);
-          continue;
+          return;
         }
         if (!s.conv) {
           finish(i);
-          continue;
+          return;
         }
         s.rec_conv = true;
         if (!(out[i].r.relres < 0.5 * s.best)) {
           finish(i);
-          continue;
+          return;
         }
         s.best = out[i].r.relres;
         if (++s.round >= s.rounds) finish(i);
       } catch (const Error& e) {
         fail(i, e);
       }
-    }
+    });
   }
   for (size_t i = 0; i < n; ++i) SIMP_CUDA(cudaStreamSynchronize(tasks[i].w->stream));
   return out;

@@ -245,6 +245,10 @@ class GpuAmg {
   // the PCG direction update).
   void op0(SolveWork& w, const double* x, double* y, const double* rhs, bool split_ready = false);
   void spmv0(const double* x, double* y) { op0(work(0), x, y, nullptr); }
+  // y = A x on FP64 vectors through the FP32 operator of the V-cycle's level
+  // 0 (matrix-free where enabled), on the context's stream: an approximate
+  // product for the start of a solve.  fp64 mode: the FP64 operator.
+  void spmv0_fast(const double* x, double* y);
   // q = A p, the CG's own product: op0, or with mf_cg() the FP32 matrix-free
   // product of p's FP32 copy (p32_ready: already in w.p32)
   void cg_op(SolveWork& w, const double* p, double* q, bool p32_ready);

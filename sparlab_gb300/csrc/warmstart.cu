@@ -15,9 +15,10 @@
 // no history, the start is the prediction's energy-optimal multiple.  A
 // non-finite or zero prediction drops out the same way, which leaves the
 // history's start (or zero).  Nearly dependent vectors are dropped by a
-// pivoted LDL^T of the Gram matrix.  Cost: one FP64 operator application per
-// basis vector, one fused multi-dot pass and (mode 3) one network inference;
-// the PCG itself is unchanged.
+// pivoted LDL^T of the Gram matrix.  The products K U use the V-cycle's FP32
+// level-0 operator (FP64 in fp64 mode): the start need not be optimal to the
+// last bit.  Cost: one such product per basis vector, one fused multi-dot pass
+// and (mode 3) one network inference; the PCG itself is unchanged.
 #include "kernels.cuh"
 #include "problem.h"
 #include "surrogate_net.h"
@@ -92,7 +93,10 @@ void GpuProblem::projected_start(int l, double* ul, bool learned) {
     return;
   }
   const double* f = b.p + static_cast<size_t>(l) * n;
-  for (int i = 0; i < k; ++i) amg.spmv0(U + i * n, khist.p + i * n);
+  // the Gram system only sets the start's coefficients: the FP32 operator of
+  // the V-cycle is accurate enough for them (the PCG then converges to the
+  // unchanged tolerance from whatever start)
+  for (int i = 0; i < k; ++i) amg.spmv0_fast(U + i * n, khist.p + i * n);
   k_history_dots<<<kRedBlocks, kRedThreads, 0, s>>>(n, k, U, khist.p, f, hpart.p);
   SIMP_CHECK_LAUNCH();
   std::vector<double> hp(static_cast<size_t>(kDots) * kRedBlocks);

@@ -472,9 +472,9 @@ def run_batched(problems: List[GpuSimpProblem], iterations: int, workers: Option
     one per problem) each drive their share of the instances, round robin
     (largest instance first), and the instances' kernels overlap on the GPU.
     Every instance computes exactly what it computes alone, whatever the
-    worker count.  With ``tune`` the first iterations try worker counts n,
-    n/2, n/4, ... (one iteration each, timed on the host) and the rest use
-    the fastest; ``report`` (a dict) receives the counts tried, their
+    worker count.  With ``tune`` the iterations after a problem set's first
+    (which builds the hierarchies) try worker counts n, n/2, n/4, ... (one
+    iteration each, timed on the host) and the rest use the fastest; ``report`` (a dict) receives the counts tried, their
     seconds and the choice.  With ``together`` every iteration is one
     :func:`iterate_batch` over all problems instead.  Returns the
     per-problem iteration records (lists, in problem order)."""
@@ -505,6 +505,9 @@ def run_batched(problems: List[GpuSimpProblem], iterations: int, workers: Option
     chosen = max(1, min(workers or os.cpu_count() or 1, n))
     done = 0
     if tune:
+        if iterations > 0 and not out[0]:
+            step(chosen, 1)   # a first iteration builds every hierarchy: not a fair sample
+            done = 1
         cands, c = [], chosen
         while c >= 1 and len(cands) < 4:
             cands.append(c)
