@@ -139,6 +139,13 @@ class GpuProblem {
   std::vector<int> hist_count;
   sg::Surrogate* surrogate = nullptr;  // warm start 3 (not owned)
   double learned_seconds = 0.0;        // time in the surrogate's predictions
+  // warm start 3: the predictions of the current evaluation (nloads x nfree),
+  // enqueued on the network's stream right after the physical density so
+  // they overlap the assembly and AMG setup; the events bracket them
+  DBuf<double> predicted;
+  cudaEvent_t pred_t0 = nullptr, pred_ready = nullptr;
+  bool pred_pending = false;
+  std::vector<double> load_absmax;     // largest load component per load case
   void projected_start(int l, double* ul, bool learned);
   void record_history(int l, const double* ul);
   // projection state: current beta, its stage, the stage's first iteration

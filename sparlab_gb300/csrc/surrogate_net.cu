@@ -626,7 +626,11 @@ void Surrogate::input_of(GpuProblem& p, int load, __nv_bfloat16* in4) {
   g.nny = p.d.ny + 1;
   g.nnz = p.d.dim == 3 ? p.d.nz + 1 : 1;
   const double* f = p.b.p + static_cast<size_t>(load) * p.nfree;
-  const double fmax = device_absmax(f, p.nfree, scratch, net.stream);
+  // the loads do not change: their largest component is taken once per problem
+  if (p.load_absmax.size() != static_cast<size_t>(p.d.nloads))
+    p.load_absmax.assign(static_cast<size_t>(p.d.nloads), -1.0);
+  double& fmax = p.load_absmax[static_cast<size_t>(load)];
+  if (fmax < 0.0) fmax = device_absmax(f, p.nfree, scratch, net.stream);
   const long long nodes = static_cast<long long>(g.nnx) * g.nny * g.nnz;
   k_problem_input<<<blocks_for(nodes), 256, 0, net.stream>>>(g, p.rho.p, f, p.dof_map.p,
                                                              fmax > 0.0 ? 1.0 / fmax : 0.0, in4);
@@ -692,10 +696,30 @@ double Surrogate::train(int epochs, double lr0, int batch, uint64_t seed) {
   return epoch_loss;
 }
 
+Surrogate::~Surrogate() {
+  if (after) cudaEventDestroy(after);
+}
+
 void Surrogate::predict(GpuProblem& p, int load, double* u_out) {
-  if (p.d.dim != 3) throw Error(kBadInput, "the surrogate serves 3-D (Hex8) problems");
+  std::lock_guard<std::mutex> lock(mu);
   // the problem's state is written on its own stream
   SIMP_CUDA(cudaStreamSynchronize(p.amg.stream));
+  enqueue(p, load, u_out);
+  SIMP_CUDA(cudaStreamSynchronize(net.stream));
+  net.check_status();
+}
+
+void Surrogate::predict_async(GpuProblem& p, int load, double* u_out, cudaEvent_t ready) {
+  std::lock_guard<std::mutex> lock(mu);
+  if (!after) SIMP_CUDA(cudaEventCreateWithFlags(&after, cudaEventDisableTiming));
+  SIMP_CUDA(cudaEventRecord(after, p.amg.stream));
+  SIMP_CUDA(cudaStreamWaitEvent(net.stream, after, 0));
+  enqueue(p, load, u_out);
+  SIMP_CUDA(cudaEventRecord(ready, net.stream));
+}
+
+void Surrogate::enqueue(GpuProblem& p, int load, double* u_out) {
+  if (p.d.dim != 3) throw Error(kBadInput, "the surrogate serves 3-D (Hex8) problems");
   net.shape(p.d.nx + 1, p.d.ny + 1, p.d.nz + 1);
   const long long nodes = static_cast<long long>(p.d.nx + 1) * (p.d.ny + 1) * (p.d.nz + 1);
   in4.alloc(static_cast<size_t>(nodes) * 4);
@@ -706,8 +730,6 @@ void Surrogate::predict(GpuProblem& p, int load, double* u_out) {
   SIMP_CUDA(cudaMemsetAsync(u_out, 0, sizeof(double) * p.nfree, net.stream));
   k_prediction_to_dofs<<<blocks_for(nodes), 256, 0, net.stream>>>(nodes, 3, net.out.p, p.dof_map.p, u_out);
   SIMP_CHECK_LAUNCH();
-  SIMP_CUDA(cudaStreamSynchronize(net.stream));
-  net.check_status();
 }
 
 }  // namespace sg

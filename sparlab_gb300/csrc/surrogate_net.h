@@ -7,6 +7,7 @@
 
 #include <cuda_bf16.h>
 
+#include <mutex>
 #include <vector>
 
 namespace simp {
@@ -74,6 +75,9 @@ struct Sample {
 class Surrogate {
  public:
   explicit Surrogate(uint64_t seed) : net(seed) {}
+  ~Surrogate();
+  Surrogate(const Surrogate&) = delete;
+  Surrogate& operator=(const Surrogate&) = delete;
   Net net;
   std::vector<Sample> samples;
   std::vector<double> losses;  // mean loss of each training epoch
@@ -87,11 +91,18 @@ class Surrogate {
   // physical density, as a free-DOF vector (device, nfree doubles; the
   // network's scale, a shape only)
   void predict(GpuProblem& p, int load, double* u_device);
+  // the same, enqueued on the network's stream after the work the problem's
+  // stream holds so far, without waiting for it: `ready` is recorded when the
+  // prediction is written (the caller makes its stream wait on it)
+  void predict_async(GpuProblem& p, int load, double* u_device, cudaEvent_t ready);
 
  private:
   DBuf<__nv_bfloat16> in4;
   DBuf<double> scratch;
+  std::mutex mu;          // one caller at a time issues work on the network's buffers
+  cudaEvent_t after = nullptr;
   void input_of(GpuProblem& p, int load, __nv_bfloat16* in4);
+  void enqueue(GpuProblem& p, int load, double* u_device);
 };
 
 }  // namespace sg

@@ -83,9 +83,16 @@ void GpuProblem::projected_start(int l, double* ul, bool learned) {
   const i64 n = nfree;
   double* U = hist.p + static_cast<size_t>(l) * kBasis * n;
   if (learned) {  // the prediction takes the slot after the history
-    const auto t0 = std::chrono::steady_clock::now();
-    surrogate->predict(*this, l, U + static_cast<size_t>(k) * n);
-    learned_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    double* slot = U + static_cast<size_t>(k) * n;
+    if (pred_pending) {  // enqueued after the physical density (evaluate_prepare)
+      SIMP_CUDA(cudaStreamWaitEvent(s, pred_ready, 0));
+      SIMP_CUDA(cudaMemcpyAsync(slot, predicted.p + static_cast<size_t>(l) * n, sizeof(double) * n,
+                                cudaMemcpyDeviceToDevice, s));
+    } else {
+      const auto t0 = std::chrono::steady_clock::now();
+      surrogate->predict(*this, l, slot);
+      learned_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
     ++k;
   }
   if (k == 0) {

@@ -15,6 +15,11 @@ oracle (the CPU restatement of the reference's algorithms):
 4. The 64 seeded uneven instances, two mixed-precision iterations run
    concurrently: every 8th instance's compliance history within 1e-6 of the
    oracle's.
+5. Hex8 192x96x96 (5,419,584 free DOFs), the benchmark's own workload: two
+   SIMP iterations with the learned start in mixed precision (an untrained
+   network: the answer must not depend on the prediction) against the
+   oracle's FP64 iterations (previous-displacement start), compliance within
+   1e-6, CG iterations at most two above the oracle's.
 
 Tolerances follow the reference's solver tests (tests/test_multigrid.cpp:
 257-360: AMG against direct 1e-8 in the solution, SIMP contrast 1e-7 in the
@@ -95,3 +100,22 @@ def test_config4_batched_64_every_eighth_against_oracle():
             assert abs(recs[q][k].volume_fraction - hist[k, 1]) < 1e-8, (q, k)
     for p in probs:
         p.close()
+
+
+def test_config5_hex8_192x96x96_learned_mixed_against_the_oracle():
+    from sparlab_gb300.surrogate import Surrogate
+    spec = P.hex8_192x96x96()
+    ref = oracle.Problem(spec)
+    _, hist = ref.run(2)
+    spec.warm_start = 3
+    sur = Surrogate(seed=7)
+    gpu = GpuSimpProblem(spec, element_matrix=ref.element_matrix(), precision="mixed")
+    gpu.set_surrogate(sur)
+    recs = [gpu.iterate() for _ in range(2)]
+    for k, r in enumerate(recs):
+        assert abs(r.compliance / hist[k, 0] - 1) < 1e-6, (k, r.compliance, hist[k, 0])
+        assert abs(r.volume_fraction - hist[k, 1]) < 1e-8, k
+        # the learned start may save iterations, never add many
+        assert r.linear_iterations <= hist[k, 4] + 2, (k, r.linear_iterations, hist[k, 4])
+    assert gpu.learned_seconds() > 0.0
+    gpu.close()
