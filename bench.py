@@ -620,8 +620,10 @@ def run_own(args):
     lib = _lib.load()
     sur, sur_info = (train_surrogate(args, local) if learned else (None, None))
 
+    tc = {} if args.tensor_cores is None else {"tensor_cores": args.tensor_cores}
+
     def make(precision, with_surrogate=True):
-        p = GpuSimpProblem(spec, precision=precision, device=local, block_pcg=together)
+        p = GpuSimpProblem(spec, precision=precision, device=local, block_pcg=together, **tc)
         if with_surrogate and sur is not None:
             p.set_surrogate(sur)
         return p
@@ -748,6 +750,7 @@ def run_own(args):
         "run": {"precision": args.precision,
                 "warm_start": "learned" if learned else spec_warm_name(spec.warm_start),
                 "nnz_kff": prob.nnz, "replicas": world,
+                "level0_tensor_cores": int(prob.options.tensor_cores),
                 "load_case_solves": "concurrent" if together else "sequential",
                 "l2": ("working set (K_ff %.2f GB) larger than the 129 MB L2" % (nnz * 12 / 1e9)
                        if nnz * 12 > 129e6 else
@@ -807,6 +810,9 @@ def main():
                          "workloads: the network is trained before the timed region)")
     ap.add_argument("--train-epochs", type=int, default=4,
                     help="training epochs of the surrogate over its 2,000 pairs (learned start)")
+    ap.add_argument("--tensor-cores", type=int, default=None, choices=[0, 1],
+                    help="matrix-free level 0 on the tensor cores (1) or on FP32 FMAs (0); "
+                         "default: the library's default")
     ap.add_argument("--sequential-loads", action="store_true",
                     help="solve a multi-load workload's load cases one after another instead of "
                          "concurrently (one workspace and stream per load case)")

@@ -83,6 +83,11 @@ typedef struct {
                                     matrix-free: FP32 element products inside CG, with
                                     the true residual of every restart taken by an FP64
                                     matrix-free product (iterative refinement) */
+  int32_t tensor_cores;          /* 3-D matrix-free level 0 (matrix_free >= 1): 1 (default)
+                                    the element products K_e^0 x_e of a layer of cells as
+                                    TF32 tensor-core GEMMs, operands split hi + lo (3 x TF32,
+                                    FP32 accumulation: about FP32 accuracy); 0 FP32 FMAs on
+                                    the CUDA cores */
 } simp_solver_options;
 
 typedef struct {
@@ -310,6 +315,14 @@ int simp_element_stiffness(int32_t dim, double hx, double hy, double hz, double 
  * the last evaluate), on device pointers of nfree doubles, on the library's
  * stream.  Exposed so a caller can time the dominant kernel in isolation. */
 int simp_problem_apply_operator(simp_problem* p, const double* x_device, double* y_device);
+
+/* y = K_ff x through the V-cycle's level-0 operator (MIXED: FP32, x rounded
+ * to FP32 and y widened; matrix-free where enabled, on the tensor cores with
+ * tensor_cores = 1; FP64: the CG operator), on device pointers of nfree
+ * doubles, on the library's stream.  For checking and timing that operator
+ * in isolation (AmgPreconditioner's level-0 spmv, src/fem/Multigrid.cpp:
+ * 783-855, is the product it replaces). */
+int simp_problem_apply_level0(simp_problem* p, const double* x_device, double* y_device);
 
 /* Times `reps` launches of the level-0 CG operator (FP64 values in FP64 mode,
  * double-float hi + lo values in mixed mode) with CUDA events on the library's

@@ -41,7 +41,7 @@ EXPORTS = [
     "simp_problem_set_surrogate", "simp_problem_learned_seconds", "simp_conv3d_bf16",
     "simp_surrogate_loss_gradient", "simp_autotune_enable", "simp_autotune_report",
     "simp_autotune_set", "simp_iterate_batch",
-    "simp_conv3d_wgrad",
+    "simp_conv3d_wgrad", "simp_problem_apply_level0",
 ]
 
 
@@ -53,7 +53,7 @@ class SolverOptions(C.Structure):
                 ("reuse_aggregates", C.c_int32), ("iterative_tolerance", C.c_double),
                 ("max_iterations", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32),
                 ("cuda_graphs", C.c_int32), ("matrix_free_transfer", C.c_int32),
-                ("matrix_free", C.c_int32)]
+                ("matrix_free", C.c_int32), ("tensor_cores", C.c_int32)]
 
 
 class AmgStats(C.Structure):

@@ -8,6 +8,7 @@
 #include "galerkin.cuh"
 #include "kernels.cuh"
 #include "mfree.cuh"
+#include "mfree_tc.cuh"
 #include "nbspmv.cuh"
 
 #include <cuda_profiler_api.h>
@@ -223,12 +224,30 @@ void mf3_shape(const MfOp& mf, const MfArgs& a, const KeF32& ke, cudaStream_t s)
   SIMP_CHECK_LAUNCH();
 }
 
+// The tensor-core kernel: CTAs of 31 x 7 node columns, each marching
+// `layers` node layers (mf.tc_layers; every chunking gives the same values).
+template <int MODE>
+void mf3_tc(const MfOp& mf, const MfArgs& a, const KeF32& ke, cudaStream_t s) {
+  const i32 nnz = mf.nz + 1;
+  const int layers = mf.tc_layers > 0 ? std::min<i32>(mf.tc_layers, nnz) : nnz;
+  const dim3 grid((mf.nnx + kTcNodesX - 1) / kTcNodesX, (mf.nny + kTcNodesY - 1) / kTcNodesY,
+                  (nnz + layers - 1) / layers);
+  raise_dynamic_smem(reinterpret_cast<const void*>(&k_mf3_tc<MODE>), kTcSmemBytes);
+  k_mf3_tc<MODE><<<grid, kTcThreads, kTcSmemBytes, s>>>(mf_view(mf), a, ke, layers, mf.status);
+  SIMP_CHECK_LAUNCH();
+}
+
 // The tiled matrix-free kernel in the tile shape the tuner chose (mf.tile
-// indexes kMfTileShape; every shape gives the same values).
+// indexes kMfTileShape; every shape gives the same values), or the
+// tensor-core kernel (mf.tensor).
 template <int MODE>
 void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
   KeF32 ke;
   std::copy(mf.ke_host, mf.ke_host + 24 * 24, ke.k);
+  if (mf.tensor) {
+    mf3_tc<MODE>(mf, a, ke, s);
+    return;
+  }
   static_assert(kMfTiles == 5, "tile table");
   switch (mf.tile) {
     case 1: mf3_shape<MODE, 32, 8, 1>(mf, a, ke, s); break;
@@ -338,6 +357,21 @@ void mf_prolong(const MfOp& mf, const Level& lv, const float* xc, float* t, floa
   mf3<5>(mf, a, s);
 }
 
+// Node layers per CTA of the tensor-core matrix-free kernel: chunkings of
+// the z march for about 2 (variant 0), 4, 1 or 8 CTAs per SM.
+constexpr int kTcChunkings = 4;
+int tc_layers_of(const MfOp& mf, int variant) {
+  int dev = 0, sms = 0;
+  SIMP_CUDA(cudaGetDevice(&dev));
+  SIMP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const i64 nnz = mf.nz + 1;
+  const i64 xy = static_cast<i64>((mf.nnx + kTcNodesX - 1) / kTcNodesX) * ((mf.nny + kTcNodesY - 1) / kTcNodesY);
+  static const int per_sm[kTcChunkings] = {2, 4, 1, 8};
+  i64 chunks = std::max<i64>(1, (static_cast<i64>(per_sm[variant]) * sms + xy / 2) / xy);
+  chunks = std::min(chunks, nnz);
+  return static_cast<int>((nnz + chunks - 1) / chunks);
+}
+
 double seconds_since(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -353,7 +387,20 @@ GpuAmg::GpuAmg(const AmgOptions& o) : opt(o) {
   part.alloc(kRedBlocks);
   scal.alloc(16);
   dstatus.alloc(4);
+  mf_status.alloc(1);
+  SIMP_CUDA(cudaMemset(mf_status.p, 0, sizeof(int)));
   main_.stream = stream;
+}
+
+void GpuAmg::check_mf_status(cudaStream_t s) {
+  if (!mf.tensor) return;
+  int h = 0;
+  SIMP_CUDA(cudaMemcpyAsync(&h, mf_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SIMP_CUDA(cudaStreamSynchronize(s));
+  if (h != 0) {
+    SIMP_CUDA(cudaMemsetAsync(mf_status.p, 0, sizeof(int), s));
+    throw Error(kCudaError, "matrix-free tensor-core operator: an MMA completion wait ran out");
+  }
 }
 
 GpuAmg::~GpuAmg() {
@@ -1097,6 +1144,11 @@ void GpuAmg::coarse_solve(SolveWork& w, size_t l) {
 void GpuAmg::setup(bool structure_changed) {
   const auto t0 = std::chrono::steady_clock::now();
   const bool reuse = opt.reuse && !structure_changed && ready_;
+  if (mf.enabled) {
+    mf.status = mf_status.p;
+    mf.tensor = mf.dim == 3 && opt.tensor_cores != 0;
+    if (mf.tensor && mf.tc_layers <= 0) mf.tc_layers = tc_layers_of(mf, 0);
+  }
   if (!reuse) {
     while (levels.size() > 1) levels.pop_back();
     Level& l0 = *levels.front();
@@ -1140,15 +1192,34 @@ void GpuAmg::setup(bool structure_changed) {
   stats.setup_seconds = seconds_since(t0);
 }
 
-// The matrix-free operator's tile shape for this grid: the fastest of the
-// shapes in kMfTileShape on y = A x with the current cell scales (all give
-// the same values).  Before the first CUDA graph capture of a structure.
+// The matrix-free operator's launch shape for this grid: the fastest of the
+// shapes in kMfTileShape (FMA kernel) or of the z-chunkings of the tensor-
+// core kernel, on y = A x with the current cell scales (each family gives
+// the same values in every shape).  Before the first CUDA graph capture of a
+// structure.
 void GpuAmg::tune_level0() {
   if (!(mf.enabled && mf.dim == 3) || !mf.scale) return;
   const i32 n = levels.front()->n;
   DBuf<float> tx(static_cast<size_t>(n)), ty(static_cast<size_t>(n));
   k_fill<float><<<grid_for(n, 256), 256, 0, stream>>>(tx.p, 1.0f, n);
   SIMP_CHECK_LAUNCH();
+  if (mf.tensor) {
+    std::ostringstream key;
+    key << "mf3tc:" << mf.nnx << "x" << mf.nny << "x" << (mf.nz + 1);
+    const int v = tune_pick(key.str(), kTcChunkings,
+                            [&](int c) {
+                              MfOp m = mf;
+                              m.tc_layers = tc_layers_of(mf, c);
+                              MfArgs a{};
+                              a.x = tx.p;
+                              a.y = ty.p;
+                              mf3<0>(m, a, stream);
+                            },
+                            stream, 0, 5);
+    mf.tc_layers = tc_layers_of(mf, v);
+    check_mf_status(stream);
+    return;
+  }
   std::ostringstream key;
   key << "mf3:" << mf.nnx << "x" << mf.nny << "x" << (mf.nz + 1);
   mf.tile = tune_pick(key.str(), kMfTiles,
@@ -1430,6 +1501,7 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x_out, doub
   }
   if (!res.converged && rec_conv) res.converged = true;
   res.iterations = total;
+  check_mf_status(stream);
   SIMP_CUDA(cudaMemcpyAsync(x_out, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream));
   return res;
 }
@@ -1787,6 +1859,15 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
     });
   }
   for (size_t i = 0; i < n; ++i) SIMP_CUDA(cudaStreamSynchronize(tasks[i].w->stream));
+  for (size_t i = 0; i < n; ++i) {
+    if (out[i].error_code != 0) continue;
+    try {
+      tasks[i].amg->check_mf_status(tasks[i].w->stream);
+    } catch (const Error& e) {
+      out[i].error_code = e.code;
+      out[i].error = e.what();
+    }
+  }
   return out;
 }
 

@@ -41,6 +41,8 @@ struct AmgOptions {
   // FP32 V-cycle's level 0 matrix-free; 2 also the CG operator (FP32 element
   // products, FP64 matrix-free true residuals at the restarts)
   int matrix_free = 1;
+  // the 3-D matrix-free level 0 on the tensor cores (3 x TF32 element GEMMs)
+  int tensor_cores = 0;
 };
 
 struct DevPattern {
@@ -138,6 +140,9 @@ struct MfOp {
   int tile = 0;                 // tile shape of the tiled 3-D kernel (kMfTileShape, tuned)
   const double* scale64 = nullptr;  // s_e, FP64 (the matrix-free CG operator's true residuals)
   double ke64_host[24 * 24] = {};   // K_e^0, FP64
+  bool tensor = false;     // 3-D: the tensor-core kernel (mfree_tc.cuh) instead of the tiled FMA kernel
+  int tc_layers = 0;       // node layers per CTA of the tensor-core kernel (tuned; 0: all)
+  int* status = nullptr;   // device word the tensor-core kernel sets when a wait runs out
 };
 
 // Work vectors of one solve: the cycle vectors of every level, the PCG
@@ -275,6 +280,10 @@ class GpuAmg {
 
   DBuf<double> part, scal;  // reductions of setup and of callers on the context stream
   DBuf<int> dstatus;
+  DBuf<int> mf_status;  // the tensor-core matrix-free kernel's wait status
+  // throws when a tensor-core matrix-free launch on this stream reported a
+  // wait that ran out (reads one word)
+  void check_mf_status(cudaStream_t s);
 
  private:
   bool ready_ = false;

@@ -40,6 +40,7 @@ AmgOptions convert(const simp_solver_options* o) {
   a.graphs = o->cuda_graphs != 0;
   a.mf_transfer = o->matrix_free_transfer != 0;
   a.matrix_free = o->matrix_free;
+  a.tensor_cores = o->tensor_cores;
   return a;
 }
 
@@ -56,6 +57,7 @@ void validate(const AmgOptions& o) {
   if (o.precision != SIMP_PRECISION_FP64 && o.precision != SIMP_PRECISION_MIXED)
     throw Error(kBadInput, "unknown precision mode");
   if (o.matrix_free < 0 || o.matrix_free > 2) throw Error(kBadInput, "matrix_free must be 0, 1 or 2");
+  if (o.tensor_cores < 0 || o.tensor_cores > 1) throw Error(kBadInput, "tensor_cores must be 0 or 1");
 }
 
 template <class F>
@@ -149,6 +151,7 @@ void simp_default_options(simp_solver_options* o) {
   o->cuda_graphs = 1;
   o->matrix_free_transfer = 1;
   o->matrix_free = 1;
+  o->tensor_cores = 0;
 }
 
 int simp_ctx_create(const simp_solver_options* opts, simp_ctx** out) {
@@ -856,6 +859,17 @@ int simp_problem_apply_operator(simp_problem* p, const double* x, double* y) {
     GpuAmg& amg = p->p->amg;
     if (!amg.ready()) throw Error(kBadInput, "the operator is assembled by the first evaluate");
     amg.spmv0(x, y);
+  });
+}
+
+int simp_problem_apply_level0(simp_problem* p, const double* x, double* y) {
+  return guarded(p->err, [&] {
+    use_device(p->device);
+    GpuAmg& amg = p->p->amg;
+    if (!amg.ready()) throw Error(kBadInput, "the operator is assembled by the first evaluate");
+    if (!x || !y) throw Error(kBadInput, "simp_problem_apply_level0: null vector");
+    amg.spmv0_fast(x, y);
+    amg.check_mf_status(amg.stream);
   });
 }
 

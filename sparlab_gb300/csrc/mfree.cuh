@@ -180,6 +180,44 @@ struct MfArgs {
   double* y64;        // mode 8: output
 };
 
+// The epilogue of a node's product o = (A x)_I (3 components) in each mode;
+// self = the input x at node I itself (mode 3: the direction d, mode 5: t).
+template <int MODE>
+__device__ __forceinline__ void mf_node_out(const MfArgs& a, i32 I, const float (&o)[3], const float (&self)[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const i64 row = static_cast<i64>(I) * 3 + k;
+    if (MODE == 0) {
+      a.y[row] = o[k];
+    } else if (MODE == 1) {
+      a.y[row] = a.b[row] - o[k];
+    } else if (MODE == 3) {
+      const float ri = a.b[row] - o[k];
+      a.r[row] = ri;
+      const float dv = self[k];
+      const float di = a.coef[0] * dv + a.coef[1] * a.dinv[row] * ri;
+      a.dn[row] = di;
+      float xi = a.xs[row];
+      if (a.add_d) xi = xi + dv;
+      a.xs[row] = xi + di;
+    } else if (MODE == 4) {
+      const float ri = a.b[row] - o[k];
+      a.r[row] = ri;
+      a.dn[row] = a.dinv[row] * ri * a.coef[0];
+    } else if (MODE == 5) {
+      a.xs[row] = a.xs[row] + (self[k] - a.coef[0] * (a.dinv[row] * o[k]));
+    } else if (MODE == 6) {
+      const float ri = a.b[row] - o[k];
+      a.y[row] = ri;
+      a.dn[row] = a.dinv[row] * ri;
+    } else if (MODE == 8) {
+      a.y64[row] = static_cast<double>(o[k]);
+    } else {
+      a.y[row] = a.b[row] - a.coef[0] * o[k];
+    }
+  }
+}
+
 template <int MODE, int TX = kTX, int TY = kTY, int TZ = kTZ>
 __global__ void __launch_bounds__(TX* TY* TZ) k_mf3_tile(MfView m, MfArgs a, const __grid_constant__ KeF32 ke) {
   constexpr int NZ = TZ * kNZ;  // node layers of the tile
@@ -275,39 +313,9 @@ __global__ void __launch_bounds__(TX* TY* TZ) k_mf3_tile(MfView m, MfArgs a, con
           out2 = fmaf(s, a2, out2);
         }
     const float o[3] = {out0, out1, out2};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const i64 row = static_cast<i64>(I) * 3 + k;
-      if (MODE == 0) {
-        a.y[row] = o[k];
-      } else if (MODE == 1) {
-        a.y[row] = a.b[row] - o[k];
-      } else if (MODE == 3) {
-        const float ri = a.b[row] - o[k];
-        a.r[row] = ri;
-        const float dv = a.x[row];
-        const float di = a.coef[0] * dv + a.coef[1] * a.dinv[row] * ri;
-        a.dn[row] = di;
-        float xi = a.xs[row];
-        if (a.add_d) xi = xi + dv;
-        a.xs[row] = xi + di;
-      } else if (MODE == 4) {
-        const float ri = a.b[row] - o[k];
-        a.r[row] = ri;
-        a.dn[row] = a.dinv[row] * ri * a.coef[0];
-      } else if (MODE == 5) {
-        const float ti = xh[k][lz + 1][ty + 1][tx + 1];  // this node's t
-        a.xs[row] = a.xs[row] + (ti - a.coef[0] * (a.dinv[row] * o[k]));
-      } else if (MODE == 6) {
-        const float ri = a.b[row] - o[k];
-        a.y[row] = ri;
-        a.dn[row] = a.dinv[row] * ri;
-      } else if (MODE == 8) {
-        a.y64[row] = static_cast<double>(o[k]);
-      } else {
-        a.y[row] = a.b[row] - a.coef[0] * o[k];
-      }
-    }
+    const float self[3] = {xh[0][lz + 1][ty + 1][tx + 1], xh[1][lz + 1][ty + 1][tx + 1],
+                           xh[2][lz + 1][ty + 1][tx + 1]};
+    mf_node_out<MODE>(a, I, o, self);
   }
 }
 

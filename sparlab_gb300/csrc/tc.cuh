@@ -148,6 +148,49 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
       : "memory");
 }
 
+// Shared-memory matrix descriptor of a K-major operand in the plain
+// (no-swizzle) canonical layout: 8-row x 16-byte core matrices stored as 128
+// contiguous bytes, core matrices adjacent in K `lbo` bytes apart (leading-
+// dimension offset, bits 16-29) and adjacent in M / N `sbo` bytes apart
+// (stride-dimension offset, bits 32-45); swizzle mode 0.
+__device__ __forceinline__ uint64_t smem_desc_plain(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4)) | (static_cast<uint64_t>((lbo & 0x3FFFFu) >> 4) << 16) |
+         (static_cast<uint64_t>((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::tf32 (A and B TF32, K-major) with an FP32
+// accumulator, M x N: D format (bits 4-5) = 1, A format (7-9) = 2, B format
+// (10-12) = 2, N >> 3 (17-22), M >> 4 (24-28).
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+         (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T with TF32 operands (K = 8 per instruction).
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// An FP32 value rounded to TF32 (10 explicit mantissa bits, to nearest, ties
+// away from zero; the low 13 bits of the result are zero).
+__device__ __forceinline__ uint32_t tf32_round(float v) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return r;
+}
+
+// Orders this thread's generic-proxy shared-memory writes before later
+// tensor-core (async-proxy) reads of them.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // Arrives (once) on the mbarrier when every MMA this thread issued before has
 // completed.
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -169,6 +212,32 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// 24 consecutive FP32 columns of this thread's tensor-memory lane (one x16
+// and one x8 load, one wait).
+__device__ __forceinline__ void tmem_ld24(uint32_t taddr, float (&v)[24]) {
+  uint32_t r[24];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23])
+      : "r"(taddr + 16u));
+  // the registers are operands of the wait, so no use of them moves above it
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                 "+r"(r[22]), "+r"(r[23])
+               :
+               : "memory");
+#pragma unroll
+  for (int k = 0; k < 24; ++k) v[k] = __uint_as_float(r[k]);
 }
 
 }  // namespace tc

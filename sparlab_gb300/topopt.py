@@ -265,6 +265,12 @@ class GpuSimpProblem:
         self._check(self._lib.simp_problem_apply_operator(self._h, C.c_void_p(x_device_ptr),
                                                           C.c_void_p(y_device_ptr)))
 
+    def apply_level0(self, x_device_ptr: int, y_device_ptr: int):
+        """y = K_ff x through the V-cycle's level-0 operator (FP32 in mixed
+        precision: matrix-free, on the tensor cores with tensor_cores=1)."""
+        self._check(self._lib.simp_problem_apply_level0(self._h, C.c_void_p(x_device_ptr),
+                                                        C.c_void_p(y_device_ptr)))
+
     def time_operator(self, reps: int = 20):
         """(ms per launch, algorithmic bytes per launch) of the FP64 level-0
         operator application (the CG operator), timed with CUDA events."""

@@ -73,6 +73,8 @@ def test_element_stiffness_matches_oracle(dim, h):
     ("lanczos_steps", 1, "lanczos_steps"),
     ("iterative_tolerance", 0.0, "tolerance"),
     ("precision", 7, "precision"),
+    ("matrix_free", 3, "matrix_free"),
+    ("tensor_cores", 2, "tensor_cores"),
 ])
 def test_context_creation_rejects_bad_options_before_touching_the_device(field, value, words):
     """AmgPreconditioner's option checks (src/fem/Multigrid.cpp:907-925;
