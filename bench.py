@@ -616,7 +616,7 @@ def run_own(args):
     spec = WORKLOADS[args.config][0]()
     learned = args.warm == "learned" and spec.dim == 3
     spec.warm_start = WARM["learned" if learned else ("previous" if args.warm == "learned" else args.warm)]
-    together = not args.sequential_loads
+    together = "graph" if args.graph_loads else not args.sequential_loads
     lib = _lib.load()
     sur, sur_info = (train_surrogate(args, local) if learned else (None, None))
 
@@ -751,7 +751,8 @@ def run_own(args):
                 "warm_start": "learned" if learned else spec_warm_name(spec.warm_start),
                 "nnz_kff": prob.nnz, "replicas": world,
                 "level0_tensor_cores": int(prob.options.tensor_cores),
-                "load_case_solves": "concurrent" if together else "sequential",
+                "load_case_solves": ("one graph, fused multi-RHS CG operator" if together == "graph" else
+                                     "concurrent" if together else "sequential"),
                 "l2": ("working set (K_ff %.2f GB) larger than the 129 MB L2" % (nnz * 12 / 1e9)
                        if nnz * 12 > 129e6 else
                        "working set (K_ff %.3f GB) fits in the 129 MB L2; not flushed between steps"
@@ -813,6 +814,9 @@ def main():
     ap.add_argument("--tensor-cores", type=int, default=None, choices=[0, 1],
                     help="matrix-free level 0 on the tensor cores (1) or on FP32 FMAs (0); "
                          "default: the library's default")
+    ap.add_argument("--graph-loads", action="store_true",
+                    help="advance a multi-load workload's load cases together in one CUDA graph, "
+                         "their CG products as one multi-RHS launch over the shared K_ff")
     ap.add_argument("--sequential-loads", action="store_true",
                     help="solve a multi-load workload's load cases one after another instead of "
                          "concurrently (one workspace and stream per load case)")

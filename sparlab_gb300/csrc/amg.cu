@@ -549,6 +549,40 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
   SIMP_CHECK_LAUNCH();
 }
 
+cudaGraphNode_t GpuAmg::add_op0_multi(cudaGraph_t g, const std::vector<SolveWork*>& ws,
+                                      const std::vector<cudaGraphNode_t>& deps) {
+  Level& l0 = *levels.front();
+  const NbOp& op = l0.opA;
+  MultiRhs m{};
+  m.n = static_cast<int>(ws.size());
+  for (size_t k = 0; k < ws.size() && k < static_cast<size_t>(kMaxRhs); ++k) {
+    m.x[k] = ws[k]->xsplit.p;
+    m.y[k] = ws[k]->pq.p;
+    m.active[k] = ws[k]->loop.p;
+  }
+  cudaGraphNode_t node = nullptr;
+  with_shape<float>(op, [&](auto vs, auto blk) {
+    constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
+    const i32* node_of = op.node_of;
+    NodeView pat = op.pat;
+    const i32* rowptr = op.rowptr;
+    const i32* col = op.col;
+    const float2* v = l0.a.v2.p;
+    i32 rows = op.rows;
+    void* args[] = {&node_of, &pat, &rowptr, &col, &v, &m, &rows};
+    cudaGraphNodeParams kp = {};
+    kp.type = cudaGraphNodeTypeKernel;
+    kp.kernel.func = reinterpret_cast<void*>(&k_rows_apply_df_multi<VS, B>);
+    kp.kernel.gridDim = dim3(rows_grid(op, VS));
+    kp.kernel.blockDim = dim3(256);
+    kp.kernel.sharedMemBytes = 0;
+    kp.kernel.kernelParams = args;
+    kp.kernel.extra = nullptr;
+    SIMP_CUDA(cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &kp));
+  });
+  return node;
+}
+
 void GpuAmg::spmv0_fast(const double* x, double* y) {
   Level& l0 = *levels.front();
   if (!mixed()) {
@@ -1362,11 +1396,11 @@ void GpuAmg::pcg_tail(SolveWork& w, float2* psplit) {
   SIMP_CHECK_LAUNCH();
 }
 
-void GpuAmg::pcg_head(SolveWork& w, double* x, bool split_ready) {
+void GpuAmg::pcg_head(SolveWork& w, double* x, bool split_ready, bool op_done) {
   const i32 n = levels.front()->n;
   const cudaStream_t stream = w.stream;
   PcgScalars* sc = reinterpret_cast<PcgScalars*>(w.scal.p + 8);
-  cg_op(w, w.pp.p, w.pq.p, split_ready);
+  if (!op_done) cg_op(w, w.pp.p, w.pq.p, split_ready);
   k_dot_partial<double, double><<<kRedBlocks, kRedThreads, 0, stream>>>(w.pp.p, w.pq.p, n, w.part.p);
   SIMP_CHECK_LAUNCH();
   k_pcg_alpha<<<1, kRedThreads, 0, stream>>>(w.part.p, kRedBlocks, sc);
@@ -1511,9 +1545,14 @@ GpuAmg::PcgResult GpuAmg::pcg(SolveWork& w, const double* b, double* x_out, doub
 // ---------------------------------------------------------------------------
 namespace {
 
-// Sets a system's conditional from its loop flag (first node of its branch).
-__global__ void k_arm(cudaGraphConditionalHandle h, const int* __restrict__ loop) {
-  cudaGraphSetConditional(h, loop[0] != 0 ? 1u : 0u);
+// Sets a system's conditionals from its loop flag (first node of its
+// branch): h guards its iteration body (or, with a fused CG operator, the
+// part before it) and h2, when `two`, the part after the fused operator.
+__global__ void k_arm(cudaGraphConditionalHandle h, cudaGraphConditionalHandle h2, int two,
+                      const int* __restrict__ loop) {
+  const unsigned v = loop[0] != 0 ? 1u : 0u;
+  cudaGraphSetConditional(h, v);
+  if (two) cudaGraphSetConditional(h2, v);
 }
 
 // After an iteration body: count the iteration and apply GpuAmg::pcg's test
@@ -1533,10 +1572,17 @@ __global__ void k_loop_test(const PcgScalars* __restrict__ sc, int* __restrict__
 // One graph over a set of (hierarchy, workspace) pairs: per pair an arm
 // kernel and a conditional node whose body is the pair's PCG iteration
 // (pcg_tail + pcg_head, as pcg_body captures it) and its loop test.
+// Mixed-precision pairs that share a hierarchy (the load cases of one
+// problem) have their CG operator fused: each one's body is split at the
+// operator into two conditional nodes, and between them one multi-RHS
+// launch (k_rows_apply_df_multi, up to kMaxRhs pairs) applies the shared
+// double-float K_ff to every pair still iterating -- K_ff is read once for
+// all of them, each product equal bit for bit to the pair's own.
 struct TogetherGraph {
   std::vector<std::pair<GpuAmg*, SolveWork*>> members;
   std::vector<uint64_t> epochs;
-  std::vector<int64_t> kernels;  // kernels of each member's body
+  std::vector<int64_t> kernels;  // kernels of each member's body (without a fused operator)
+  int64_t fused_nodes = 0;       // fused operator launches per graph launch
   cudaGraphExec_t exec = nullptr;
   cudaStream_t stream = nullptr;
   DBuf<int> flags;
@@ -1555,23 +1601,78 @@ struct TogetherGraph {
     return true;
   }
 
+  // conditional node after `dep` guarded by h; `body` is captured into it on
+  // w's stream.  Returns the node; adds the captured kernels to `count`.
+  template <class F>
+  static cudaGraphNode_t add_conditional(cudaGraph_t g, cudaGraphNode_t dep, cudaGraphConditionalHandle h,
+                                         SolveWork& w, int64_t& count, F&& body) {
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond = nullptr;
+    SIMP_CUDA(cudaGraphAddNode(&cond, g, &dep, nullptr, 1, &cp));
+    SIMP_CUDA(cudaStreamBeginCaptureToGraph(w.stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeThreadLocal));
+    const int64_t before = t_launches;
+    try {
+      body();
+    } catch (...) {
+      cudaGraph_t tmp = nullptr;
+      cudaStreamEndCapture(w.stream, &tmp);
+      throw;
+    }
+    const int64_t k = t_launches - before;
+    cudaGraph_t tmp = nullptr;
+    SIMP_CUDA(cudaStreamEndCapture(w.stream, &tmp));
+    // captured launches ran nothing: counted when the graph runs
+    g_launches.fetch_sub(k, std::memory_order_relaxed);
+    count += k;
+    return cond;
+  }
+
   void build() {
     const size_t n = members.size();
     if (!stream) SIMP_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     flags.alloc(n);
     kernels.assign(n, 0);
+    fused_nodes = 0;
     epochs.clear();
+    // pairs whose CG operator is fused: double-float operators of a hierarchy
+    // that two or more pairs share, in member order
+    std::vector<std::vector<size_t>> groups;
+    std::vector<char> fused(n, 0);
+    for (size_t i = 0; i < n; ++i) {
+      GpuAmg* a = members[i].first;
+      if (!a->mixed() || a->mf_cg()) continue;
+      bool placed = false;
+      for (auto& grp : groups)
+        if (members[grp.front()].first == a) {
+          grp.push_back(i);
+          placed = true;
+        }
+      if (!placed) groups.push_back({i});
+    }
+    for (auto& grp : groups)
+      if (grp.size() > 1)
+        for (size_t i : grp) fused[i] = 1;
     cudaGraph_t g = nullptr;
     SIMP_CUDA(cudaGraphCreate(&g, 0));
     try {
+      std::vector<cudaGraphNode_t> first(n, nullptr);
+      std::vector<cudaGraphConditionalHandle> second(n);
       for (size_t i = 0; i < n; ++i) {
         GpuAmg& a = *members[i].first;
         SolveWork& w = *members[i].second;
         epochs.push_back(a.epoch_);
-        cudaGraphConditionalHandle h;
+        cudaGraphConditionalHandle h, h2 = 0;
         SIMP_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+        if (fused[i]) SIMP_CUDA(cudaGraphConditionalHandleCreate(&h2, g, 0, 0));
+        second[i] = h2;
         const int* loop = w.loop.p;
-        void* args[] = {&h, &loop};
+        int two = fused[i];
+        void* args[] = {&h, &h2, &two, &loop};
         cudaGraphNodeParams kp = {};
         kp.type = cudaGraphNodeTypeKernel;
         kp.kernel.func = reinterpret_cast<void*>(k_arm);
@@ -1582,34 +1683,40 @@ struct TogetherGraph {
         kp.kernel.extra = nullptr;
         cudaGraphNode_t arm = nullptr;
         SIMP_CUDA(cudaGraphAddNode(&arm, g, nullptr, nullptr, 0, &kp));
-        cudaGraphNodeParams cp = {};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = h;
-        cp.conditional.type = cudaGraphCondTypeIf;
-        cp.conditional.size = 1;
-        cudaGraphNode_t cond = nullptr;
-        SIMP_CUDA(cudaGraphAddNode(&cond, g, &arm, nullptr, 1, &cp));
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        SIMP_CUDA(cudaStreamBeginCaptureToGraph(w.stream, body, nullptr, nullptr, 0,
-                                                cudaStreamCaptureModeThreadLocal));
-        const int64_t before = t_launches;
-        try {
+        first[i] = add_conditional(g, arm, h, w, kernels[i], [&] {
           float2* ps = a.psplit_of(w);
           a.pcg_tail(w, ps);
+          if (fused[i]) return;
           a.pcg_head(w, w.px.p, ps != nullptr || a.mf_cg());
           k_loop_test<<<1, 1, 0, w.stream>>>(reinterpret_cast<const PcgScalars*>(w.scal.p + 8), w.loop.p,
                                              w.loopd.p, flags.p + i);
           SIMP_CHECK_LAUNCH();
-        } catch (...) {
-          cudaGraph_t tmp = nullptr;
-          cudaStreamEndCapture(w.stream, &tmp);
-          throw;
+        });
+      }
+      for (auto& grp : groups) {
+        if (grp.size() < 2) continue;
+        GpuAmg& a = *members[grp.front()].first;
+        for (size_t c0 = 0; c0 < grp.size(); c0 += kMaxRhs) {
+          const size_t c1 = std::min(grp.size(), c0 + kMaxRhs);
+          std::vector<SolveWork*> ws;
+          std::vector<cudaGraphNode_t> deps;
+          for (size_t c = c0; c < c1; ++c) {
+            ws.push_back(members[grp[c]].second);
+            deps.push_back(first[grp[c]]);
+          }
+          cudaGraphNode_t op = a.add_op0_multi(g, ws, deps);
+          ++fused_nodes;
+          for (size_t c = c0; c < c1; ++c) {
+            const size_t i = grp[c];
+            SolveWork& w = *members[i].second;
+            add_conditional(g, op, second[i], w, kernels[i], [&] {
+              a.pcg_head(w, w.px.p, true, true);
+              k_loop_test<<<1, 1, 0, w.stream>>>(reinterpret_cast<const PcgScalars*>(w.scal.p + 8), w.loop.p,
+                                                 w.loopd.p, flags.p + i);
+              SIMP_CHECK_LAUNCH();
+            });
+          }
         }
-        kernels[i] = t_launches - before;
-        cudaGraph_t tmp = nullptr;
-        SIMP_CUDA(cudaStreamEndCapture(w.stream, &tmp));
-        // captured launches ran nothing: counted when the graph runs
-        g_launches.fetch_sub(kernels[i], std::memory_order_relaxed);
       }
       if (exec) {
         cudaGraphExecDestroy(exec);
@@ -1800,7 +1907,8 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
         for (size_t k = 0; k < idx.size(); ++k)
           if (active[k]) launched += tg.kernels[k];
         SIMP_CUDA(cudaGraphLaunch(tg.exec, tg.stream));
-        g_launches.fetch_add(launched + static_cast<int64_t>(idx.size()), std::memory_order_relaxed);
+        g_launches.fetch_add(launched + tg.fused_nodes + static_cast<int64_t>(idx.size()),
+                             std::memory_order_relaxed);
         SIMP_CUDA(cudaMemcpyAsync(hf.data(), tg.flags.p, sizeof(int) * idx.size(), cudaMemcpyDeviceToHost,
                                   tg.stream));
         SIMP_CUDA(cudaStreamSynchronize(tg.stream));

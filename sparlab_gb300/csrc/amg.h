@@ -310,7 +310,13 @@ class GpuAmg {
   // the iterations after the first: [V-cycle, beta, direction, operator,
   // alpha, update] -- launched one by one, or as w's captured graph
   void pcg_tail(SolveWork& w, float2* psplit);
-  void pcg_head(SolveWork& w, double* x, bool split_ready);
+  // op_done: q = A p is already in w.pq (a fused multi-RHS launch)
+  void pcg_head(SolveWork& w, double* x, bool split_ready, bool op_done = false);
+  // q = A0 p of several workspaces of this hierarchy (mixed precision, p's
+  // split in each xsplit) as one fused multi-RHS kernel node of g after
+  // deps; a workspace whose loop flag is clear is skipped
+  cudaGraphNode_t add_op0_multi(cudaGraph_t g, const std::vector<SolveWork*>& ws,
+                                const std::vector<cudaGraphNode_t>& deps);
   void pcg_body(SolveWork& w, double* x, float2* psplit);
   float2* psplit_of(SolveWork& w) { return mixed() && !mf_cg() ? w.xsplit.p : nullptr; }
   friend struct TogetherGraph;

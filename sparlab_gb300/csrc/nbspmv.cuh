@@ -198,5 +198,87 @@ __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ n
   }
 }
 
+// y_k = A x_k for up to kMaxRhs right-hand sides of one double-float
+// operator (the load cases of one problem): each (hi, lo) value pair of A is
+// loaded once per row step for all of them, so A's bytes are read once for
+// the k vectors.  A vector takes part while its flag *active[k] is nonzero
+// (a solve that has stopped is skipped; null: always).  Every y_k is summed
+// in exactly the lanes, steps and butterfly of k_rows_apply_df, so it equals
+// that kernel's product bit for bit.
+constexpr int kMaxRhs = 4;
+struct MultiRhs {
+  const float2* x[kMaxRhs];
+  double* y[kMaxRhs];
+  const int* active[kMaxRhs];
+  int n;
+};
+
+template <int VS, int B>
+__global__ void __launch_bounds__(256) k_rows_apply_df_multi(const i32* __restrict__ node_of, NodeView pat,
+                                                             const i32* __restrict__ rowptr,
+                                                             const i32* __restrict__ col,
+                                                             const float2* __restrict__ v,
+                                                             const __grid_constant__ MultiRhs m, i32 rows) {
+  const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+  const i32 row = static_cast<i32>(t / VS);
+  const int lane = static_cast<int>(t % VS);
+  bool on[kMaxRhs];
+  float sh[kMaxRhs], sl[kMaxRhs];
+#pragma unroll
+  for (int k = 0; k < kMaxRhs; ++k) {
+    on[k] = k < m.n && (m.active[k] == nullptr || *m.active[k] != 0);
+    sh[k] = sl[k] = 0.0f;
+  }
+  if (row < rows) {
+    const i32 k0 = rowptr[row], len = rowptr[row + 1] - k0;
+    const float2* vp = v + k0;
+    const i32* cl = col + k0;
+    const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
+    i32 w = lane;
+    for (; w + (kUnroll - 1) * VS < len; w += kUnroll * VS) {
+      float2 hv[kUnroll];
+      i32 cw[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        hv[u] = vp[w + u * VS];
+        cw[u] = row_col<B>(w + u * VS, s0, pat.nbr, cl);
+      }
+#pragma unroll
+      for (int k = 0; k < kMaxRhs; ++k) {
+        if (!on[k]) continue;
+        float2 xv[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) xv[u] = m.x[k][cw[u]];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) df_fma(hv[u].x, hv[u].y, xv[u].x, xv[u].y, sh[k], sl[k]);
+      }
+    }
+    for (; w < len; w += VS) {
+      const float2 hv = vp[w];
+      const i32 cw = row_col<B>(w, s0, pat.nbr, cl);
+#pragma unroll
+      for (int k = 0; k < kMaxRhs; ++k) {
+        if (!on[k]) continue;
+        const float2 xv = m.x[k][cw];
+        df_fma(hv.x, hv.y, xv.x, xv.y, sh[k], sl[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kMaxRhs; ++k) {
+    if (!on[k]) continue;  // the same for every thread
+#pragma unroll
+    for (int o = VS / 2; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, sh[k], o, VS);
+      const float ol = __shfl_xor_sync(0xffffffffu, sl[k], o, VS);
+      float s, e;
+      two_sum(sh[k], oh, s, e);
+      sh[k] = s;
+      sl[k] = __fadd_rn(sl[k], __fadd_rn(ol, e));
+    }
+    if (row < rows && lane == 0) m.y[k][row] = static_cast<double>(sh[k]) + static_cast<double>(sl[k]);
+  }
+}
+
 }  // namespace
 }  // namespace simp

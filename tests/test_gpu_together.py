@@ -51,6 +51,30 @@ def test_load_cases_in_one_graph_match_one_after_another(precision):
         assert abs(r[0] / hist[k, 0] - 1) < 1e-6
 
 
+def test_five_load_cases_with_fused_operators_match_one_after_another():
+    """Five load cases of one Hex8 problem in mixed precision: in the graph
+    the cases' CG products run as fused multi-RHS launches over the shared
+    double-float K_ff (four cases per launch, so two launches), and every
+    iteration's compliance, iteration count and OC multiplier equal the
+    one-after-another solves bit for bit."""
+    spec = P.hex8_cantilever(24, 12, 12, 0.3, "five_loads")
+    loads = []
+    for i in range(5):
+        rng = P.SplitMix64(9, i)
+        j, k = int(rng.uniform(0.0, 12.99)), int(rng.uniform(0.0, 12.99))
+        t = np.radians(rng.uniform(-90.0, 90.0))
+        loads.append(P.point_load(spec, [spec.node_index(24, j, k)], (0.0, np.sin(t), -np.cos(t))))
+    spec.loads = np.stack(loads)
+    spec.weights = np.full(5, 0.2)
+    spec.rtol = 1e-10
+    out = {}
+    for mode in (False, "graph"):
+        gpu = GpuSimpProblem(spec, precision="mixed", block_pcg=mode)
+        out[mode] = rows([gpu.iterate() for _ in range(3)])
+        gpu.close()
+    assert out["graph"] == out[False]
+
+
 def test_batch_of_uneven_problems_matches_one_at_a_time():
     specs = P.batched_instances(seed=4, count_q4=4, count_hex=3)
     alone = []
