@@ -180,42 +180,83 @@ struct MfArgs {
   double* y64;        // mode 8: output
 };
 
-// The epilogue of a node's product o = (A x)_I (3 components) in each mode;
-// self = the input x at node I itself (mode 3: the direction d, mode 5: t).
+// The epilogue of a node's product o = (A x)_I (3 components) in each mode,
+// in two parts: the node's operand loads (mf_node_load: right-hand side,
+// inverse diagonal, smoothed iterate, as the mode reads them) and the
+// arithmetic and stores (mf_node_store), so a kernel can issue the loads
+// early.  self = the input x at node I itself (mode 3: the direction d,
+// mode 5: t); c0, c1 = coef[0], coef[1] of the modes that read them.
+struct MfNodeIn {
+  float b[3], dinv[3], xs[3];
+};
+
 template <int MODE>
-__device__ __forceinline__ void mf_node_out(const MfArgs& a, i32 I, const float (&o)[3], const float (&self)[3]) {
+__device__ __forceinline__ void mf_node_load(const MfArgs& a, i32 I, MfNodeIn& in) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const i64 row = static_cast<i64>(I) * 3 + k;
+    if (MODE == 1 || MODE == 3 || MODE == 4 || MODE == 6 || MODE == 7) in.b[k] = a.b[row];
+    if (MODE == 3 || MODE == 4 || MODE == 5 || MODE == 6) in.dinv[k] = a.dinv[row];
+    if (MODE == 3 || MODE == 5) in.xs[k] = a.xs[row];
+  }
+}
+
+template <int MODE>
+__device__ __forceinline__ void mf_node_store(const MfArgs& a, i32 I, const float (&o)[3], const float (&self)[3],
+                                              const MfNodeIn& in, float c0, float c1) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const i64 row = static_cast<i64>(I) * 3 + k;
     if (MODE == 0) {
       a.y[row] = o[k];
     } else if (MODE == 1) {
-      a.y[row] = a.b[row] - o[k];
+      a.y[row] = in.b[k] - o[k];
     } else if (MODE == 3) {
-      const float ri = a.b[row] - o[k];
+      const float ri = in.b[k] - o[k];
       a.r[row] = ri;
       const float dv = self[k];
-      const float di = a.coef[0] * dv + a.coef[1] * a.dinv[row] * ri;
+      const float di = c0 * dv + c1 * in.dinv[k] * ri;
       a.dn[row] = di;
-      float xi = a.xs[row];
+      float xi = in.xs[k];
       if (a.add_d) xi = xi + dv;
       a.xs[row] = xi + di;
     } else if (MODE == 4) {
-      const float ri = a.b[row] - o[k];
+      const float ri = in.b[k] - o[k];
       a.r[row] = ri;
-      a.dn[row] = a.dinv[row] * ri * a.coef[0];
+      a.dn[row] = in.dinv[k] * ri * c0;
     } else if (MODE == 5) {
-      a.xs[row] = a.xs[row] + (self[k] - a.coef[0] * (a.dinv[row] * o[k]));
+      a.xs[row] = in.xs[k] + (self[k] - c0 * (in.dinv[k] * o[k]));
     } else if (MODE == 6) {
-      const float ri = a.b[row] - o[k];
+      const float ri = in.b[k] - o[k];
       a.y[row] = ri;
-      a.dn[row] = a.dinv[row] * ri;
+      a.dn[row] = in.dinv[k] * ri;
     } else if (MODE == 8) {
       a.y64[row] = static_cast<double>(o[k]);
     } else {
-      a.y[row] = a.b[row] - a.coef[0] * o[k];
+      a.y[row] = in.b[k] - c0 * o[k];
     }
   }
+}
+
+// coef[0], coef[1] of the modes that read them (device scalars)
+template <int MODE>
+__device__ __forceinline__ void mf_coefs(const MfArgs& a, float& c0, float& c1) {
+  c0 = c1 = 0.0f;
+  if (MODE == 3) {
+    c0 = a.coef[0];
+    c1 = a.coef[1];
+  } else if (MODE == 4 || MODE == 5 || MODE == 7) {
+    c0 = a.coef[0];
+  }
+}
+
+template <int MODE>
+__device__ __forceinline__ void mf_node_out(const MfArgs& a, i32 I, const float (&o)[3], const float (&self)[3]) {
+  MfNodeIn in;
+  mf_node_load<MODE>(a, I, in);
+  float c0, c1;
+  mf_coefs<MODE>(a, c0, c1);
+  mf_node_store<MODE>(a, I, o, self, in, c0, c1);
 }
 
 template <int MODE, int TX = kTX, int TY = kTY, int TZ = kTZ>
