@@ -535,18 +535,53 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
     k_split_pairs<<<grid_for(l0.n, 256, 8192), 256, 0, stream>>>(l0.n, x, xsplit);
     SIMP_CHECK_LAUNCH();
   }
+  df_apply(xsplit, y, rhs, stream, df_whole_);
+}
+
+// The double-float level-0 product in the load schedule `whole` selects
+// (both give the same bits).
+void GpuAmg::df_apply(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream, int whole) {
+  Level& l0 = *levels.front();
+  const NbOp& op = l0.opA;
   with_shape<float>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
-    if (rhs)
-      k_rows_apply_df<VS, B, 1><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
-                                                                       l0.a.v2.p, xsplit, y, rhs,
-                                                                       op.rows);
-    else
-      k_rows_apply_df<VS, B, 0><<<rows_grid(op, VS), 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
-                                                                       l0.a.v2.p, xsplit, y,
-                                                                       nullptr, op.rows);
+    const unsigned grid = rows_grid(op, VS);
+    if (rhs) {
+      if (whole)
+        k_rows_apply_df<VS, B, 1, true><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
+                                                                   l0.a.v2.p, xsplit, y, rhs, op.rows);
+      else
+        k_rows_apply_df<VS, B, 1, false><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
+                                                                    l0.a.v2.p, xsplit, y, rhs, op.rows);
+    } else {
+      if (whole)
+        k_rows_apply_df<VS, B, 0, true><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
+                                                                   l0.a.v2.p, xsplit, y, nullptr, op.rows);
+      else
+        k_rows_apply_df<VS, B, 0, false><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col,
+                                                                    l0.a.v2.p, xsplit, y, nullptr, op.rows);
+    }
   });
   SIMP_CHECK_LAUNCH();
+}
+
+// The double-float operator's load schedule for this level 0: the faster of
+// the step-wise and whole-row variants on y = A x (same bits), before the
+// first CUDA graph capture of a structure.
+void GpuAmg::tune_df() {
+  if (!mixed() || mf_cg()) return;
+  Level& l0 = *levels.front();
+  const i32 n = l0.n;
+  DBuf<float2> xs(static_cast<size_t>(n));
+  DBuf<double> ys(static_cast<size_t>(n));
+  SIMP_CUDA(cudaMemsetAsync(xs.p, 0, sizeof(float2) * n, stream));
+  std::ostringstream key;
+  key << "df0:" << n << "x" << l0.a.nnz << "x" << l0.opA.lanes32;
+  df_whole_ = tune_pick(key.str(), 2, [&](int v) { df_apply(xs.p, ys.p, nullptr, stream, v == 0 ? 1 : 0); }, stream,
+                        0, 5) == 0
+                  ? 1
+                  : 0;
+  SIMP_CUDA(cudaStreamSynchronize(stream));
 }
 
 cudaGraphNode_t GpuAmg::add_op0_multi(cudaGraph_t g, const std::vector<SolveWork*>& ws,
@@ -1215,7 +1250,10 @@ void GpuAmg::setup(bool structure_changed) {
   coarse_factorize();
   ensure(main_);
   for (auto& w : extra_) ensure(*w);
-  if (!reuse) tune_level0();
+  if (!reuse) {
+    tune_level0();
+    tune_df();
+  }
   ready_ = true;
   // captured iteration bodies stay valid across reuse setups: their launches
   // take only workspace and level pointers, which a reuse setup keeps
@@ -1557,14 +1595,16 @@ __global__ void k_arm(cudaGraphConditionalHandle h, cudaGraphConditionalHandle h
 
 // After an iteration body: count the iteration and apply GpuAmg::pcg's test
 // (no breakdown, sqrt(||r||^2) above the stopping norm, budget left); the
-// flag is the host's view of whether the system iterates on.
+// flag is the host's view of whether the system iterates on, flag[n] counts
+// the bodies that ran since the host last cleared it.
 __global__ void k_loop_test(const PcgScalars* __restrict__ sc, int* __restrict__ loop,
-                            const double* __restrict__ target, int* __restrict__ flag) {
+                            const double* __restrict__ target, int* __restrict__ flag, int n) {
   const int total = loop[1] + 1;
   loop[1] = total;
   const bool go = sc->status == 0 && !(sqrt(sc->rr) <= target[0]) && total < loop[2];
   loop[0] = go ? 1 : 0;
-  *flag = go ? 1 : 0;
+  flag[0] = go ? 1 : 0;
+  flag[n] += 1;
 }
 
 }  // namespace
@@ -1635,7 +1675,7 @@ struct TogetherGraph {
   void build() {
     const size_t n = members.size();
     if (!stream) SIMP_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    flags.alloc(n);
+    flags.alloc(2 * n);  // [0, n) iterate-on flags, [n, 2n) bodies run
     kernels.assign(n, 0);
     fused_nodes = 0;
     epochs.clear();
@@ -1689,7 +1729,7 @@ struct TogetherGraph {
           if (fused[i]) return;
           a.pcg_head(w, w.px.p, ps != nullptr || a.mf_cg());
           k_loop_test<<<1, 1, 0, w.stream>>>(reinterpret_cast<const PcgScalars*>(w.scal.p + 8), w.loop.p,
-                                             w.loopd.p, flags.p + i);
+                                             w.loopd.p, flags.p + i, static_cast<int>(n));
           SIMP_CHECK_LAUNCH();
         });
       }
@@ -1712,7 +1752,7 @@ struct TogetherGraph {
             add_conditional(g, op, second[i], w, kernels[i], [&] {
               a.pcg_head(w, w.px.p, true, true);
               k_loop_test<<<1, 1, 0, w.stream>>>(reinterpret_cast<const PcgScalars*>(w.scal.p + 8), w.loop.p,
-                                                 w.loopd.p, flags.p + i);
+                                                 w.loopd.p, flags.p + i, static_cast<int>(n));
               SIMP_CHECK_LAUNCH();
             });
           }
@@ -1899,24 +1939,30 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
       for (size_t i : idx) members.emplace_back(tasks[i].amg, tasks[i].w);
       std::lock_guard<std::mutex> lock(g_together_mu);
       TogetherGraph& tg = together_graph(members);
-      std::vector<int> hf(idx.size(), 1);
-      std::vector<int> active(idx.size(), 1);
-      size_t alive = idx.size();
+      // several launches per host check: a system that has stopped runs no
+      // body (its conditionals stay false), so the extra launches change
+      // nothing; the bodies that ran are counted on the device
+      const size_t m = idx.size();
+      std::vector<int> hf(2 * m, 1);
+      std::vector<int> active(m, 1);
+      size_t alive = m;
+      SIMP_CUDA(cudaMemsetAsync(tg.flags.p + m, 0, sizeof(int) * m, tg.stream));
+      std::vector<int> seen(m, 0);
+      int per_check = 1;
       while (alive > 0) {
-        int64_t launched = 0;
-        for (size_t k = 0; k < idx.size(); ++k)
-          if (active[k]) launched += tg.kernels[k];
-        SIMP_CUDA(cudaGraphLaunch(tg.exec, tg.stream));
-        g_launches.fetch_add(launched + tg.fused_nodes + static_cast<int64_t>(idx.size()),
-                             std::memory_order_relaxed);
-        SIMP_CUDA(cudaMemcpyAsync(hf.data(), tg.flags.p, sizeof(int) * idx.size(), cudaMemcpyDeviceToHost,
-                                  tg.stream));
+        for (int r = 0; r < per_check; ++r) SIMP_CUDA(cudaGraphLaunch(tg.exec, tg.stream));
+        SIMP_CUDA(cudaMemcpyAsync(hf.data(), tg.flags.p, sizeof(int) * 2 * m, cudaMemcpyDeviceToHost, tg.stream));
         SIMP_CUDA(cudaStreamSynchronize(tg.stream));
+        int64_t launched = static_cast<int64_t>(per_check) * (tg.fused_nodes + static_cast<int64_t>(m));
         alive = 0;
-        for (size_t k = 0; k < idx.size(); ++k) {
+        for (size_t k = 0; k < m; ++k) {
+          launched += static_cast<int64_t>(hf[m + k] - seen[k]) * tg.kernels[k];
+          seen[k] = hf[m + k];
           active[k] = active[k] && hf[k];
           alive += active[k] ? 1 : 0;
         }
+        g_launches.fetch_add(launched, std::memory_order_relaxed);
+        per_check = std::min(per_check * 2, 4);
       }
       for (size_t k = 0; k < idx.size(); ++k) {
         const size_t i = idx[k];

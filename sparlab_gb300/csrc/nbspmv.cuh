@@ -20,6 +20,7 @@ namespace simp {
 namespace {
 
 constexpr int kUnroll = 4;  // row steps whose loads a lane issues before their products
+constexpr int kRowSteps = 11;  // double-float rows of up to VS * 11 entries load all steps at once
 
 // Column of entry w of a row: column-free decode (B > 0) or the column array.
 template <int B>
@@ -149,7 +150,11 @@ __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __
 // double-float arithmetic on the FP32 pipes, y in FP64.  About 2^-44 relative
 // to the FP64 product, at FP32 instruction rates: bandwidth bound where the
 // FP64 kernel is bound by GB300's FP64 rate.  mode 0: y = A x ; 1: y = b - A x.
-template <int VS, int B, int MODE>
+// WHOLE: a lane issues the loads of all its steps of a row (up to kRowSteps)
+// before the first product -- two memory round trips per row instead of two
+// per kUnroll steps, at more registers; the products run in the same order
+// either way, so both variants give the same bits (the tuner picks one).
+template <int VS, int B, int MODE, bool WHOLE>
 __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ node_of, NodeView pat,
                                                        const i32* __restrict__ rowptr, const i32* __restrict__ col,
                                                        const float2* __restrict__ v, const float2* __restrict__ x,
@@ -165,6 +170,25 @@ __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ n
     const i32* cl = col + k0;
     const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
     i32 w = lane;
+    if (WHOLE && len <= VS * kRowSteps) {
+      // the whole row in flight: every step's value and column, then every
+      // x gather, then the products in the same order as the loop below
+      float2 hv[kRowSteps], xv[kRowSteps];
+      i32 cw[kRowSteps];
+#pragma unroll
+      for (int u = 0; u < kRowSteps; ++u)
+        if (lane + u * VS < len) {
+          hv[u] = vp[lane + u * VS];
+          cw[u] = row_col<B>(lane + u * VS, s0, pat.nbr, cl);
+        }
+#pragma unroll
+      for (int u = 0; u < kRowSteps; ++u)
+        if (lane + u * VS < len) xv[u] = x[cw[u]];
+#pragma unroll
+      for (int u = 0; u < kRowSteps; ++u)
+        if (lane + u * VS < len) df_fma(hv[u].x, hv[u].y, xv[u].x, xv[u].y, sh, sl);
+      w = len;
+    }
     for (; w + (kUnroll - 1) * VS < len; w += kUnroll * VS) {
       float2 hv[kUnroll];
       float2 xv[kUnroll];
