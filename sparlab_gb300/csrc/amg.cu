@@ -218,9 +218,10 @@ void mf3_64(const MfOp& mf, const double* x, double* y, const double* b, cudaStr
 }
 
 template <int MODE, int TX, int TY, int TZ>
-void mf3_shape(const MfOp& mf, const MfArgs& a, const KeF32& ke, cudaStream_t s) {
+void mf3_shape(const MfOp& mf, const MfArgs& a, const KeF32& ke, cudaStream_t s, bool v4) {
   const dim3 grid((mf.nnx + TX - 1) / TX, (mf.nny + TY - 1) / TY, (mf.nz + 1 + TZ - 1) / TZ);
-  k_mf3_tile<MODE, TX, TY, TZ><<<grid, TX * TY * TZ, 0, s>>>(mf_view(mf), a, ke);
+  if (v4) k_mf3_tile<MODE, TX, TY, TZ, true><<<grid, TX * TY * TZ, 0, s>>>(mf_view(mf), a, ke);
+  else k_mf3_tile<MODE, TX, TY, TZ, false><<<grid, TX * TY * TZ, 0, s>>>(mf_view(mf), a, ke);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -237,8 +238,9 @@ void mf3_tc(const MfOp& mf, const MfArgs& a, const KeF32& ke, cudaStream_t s) {
   SIMP_CHECK_LAUNCH();
 }
 
-// The tiled matrix-free kernel in the tile shape the tuner chose (mf.tile
-// indexes kMfTileShape; every shape gives the same values), or the
+// The tiled matrix-free kernel in the variant the tuner chose (mf.tile:
+// shape kMfTileShape[tile % 5], float4 halo for tile >= 5; every variant
+// gives the same values), or the
 // tensor-core kernel (mf.tensor).
 template <int MODE>
 void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
@@ -248,13 +250,14 @@ void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
     mf3_tc<MODE>(mf, a, ke, s);
     return;
   }
-  static_assert(kMfTiles == 5, "tile table");
-  switch (mf.tile) {
-    case 1: mf3_shape<MODE, 32, 8, 1>(mf, a, ke, s); break;
-    case 2: mf3_shape<MODE, 32, 2, 4>(mf, a, ke, s); break;
-    case 3: mf3_shape<MODE, 64, 2, 2>(mf, a, ke, s); break;
-    case 4: mf3_shape<MODE, 32, 4, 1>(mf, a, ke, s); break;
-    default: mf3_shape<MODE, 32, 4, 2>(mf, a, ke, s); break;
+  static_assert(kMfTiles == 10, "tile table");
+  const bool v4 = mf.tile >= 5;
+  switch (mf.tile % 5) {
+    case 1: mf3_shape<MODE, 32, 8, 1>(mf, a, ke, s, v4); break;
+    case 2: mf3_shape<MODE, 32, 2, 4>(mf, a, ke, s, v4); break;
+    case 3: mf3_shape<MODE, 64, 2, 2>(mf, a, ke, s, v4); break;
+    case 4: mf3_shape<MODE, 32, 4, 1>(mf, a, ke, s, v4); break;
+    default: mf3_shape<MODE, 32, 4, 2>(mf, a, ke, s, v4); break;
   }
 }
 

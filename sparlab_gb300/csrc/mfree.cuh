@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 // tile of grid nodes (kNZ node layers per thread; two layers per thread
 // measured slower at 192 x 96 x 96, 109 against 105 us); the tile's node
 // values plus a one-node halo (one shared array per component) and the
-// scales of the cells that touch it are staged in shared memory once.  Each thread loads its 27 neighbour values into registers and sums
+// scales of the cells that touch it are staged in shared memory once (see
+// MfHalo for the node values' layouts).  Each thread sums
 // the 64 (cell, corner) 3 x 3 block products with K_e^0 taken from the kernel
 // parameter (a __grid_constant__ struct indexed by compile-time constants,
 // so its entries are constant-bank operands of the FMAs rather than loads).
@@ -158,10 +159,11 @@ __global__ void __launch_bounds__(256) k_mf_cheb_first(MfView m, i32 nodes, cons
 constexpr int kTX = 32, kTY = 4, kTZ = 2;  // threads per block axis (the default tile)
 constexpr int kNZ = 1;                      // node layers per thread
 // Tile shapes the launch-shape tuner chooses among (TX x TY x TZ threads,
-// one node each): every shape sums each node's cells and corners in the same
-// order, so all give the same values bit for bit.
-constexpr int kMfTiles = 5;
-constexpr int kMfTileShape[kMfTiles][3] = {{32, 4, 2}, {32, 8, 1}, {32, 2, 4}, {64, 2, 2}, {32, 4, 1}};
+// one node each), each with both halo layouts (variant v: shape v % 5, the
+// float4 layout for v >= 5): every variant sums each node's cells and
+// corners in the same order, so all give the same values bit for bit.
+constexpr int kMfTiles = 10;
+constexpr int kMfTileShape[5][3] = {{32, 4, 2}, {32, 8, 1}, {32, 2, 4}, {64, 2, 2}, {32, 4, 1}};
 
 struct KeF32 {
   float k[24 * 24];  // K_e^0, row-major
@@ -259,10 +261,44 @@ __device__ __forceinline__ void mf_node_out(const MfArgs& a, i32 I, const float 
   mf_node_store<MODE>(a, I, o, self, in, c0, c1);
 }
 
-template <int MODE, int TX = kTX, int TY = kTY, int TZ = kTZ>
+// Node values of a tile in shared memory: one array per component (V4
+// false: three 4-byte loads per corner, fewer registers) or (x, y, z,
+// unused) per node (V4 true: one 16-byte load per corner).  The tuner picks;
+// the arithmetic is the same.
+template <bool V4, int NZ, int TY, int TX>
+struct MfHalo;
+template <int NZ, int TY, int TX>
+struct MfHalo<false, NZ, TY, TX> {
+  float v[3][NZ + 2][TY + 2][TX + 2];
+  __device__ __forceinline__ void put(int z, int y, int x, float a, float b, float c) {
+    v[0][z][y][x] = a;
+    v[1][z][y][x] = b;
+    v[2][z][y][x] = c;
+  }
+  __device__ __forceinline__ void get(int z, int y, int x, float (&o)[3]) const {
+    o[0] = v[0][z][y][x];
+    o[1] = v[1][z][y][x];
+    o[2] = v[2][z][y][x];
+  }
+};
+template <int NZ, int TY, int TX>
+struct MfHalo<true, NZ, TY, TX> {
+  float4 v[NZ + 2][TY + 2][TX + 2];
+  __device__ __forceinline__ void put(int z, int y, int x, float a, float b, float c) {
+    v[z][y][x] = make_float4(a, b, c, 0.0f);
+  }
+  __device__ __forceinline__ void get(int z, int y, int x, float (&o)[3]) const {
+    const float4 t = v[z][y][x];
+    o[0] = t.x;
+    o[1] = t.y;
+    o[2] = t.z;
+  }
+};
+
+template <int MODE, int TX = kTX, int TY = kTY, int TZ = kTZ, bool V4 = false>
 __global__ void __launch_bounds__(TX* TY* TZ) k_mf3_tile(MfView m, MfArgs a, const __grid_constant__ KeF32 ke) {
   constexpr int NZ = TZ * kNZ;  // node layers of the tile
-  __shared__ float xh[3][NZ + 2][TY + 2][TX + 2];
+  __shared__ MfHalo<V4, NZ, TY, TX> xh;
   __shared__ float sc[NZ + 1][TY + 1][TX + 1];
   const int tid = threadIdx.x;
   const i32 x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * NZ;
@@ -298,9 +334,7 @@ __global__ void __launch_bounds__(TX* TY* TZ) k_mf3_tile(MfView m, MfArgs a, con
     const int e = tid + q * TX * TY * TZ;
     if (e < kHalo) {
       const int hx = e % (TX + 2), hy = (e / (TX + 2)) % (TY + 2), hz = e / ((TX + 2) * (TY + 2));
-      xh[0][hz][hy][hx] = hv[q][0];
-      xh[1][hz][hy][hx] = hv[q][1];
-      xh[2][hz][hy][hx] = hv[q][2];
+      xh.put(hz, hy, hx, hv[q][0], hv[q][1], hv[q][2]);
     }
   }
   // cell scales (zero outside the grid)
@@ -341,9 +375,11 @@ __global__ void __launch_bounds__(TX* TY* TZ) k_mf3_tile(MfView m, MfArgs a, con
             const int bx = (b == 1 || b == 2 || b == 5 || b == 6) ? 1 : 0;
             const int by = (b == 2 || b == 3 || b == 6 || b == 7) ? 1 : 0;
             const int bz = b >= 4 ? 1 : 0;
+            float xb[3];
+            xh.get(lz + dz + 1 + bz, ty + dy + 1 + by, tx + dx + 1 + bx, xb);
 #pragma unroll
             for (int kb = 0; kb < 3; ++kb) {
-              const float xv = xh[kb][lz + dz + 1 + bz][ty + dy + 1 + by][tx + dx + 1 + bx];
+              const float xv = xb[kb];
               a0 = fmaf(ke.k[(3 * aI + 0) * 24 + 3 * b + kb], xv, a0);
               a1 = fmaf(ke.k[(3 * aI + 1) * 24 + 3 * b + kb], xv, a1);
               a2 = fmaf(ke.k[(3 * aI + 2) * 24 + 3 * b + kb], xv, a2);
@@ -354,8 +390,8 @@ __global__ void __launch_bounds__(TX* TY* TZ) k_mf3_tile(MfView m, MfArgs a, con
           out2 = fmaf(s, a2, out2);
         }
     const float o[3] = {out0, out1, out2};
-    const float self[3] = {xh[0][lz + 1][ty + 1][tx + 1], xh[1][lz + 1][ty + 1][tx + 1],
-                           xh[2][lz + 1][ty + 1][tx + 1]};
+    float self[3];
+    xh.get(lz + 1, ty + 1, tx + 1, self);
     mf_node_out<MODE>(a, I, o, self);
   }
 }

@@ -7,36 +7,41 @@
 // cells e around node I of s_e (K_e^0 x_e)[rows of I's corner].  A CTA owns
 // a column of 31 x 7 nodes and marches it along z over a chunk of node
 // layers.  Per cell layer it
-//   1. gathers each cell's 24 corner values (8 corners x 3) from the node
-//      values of the two node layers the cells span (a ring of four node
-//      layers with a one-node halo, staged in shared memory), splits each
-//      value into TF32 hi + lo (v = hi + lo exactly, lo rounded to TF32), and
-//      writes the rows of A (256 cells x 24) in the plain canonical K-major
-//      layout;
-//   2. one thread issues, per 128-cell M tile, the 3 x TF32 products
-//      A_lo K_hi + A_hi K_lo + A_hi K_hi (K = 8 per instruction, N = 32 with
-//      rows 24..31 of B zero) into 32 tensor-memory columns: about FP32
-//      accuracy (the dropped A_lo K_lo term is ~2^-22 relative);
-//   3. every thread reads its cell's row of F from tensor memory, scales it
-//      by s_e and stores the bottom-corner half (the node layer below the
-//      cell's centre) and the top-corner half (the layer above) in shared
-//      memory;
-//   4. while the next cell layer's MMA runs, the threads of the node layer
-//      between the last two cell layers sum their 8 cells' corner rows in a
-//      fixed order (cells below first, then dy, dx ascending) and apply the
-//      mode's epilogue (mf_node_store; the node's free index and operands
-//      are loaded two and one layers ahead).
+//   1. gathers each cell's 24 corner values (8 corners x 3) as TF32 hi + lo
+//      pairs (v = hi + lo to about 2^-22, each rounded to nearest) from a
+//      ring of four node layers with a one-node halo in shared memory (a
+//      node's values are split once, when its layer enters the ring), and
+//      writes the cell's row of A = [A_hi | A_lo] (K = 48) in the plain
+//      canonical K-major layout;
+//   2. one thread issues, per 128-cell M tile, six K = 8 steps of
+//      A · B^T with B = [[K_hi, K_hi], [K_lo, 0]] (N = 48): columns 0-23
+//      accumulate A_hi K_hi + A_lo K_hi and columns 24-47 A_hi K_lo, all in
+//      FP32 in tensor memory (3 x TF32: the dropped A_lo K_lo term is about
+//      2^-22 relative);
+//   3. every thread reads its cell's 48 accumulator columns back, forms
+//      F_e = s_e (D[0:24] + D[24:48]) and stores its bottom-corner and
+//      top-corner halves (the node layers below and above the cell centre)
+//      in shared memory;
+//   4. while the next cell layer's MMA runs, the threads of the owned nodes
+//      finish the node layer below the last cell layer (the partial sum of
+//      its four cells below, carried in registers, plus the bottom corners
+//      of its four cells above) and start the next one (the top corners of
+//      the cells below it), each in a fixed order (cells below first, then
+//      dy, dx ascending), then apply the mode's epilogue (mf_node_store; the
+//      node's free index, operands and own input value are loaded two and
+//      one layers ahead).
+// Every node's value is summed by one thread from the same F rows whatever
+// the chunking, so the result does not depend on the launch shape.
 // One thread waits for each MMA; the others wait at the barrier after it.
 // Node values are loaded in two stages (free-node indices, then values) and
 // enter the ring three layers ahead of the layer that reads them.
-// Every node's value is summed by one thread from the same F rows whatever
-// the chunking, so the result does not depend on the launch shape.
 //
 // The cells of a CTA's layer are 32 x 8 = 256 (two M = 128 tiles: TMEM
-// lanes = cells, columns 0-31 and 32-63); the CTA owns their 31 x 7 interior
-// nodes, so neighbouring CTAs recompute one cell row / column (the halo).
-// Thread t owns cell (t % 32, t / 32) of every layer; warp w reads TMEM lanes
-// 32 (w % 4) .. + 31 of M tile w / 4, which are exactly its threads' cells.
+// lanes = cells, columns 0-47 and 64-111); the CTA owns their 31 x 7
+// interior nodes, so neighbouring CTAs recompute one cell row / column (the
+// halo).  Thread t owns cell (t % 32, t / 32) of every layer; warp w reads
+// TMEM lanes 32 (w % 4) .. + 31 of M tile w / 4, which are exactly its
+// threads' cells.
 //
 // The MMA completion is waited on with the bounded mbarrier wait of tc.cuh;
 // a wait that runs out sets *status (kTcTimeout) and all threads leave the
@@ -57,25 +62,25 @@ constexpr int kTcHalo = kTcHaloX * kTcHaloY;                         // 297
 constexpr int kTcThreads = kTcCellsX * kTcCellsY;                    // one cell per thread
 constexpr int kTcRing = 4;                                           // node layers in shared memory
 constexpr int kTcHaloPer = (kTcHalo + kTcThreads - 1) / kTcThreads;  // halo entries per thread (2)
+constexpr int kTcN = 48;                                             // GEMM N (see B)
 
-// Shared memory (bytes from a 128-byte aligned base).  A: two parts (hi, lo)
-// of 256 rows x 24 TF32, element (r, j) at (j / 4) 4096 + (r / 8) 128 +
-// (r % 8) 16 + (j % 4) 4 (leading-dimension offset 4096, stride 128).  B: two
-// parts of 32 rows x 24, (n, k) at (k / 4) 512 + (n / 8) 128 + (n % 8) 16 +
-// (k % 4) 4.  Then the node ring (float4 per node), the bottom-corner rows
-// of F ([12][256] floats) and the top-corner rows of the last two cell layers
-// ([2][12][256]), the mbarrier and the tensor-memory address.
-constexpr int kTcAPart = kTcThreads * 24 * 4;  // 24,576
-constexpr int kTcBPart = 32 * 24 * 4;          // 3,072
+// Shared memory (bytes from a 128-byte aligned base).  A: 256 rows x 48
+// TF32 (hi in K 0-23, lo in K 24-47), element (r, k) at (k / 4) 4096 +
+// (r / 8) 128 + (r % 8) 16 + (k % 4) 4 (leading-dimension offset 4096,
+// stride 128).  B: 48 rows x 48, (n, k) at (k / 4) 768 + (n / 8) 128 +
+// (n % 8) 16 + (k % 4) 4.  Then the node ring (per node: (hi_x, hi_y, hi_z,
+// lo_x) as a float4 and (lo_y, lo_z) as a float2, two arrays), the corner
+// rows of F ([12][256] floats, bottom then top), the mbarrier and the
+// tensor-memory address.
 constexpr int kTcALbo = kTcThreads / 8 * 128;  // 4,096
-constexpr int kTcBLbo = 32 / 8 * 128;          // 512
-constexpr int kTcOffB = 2 * kTcAPart;
-constexpr int kTcOffRing = kTcOffB + 2 * kTcBPart;
-constexpr int kTcOffF0 = kTcOffRing + kTcRing * kTcHalo * 16;
-constexpr int kTcOffF1 = kTcOffF0 + 12 * kTcThreads * 4;
-constexpr int kTcOffBar = kTcOffF1 + 2 * 12 * kTcThreads * 4;
-constexpr int kTcSmemBytes = kTcOffBar + 16 + 128;  // + alignment slack (111,312: two CTAs per SM)
-constexpr uint32_t kTcTmemCols = 64;
+constexpr int kTcBLbo = kTcN / 8 * 128;        // 768
+constexpr int kTcOffB = 12 * kTcALbo;          // 49,152
+constexpr int kTcOffRingA = kTcOffB + 12 * kTcBLbo;
+constexpr int kTcOffRingB = kTcOffRingA + kTcRing * kTcHalo * 16;
+constexpr int kTcOffF = kTcOffRingB + kTcRing * kTcHalo * 8;
+constexpr int kTcOffBar = kTcOffF + 24 * kTcThreads * 4;
+constexpr int kTcSmemBytes = kTcOffBar + 16 + 128;  // + alignment slack (111,600: two CTAs per SM)
+constexpr uint32_t kTcTmemCols = 128;               // two tiles of 48 columns at 0 and 64
 
 // Corner b of a cell (the K_e^0 column block 3 b .. 3 b + 2): offsets
 // (bx, by, bz) = (0,0,0) (1,0,0) (1,1,0) (0,1,0) and the same at z + 1.
@@ -87,9 +92,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     k_mf3_tc(MfView m, MfArgs a, const __grid_constant__ KeF32 ke, int layers, int* status) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-  float4* ring = reinterpret_cast<float4*>(smem + kTcOffRing);
-  float* f0 = reinterpret_cast<float*>(smem + kTcOffF0);
-  float* f1 = reinterpret_cast<float*>(smem + kTcOffF1);
+  float4* ring_a = reinterpret_cast<float4*>(smem + kTcOffRingA);
+  float2* ring_b = reinterpret_cast<float2*>(smem + kTcOffRingB);
+  float* fb = reinterpret_cast<float*>(smem + kTcOffF);  // bottom corners (rows 0-11)
+  float* ft = fb + 12 * kTcThreads;                      // top corners (rows 12-23)
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kTcOffBar);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + kTcOffBar + 8);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -100,15 +106,17 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const int ncl = nz1 - nz0 + 1;  // cell layers nz0 - 1 .. nz1 - 1
   const i64 node_layer = static_cast<i64>(m.nnx) * m.nny, cell_layer = static_cast<i64>(m.nx) * m.ny;
 
-  // B = K_e^0 (symmetric: row n of B is row n of K) as TF32 hi + lo
-  for (int e = tid; e < 32 * 24; e += kTcThreads) {
-    const int n = e / 24, k = e % 24;
-    const float v = n < 24 ? ke.k[n * 24 + k] : 0.0f;
+  // B = [[K_hi, K_hi], [K_lo, 0]] (K_e^0 is symmetric: row n of B's blocks
+  // is row n of K)
+  for (int e = tid; e < kTcN * 48; e += kTcThreads) {
+    const int n = e / 48, k = e % 48;
+    const int r = n % 24, c = k % 24;
+    const float v = ke.k[r * 24 + c];
     const uint32_t hi = tc::tf32_round(v);
     const uint32_t lo = tc::tf32_round(v - __uint_as_float(hi));
+    const uint32_t w = n < 24 ? hi : (k < 24 ? lo : 0u);
     const int off = (k >> 2) * kTcBLbo + (n >> 3) * 128 + (n & 7) * 16 + (k & 3) * 4;
-    *reinterpret_cast<uint32_t*>(smem + kTcOffB + off) = hi;
-    *reinterpret_cast<uint32_t*>(smem + kTcOffB + kTcBPart + off) = lo;
+    *reinterpret_cast<uint32_t*>(smem + kTcOffB + off) = w;
   }
   if (tid == 0) {
     tc::mbar_init(bar, 1);
@@ -146,11 +154,22 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       }
     }
   };
+  // a layer enters the ring split into TF32 hi + lo
   auto put = [&](int slot, const float4 (&v)[kTcHaloPer]) {
 #pragma unroll
     for (int q = 0; q < kTcHaloPer; ++q) {
       const int e = tid + q * kTcThreads;
-      if (e < kTcHalo) ring[slot * kTcHalo + e] = v[q];
+      if (e < kTcHalo) {
+        const float c[3] = {v[q].x, v[q].y, v[q].z};
+        float h[3], l[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          h[k] = __uint_as_float(tc::tf32_round(c[k]));
+          l[k] = __uint_as_float(tc::tf32_round(c[k] - h[k]));
+        }
+        ring_a[slot * kTcHalo + e] = make_float4(h[0], h[1], h[2], l[0]);
+        ring_b[slot * kTcHalo + e] = make_float2(l[1], l[2]);
+      }
     }
   };
   // this thread's cell: its in-layer offset or -1 outside the grid
@@ -166,6 +185,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                       ? static_cast<i64>(gy0 + nyl) * m.nnx + gx0 + nxl
                       : -1;
   auto node_of = [&](i32 L) { return (n2d >= 0 && L >= nz0 && L < nz1) ? m.nindex[L * node_layer + n2d] : -1; };
+  auto load_node = [&](i32 I, MfNodeIn& in, float (&self)[3]) {
+    mf_node_load<MODE>(a, I, in);
+    if (MODE == 3 || MODE == 5) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) self[k] = a.x[static_cast<i64>(I) * 3 + k];
+    }
+  };
   float c0, c1;
   mf_coefs<MODE>(a, c0, c1);
 
@@ -186,98 +212,100 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   float s_cur = scale_of(nz0 - 1);
   i32 I_cur = node_of(nz0), I_next = node_of(nz0 + 1);
   MfNodeIn in_cur;
-  if (I_cur >= 0) mf_node_load<MODE>(a, I_cur, in_cur);
+  float self_cur[3] = {0.0f, 0.0f, 0.0f};
+  if (I_cur >= 0) load_node(I_cur, in_cur, self_cur);
+  float part[3] = {0.0f, 0.0f, 0.0f};  // the cells below the next summed node layer
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = tc::idesc_tf32(128, 32);
+  const uint32_t idesc = tc::idesc_tf32(128, kTcN);
   const uint64_t a_desc = tc::smem_desc_plain(tc::smem_u32(smem), kTcALbo, 128);
   const uint64_t b_desc = tc::smem_desc_plain(tc::smem_u32(smem + kTcOffB), kTcBLbo, 128);
   // this thread's A row: (r / 8) 128 + (r % 8) 16 within each 16-byte column group
   uint8_t* arow = smem + (tid >> 3) * 128 + (tid & 7) * 16;
 
-  // Node layer nz0 - 2 + it is summed in iteration it (it >= 2) while the
-  // MMA of cell layer it runs, from the bottom-corner rows of cell layer
-  // it - 1 (f0) and the top-corner rows of it - 2 (f1); the last node layer
-  // after the march.
-  auto node_sum = [&](int it) {
+  // the corner rows of the node's cells in the last cell layer (F holds it):
+  // the bottom corners finish the node layer below it, the top corners start
+  // the node layer above it
+  auto finish = [&]() {
     if (I_cur < 0) return;
-    const float* below = f1 + (it & 1) * 12 * kTcThreads;  // cell layer it - 2
-    float o[3] = {0.0f, 0.0f, 0.0f};
+    float o[3] = {part[0], part[1], part[2]};
 #pragma unroll
-    for (int dz = -1; dz <= 0; ++dz)
+    for (int dy = -1; dy <= 0; ++dy)
 #pragma unroll
-      for (int dy = -1; dy <= 0; ++dy)
+      for (int dx = -1; dx <= 0; ++dx) {
+        const int c = (nyl + dy + 1) * kTcCellsX + nxl + dx + 1;
+        const int aI = -dy ? 3 + dx : -dx;  // the node's bottom corner in the cell
 #pragma unroll
-        for (int dx = -1; dx <= 0; ++dx) {
-          const int c = (nyl + dy + 1) * kTcCellsX + nxl + dx + 1;
-          const int ox = -dx, oy = -dy, oz = -dz;
-          const int aI = 4 * oz + (oy ? 3 - ox : ox);  // the node's corner in the cell
-          const float* src = oz ? below + (3 * aI - 12) * kTcThreads : f0 + 3 * aI * kTcThreads;
+        for (int k = 0; k < 3; ++k) o[k] += fb[(3 * aI + k) * kTcThreads + c];
+      }
+    mf_node_store<MODE>(a, I_cur, o, self_cur, in_cur, c0, c1);
+  };
+  auto start = [&]() {
+    part[0] = part[1] = part[2] = 0.0f;
+    if (n2d < 0) return;
 #pragma unroll
-          for (int k = 0; k < 3; ++k) o[k] += src[k * kTcThreads + c];
-        }
-    const float4 sv = ring[((it - 1) % kTcRing) * kTcHalo + (nyl + 1) * kTcHaloX + nxl + 1];
-    const float self[3] = {sv.x, sv.y, sv.z};
-    mf_node_store<MODE>(a, I_cur, o, self, in_cur, c0, c1);
+    for (int dy = -1; dy <= 0; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 0; ++dx) {
+        const int c = (nyl + dy + 1) * kTcCellsX + nxl + dx + 1;
+        const int aI = -dy ? 3 + dx : -dx;  // the node's top corner in the cell is 4 + aI
+#pragma unroll
+        for (int k = 0; k < 3; ++k) part[k] += ft[(3 * aI + k) * kTcThreads + c];
+      }
   };
 
   bool ok = true;
   int it = 0;
   for (; it < ncl; ++it) {
     const i32 cz = nz0 - 1 + it;
-    // 1. A rows of this cell from node layers cz (slot it % 3) and cz + 1
+    // 1. A rows of this cell from node layers cz (slot it % 4) and cz + 1
     {
-      const float4* r0 = ring + (it % kTcRing) * kTcHalo;
-      const float4* r1 = ring + ((it + 1) % kTcRing) * kTcHalo;
-      float xv[24];
+      const int s0 = (it % kTcRing) * kTcHalo, s1 = ((it + 1) % kTcRing) * kTcHalo;
+      float hv[24], lv[24];
 #pragma unroll
       for (int b = 0; b < 8; ++b) {
-        const float4 v = (b < 4 ? r0 : r1)[(cyl + corner_y(b)) * kTcHaloX + cxl + corner_x(b)];
-        xv[3 * b + 0] = v.x;
-        xv[3 * b + 1] = v.y;
-        xv[3 * b + 2] = v.z;
+        const int e = (b < 4 ? s0 : s1) + (cyl + corner_y(b)) * kTcHaloX + cxl + corner_x(b);
+        const float4 u = ring_a[e];
+        const float2 w = ring_b[e];
+        hv[3 * b + 0] = u.x;
+        hv[3 * b + 1] = u.y;
+        hv[3 * b + 2] = u.z;
+        lv[3 * b + 0] = u.w;
+        lv[3 * b + 1] = w.x;
+        lv[3 * b + 2] = w.y;
       }
 #pragma unroll
       for (int g = 0; g < 6; ++g) {
-        uint32_t hi[4], lo[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          hi[q] = tc::tf32_round(xv[4 * g + q]);
-          lo[q] = tc::tf32_round(xv[4 * g + q] - __uint_as_float(hi[q]));
-        }
-        *reinterpret_cast<uint4*>(arow + g * kTcALbo) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4*>(arow + kTcAPart + g * kTcALbo) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        *reinterpret_cast<float4*>(arow + g * kTcALbo) =
+            make_float4(hv[4 * g], hv[4 * g + 1], hv[4 * g + 2], hv[4 * g + 3]);
+        *reinterpret_cast<float4*>(arow + (6 + g) * kTcALbo) =
+            make_float4(lv[4 * g], lv[4 * g + 1], lv[4 * g + 2], lv[4 * g + 3]);
       }
     }
     tc::fence_proxy_async_smem();
     __syncthreads();
-    // 2. F = A K^T for the two 128-cell tiles (3 x TF32); descriptors advance
-    // by (byte offset >> 4) in their start-address field
+    // 2. D = A B^T for the two 128-cell tiles (six K = 8 steps each);
+    // descriptors advance by (byte offset >> 4) in their start-address field
     if (tid == 0) {
       tc::fence_after_sync();
 #pragma unroll
       for (int mt = 0; mt < 2; ++mt) {
-        const uint32_t d = tmem + static_cast<uint32_t>(mt * 32);
+        const uint32_t d = tmem + static_cast<uint32_t>(mt * 64);
 #pragma unroll
-        for (int s = 0; s < 3; ++s) {
+        for (int s = 0; s < 6; ++s) {
           const uint64_t ao = static_cast<uint64_t>((s * 2 * kTcALbo + mt * 16 * 128) >> 4);
           const uint64_t bo = static_cast<uint64_t>((s * 2 * kTcBLbo) >> 4);
-          const uint64_t ahi = a_desc + ao, alo = a_desc + ao + (kTcAPart >> 4);
-          const uint64_t bhi = b_desc + bo, blo = b_desc + bo + (kTcBPart >> 4);
-          tc::mma_tf32(d, alo, bhi, idesc, s > 0 ? 1u : 0u);
-          tc::mma_tf32(d, ahi, blo, idesc, 1u);
-          tc::mma_tf32(d, ahi, bhi, idesc, 1u);
+          tc::mma_tf32(d, a_desc + ao, b_desc + bo, idesc, s > 0 ? 1u : 0u);
         }
       }
       tc::mma_commit(bar);
     }
-    // meanwhile: the sums of node layer cz - 1, and the loads of later layers
-    // (node values of layer cz + 3 enter the ring after this iteration's
-    // second barrier, so the next iteration's first barrier orders them
-    // before the A rows of iteration it + 2 read them)
-    if (it >= 2) node_sum(it);
+    // meanwhile: the node layer below the last cell layer, the partial sums
+    // of the one above it, and the loads of later layers
+    if (it >= 2) finish();
+    if (it >= 1) start();
     const bool more = it + 3 <= ncl;  // node layer cz + 3 is still read
     float4 pv[kTcHaloPer];
     if (more) values(hj, pv);
@@ -286,31 +314,32 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     if (it >= 2) {
       I_cur = I_next;
       I_next = node_of(nz0 + it);  // summed in iteration it + 2
-      if (I_cur >= 0) mf_node_load<MODE>(a, I_cur, in_cur);  // summed in iteration it + 1
+      if (I_cur >= 0) load_node(I_cur, in_cur, self_cur);  // summed in iteration it + 1
     }
     // 3. wait for the MMA (one thread), then every thread's row of F
     if (tid == 0) ok = tc::mbar_wait(bar, static_cast<uint32_t>(it & 1), status);
     if (__syncthreads_or(!ok)) break;
     tc::fence_after_sync();
     {
-      float fv[24];
-      tc::tmem_ld24(tmem + (static_cast<uint32_t>((warp & 3) * 32) << 16) + static_cast<uint32_t>((warp >> 2) * 32),
-                    fv);
-      float* top = f1 + (it & 1) * 12 * kTcThreads;
+      uint32_t r[48];
+      tc::tmem_ld48_start(tmem + (static_cast<uint32_t>((warp & 3) * 32) << 16) +
+                              static_cast<uint32_t>((warp >> 2) * 64),
+                          r);
+      if (more) put((it + 3) % kTcRing, pv);
+      tc::tmem_ld48_wait(r);
 #pragma unroll
       for (int jj = 0; jj < 12; ++jj) {
-        f0[jj * kTcThreads + tid] = s_cur * fv[jj];
-        top[jj * kTcThreads + tid] = s_cur * fv[12 + jj];
+        fb[jj * kTcThreads + tid] = s_cur * (__uint_as_float(r[jj]) + __uint_as_float(r[jj + 24]));
+        ft[jj * kTcThreads + tid] = s_cur * (__uint_as_float(r[12 + jj]) + __uint_as_float(r[36 + jj]));
       }
     }
-    if (more) put((it + 3) % kTcRing, pv);
     s_cur = s_next;
     tc::fence_before_sync();
   }
   if (it == ncl) {
     // the last node layer, nz1 - 1
     __syncthreads();
-    node_sum(it);
+    finish();
   } else if (tid == 0) {
     tc::mbar_wait(bar, static_cast<uint32_t>(it & 1), nullptr);  // the MMA in flight
   }
