@@ -177,11 +177,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const i32 cgx = gx0 - 1 + cxl, cgy = gy0 - 1 + cyl;
   const i64 c2d = (cgx >= 0 && cgx < m.nx && cgy >= 0 && cgy < m.ny) ? static_cast<i64>(cgy) * m.nx + cgx : -1;
   auto scale_of = [&](i32 cz) { return (c2d >= 0 && cz >= 0 && cz < m.nz) ? m.scale[cz * cell_layer + c2d] : 0.0f; };
-  // this thread's node of the sums (threads < 217): in-layer offset or -1;
-  // its free index and epilogue operands are loaded two and one iterations
-  // ahead of its sum
-  const int nxl = tid % kTcNodesX, nyl = tid / kTcNodesX;
-  const i64 n2d = (tid < kTcNodesX * kTcNodesY && gx0 + nxl < m.nnx && gy0 + nyl < m.nny)
+  // this thread's node of the sums (threads 32 .. 248, so warp 0, whose
+  // thread 0 issues the MMAs, has none): in-layer offset or -1; its free
+  // index and epilogue operands are loaded two and one iterations ahead of
+  // its sum
+  const int nt = tid - 32;
+  const int nxl = nt % kTcNodesX, nyl = nt / kTcNodesX;
+  const i64 n2d = (nt >= 0 && nt < kTcNodesX * kTcNodesY && gx0 + nxl < m.nnx && gy0 + nyl < m.nny)
                       ? static_cast<i64>(gy0 + nyl) * m.nnx + gx0 + nxl
                       : -1;
   auto node_of = [&](i32 L) { return (n2d >= 0 && L >= nz0 && L < nz1) ? m.nindex[L * node_layer + n2d] : -1; };
