@@ -323,9 +323,7 @@ class GpuAmg {
   uint64_t epoch_ = 1;  // bumped by every setup: captured graphs are stale
   void compute_stats();
   void tune_level0();
-  void tune_df();
-  int df_whole_ = 1;  // load schedule of the double-float level-0 operator (tuned)
-  void df_apply(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream, int whole);
+  void df_apply(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream);
 };
 
 }  // namespace simp

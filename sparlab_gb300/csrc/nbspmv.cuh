@@ -20,7 +20,6 @@ namespace simp {
 namespace {
 
 constexpr int kUnroll = 4;  // row steps whose loads a lane issues before their products
-constexpr int kRowSteps = 11;  // double-float rows of up to VS * 11 entries load all steps at once
 
 // Column of entry w of a row: column-free decode (B > 0) or the column array.
 template <int B>
@@ -150,11 +149,7 @@ __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __
 // double-float arithmetic on the FP32 pipes, y in FP64.  About 2^-44 relative
 // to the FP64 product, at FP32 instruction rates: bandwidth bound where the
 // FP64 kernel is bound by GB300's FP64 rate.  mode 0: y = A x ; 1: y = b - A x.
-// WHOLE: a lane issues the loads of all its steps of a row (up to kRowSteps)
-// before the first product -- two memory round trips per row instead of two
-// per kUnroll steps, at more registers; the products run in the same order
-// either way, so both variants give the same bits (the tuner picks one).
-template <int VS, int B, int MODE, bool WHOLE>
+template <int VS, int B, int MODE>
 __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ node_of, NodeView pat,
                                                        const i32* __restrict__ rowptr, const i32* __restrict__ col,
                                                        const float2* __restrict__ v, const float2* __restrict__ x,
@@ -170,25 +165,6 @@ __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ n
     const i32* cl = col + k0;
     const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
     i32 w = lane;
-    if (WHOLE && len <= VS * kRowSteps) {
-      // the whole row in flight: every step's value and column, then every
-      // x gather, then the products in the same order as the loop below
-      float2 hv[kRowSteps], xv[kRowSteps];
-      i32 cw[kRowSteps];
-#pragma unroll
-      for (int u = 0; u < kRowSteps; ++u)
-        if (lane + u * VS < len) {
-          hv[u] = vp[lane + u * VS];
-          cw[u] = row_col<B>(lane + u * VS, s0, pat.nbr, cl);
-        }
-#pragma unroll
-      for (int u = 0; u < kRowSteps; ++u)
-        if (lane + u * VS < len) xv[u] = x[cw[u]];
-#pragma unroll
-      for (int u = 0; u < kRowSteps; ++u)
-        if (lane + u * VS < len) df_fma(hv[u].x, hv[u].y, xv[u].x, xv[u].y, sh, sl);
-      w = len;
-    }
     for (; w + (kUnroll - 1) * VS < len; w += kUnroll * VS) {
       float2 hv[kUnroll];
       float2 xv[kUnroll];
@@ -301,6 +277,94 @@ __global__ void __launch_bounds__(256) k_rows_apply_df_multi(const i32* __restri
       sl[k] = __fadd_rn(sl[k], __fadd_rn(ol, e));
     }
     if (row < rows && lane == 0) m.y[k][row] = static_cast<double>(sh[k]) + static_cast<double>(sl[k]);
+  }
+}
+
+// The double-float operator node by node, where every column node has 3
+// unknowns and so every row node's 3 rows share one column list, stored
+// back to back (level 0 of a 3-D grid whose nodes are fully free or
+// clamped).  A warp owns a row node; its lanes stride over the columns and
+// load each column's slot record and x pair once for the three rows (the
+// row kernel loads them once per row), all of a lane's columns (up to
+// kNodeSteps) before the first product.  Per row the products are summed
+// in double-float arithmetic, then by a fixed 32-lane butterfly.  Up to NV
+// right-hand sides (m.n of them; a fused multi-RHS launch gates each by its
+// flag, as k_rows_apply_df_multi does); mode 0: y_k = A x_k, mode 1 (one
+// right-hand side): y = b - A x.
+constexpr int kNodeSteps = 3;  // columns a lane holds in flight (rows of up to 96 entries in one pass)
+
+template <int NV, int MODE>
+__global__ void __launch_bounds__(256) k_nodes_apply_df(i32 nodes, const i32* __restrict__ row_first, NodeView pat,
+                                                        const i32* __restrict__ rowptr,
+                                                        const float2* __restrict__ v,
+                                                        const __grid_constant__ MultiRhs m,
+                                                        const double* __restrict__ b) {
+  const i64 gw = (blockIdx.x * static_cast<i64>(blockDim.x) + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= nodes) return;  // the whole warp
+  const i32 I = static_cast<i32>(gw);
+  const i32 r0 = row_first[I];
+  bool on[NV];
+  float sh[NV][3], sl[NV][3];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    on[k] = k < m.n && (m.active[k] == nullptr || *m.active[k] != 0);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) sh[k][r] = sl[k][r] = 0.0f;
+  }
+  const i32 len = rowptr[r0 + 1] - rowptr[r0];
+  const float2* vr[3] = {v + rowptr[r0], v + rowptr[r0 + 1], v + rowptr[r0 + 2]};
+  const i32 s0 = pat.ptr[I];
+  for (i32 w = lane; w < len; w += kNodeSteps * 32) {
+    i32 cw[kNodeSteps];
+    float2 hv[kNodeSteps][3];
+#pragma unroll
+    for (int u = 0; u < kNodeSteps; ++u) {
+      const i32 q = w + u * 32;
+      if (q < len) {
+        cw[u] = row_col<3>(q, s0, pat.nbr, nullptr);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) hv[u][r] = vr[r][q];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      if (!on[k]) continue;
+      float2 xv[kNodeSteps];
+#pragma unroll
+      for (int u = 0; u < kNodeSteps; ++u)
+        if (w + u * 32 < len) xv[u] = m.x[k][cw[u]];
+#pragma unroll
+      for (int u = 0; u < kNodeSteps; ++u)
+        if (w + u * 32 < len) {
+#pragma unroll
+          for (int r = 0; r < 3; ++r) df_fma(hv[u][r].x, hv[u][r].y, xv[u].x, xv[u].y, sh[k][r], sl[k][r]);
+        }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    if (!on[k]) continue;  // the same for every lane
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, sh[k][r], o);
+        const float ol = __shfl_xor_sync(0xffffffffu, sl[k][r], o);
+        float s, e;
+        two_sum(sh[k][r], oh, s, e);
+        sh[k][r] = s;
+        sl[k][r] = __fadd_rn(sl[k][r], __fadd_rn(ol, e));
+      }
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const double y = static_cast<double>(sh[k][r]) + static_cast<double>(sl[k][r]);
+        if (MODE == 0) m.y[k][r0 + r] = y;
+        else m.y[k][r0 + r] = b[r0 + r] - y;
+      }
+    }
   }
 }
 
