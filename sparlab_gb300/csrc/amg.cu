@@ -1600,6 +1600,13 @@ __global__ void k_arm(cudaGraphConditionalHandle h, cudaGraphConditionalHandle h
   if (two) cudaGraphSetConditional(h2, v);
 }
 
+// Sets a fused operator's conditional: on while any of its systems iterates.
+__global__ void k_arm_any(cudaGraphConditionalHandle h, const int* __restrict__ l0, const int* __restrict__ l1,
+                          const int* __restrict__ l2, const int* __restrict__ l3) {
+  const bool on = (l0 && l0[0] != 0) || (l1 && l1[0] != 0) || (l2 && l2[0] != 0) || (l3 && l3[0] != 0);
+  cudaGraphSetConditional(h, on ? 1u : 0u);
+}
+
 // After an iteration body: count the iteration and apply GpuAmg::pcg's test
 // (no breakdown, sqrt(||r||^2) above the stopping norm, budget left); the
 // flag is the host's view of whether the system iterates on, flag[n] counts
@@ -1629,7 +1636,8 @@ struct TogetherGraph {
   std::vector<std::pair<GpuAmg*, SolveWork*>> members;
   std::vector<uint64_t> epochs;
   std::vector<int64_t> kernels;  // kernels of each member's body (without a fused operator)
-  int64_t fused_nodes = 0;       // fused operator launches per graph launch
+  int64_t fused_nodes = 0;       // fused operators (one arm kernel each per graph launch)
+  std::vector<std::vector<int>> fused_members;  // members of each fused operator
   cudaGraphExec_t exec = nullptr;
   cudaStream_t stream = nullptr;
   DBuf<int> flags;
@@ -1685,6 +1693,7 @@ struct TogetherGraph {
     flags.alloc(2 * n);  // [0, n) iterate-on flags, [n, 2n) bodies run
     kernels.assign(n, 0);
     fused_nodes = 0;
+    fused_members.clear();
     epochs.clear();
     // pairs whose CG operator is fused: double-float operators of a hierarchy
     // that two or more pairs share, in member order
@@ -1747,11 +1756,36 @@ struct TogetherGraph {
           const size_t c1 = std::min(grp.size(), c0 + kMaxRhs);
           std::vector<SolveWork*> ws;
           std::vector<cudaGraphNode_t> deps;
+          const int* loops[kMaxRhs] = {nullptr, nullptr, nullptr, nullptr};
+          fused_members.emplace_back();
           for (size_t c = c0; c < c1; ++c) {
             ws.push_back(members[grp[c]].second);
             deps.push_back(first[grp[c]]);
+            loops[c - c0] = members[grp[c]].second->loop.p;
+            fused_members.back().push_back(static_cast<int>(grp[c]));
           }
-          cudaGraphNode_t op = a.add_op0_multi(g, ws, deps);
+          // the fused launch runs only while one of its systems iterates
+          cudaGraphConditionalHandle hf;
+          SIMP_CUDA(cudaGraphConditionalHandleCreate(&hf, g, 0, 0));
+          void* aargs[] = {&hf, &loops[0], &loops[1], &loops[2], &loops[3]};
+          cudaGraphNodeParams ap = {};
+          ap.type = cudaGraphNodeTypeKernel;
+          ap.kernel.func = reinterpret_cast<void*>(k_arm_any);
+          ap.kernel.gridDim = dim3(1);
+          ap.kernel.blockDim = dim3(1);
+          ap.kernel.sharedMemBytes = 0;
+          ap.kernel.kernelParams = aargs;
+          ap.kernel.extra = nullptr;
+          cudaGraphNode_t arm_f = nullptr;
+          SIMP_CUDA(cudaGraphAddNode(&arm_f, g, deps.data(), nullptr, deps.size(), &ap));
+          cudaGraphNodeParams cp = {};
+          cp.type = cudaGraphNodeTypeConditional;
+          cp.conditional.handle = hf;
+          cp.conditional.type = cudaGraphCondTypeIf;
+          cp.conditional.size = 1;
+          cudaGraphNode_t op = nullptr;
+          SIMP_CUDA(cudaGraphAddNode(&op, g, &arm_f, nullptr, 1, &cp));
+          a.add_op0_multi(cp.conditional.phGraph_out[0], ws, {});
           ++fused_nodes;
           for (size_t c = c0; c < c1; ++c) {
             const size_t i = grp[c];
@@ -1961,6 +1995,12 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
         SIMP_CUDA(cudaMemcpyAsync(hf.data(), tg.flags.p, sizeof(int) * 2 * m, cudaMemcpyDeviceToHost, tg.stream));
         SIMP_CUDA(cudaStreamSynchronize(tg.stream));
         int64_t launched = static_cast<int64_t>(per_check) * (tg.fused_nodes + static_cast<int64_t>(m));
+        // a fused operator ran in every launch in which one of its systems ran a body
+        for (const auto& fm : tg.fused_members) {
+          int most = 0;
+          for (int k : fm) most = std::max(most, hf[m + k] - seen[k]);
+          launched += most;
+        }
         alive = 0;
         for (size_t k = 0; k < m; ++k) {
           launched += static_cast<int64_t>(hf[m + k] - seen[k]) * tg.kernels[k];
