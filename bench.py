@@ -775,11 +775,8 @@ def run_own(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": (f"k_rows_apply<4,{spec.dim},0,double> (level-0 K_ff operator of the CG, "
                                 "FP64 values; FP64-pipe bound on GB300)" if args.precision == "fp64" else
-                                ("k_nodes_apply_df<1,0> (level-0 K_ff operator of the CG, a warp per "
-                                 "node's three rows, double-float values and arithmetic on the FP32 pipes)"
-                                 if spec.dim == 3 else
-                                 "k_rows_apply_df<8,2,0> (level-0 K_ff operator of the CG, double-float "
-                                 "values and arithmetic on the FP32 pipes)")),
+                                f"k_rows_apply_df<8,{spec.dim},0> (level-0 K_ff operator of the CG, "
+                                "double-float values and arithmetic on the FP32 pipes)"),
                      "bytes_per_launch": alg_bytes, "ms_per_launch": kms,
                      "peak_kind": f"{peak_kind} hbm_gbs (burst copy)"},
         "cpu_baseline": cpu,

@@ -541,25 +541,10 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
   df_apply(xsplit, y, rhs, stream);
 }
 
-// The double-float level-0 product: node by node where every node has 3
-// unknowns (k_nodes_apply_df), otherwise row by row (k_rows_apply_df).
+// The double-float level-0 product, row by row (k_rows_apply_df).
 void GpuAmg::df_apply(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream) {
   Level& l0 = *levels.front();
   const NbOp& op = l0.opA;
-  if (op.block == 3) {
-    MultiRhs m{};
-    m.n = 1;
-    m.x[0] = xsplit;
-    m.y[0] = y;
-    const unsigned grid = static_cast<unsigned>((static_cast<i64>(op.nodes) * 32 + 255) / 256);
-    if (rhs)
-      k_nodes_apply_df<1, 1><<<grid, 256, 0, stream>>>(op.nodes, op.row_first, op.pat, op.rowptr, l0.a.v2.p, m, rhs);
-    else
-      k_nodes_apply_df<1, 0><<<grid, 256, 0, stream>>>(op.nodes, op.row_first, op.pat, op.rowptr, l0.a.v2.p, m,
-                                                        nullptr);
-    SIMP_CHECK_LAUNCH();
-    return;
-  }
   with_shape<float>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     const unsigned grid = rows_grid(op, VS);
@@ -585,25 +570,6 @@ cudaGraphNode_t GpuAmg::add_op0_multi(cudaGraph_t g, const std::vector<SolveWork
     m.active[k] = ws[k]->loop.p;
   }
   cudaGraphNode_t node = nullptr;
-  if (op.block == 3) {
-    i32 nodes = op.nodes;
-    const i32* row_first = op.row_first;
-    NodeView pat = op.pat;
-    const i32* rowptr = op.rowptr;
-    const float2* v = l0.a.v2.p;
-    const double* b = nullptr;
-    void* args[] = {&nodes, &row_first, &pat, &rowptr, &v, &m, &b};
-    cudaGraphNodeParams kp = {};
-    kp.type = cudaGraphNodeTypeKernel;
-    kp.kernel.func = reinterpret_cast<void*>(&k_nodes_apply_df<kMaxRhs, 0>);
-    kp.kernel.gridDim = dim3(static_cast<unsigned>((static_cast<i64>(op.nodes) * 32 + 255) / 256));
-    kp.kernel.blockDim = dim3(256);
-    kp.kernel.sharedMemBytes = 0;
-    kp.kernel.kernelParams = args;
-    kp.kernel.extra = nullptr;
-    SIMP_CUDA(cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &kp));
-    return node;
-  }
   with_shape<float>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     const i32* node_of = op.node_of;
@@ -693,14 +659,12 @@ void GpuAmg::time_operator(int reps, double* ms, double* bytes) {
   cudaEventDestroy(e1);
   *ms = t / std::max(reps, 1);
   // values, then the index data the kernel reads: one slot record per block
-  // with the column-free decode (else a column per value), row pointers, the
-  // row -> node map (row kernel) or node -> first row map (node kernel) and
-  // node pointers; then x once and y once
+  // with the column-free decode (else a column per value), row pointers,
+  // row -> node map and node pointers; then x once and y once
   const double index = l0.opA.block > 0 ? static_cast<double>(l0.apat.slots()) * 4.0
                                         : static_cast<double>(l0.a.nnz) * 4.0;
-  const double map = l0.opA.block == 3 ? static_cast<double>(l0.nnodes + 1) * 4.0 : static_cast<double>(n) * 4.0;
-  *bytes = static_cast<double>(l0.a.nnz) * 8.0 + index + static_cast<double>(n + 1) * 4.0 + map +
-           static_cast<double>(l0.nnodes + 1) * 4.0 + 2.0 * static_cast<double>(n) * 8.0;
+  *bytes = static_cast<double>(l0.a.nnz) * 8.0 + index + static_cast<double>(n + 1) * 4.0 +
+           static_cast<double>(n) * 4.0 + static_cast<double>(l0.nnodes + 1) * 4.0 + 2.0 * static_cast<double>(n) * 8.0;
 }
 
 void GpuAmg::refresh_level0_fp32() {

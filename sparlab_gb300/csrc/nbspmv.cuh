@@ -280,93 +280,5 @@ __global__ void __launch_bounds__(256) k_rows_apply_df_multi(const i32* __restri
   }
 }
 
-// The double-float operator node by node, where every column node has 3
-// unknowns and so every row node's 3 rows share one column list, stored
-// back to back (level 0 of a 3-D grid whose nodes are fully free or
-// clamped).  A warp owns a row node; its lanes stride over the columns and
-// load each column's slot record and x pair once for the three rows (the
-// row kernel loads them once per row), all of a lane's columns (up to
-// kNodeSteps) before the first product.  Per row the products are summed
-// in double-float arithmetic, then by a fixed 32-lane butterfly.  Up to NV
-// right-hand sides (m.n of them; a fused multi-RHS launch gates each by its
-// flag, as k_rows_apply_df_multi does); mode 0: y_k = A x_k, mode 1 (one
-// right-hand side): y = b - A x.
-constexpr int kNodeSteps = 3;  // columns a lane holds in flight (rows of up to 96 entries in one pass)
-
-template <int NV, int MODE>
-__global__ void __launch_bounds__(256) k_nodes_apply_df(i32 nodes, const i32* __restrict__ row_first, NodeView pat,
-                                                        const i32* __restrict__ rowptr,
-                                                        const float2* __restrict__ v,
-                                                        const __grid_constant__ MultiRhs m,
-                                                        const double* __restrict__ b) {
-  const i64 gw = (blockIdx.x * static_cast<i64>(blockDim.x) + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (gw >= nodes) return;  // the whole warp
-  const i32 I = static_cast<i32>(gw);
-  const i32 r0 = row_first[I];
-  bool on[NV];
-  float sh[NV][3], sl[NV][3];
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    on[k] = k < m.n && (m.active[k] == nullptr || *m.active[k] != 0);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) sh[k][r] = sl[k][r] = 0.0f;
-  }
-  const i32 len = rowptr[r0 + 1] - rowptr[r0];
-  const float2* vr[3] = {v + rowptr[r0], v + rowptr[r0 + 1], v + rowptr[r0 + 2]};
-  const i32 s0 = pat.ptr[I];
-  for (i32 w = lane; w < len; w += kNodeSteps * 32) {
-    i32 cw[kNodeSteps];
-    float2 hv[kNodeSteps][3];
-#pragma unroll
-    for (int u = 0; u < kNodeSteps; ++u) {
-      const i32 q = w + u * 32;
-      if (q < len) {
-        cw[u] = row_col<3>(q, s0, pat.nbr, nullptr);
-#pragma unroll
-        for (int r = 0; r < 3; ++r) hv[u][r] = vr[r][q];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      if (!on[k]) continue;
-      float2 xv[kNodeSteps];
-#pragma unroll
-      for (int u = 0; u < kNodeSteps; ++u)
-        if (w + u * 32 < len) xv[u] = m.x[k][cw[u]];
-#pragma unroll
-      for (int u = 0; u < kNodeSteps; ++u)
-        if (w + u * 32 < len) {
-#pragma unroll
-          for (int r = 0; r < 3; ++r) df_fma(hv[u][r].x, hv[u][r].y, xv[u].x, xv[u].y, sh[k][r], sl[k][r]);
-        }
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    if (!on[k]) continue;  // the same for every lane
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float oh = __shfl_xor_sync(0xffffffffu, sh[k][r], o);
-        const float ol = __shfl_xor_sync(0xffffffffu, sl[k][r], o);
-        float s, e;
-        two_sum(sh[k][r], oh, s, e);
-        sh[k][r] = s;
-        sl[k][r] = __fadd_rn(sl[k][r], __fadd_rn(ol, e));
-      }
-    }
-    if (lane == 0) {
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        const double y = static_cast<double>(sh[k][r]) + static_cast<double>(sl[k][r]);
-        if (MODE == 0) m.y[k][r0 + r] = y;
-        else m.y[k][r0 + r] = b[r0 + r] - y;
-      }
-    }
-  }
-}
-
 }  // namespace
 }  // namespace simp
