@@ -1564,6 +1564,11 @@ __global__ void k_arm(cudaGraphConditionalHandle h, cudaGraphConditionalHandle h
   if (two) cudaGraphSetConditional(h2, v);
 }
 
+// K_ff size (double-float value pairs, bytes) from which the CG products of
+// load cases sharing a hierarchy are fused in the lock-step graph (GB300's
+// L2 holds 126 MB)
+constexpr double kFuseBytes = 128.0 * 1024 * 1024;
+
 // Sets a fused operator's conditional: on while any of its systems iterates.
 __global__ void k_arm_any(cudaGraphConditionalHandle h, const int* __restrict__ l0, const int* __restrict__ l1,
                           const int* __restrict__ l2, const int* __restrict__ l3) {
@@ -1660,12 +1665,17 @@ struct TogetherGraph {
     fused_members.clear();
     epochs.clear();
     // pairs whose CG operator is fused: double-float operators of a hierarchy
-    // that two or more pairs share, in member order
+    // that two or more pairs share, in member order, where K_ff's value pairs
+    // do not fit in L2 (kFuseBytes): reading them once per launch instead of
+    // once per system then saves DRAM traffic, while below that size the
+    // values stay in L2 and the join of the systems' bodies at the fused
+    // launch costs more concurrency than it saves
     std::vector<std::vector<size_t>> groups;
     std::vector<char> fused(n, 0);
     for (size_t i = 0; i < n; ++i) {
       GpuAmg* a = members[i].first;
       if (!a->mixed() || a->mf_cg()) continue;
+      if (static_cast<double>(a->levels.front()->a.nnz) * 8.0 < kFuseBytes) continue;
       bool placed = false;
       for (auto& grp : groups)
         if (members[grp.front()].first == a) {

@@ -52,24 +52,26 @@ def test_load_cases_in_one_graph_match_one_after_another(precision):
 
 
 def test_five_load_cases_with_fused_operators_match_one_after_another():
-    """Five load cases of one Hex8 problem in mixed precision: in the graph
-    the cases' CG products run as fused multi-RHS launches over the shared
-    double-float K_ff (four cases per launch, so two launches), and every
-    iteration's compliance, iteration count and OC multiplier equal the
-    one-after-another solves bit for bit."""
-    spec = P.hex8_cantilever(24, 12, 12, 0.3, "five_loads")
+    """Five load cases of one Hex8 problem in mixed precision whose K_ff
+    (double-float value pairs) exceeds L2, so that in the graph the cases'
+    CG products run as fused multi-RHS launches over the shared K_ff (four
+    cases per launch, so two launches): every iteration's compliance,
+    iteration count and OC multiplier equal the one-after-another solves bit
+    for bit."""
+    spec = P.hex8_cantilever(64, 36, 36, 0.3, "five_loads")   # K_ff 20.3 M values, 155 MiB
     loads = []
     for i in range(5):
         rng = P.SplitMix64(9, i)
-        j, k = int(rng.uniform(0.0, 12.99)), int(rng.uniform(0.0, 12.99))
+        j, k = int(rng.uniform(0.0, 36.99)), int(rng.uniform(0.0, 36.99))
         t = np.radians(rng.uniform(-90.0, 90.0))
-        loads.append(P.point_load(spec, [spec.node_index(24, j, k)], (0.0, np.sin(t), -np.cos(t))))
+        loads.append(P.point_load(spec, [spec.node_index(64, j, k)], (0.0, np.sin(t), -np.cos(t))))
     spec.loads = np.stack(loads)
     spec.weights = np.full(5, 0.2)
     spec.rtol = 1e-10
     out = {}
     for mode in (False, "graph"):
         gpu = GpuSimpProblem(spec, precision="mixed", block_pcg=mode)
+        assert gpu.nnz * 8 >= 128 * 1024 * 1024   # the fused launches apply from this size
         out[mode] = rows([gpu.iterate() for _ in range(3)])
         gpu.close()
     assert out["graph"] == out[False]
