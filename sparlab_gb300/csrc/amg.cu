@@ -1954,16 +1954,16 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
       for (size_t i : idx) members.emplace_back(tasks[i].amg, tasks[i].w);
       std::lock_guard<std::mutex> lock(g_together_mu);
       TogetherGraph& tg = together_graph(members);
-      // several launches per host check: a system that has stopped runs no
-      // body (its conditionals stay false), so the extra launches change
-      // nothing; the bodies that ran are counted on the device
+      // one launch per host check (several launches per check measured
+      // slower: the launches after a system stops still run every member's
+      // arm and conditional); the bodies that ran are counted on the device
       const size_t m = idx.size();
       std::vector<int> hf(2 * m, 1);
       std::vector<int> active(m, 1);
       size_t alive = m;
       SIMP_CUDA(cudaMemsetAsync(tg.flags.p + m, 0, sizeof(int) * m, tg.stream));
       std::vector<int> seen(m, 0);
-      int per_check = 1;
+      const int per_check = 1;
       while (alive > 0) {
         for (int r = 0; r < per_check; ++r) SIMP_CUDA(cudaGraphLaunch(tg.exec, tg.stream));
         SIMP_CUDA(cudaMemcpyAsync(hf.data(), tg.flags.p, sizeof(int) * 2 * m, cudaMemcpyDeviceToHost, tg.stream));
@@ -1983,7 +1983,6 @@ std::vector<GpuAmg::TaskResult> GpuAmg::solve_together(std::vector<SolveTask>& t
           alive += active[k] ? 1 : 0;
         }
         g_launches.fetch_add(launched, std::memory_order_relaxed);
-        per_check = std::min(per_check * 2, 4);
       }
       for (size_t k = 0; k < idx.size(); ++k) {
         const size_t i = idx[k];
