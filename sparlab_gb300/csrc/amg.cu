@@ -59,16 +59,29 @@ __global__ void k_expand_columns(i32 n, const i32* __restrict__ node_of, NodeVie
 
 namespace {
 
-// w = s .* w - beta vp (beta from device memory); nothing once stopped
+// w = s .* w - beta vp (beta from device memory); nothing once stopped.
+// FP64 vectors: FP64 arithmetic; FP32 vectors (the reuse setups): FP32
+// arithmetic, with beta rounded to FP32 (GB300 runs FP64 at 1/64 of the
+// FP32 rate, so conversions and FP64 operations per element would bound
+// these vector passes)
 template <class T>
 __global__ void k_lanczos_finish(T* __restrict__ w, const T* __restrict__ s, const T* __restrict__ vp,
                                  const double* __restrict__ beta, const double* __restrict__ stop, i64 n) {
   if (*stop != 0.0) return;
   const double bj = vp ? *beta : 0.0;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
-    double wi = todbl(w[i]) * todbl(s[i]);
-    if (vp) wi -= bj * todbl(vp[i]);
-    w[i] = static_cast<T>(wi);
+  if constexpr (std::is_same<T, float>::value) {
+    const float bf = static_cast<float>(bj);
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+      float wi = w[i] * s[i];
+      if (vp) wi = fmaf(-bf, vp[i], wi);
+      w[i] = wi;
+    }
+  } else {
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+      double wi = todbl(w[i]) * todbl(s[i]);
+      if (vp) wi -= bj * todbl(vp[i]);
+      w[i] = static_cast<T>(wi);
+    }
   }
 }
 

@@ -12,6 +12,8 @@
 
 #include "common.h"
 
+#include <type_traits>
+
 #include <cuda_runtime.h>
 
 namespace simp {
@@ -131,8 +133,17 @@ __global__ void __launch_bounds__(kRedThreads) k_dot_partial(const TA* __restric
                                                              const TB* __restrict__ b, i64 n,
                                                              double* __restrict__ part) {
   double s = 0.0;
-  for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads)
-    s += todbl(a[i]) * todbl(b[i]);
+  if constexpr (std::is_same<TA, float>::value && std::is_same<TB, float>::value) {
+    // FP32 vectors (the reuse setups' Lanczos): each thread's products summed
+    // in FP32 before the FP64 block sum (no per-element FP64 work)
+    float sf = 0.0f;
+    for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads)
+      sf = fmaf(a[i], b[i], sf);
+    s = static_cast<double>(sf);
+  } else {
+    for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads)
+      s += todbl(a[i]) * todbl(b[i]);
+  }
   s = block_sum<kRedThreads>(s);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
@@ -253,10 +264,23 @@ __global__ void __launch_bounds__(kRedThreads) k_axpy_norm(T* __restrict__ w, co
                                                            double* __restrict__ part) {
   const double a = *a_dev;
   double s = 0.0;
-  for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads) {
-    const T wi = static_cast<T>(todbl(w[i]) - a * todbl(v[i]));
-    w[i] = wi;
-    s += todbl(wi) * todbl(wi);
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 vectors: FP32 update, each thread's squares summed in FP32 before
+    // the FP64 block sum (no per-element FP64 work)
+    const float af = static_cast<float>(a);
+    float sf = 0.0f;
+    for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads) {
+      const float wi = fmaf(-af, v[i], w[i]);
+      w[i] = wi;
+      sf = fmaf(wi, wi, sf);
+    }
+    s = static_cast<double>(sf);
+  } else {
+    for (i64 i = blockIdx.x * (i64)kRedThreads + threadIdx.x; i < n; i += (i64)gridDim.x * kRedThreads) {
+      const T wi = static_cast<T>(todbl(w[i]) - a * todbl(v[i]));
+      w[i] = wi;
+      s += todbl(wi) * todbl(wi);
+    }
   }
   s = block_sum<kRedThreads>(s);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
@@ -270,11 +294,25 @@ __global__ void k_lanczos_shift(T* __restrict__ v, T* __restrict__ vp, const T* 
                                 const double* __restrict__ b, const double* __restrict__ stop, i64 n) {
   if (*stop != 0.0) return;
   const double bj = *b;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
-    vp[i] = v[i];
-    const T vi = static_cast<T>(todbl(w[i]) / bj);
-    v[i] = vi;
-    tmp[i] = static_cast<T>(todbl(s[i]) * todbl(vi));
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 vectors: FP32 arithmetic with 1 / beta formed once per block
+    __shared__ float inv_b;
+    if (threadIdx.x == 0) inv_b = static_cast<float>(1.0 / bj);
+    __syncthreads();
+    const float ib = inv_b;
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+      vp[i] = v[i];
+      const float vi = w[i] * ib;
+      v[i] = vi;
+      tmp[i] = s[i] * vi;
+    }
+  } else {
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+      vp[i] = v[i];
+      const T vi = static_cast<T>(todbl(w[i]) / bj);
+      v[i] = vi;
+      tmp[i] = static_cast<T>(todbl(s[i]) * todbl(vi));
+    }
   }
 }
 
