@@ -621,8 +621,6 @@ def run_own(args):
     sur, sur_info = (train_surrogate(args, local) if learned else (None, None))
 
     tc = {} if args.tensor_cores is None else {"tensor_cores": args.tensor_cores}
-    if args.coarse_bf16 is not None:
-        tc["coarse_bf16"] = args.coarse_bf16
 
     def make(precision, with_surrogate=True):
         p = GpuSimpProblem(spec, precision=precision, device=local, block_pcg=together, **tc)
@@ -753,7 +751,6 @@ def run_own(args):
                 "warm_start": "learned" if learned else spec_warm_name(spec.warm_start),
                 "nnz_kff": prob.nnz, "replicas": world,
                 "level0_tensor_cores": int(prob.options.tensor_cores),
-                "coarse_bf16": int(prob.options.coarse_bf16),
                 "load_case_solves": ("one graph, fused multi-RHS CG operator" if together == "graph" else
                                      "concurrent" if together else "sequential"),
                 "l2": ("working set (K_ff %.2f GB) larger than the 129 MB L2" % (nnz * 12 / 1e9)
@@ -817,9 +814,6 @@ def main():
     ap.add_argument("--tensor-cores", type=int, default=None, choices=[0, 1],
                     help="matrix-free level 0 on the tensor cores (1) or on FP32 FMAs (0); "
                          "default: the library's default")
-    ap.add_argument("--coarse-bf16", type=int, default=None, choices=[0, 1],
-                    help="V-cycle operators of levels 1 .. L-2 read BF16 copies of their values (1) or "
-                         "FP32 (0); default: the library's default")
     ap.add_argument("--graph-loads", action="store_true",
                     help="advance a multi-load workload's load cases together in one CUDA graph, "
                          "their CG products as one multi-RHS launch over the shared K_ff")

@@ -88,11 +88,6 @@ typedef struct {
                                     TF32 tensor-core GEMMs, operands split hi + lo (3 x TF32,
                                     FP32 accumulation: about FP32 accuracy); 0 FP32 FMAs on
                                     the CUDA cores */
-  int32_t coarse_bf16;           /* MIXED: 1 the FP32 V-cycle's smoothers and residuals on
-                                    levels 1 .. L-2 read BF16 copies of those levels' values
-                                    (half the bytes; Galerkin products, Lanczos estimates
-                                    and the coarsest inverse keep FP32 / FP64); 0 (default)
-                                    FP32 values */
 } simp_solver_options;
 
 typedef struct {

@@ -53,7 +53,7 @@ class SolverOptions(C.Structure):
                 ("reuse_aggregates", C.c_int32), ("iterative_tolerance", C.c_double),
                 ("max_iterations", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32),
                 ("cuda_graphs", C.c_int32), ("matrix_free_transfer", C.c_int32),
-                ("matrix_free", C.c_int32), ("tensor_cores", C.c_int32), ("coarse_bf16", C.c_int32)]
+                ("matrix_free", C.c_int32), ("tensor_cores", C.c_int32)]
 
 
 class AmgStats(C.Structure):

@@ -127,23 +127,23 @@ void nb_apply(const NbOp& op, const TV* val, const TX* x, TX* y, const TX* b, cu
   SIMP_CHECK_LAUNCH();
 }
 
-template <class T, class TV = T>
-void nb_cheb_step(const NbOp& op, const TV* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
+template <class T>
+void nb_cheb_step(const NbOp& op, const T* val, const T* d, const T* rin, T* r, T* dn, T* x, const T* dinv,
                   const T* c12, int add_d, cudaStream_t s) {
   with_shape<T>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
-    k_rows_cheb_step<VS, B, T, TV><<<rows_grid(op, VS), 256, 0, s>>>(
+    k_rows_cheb_step<VS, B, T><<<rows_grid(op, VS), 256, 0, s>>>(
         op.rows, op.node_of, op.pat, op.rowptr, op.col, val, d, rin, r, dn, x, dinv, c12, add_d);
   });
   SIMP_CHECK_LAUNCH();
 }
 
-template <class T, class TV = T>
-void nb_cheb_first(const NbOp& op, const TV* val, const T* x, const T* b, T* r, T* d, const T* dinv,
+template <class T>
+void nb_cheb_first(const NbOp& op, const T* val, const T* x, const T* b, T* r, T* d, const T* dinv,
                    const T* inv_theta, cudaStream_t s) {
   with_shape<T>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
-    k_rows_cheb_first<VS, B, T, TV><<<rows_grid(op, VS), 256, 0, s>>>(
+    k_rows_cheb_first<VS, B, T><<<rows_grid(op, VS), 256, 0, s>>>(
         op.rows, op.node_of, op.pat, op.rowptr, op.col, val, x, b, r, d, dinv, inv_theta);
   });
   SIMP_CHECK_LAUNCH();
@@ -386,13 +386,6 @@ int tc_layers_of(const MfOp& mf, int variant) {
   i64 chunks = std::max<i64>(1, (static_cast<i64>(per_sm[variant]) * sms + xy / 2) / xy);
   chunks = std::min(chunks, nnz);
   return static_cast<int>((nnz + chunks - 1) / chunks);
-}
-
-// The FP32 cycle reads level l's BF16 values (coarse_bf16): they exist for
-// levels 1 .. L-2 of a mixed hierarchy.
-template <class T>
-bool half_values(const Level& lv) {
-  return std::is_same<T, float>::value && lv.a.v16.p != nullptr;
 }
 
 double seconds_since(std::chrono::steady_clock::time_point t0) {
@@ -1241,17 +1234,6 @@ void GpuAmg::setup(bool structure_changed) {
   }
   levels.resize(l + 1);
   for (size_t k = 0; k < levels.size(); ++k) make_ops(k);
-  // BF16 copies of the V-cycle's operators on levels 1 .. L-2
-  for (size_t k = 1; k + 1 < levels.size(); ++k) {
-    DevCsr& a = levels[k]->a;
-    if (mixed() && opt.coarse_bf16) {
-      a.v16.alloc(static_cast<size_t>(a.nnz));
-      k_convert<float, __nv_bfloat16><<<grid_for(a.nnz, 256, 8192), 256, 0, stream>>>(a.v32.p, a.v16.p, a.nnz);
-      SIMP_CHECK_LAUNCH();
-    } else {
-      a.v16.release();
-    }
-  }
   coarse_factorize();
   ensure(main_);
   for (auto& w : extra_) ensure(*w);
@@ -1348,11 +1330,6 @@ void GpuAmg::smooth(SolveWork& w, size_t l, bool zero_guess) {
   } else if (matrix_free) {
     if constexpr (std::is_same<T, float>::value)
       mf_cheb_first(mf, lv.nnodes, x, b, r, d, dinv, lv.cheb32.p, stream);
-  } else if (half_values<T>(lv)) {
-    nb_cheb_first<float, __nv_bfloat16>(lv.opA, lv.a.v16.p, reinterpret_cast<const float*>(x),
-                                        reinterpret_cast<const float*>(b), reinterpret_cast<float*>(r),
-                                        reinterpret_cast<float*>(d), reinterpret_cast<const float*>(dinv),
-                                        reinterpret_cast<const float*>(V<T>::cheb(lv)), stream);
   } else {
     nb_cheb_first<T>(lv.opA, A, x, b, r, d, dinv, V<T>::cheb(lv), stream);
   }
@@ -1362,12 +1339,6 @@ void GpuAmg::smooth(SolveWork& w, size_t l, bool zero_guess) {
     if (matrix_free) {
       if constexpr (std::is_same<T, float>::value)
         mf_cheb_step(mf, lv.nnodes, d, rin, r, e, x, dinv, lv.cheb32.p + 2 * k - 1, add_d, stream);
-    } else if (half_values<T>(lv)) {
-      nb_cheb_step<float, __nv_bfloat16>(lv.opA, lv.a.v16.p, reinterpret_cast<const float*>(d),
-                                         reinterpret_cast<const float*>(rin), reinterpret_cast<float*>(r),
-                                         reinterpret_cast<float*>(e), reinterpret_cast<float*>(x),
-                                         reinterpret_cast<const float*>(dinv),
-                                         reinterpret_cast<const float*>(V<T>::cheb(lv) + 2 * k - 1), add_d, stream);
     } else {
       nb_cheb_step<T>(lv.opA, A, d, rin, r, e, x, dinv, V<T>::cheb(lv) + 2 * k - 1, add_d, stream);
     }
@@ -1403,10 +1374,6 @@ void GpuAmg::cycle(SolveWork& w, size_t l) {
   if (matrix_free) {  // residual
     if constexpr (std::is_same<T, float>::value)
       mf_residual(mf, lv.nnodes, V<T>::x(v), V<T>::r(v), V<T>::b(v), stream);
-  } else if (half_values<T>(lv)) {
-    nb_apply<1, __nv_bfloat16, float, float>(lv.opA, lv.a.v16.p, reinterpret_cast<const float*>(V<T>::x(v)),
-                                             reinterpret_cast<float*>(V<T>::r(v)),
-                                             reinterpret_cast<const float*>(V<T>::b(v)), stream);
   } else {
     nb_apply<1, T, T, T>(lv.opA, V<T>::a(lv.a), V<T>::x(v), V<T>::r(v), V<T>::b(v), stream);
   }

@@ -16,8 +16,6 @@
 #include "common.h"
 #include "structure.h"
 
-#include <cuda_bf16.h>
-
 #include <memory>
 #include <string>
 #include <vector>
@@ -45,10 +43,6 @@ struct AmgOptions {
   int matrix_free = 1;
   // the 3-D matrix-free level 0 on the tensor cores (3 x TF32 element GEMMs)
   int tensor_cores = 0;
-  // mixed: the FP32 V-cycle's operators of levels 1 .. L-2 read BF16 copies
-  // of their values (half the bytes; the Galerkin products, Lanczos and the
-  // coarsest inverse keep FP32 / FP64)
-  int coarse_bf16 = 0;
 };
 
 struct DevPattern {
@@ -64,7 +58,6 @@ struct DevCsr {
   DBuf<double> v64;
   DBuf<float> v32;
   DBuf<float2> v2;    // level 0, mixed: (v32, v64 - v32) pairs, interleaved (the double-float CG operator)
-  DBuf<__nv_bfloat16> v16;  // levels 1 .. L-2, mixed with coarse_bf16: the V-cycle's copy of v32
 };
 
 // A node-chunked matrix as the operator kernels see it (see nbspmv.cuh).

@@ -41,7 +41,6 @@ AmgOptions convert(const simp_solver_options* o) {
   a.mf_transfer = o->matrix_free_transfer != 0;
   a.matrix_free = o->matrix_free;
   a.tensor_cores = o->tensor_cores;
-  a.coarse_bf16 = o->coarse_bf16;
   return a;
 }
 
@@ -59,7 +58,6 @@ void validate(const AmgOptions& o) {
     throw Error(kBadInput, "unknown precision mode");
   if (o.matrix_free < 0 || o.matrix_free > 2) throw Error(kBadInput, "matrix_free must be 0, 1 or 2");
   if (o.tensor_cores < 0 || o.tensor_cores > 1) throw Error(kBadInput, "tensor_cores must be 0 or 1");
-  if (o.coarse_bf16 < 0 || o.coarse_bf16 > 1) throw Error(kBadInput, "coarse_bf16 must be 0 or 1");
 }
 
 template <class F>
@@ -154,7 +152,6 @@ void simp_default_options(simp_solver_options* o) {
   o->matrix_free_transfer = 1;
   o->matrix_free = 1;
   o->tensor_cores = 0;
-  o->coarse_bf16 = 0;
 }
 
 int simp_ctx_create(const simp_solver_options* opts, simp_ctx** out) {

@@ -14,8 +14,6 @@
 // traffic is one slot record per block.
 #pragma once
 
-#include <cuda_bf16.h>
-
 #include "kernels.cuh"
 
 namespace simp {
@@ -102,10 +100,10 @@ __device__ __forceinline__ TX rows_dot(i32 row, int lane, bool valid, const i32*
 // Chebyshev step: r = r_in - A d ; dn = c1 d + c2 dinv r ; x = (x [+ d]) + dn,
 // (c1, c2) = c12[0..1] in device memory (the level's coefficients change with
 // every setup; a captured launch keeps reading them)
-template <int VS, int B, class T, class TV = T>
+template <int VS, int B, class T>
 __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __restrict__ node_of, NodeView pat,
                                                         const i32* __restrict__ rowptr, const i32* __restrict__ col,
-                                                        const TV* __restrict__ val, const T* __restrict__ d,
+                                                        const T* __restrict__ val, const T* __restrict__ d,
                                                         const T* __restrict__ r_in, T* __restrict__ r,
                                                         T* __restrict__ dn, T* __restrict__ x,
                                                         const T* __restrict__ dinv, const T* __restrict__ c12,
@@ -114,7 +112,7 @@ __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __r
   const i32 row = static_cast<i32>(t / VS);
   const int lane = static_cast<int>(t % VS);
   const bool valid = row < rows;
-  const T s = rows_dot<VS, B, TV, T>(row, lane, valid, node_of, pat, rowptr, col, val, d);
+  const T s = rows_dot<VS, B, T, T>(row, lane, valid, node_of, pat, rowptr, col, val, d);
   if (valid && lane == 0) {
     const T ri = r_in[row] - s;
     r[row] = ri;
@@ -127,10 +125,10 @@ __global__ void __launch_bounds__(256) k_rows_cheb_step(i32 rows, const i32* __r
 }
 
 // r = b - A x ; d = dinv r / theta (1 / theta = *inv_theta, device memory)
-template <int VS, int B, class T, class TV = T>
+template <int VS, int B, class T>
 __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __restrict__ node_of, NodeView pat,
                                                          const i32* __restrict__ rowptr, const i32* __restrict__ col,
-                                                         const TV* __restrict__ val, const T* __restrict__ x,
+                                                         const T* __restrict__ val, const T* __restrict__ x,
                                                          const T* __restrict__ b, T* __restrict__ r,
                                                          T* __restrict__ d, const T* __restrict__ dinv,
                                                          const T* __restrict__ inv_theta) {
@@ -138,7 +136,7 @@ __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __
   const i32 row = static_cast<i32>(t / VS);
   const int lane = static_cast<int>(t % VS);
   const bool valid = row < rows;
-  const T s = rows_dot<VS, B, TV, T>(row, lane, valid, node_of, pat, rowptr, col, val, x);
+  const T s = rows_dot<VS, B, T, T>(row, lane, valid, node_of, pat, rowptr, col, val, x);
   if (valid && lane == 0) {
     const T ri = b[row] - s;
     r[row] = ri;

@@ -75,7 +75,6 @@ def test_element_stiffness_matches_oracle(dim, h):
     ("precision", 7, "precision"),
     ("matrix_free", 3, "matrix_free"),
     ("tensor_cores", 2, "tensor_cores"),
-    ("coarse_bf16", 2, "coarse_bf16"),
 ])
 def test_context_creation_rejects_bad_options_before_touching_the_device(field, value, words):
     """AmgPreconditioner's option checks (src/fem/Multigrid.cpp:907-925;
