@@ -57,8 +57,33 @@ __device__ __forceinline__ void df_fma(float ah, float al, float bh, float bl, f
   sl = __fadd_rn(sl, __fadd_rn(e, pe));
 }
 
-// hi = fl32(v), lo = fl32(v - hi)
+// hi = fl32(v), lo = fl32(v - hi), both rounded to nearest even.  Where
+// both halves are normal floats (v's exponent field in [949, 1149]: |v| in
+// [2^-74, 2^127)), from v's bits with integer operations -- GB300 runs FP64
+// conversions and arithmetic at 1/64 of its FP32 rate -- and otherwise by
+// FP64 conversion.  The 53-bit significand M splits into its top 24 bits K
+// and low 29 bits R; K rounds to nearest even on R (a carry out of K moves
+// into the float exponent field), and v - hi is the remainder r = R or
+// R - 2^29 in units of 2^(e - 1075), which one int -> float conversion
+// rounds to 24 bits and a power of two scales exactly.
 __device__ __forceinline__ void df_split(double v, float& hi, float& lo) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(v));
+  const int e = static_cast<int>((u >> 52) & 0x7FFull);
+  if (e >= 949 && e <= 1149) {
+    const unsigned long long m = (u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    unsigned k = static_cast<unsigned>(m >> 29);
+    const int rr = static_cast<int>(m & 0x1FFFFFFFull);
+    int r = rr;
+    if (rr > 0x10000000 || (rr == 0x10000000 && (k & 1u))) {
+      k += 1u;
+      r = rr - 0x20000000;
+    }
+    const bool neg = (u >> 63) != 0;
+    const unsigned bits = (static_cast<unsigned>(neg) << 31) | ((static_cast<unsigned>(e - 896) << 23) + (k - 0x800000u));
+    hi = __uint_as_float(bits);
+    lo = __int2float_rn(neg ? -r : r) * __uint_as_float(static_cast<unsigned>(e - 948) << 23);
+    return;
+  }
   hi = __double2float_rn(v);
   lo = __double2float_rn(v - static_cast<double>(hi));
 }
@@ -228,8 +253,9 @@ __global__ void k_pcg_direction(double* __restrict__ p, const double* __restrict
     const double v = z[i] + beta * p[i];
     p[i] = v;
     if (ps) {
-      const float h = __double2float_rn(v);
-      ps[i] = make_float2(h, __double2float_rn(v - static_cast<double>(h)));
+      float h, l;
+      df_split(v, h, l);
+      ps[i] = make_float2(h, l);
     }
     if (p32) p32[i] = __double2float_rn(v);
   }
