@@ -95,9 +95,9 @@ __global__ void k_lanczos_check(const double* __restrict__ ab, int j, double* __
 // its column nodes (column-free decode) or 0, VS = the lanes per row chosen
 // for the arithmetic type.
 template <class TA, class F>
-void with_shape(const NbOp& op, F&& f) {
+void with_shape(const NbOp& op, F&& f, int lanes_override = 0) {
   auto lanes = [&](auto b) {
-    switch (std::is_same<TA, double>::value ? op.lanes64 : op.lanes32) {
+    switch (lanes_override > 0 ? lanes_override : (std::is_same<TA, double>::value ? op.lanes64 : op.lanes32)) {
       case 32: f(std::integral_constant<int, 32>{}, b); break;
       case 8: f(std::integral_constant<int, 8>{}, b); break;
       default: f(std::integral_constant<int, 4>{}, b); break;
@@ -567,7 +567,7 @@ void GpuAmg::df_apply(const float2* xsplit, double* y, const double* rhs, cudaSt
     else
       k_rows_apply_df<VS, B, 0><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col, l0.a.v2.p, xsplit, y,
                                                           nullptr, op.rows);
-  });
+  }, op.lanes_df);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -601,7 +601,7 @@ cudaGraphNode_t GpuAmg::add_op0_multi(cudaGraph_t g, const std::vector<SolveWork
     kp.kernel.kernelParams = args;
     kp.kernel.extra = nullptr;
     SIMP_CUDA(cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &kp));
-  });
+  }, op.lanes_df);
   return node;
 }
 

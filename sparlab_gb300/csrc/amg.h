@@ -71,6 +71,7 @@ struct NbOp {
   const i32* node_of = nullptr; // row -> row node
   i32 rows = 0;
   int lanes32 = 8, lanes64 = 4; // lanes per row of the FP32 / FP64 kernels
+  int lanes_df = 8;             // lanes per row of the double-float kernels (level 0)
 };
 
 // Shared-memory shape of a warp-per-row-node product (galerkin.cuh).
