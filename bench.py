@@ -707,7 +707,7 @@ def run_own(args):
     # the plain FP64 loop (the reference's warm start) on the same iterations,
     # for the metric's plain-vs-learned+mixed ratio and the compliance bar;
     # with the learned start also the mixed loop without it
-    plain = mixed_only = None
+    plain = mixed_only = mixed_projected = None
     plain_first = None
     if args.precision == "mixed" and not args.no_plain and world == 1:
         if learned:
@@ -717,6 +717,15 @@ def run_own(args):
                           "cg_iterations_per_step": [r.linear_iterations for r in mrec],
                           "max_rel_compliance_diff": max(abs(a.compliance / b.compliance - 1)
                                                          for a, b in zip(recs, mrec))}
+            # the learned start without the network: the energy-optimal start
+            # over the displacement history alone (what the prediction adds)
+            spec.warm_start = WARM["projection"]
+            _, jrec, jms = timed_run("mixed", False)
+            mixed_projected = {"value": args.steps / (jms * 1e-3), "unit": "iter/s",
+                               "ms_per_step": jms / args.steps,
+                               "cg_iterations_per_step": [r.linear_iterations for r in jrec],
+                               "max_rel_compliance_diff": max(abs(a.compliance / b.compliance - 1)
+                                                              for a, b in zip(recs, jrec))}
         spec.warm_start = WARM["previous"]
         plain_first, prec, pms = timed_run("fp64", False)
         plain = {"value": args.steps / (pms * 1e-3), "unit": "iter/s", "ms_per_step": pms / args.steps,
@@ -767,6 +776,7 @@ def run_own(args):
                 "surrogate_seconds_in_timed_steps": round(learned_s, 4) if learned else None,
                 "surrogate": sur_info,
                 "mixed_previous_start": mixed_only,
+                "mixed_projected_start_without_network": mixed_projected,
                 "autotune": {k: {"chosen": v[0], "ms": [round(t, 4) for t in v[1]]}
                              for k, v in _lib.autotune_report().items()},
                 "plain_fp64": plain,
