@@ -785,7 +785,7 @@ def run_own(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": (f"k_rows_apply<4,{spec.dim},0,double> (level-0 K_ff operator of the CG, "
                                 "FP64 values; FP64-pipe bound on GB300)" if args.precision == "fp64" else
-                                f"k_rows_apply_df<8,{spec.dim},0> (level-0 K_ff operator of the CG, "
+                                f"k_rows_apply_df<4,{spec.dim},0> (level-0 K_ff operator of the CG, "
                                 "double-float values and arithmetic on the FP32 pipes)"),
                      "bytes_per_launch": alg_bytes, "ms_per_launch": kms,
                      "peak_kind": f"{peak_kind} hbm_gbs (burst copy)"},
