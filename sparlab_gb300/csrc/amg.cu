@@ -554,21 +554,50 @@ void GpuAmg::op0(SolveWork& w, const double* x, double* y, const double* rhs, bo
   df_apply(xsplit, y, rhs, stream);
 }
 
-// The double-float level-0 product, row by row (k_rows_apply_df).
+// The double-float level-0 product, row by row (k_rows_apply_df), with the
+// tuned unroll (df_unroll_: 4 or 8 row steps in flight per lane, the same
+// bits).
 void GpuAmg::df_apply(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream) {
+  df_apply_unroll(xsplit, y, rhs, stream, df_unroll_);
+}
+
+void GpuAmg::df_apply_unroll(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream, int unroll) {
   Level& l0 = *levels.front();
   const NbOp& op = l0.opA;
   with_shape<float>(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     const unsigned grid = rows_grid(op, VS);
-    if (rhs)
-      k_rows_apply_df<VS, B, 1><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col, l0.a.v2.p, xsplit, y,
-                                                          rhs, op.rows);
-    else
-      k_rows_apply_df<VS, B, 0><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col, l0.a.v2.p, xsplit, y,
-                                                          nullptr, op.rows);
+    auto go = [&](auto ur) {
+      constexpr int U = decltype(ur)::value;
+      if (rhs)
+        k_rows_apply_df<VS, B, 1, U><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col, l0.a.v2.p,
+                                                               xsplit, y, rhs, op.rows);
+      else
+        k_rows_apply_df<VS, B, 0, U><<<grid, 256, 0, stream>>>(op.node_of, op.pat, op.rowptr, op.col, l0.a.v2.p,
+                                                               xsplit, y, nullptr, op.rows);
+    };
+    if (unroll == 8) go(std::integral_constant<int, 8>{});
+    else go(std::integral_constant<int, 4>{});
   }, op.lanes_df);
   SIMP_CHECK_LAUNCH();
+}
+
+// The double-float operator's unroll for this level 0: the faster of 4 and
+// 8 row steps in flight per lane on y = A x (the same bits), before the
+// first CUDA graph capture of a structure.
+void GpuAmg::tune_df() {
+  if (!mixed() || mf_cg()) return;
+  Level& l0 = *levels.front();
+  const i32 n = l0.n;
+  DBuf<float2> xs(static_cast<size_t>(n));
+  DBuf<double> ys(static_cast<size_t>(n));
+  SIMP_CUDA(cudaMemsetAsync(xs.p, 0, sizeof(float2) * n, stream));
+  std::ostringstream key;
+  key << "df0:" << n << "x" << l0.a.nnz << "x" << l0.opA.lanes_df;
+  const int v = tune_pick(key.str(), 2, [&](int c) { df_apply_unroll(xs.p, ys.p, nullptr, stream, c ? 8 : 4); },
+                          stream, 0, 5);
+  df_unroll_ = v ? 8 : 4;
+  SIMP_CUDA(cudaStreamSynchronize(stream));
 }
 
 cudaGraphNode_t GpuAmg::add_op0_multi(cudaGraph_t g, const std::vector<SolveWork*>& ws,
@@ -1237,7 +1266,10 @@ void GpuAmg::setup(bool structure_changed) {
   coarse_factorize();
   ensure(main_);
   for (auto& w : extra_) ensure(*w);
-  if (!reuse) tune_level0();
+  if (!reuse) {
+    tune_level0();
+    tune_df();
+  }
   ready_ = true;
   // captured iteration bodies stay valid across reuse setups: their launches
   // take only workspace and level pointers, which a reuse setup keeps

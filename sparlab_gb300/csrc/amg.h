@@ -327,7 +327,10 @@ class GpuAmg {
   uint64_t epoch_ = 1;  // bumped by every setup: captured graphs are stale
   void compute_stats();
   void tune_level0();
+  void tune_df();
+  int df_unroll_ = 4;  // row steps in flight per lane of the double-float operator (tuned)
   void df_apply(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream);
+  void df_apply_unroll(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream, int unroll);
 };
 
 }  // namespace simp

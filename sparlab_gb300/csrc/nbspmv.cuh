@@ -149,7 +149,10 @@ __global__ void __launch_bounds__(256) k_rows_cheb_first(i32 rows, const i32* __
 // double-float arithmetic on the FP32 pipes, y in FP64.  About 2^-44 relative
 // to the FP64 product, at FP32 instruction rates: bandwidth bound where the
 // FP64 kernel is bound by GB300's FP64 rate.  mode 0: y = A x ; 1: y = b - A x.
-template <int VS, int B, int MODE>
+// UNROLL: row steps whose loads a lane issues before their products (the
+// products run in the same order for every UNROLL, so all give the same
+// bits; the launch-shape tuner picks one).
+template <int VS, int B, int MODE, int UNROLL = kUnroll>
 __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ node_of, NodeView pat,
                                                        const i32* __restrict__ rowptr, const i32* __restrict__ col,
                                                        const float2* __restrict__ v, const float2* __restrict__ x,
@@ -165,16 +168,16 @@ __global__ void __launch_bounds__(256) k_rows_apply_df(const i32* __restrict__ n
     const i32* cl = col + k0;
     const i32 s0 = B > 0 ? pat.ptr[node_of[row]] : 0;
     i32 w = lane;
-    for (; w + (kUnroll - 1) * VS < len; w += kUnroll * VS) {
-      float2 hv[kUnroll];
-      float2 xv[kUnroll];
+    for (; w + (UNROLL - 1) * VS < len; w += UNROLL * VS) {
+      float2 hv[UNROLL];
+      float2 xv[UNROLL];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
+      for (int u = 0; u < UNROLL; ++u) {
         hv[u] = vp[w + u * VS];
         xv[u] = x[row_col<B>(w + u * VS, s0, pat.nbr, cl)];
       }
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) df_fma(hv[u].x, hv[u].y, xv[u].x, xv[u].y, sh, sl);
+      for (int u = 0; u < UNROLL; ++u) df_fma(hv[u].x, hv[u].y, xv[u].x, xv[u].y, sh, sl);
     }
     for (; w < len; w += VS) {
       const float2 xv = x[row_col<B>(w, s0, pat.nbr, cl)];

@@ -1,7 +1,7 @@
 """The launch-shape tuner changes speed, never results: every tile shape of
-the matrix-free operator (both halo layouts) and every Galerkin launch
-variant give the same iteration history bit for bit, and the tuner records
-its choices."""
+the matrix-free operator (both halo layouts), every Galerkin launch
+variant and both unrolls of the double-float CG operator give the same
+iteration history bit for bit, and the tuner records its choices."""
 import ctypes as C
 
 import pytest
@@ -28,12 +28,16 @@ def test_every_launch_shape_gives_the_same_iterations():
     report = _lib.autotune_report()
     mf_keys = [k for k in report if k.startswith("mf3:29x15x14")]
     row_keys = [k for k in report if "_rows" in k]
-    assert mf_keys and row_keys
+    df_keys = [k for k in report if k.startswith("df0:")]
+    assert mf_keys and row_keys and df_keys
     assert len(report[mf_keys[0]][1]) == 10           # five tile shapes x two halo layouts timed
+    assert len(report[df_keys[0]][1]) == 2            # the CG operator's two unrolls timed
     for v in range(10):
         lib.simp_autotune_set(mf_keys[0].encode(), C.c_int32(v))
         for k in row_keys:
             lib.simp_autotune_set(k.encode(), C.c_int32(v % 4))
+        for k in df_keys:
+            lib.simp_autotune_set(k.encode(), C.c_int32(v % 2))
         assert history() == base, v
     lib.simp_autotune_enable(0)
     try:
