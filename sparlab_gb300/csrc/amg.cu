@@ -95,10 +95,29 @@ __global__ void k_lanczos_check(const double* __restrict__ ab, int j, double* __
 // its column nodes (column-free decode) or 0, VS = the lanes per row chosen
 // for the arithmetic type.
 template <class TA, class F>
-void with_shape(const NbOp& op, F&& f, int lanes_override = 0) {
+void with_shape(const NbOp& op, F&& f) {
   auto lanes = [&](auto b) {
-    switch (lanes_override > 0 ? lanes_override : (std::is_same<TA, double>::value ? op.lanes64 : op.lanes32)) {
+    switch (std::is_same<TA, double>::value ? op.lanes64 : op.lanes32) {
       case 32: f(std::integral_constant<int, 32>{}, b); break;
+      case 8: f(std::integral_constant<int, 8>{}, b); break;
+      default: f(std::integral_constant<int, 4>{}, b); break;
+    }
+  };
+  switch (op.block) {
+    case 2: lanes(std::integral_constant<int, 2>{}); break;
+    case 3: lanes(std::integral_constant<int, 3>{}); break;
+    case 6: lanes(std::integral_constant<int, 6>{}); break;
+    default: lanes(std::integral_constant<int, 0>{}); break;
+  }
+}
+
+// The double-float operator's shape: its own lanes per row (2, 4 or 8) and
+// the column-node width.
+template <class F>
+void with_shape_df(const NbOp& op, F&& f) {
+  auto lanes = [&](auto b) {
+    switch (op.lanes_df) {
+      case 2: f(std::integral_constant<int, 2>{}, b); break;
       case 8: f(std::integral_constant<int, 8>{}, b); break;
       default: f(std::integral_constant<int, 4>{}, b); break;
     }
@@ -564,7 +583,7 @@ void GpuAmg::df_apply(const float2* xsplit, double* y, const double* rhs, cudaSt
 void GpuAmg::df_apply_unroll(const float2* xsplit, double* y, const double* rhs, cudaStream_t stream, int unroll) {
   Level& l0 = *levels.front();
   const NbOp& op = l0.opA;
-  with_shape<float>(op, [&](auto vs, auto blk) {
+  with_shape_df(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     const unsigned grid = rows_grid(op, VS);
     auto go = [&](auto ur) {
@@ -578,7 +597,7 @@ void GpuAmg::df_apply_unroll(const float2* xsplit, double* y, const double* rhs,
     };
     if (unroll == 8) go(std::integral_constant<int, 8>{});
     else go(std::integral_constant<int, 4>{});
-  }, op.lanes_df);
+  });
   SIMP_CHECK_LAUNCH();
 }
 
@@ -612,7 +631,7 @@ cudaGraphNode_t GpuAmg::add_op0_multi(cudaGraph_t g, const std::vector<SolveWork
     m.active[k] = ws[k]->loop.p;
   }
   cudaGraphNode_t node = nullptr;
-  with_shape<float>(op, [&](auto vs, auto blk) {
+  with_shape_df(op, [&](auto vs, auto blk) {
     constexpr int VS = decltype(vs)::value, B = decltype(blk)::value;
     const i32* node_of = op.node_of;
     NodeView pat = op.pat;
@@ -630,7 +649,7 @@ cudaGraphNode_t GpuAmg::add_op0_multi(cudaGraph_t g, const std::vector<SolveWork
     kp.kernel.kernelParams = args;
     kp.kernel.extra = nullptr;
     SIMP_CUDA(cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &kp));
-  }, op.lanes_df);
+  });
   return node;
 }
 
