@@ -270,9 +270,9 @@ void mf3_tc(const MfOp& mf, const MfArgs& a, const KeF32& ke, cudaStream_t s) {
   SIMP_CHECK_LAUNCH();
 }
 
-// The tiled matrix-free kernel in the variant the tuner chose (mf.tile:
-// shape kMfTileShape[tile % 5], float4 halo for tile >= 5; every variant
-// gives the same values), or the
+// The tiled matrix-free kernel in the variant the tuner chose for the mode
+// (mf.tile[MODE]: shape kMfTileShape[tile % 5], float4 halo for tile >= 5;
+// every variant gives the same values), or the
 // tensor-core kernel (mf.tensor).
 template <int MODE>
 void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
@@ -283,8 +283,9 @@ void mf3(const MfOp& mf, const MfArgs& a, cudaStream_t s) {
     return;
   }
   static_assert(kMfTiles == 10, "tile table");
-  const bool v4 = mf.tile >= 5;
-  switch (mf.tile % 5) {
+  const int tile = mf.tile[MODE];
+  const bool v4 = tile >= 5;
+  switch (tile % 5) {
     case 1: mf3_shape<MODE, 32, 8, 1>(mf, a, ke, s, v4); break;
     case 2: mf3_shape<MODE, 32, 2, 4>(mf, a, ke, s, v4); break;
     case 3: mf3_shape<MODE, 64, 2, 2>(mf, a, ke, s, v4); break;
@@ -1327,18 +1328,44 @@ void GpuAmg::tune_level0() {
     check_mf_status(stream);
     return;
   }
-  std::ostringstream key;
-  key << "mf3:" << mf.nnx << "x" << mf.nny << "x" << (mf.nz + 1);
-  mf.tile = tune_pick(key.str(), kMfTiles,
-                      [&](int v) {
-                        MfOp m = mf;
-                        m.tile = v;
-                        MfArgs a{};
-                        a.x = tx.p;
-                        a.y = ty.p;
-                        mf3<0>(m, a, stream);
-                      },
-                      stream, 0, 5);
+  // each mode's epilogue reads and writes different vectors: tune each one
+  // on scratch vectors (the values do not matter to the timing)
+  DBuf<float> tb(static_cast<size_t>(n)), tr(static_cast<size_t>(n)), td(static_cast<size_t>(n)),
+      ts(static_cast<size_t>(n)), coef(2);
+  DBuf<double> t64(static_cast<size_t>(n));
+  for (DBuf<float>* v : {&tb, &tr, &td, &ts})
+    k_fill<float><<<grid_for(n, 256), 256, 0, stream>>>(v->p, 1.0f, n);
+  k_fill<float><<<1, 32, 0, stream>>>(coef.p, 0.5f, 2);
+  SIMP_CHECK_LAUNCH();
+  MfArgs a{};
+  a.x = tx.p;
+  a.y = ty.p;
+  a.b = tb.p;
+  a.r = tr.p;
+  a.dn = td.p;
+  a.xs = ts.p;
+  a.dinv = tb.p;
+  a.coef = coef.p;
+  a.y64 = t64.p;
+  auto tune_mode = [&](int mode, auto launch) {
+    std::ostringstream key;
+    key << "mf3:" << mf.nnx << "x" << mf.nny << "x" << (mf.nz + 1) << ":m" << mode;
+    mf.tile[mode] = tune_pick(key.str(), kMfTiles,
+                              [&](int v) {
+                                MfOp m = mf;
+                                m.tile[mode] = v;
+                                launch(m);
+                              },
+                              stream, 0, 5);
+  };
+  tune_mode(0, [&](const MfOp& m) { mf3<0>(m, a, stream); });
+  tune_mode(1, [&](const MfOp& m) { mf3<1>(m, a, stream); });
+  tune_mode(3, [&](const MfOp& m) { mf3<3>(m, a, stream); });
+  tune_mode(4, [&](const MfOp& m) { mf3<4>(m, a, stream); });
+  tune_mode(5, [&](const MfOp& m) { mf3<5>(m, a, stream); });
+  tune_mode(6, [&](const MfOp& m) { mf3<6>(m, a, stream); });
+  tune_mode(7, [&](const MfOp& m) { mf3<7>(m, a, stream); });
+  if (mf_cg()) tune_mode(8, [&](const MfOp& m) { mf3<8>(m, a, stream); });
   SIMP_CUDA(cudaStreamSynchronize(stream));
 }
 

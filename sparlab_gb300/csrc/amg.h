@@ -141,7 +141,9 @@ struct MfOp {
   const float* ke = nullptr;    // K_e^0, FP32
   const float* scale = nullptr; // s_e, FP32
   float ke_host[24 * 24] = {};  // K_e^0, FP32 (kernel parameter of the tiled 3-D kernel)
-  int tile = 0;                 // variant of the tiled 3-D kernel: shape kMfTileShape[tile % 5], float4 halo if >= 5 (tuned)
+  // variant of the tiled 3-D kernel per mode (0..8): shape
+  // kMfTileShape[tile % 5], float4 halo if >= 5 (tuned per mode)
+  int tile[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   const double* scale64 = nullptr;  // s_e, FP64 (the matrix-free CG operator's true residuals)
   double ke64_host[24 * 24] = {};   // K_e^0, FP64
   bool tensor = false;     // 3-D: the tensor-core kernel (mfree_tc.cuh) instead of the tiled FMA kernel

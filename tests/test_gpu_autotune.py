@@ -30,10 +30,12 @@ def test_every_launch_shape_gives_the_same_iterations():
     row_keys = [k for k in report if "_rows" in k]
     df_keys = [k for k in report if k.startswith("df0:")]
     assert mf_keys and row_keys and df_keys
+    assert len(mf_keys) >= 7                          # one key per mode of the operator
     assert len(report[mf_keys[0]][1]) == 10           # five tile shapes x two halo layouts timed
     assert len(report[df_keys[0]][1]) == 2            # the CG operator's two unrolls timed
     for v in range(10):
-        lib.simp_autotune_set(mf_keys[0].encode(), C.c_int32(v))
+        for k in mf_keys:
+            lib.simp_autotune_set(k.encode(), C.c_int32(v))
         for k in row_keys:
             lib.simp_autotune_set(k.encode(), C.c_int32(v % 4))
         for k in df_keys:
