@@ -453,14 +453,13 @@ void GpuProblem::assemble_into(const double* elem, const double* scale, bool exa
                                float2* pair, cudaStream_t stream) {
   Level& l0 = *amg.levels.front();
   if (l0.nnodes == 0) return;
-  const int offsets = d.dim == 3 ? 27 : 9;
   const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
   const size_t smem = assemble_smem(d.dim);
   auto kernel = exact ? k_assemble_tiles<true, false> : k_assemble_tiles<false, false>;
   raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
-  kernel<<<blocks, offsets * kAsmTile, smem, stream>>>(grid_of(d), l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
-                                                       nmask.p, l0.d_apat.view(), l0.a.ptr.p, elem, scale, nullptr,
-                                                       nullptr, v64, hi, pair);
+  kernel<<<blocks, assemble_threads(d.dim), smem, stream>>>(grid_of(d), l0.nnodes, l0.d_first.p, gnode.p, cmask.p,
+                                                            nmask.p, l0.d_apat.view(), l0.a.ptr.p, elem, scale,
+                                                            nullptr, nullptr, v64, hi, pair);
   SIMP_CHECK_LAUNCH();
 }
 
@@ -468,14 +467,14 @@ void GpuProblem::assemble(const double* scale, bool exact) {
   Level& l0 = *amg.levels.front();
   if (l0.nnodes == 0) return;
   const GridView g = grid_of(d);
-  const int offsets = d.dim == 3 ? 27 : 9;
   const unsigned blocks = static_cast<unsigned>((l0.nnodes + kAsmTile - 1) / kAsmTile);
   const size_t smem = assemble_smem(d.dim);
+  const int threads = assemble_threads(d.dim);
   auto launch = [&](auto kernel, const float* sh, const float* sl, double* v64, float* hi, float2* pair) {
     raise_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
-    kernel<<<blocks, offsets * kAsmTile, smem, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p, nmask.p,
-                                                              l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale, sh, sl,
-                                                              v64, hi, pair);
+    kernel<<<blocks, threads, smem, amg.stream>>>(g, l0.nnodes, l0.d_first.p, gnode.p, cmask.p, nmask.p,
+                                                  l0.d_apat.view(), l0.a.ptr.p, ke_d.p, scale, sh, sl, v64, hi,
+                                                  pair);
     SIMP_CHECK_LAUNCH();
   };
   if (!amg.mixed()) {

@@ -26,16 +26,30 @@ __device__ __forceinline__ int corner_of(int dx, int dy, int dz) { return 4 * dz
 // 182-214), so the FP64 values equal a sequential assembly bit for bit;
 // otherwise fused multiply-adds.
 //
-// One block per tile of 32 consecutive free nodes; warp o of the block owns
-// neighbour offset o (27 in 3-D, 9 in 2-D) and lane i node I0 + i, so a
-// warp's lanes walk the same cells with the same corner indices (uniform
-// trip counts, K_e^0 read as a shared-memory broadcast).  Each thread's 3 x 3
-// block goes to a shared staging copy of the tile's rows, which are one
-// contiguous range of the CSR values; the block then writes that range with
-// coalesced stores.  nmask[I] has bit o set when the neighbour at offset o is
-// a free node; its slot is the rank of o among the set bits (the node
-// pattern lists neighbours in ascending order = ascending offset order).
+// One block per tile of 32 consecutive free nodes; lane i of every warp owns
+// node I0 + i, and warp g walks the neighbour offsets of group g (27 offsets
+// in 3-D, 9 in 2-D).  An offset's work is the number of cells the two nodes
+// share (8 for the centre, 4 for a face, 2 for an edge, 1 for a corner in
+// 3-D), so the groups hold equal totals -- 3-D: the centre; two faces (three
+// groups); four edges (three groups); the eight corners; 2-D: the centre
+// and the corners; the four edges -- and no warp waits on another at the
+// block's staging barrier.  A warp's lanes walk the same cells with the
+// same corner indices (uniform trip counts, K_e^0 read as a shared-memory
+// broadcast).  Each (node, offset) 3 x 3 block is computed by one thread in
+// ascending cell order, whatever the grouping.  The block goes to a shared
+// staging copy of the tile's rows, which are one contiguous range of the
+// CSR values; the block then writes that range with coalesced stores.
+// nmask[I] has bit o set when the neighbour at offset o is a free node; its
+// slot is the rank of o among the set bits (the node pattern lists
+// neighbours in ascending order = ascending offset order).
 constexpr int kAsmTile = 32;
+constexpr int kAsmGroups3 = 8, kAsmGroups2 = 2;  // warps per block
+__device__ constexpr int kAsmOff3[27] = {13, 4, 10, 12, 14, 16, 22, 1, 3, 5, 7, 9, 11, 15,
+                                         17, 19, 21, 23, 25, 0, 2, 6, 8, 18, 20, 24, 26};
+__device__ constexpr int kAsmStart3[kAsmGroups3 + 1] = {0, 1, 3, 5, 7, 11, 15, 19, 27};
+__device__ constexpr int kAsmOff2[9] = {4, 0, 2, 6, 8, 1, 3, 5, 7};
+__device__ constexpr int kAsmStart2[kAsmGroups2 + 1] = {0, 5, 9};
+inline int assemble_threads(int dim) { return (dim == 3 ? kAsmGroups3 : kAsmGroups2) * kAsmTile; }
 
 inline size_t assemble_smem(int dim) {
   const int ed = dim == 3 ? 24 : 8, rowvals = dim == 3 ? 3 * 81 : 2 * 18;
@@ -48,7 +62,7 @@ inline size_t assemble_smem(int dim) {
 // (the mixed-precision reuse assemblies, which write hi/lo only); otherwise
 // in FP64 (EXACT: rounded products and sums; else fused multiply-adds).
 template <bool EXACT, bool DF>
-__global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
+__global__ void __launch_bounds__(kAsmGroups3 * kAsmTile) k_assemble_tiles(
     GridView g, i32 nodes, const i32* __restrict__ first, const i32* __restrict__ gnode,
     const uint8_t* __restrict__ cmask, const uint32_t* __restrict__ nmask, NodeView a,
     const i32* __restrict__ rowptr, const double* __restrict__ ke, const double* __restrict__ scale,
@@ -73,10 +87,14 @@ __global__ void __launch_bounds__(27 * kAsmTile) k_assemble_tiles(
   const i32 I1 = min(I0 + kAsmTile, nodes);
   const i32 base = rowptr[first[I0]], end = rowptr[first[I1]];
   __syncthreads();
-  const int o = threadIdx.x >> 5;
+  const int grp = threadIdx.x >> 5;
   const i32 I = I0 + (threadIdx.x & 31);
   const uint32_t mk = I < I1 ? nmask[I] : 0u;
-  if (mk & (1u << o)) {
+  const int q0 = g.dim == 3 ? kAsmStart3[grp] : kAsmStart2[grp];
+  const int q1 = g.dim == 3 ? kAsmStart3[grp + 1] : kAsmStart2[grp + 1];
+  for (int q = q0; q < q1; ++q) {
+    const int o = g.dim == 3 ? kAsmOff3[q] : kAsmOff2[q];
+    if (!(mk & (1u << o))) continue;
     const int odx = o % 3 - 1, ody = (o / 3) % 3 - 1, odz = g.dim == 3 ? o / 9 - 1 : 0;
     const i32 t = a.ptr[I] + __popc(mk & ((1u << o) - 1u));
     const i32 gi = gnode[I];
