@@ -435,9 +435,12 @@ typedef struct simp_buckling_options {
   double residual_tolerance;  /* eigenpair residual bound (1e-6) */
   double young;               /* Young's modulus of the material (required) */
   double poisson;             /* Poisson ratio (plane stress in 2-D) */
-  int32_t transform;          /* 0 auto; 1 the spectral transformation from the start:
-                                 not available (SIMP_BAD_INPUT), see below */
+  int32_t transform;          /* 0 auto (plain, transformed once reversed-load modes
+                                 crowd the subspace); 1 the spectral transformation
+                                 from the start */
   int32_t concurrent_solves;  /* subspace columns solved at the same time (4) */
+  double shift_hint;          /* positive: an estimate of the smallest load factor the
+                                 transformation's shift search starts from (0) */
 } simp_buckling_options;
 
 /* BucklingResult's scalars (include/sparlab/fem/Buckling.hpp:111-140). */
@@ -451,6 +454,9 @@ typedef struct simp_buckling_info {
   int64_t linear_iterations;       /* PCG iterations, the static solve included */
   double final_change;
   int32_t num_warnings;            /* texts: simp_buckling_warning */
+  int32_t transformed;             /* the spectral transformation was used */
+  double sigma;                    /* its shift, a lower bound on lambda_1 */
+  int32_t factorizations;          /* factorisations of K_ff + sigma K_G,ff */
 } simp_buckling_info;
 
 void simp_default_buckling_options(simp_buckling_options* o);
@@ -466,11 +472,11 @@ void simp_default_buckling_options(simp_buckling_options* o);
  * load_factors, residuals and solid_energy_fraction (num_modes each),
  * mode_shapes (num_modes x num_dofs, phi^T K phi = 1, zero on the supports),
  * subspace (nfree x subspace_size, column-major).  Systems with at most 400
- * free DOFs take the dense path.  Not available: the reference's spectral
- * transformation, which it uses when reversed-load modes crowd the subspace
- * (mostly tensile stress states): it places its shift by the inertia of
- * sparse LDL^T factorisations and this library has none, so those cases
- * return SIMP_BAD_INPUT with a message saying so. */
+ * free DOFs take the dense path.  The spectral transformation
+ * X <- (K - sigma G)^-1 K X (on request, or when reversed-load modes crowd
+ * the subspace: mostly tensile stress states) places sigma by the inertia of
+ * K - sigma G, which it factors densely on the device: systems above 16000
+ * free DOFs that need it return SIMP_BAD_INPUT with a message saying so. */
 int simp_buckling(simp_problem* p, const simp_buckling_options* options, int32_t load_case,
                   const double* stiffness_scale, const double* stress_scale,
                   const uint8_t* solid_mask, const double* start_subspace, int32_t start_cols,

@@ -143,14 +143,15 @@ class RobustRecord(C.Structure):
 class BucklingOptions(C.Structure):
     _fields_ = [("num_modes", C.c_int32), ("max_iterations", C.c_int32), ("tolerance", C.c_double),
                 ("residual_tolerance", C.c_double), ("young", C.c_double), ("poisson", C.c_double),
-                ("transform", C.c_int32), ("concurrent_solves", C.c_int32)]
+                ("transform", C.c_int32), ("concurrent_solves", C.c_int32), ("shift_hint", C.c_double)]
 
 
 class BucklingInfo(C.Structure):
     _fields_ = [("num_modes", C.c_int32), ("iterations", C.c_int32), ("subspace_size", C.c_int32),
                 ("converged", C.c_int32), ("no_positive_load_factor", C.c_int32),
                 ("subspace_cols", C.c_int32), ("linear_iterations", C.c_int64),
-                ("final_change", C.c_double), ("num_warnings", C.c_int32)]
+                ("final_change", C.c_double), ("num_warnings", C.c_int32), ("transformed", C.c_int32),
+                ("sigma", C.c_double), ("factorizations", C.c_int32)]
 
 
 _lock = threading.Lock()

@@ -1209,8 +1209,8 @@ void GpuAmg::coarse_factorize() {
   const dim3 tiles(nt, nt);
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int kb = std::min(kNB, n - k0);
-    k_sweep_pivot<<<(n + kSweepRows - 1) / kSweepRows, 256, 0, stream>>>(swept_.p, n, k0, kb, pu, pv, pp,
-                                                                          piv_.p, dstatus.p);
+    k_sweep_pivot<false><<<(n + kSweepRows - 1) / kSweepRows, 256, 0, stream>>>(swept_.p, n, k0, kb, pu, pv,
+                                                                                 pp, piv_.p, dstatus.p);
     SIMP_CHECK_LAUNCH();
     k_sweep_update<<<tiles, 256, 0, stream>>>(swept_.p, n, k0, kb, pu, pv, pp);
     SIMP_CHECK_LAUNCH();

@@ -11,17 +11,24 @@
 // largest singular value dropped), the projected pencil is two tall-skinny
 // Gram products, and the dense q x q problem is solved on the host.
 //
-// The reference switches to the buckling spectral transformation
-// (K - sigma G)^-1 K when reversed-load modes crowd the subspace, placing
-// sigma below lambda_1 by the inertia of sparse LDL^T factorisations; this
-// library has no sparse factorisation, so such cases (and transform =
-// shift-invert) end with SIMP_BAD_INPUT and a message saying so.
+// When reversed-load modes crowd the subspace (or on request), the iteration
+// switches to the buckling spectral transformation X <- (K - sigma G)^-1 K X
+// with sigma placed below lambda_1 by the inertia of K - sigma G
+// (src/fem/Buckling.cpp:184-245, 318-347).  The reference reads the inertia
+// off a sparse LDL^T; here K - sigma G is formed densely on the device and
+// inverted by the blocked symmetric sweep of the coarse solve with signed
+// pivots, which are the D of its natural-order LDL^T (the same negative
+// count by Sylvester's law), and the shifted solves are one dense product
+// per iteration.  Systems above kShiftDenseLimit free DOFs (beyond a dense
+// factorisation) end with SIMP_BAD_INPUT and a message saying so.
+#include "dense.cuh"
 #include "subspace.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <exception>
 #include <limits>
+#include <memory>
 #include <numeric>
 #include <sstream>
 #include <thread>
@@ -32,6 +39,7 @@ namespace {
 
 constexpr double kZeroFraction = 1.0e-10;  // |mu| below this share of the largest is zero
 constexpr i32 kDenseLimit = 400;
+constexpr i32 kShiftDenseLimit = 16000;  // dense K - sigma G: 2 x 2 GB at the limit
 constexpr uint64_t kStartSeed = 20240917u;
 
 // The project's SplitMix64 stream (the same numbers as problems.SplitMix64).
@@ -245,6 +253,73 @@ std::vector<double> geometric_tensor(int dim, double hx, double hy, double hz, d
   return Cs;
 }
 
+// (K - sigma G)^-1 for the spectral transformation: factor(s) forms K - s G
+// from the CSR values on the device, sweeps it into its inverse and returns
+// the number of negative pivots (the number of load factors in (0, s) when
+// K is positive definite), or -1 when a pivot is zero or not finite;
+// apply() multiplies the last inverse into q columns.
+struct ShiftedInverse {
+  i32 n = 0;
+  DBuf<double> swept, inv, panel, piv;
+  DBuf<int> status;
+  cudaStream_t s = nullptr;
+
+  ShiftedInverse(i32 n_, cudaStream_t stream) : n(n_), s(stream) {
+    if (n > kShiftDenseLimit) {
+      std::ostringstream os;
+      os << "buckling: the spectral transformation factors K - sigma K_G densely, up to " << kShiftDenseLimit
+         << " free DOFs; this system has " << n << " (a sparse LDL^T is not provided): request more modes, or "
+         << "run this load case on the reference's CPU path";
+      throw Error(kBadInput, os.str());
+    }
+    const size_t nn = static_cast<size_t>(n) * n;
+    swept.alloc(nn);
+    inv.alloc(nn);
+    panel.alloc(2 * static_cast<size_t>(n) * kNB + kNB * kNB);
+    piv.alloc(static_cast<size_t>(n));
+    status.alloc(1);
+  }
+
+  int factor(const Level& l0, const double* kval, const double* gval, double sig) {
+    const size_t nn = static_cast<size_t>(n) * n;
+    double* pu = panel.p;
+    double* pv = pu + static_cast<size_t>(n) * kNB;
+    double* pp = pv + static_cast<size_t>(n) * kNB;
+    SIMP_CUDA(cudaMemsetAsync(swept.p, 0, nn * sizeof(double), s));
+    SIMP_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+    k_dense_shifted<<<grid_for(n, 128), 128, 0, s>>>(n, l0.a.ptr.p, l0.a.col.p, kval, gval, sig, swept.p);
+    SIMP_CHECK_LAUNCH();
+    const int nt = (n + kNB - 1) / kNB;
+    const dim3 tiles(nt, nt);
+    for (int k0 = 0; k0 < n; k0 += kNB) {
+      const int kb = std::min(kNB, n - k0);
+      k_sweep_pivot<true><<<(n + kSweepRows - 1) / kSweepRows, 256, 0, s>>>(swept.p, n, k0, kb, pu, pv, pp,
+                                                                            piv.p, status.p);
+      SIMP_CHECK_LAUNCH();
+      k_sweep_update<<<tiles, 256, 0, s>>>(swept.p, n, k0, kb, pu, pv, pp);
+      SIMP_CHECK_LAUNCH();
+    }
+    k_sweep_finish<<<tiles, 256, 0, s>>>(swept.p, inv.p, n);
+    SIMP_CHECK_LAUNCH();
+    int bad = 0;
+    SIMP_CUDA(cudaMemcpyAsync(&bad, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    const std::vector<double> d = piv.to_host(s);
+    if (bad != 0) return -1;
+    int negative = 0;
+    for (double v : d) {
+      if (!(v != 0.0) || !std::isfinite(v)) return -1;
+      negative += v < 0.0 ? 1 : 0;
+    }
+    return negative;
+  }
+
+  void apply(const double* y, double* z, int q) {
+    const dim3 grid((n + kNB - 1) / kNB, (q + kNB - 1) / kNB);
+    k_dense_gemm_cols<<<grid, 256, 0, s>>>(inv.p, n, q, y, z);
+    SIMP_CHECK_LAUNCH();
+  }
+};
+
 // An orthonormalising transform T (q x r, row-major) of the columns whose
 // Gram matrix is w: T = V_r Lambda_r^-1/2 over the eigenpairs above
 // (1e-10)^2 of the largest eigenvalue.
@@ -279,10 +354,8 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
     throw Error(kBadInput, "buckling analysis asked for a load case the model does not have");
   if (!(o.young > 0.0) || !(o.poisson > -1.0 && o.poisson < 0.5))
     throw Error(kBadInput, "buckling needs the material's Young's modulus and Poisson ratio");
-  if (o.transform != 0)
-    throw Error(kBadInput,
-                "the buckling spectral transformation places its shift by the inertia of sparse LDL^T "
-                "factorisations, which this library does not provide; use transform = auto");
+  if (o.transform != 0 && o.transform != 1)
+    throw Error(kBadInput, "buckling.transform must be 0 (auto) or 1 (shift-invert)");
   const ProblemDesc& d = p.d;
   const int dim = d.dim;
   const i32 n = p.nfree;
@@ -434,16 +507,68 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
       SIMP_CHECK_LAUNCH();
       SIMP_CUDA(cudaMemcpyAsync(out, Y.p, sizeof(double) * n * cols_out, cudaMemcpyDeviceToDevice, s));
     };
+    // the spectral transformation's shift (src/fem/Buckling.cpp:184-245):
+    // inertia(s) factors K - s G; choose_sigma places sigma below the
+    // smallest positive load factor, from a guess (lowered by halving until
+    // no load factor lies below it) or, without one, growing from 1 by
+    // factors of 8; false when no positive load factor lies below 1e15
+    std::unique_ptr<ShiftedInverse> shifted;
+    bool refined = false;
+    auto inertia = [&](double sg) {
+      if (!shifted) shifted.reset(new ShiftedInverse(n, s));
+      ++res.factorizations;
+      return shifted->factor(l0, kval, gval.p, sg);
+    };
+    auto choose_sigma = [&](double guess) -> bool {
+      double sg = guess > 0.0 ? guess : 1.0;
+      int negative = inertia(sg);
+      if (negative != 0) {
+        for (int halvings = 1; negative != 0; ++halvings) {
+          if (halvings > 120)
+            throw Error(kBreakdown,
+                        "the buckling shift search found no shift below the smallest load factor; K_ff is not "
+                        "positive definite");
+          sg *= 0.5;
+          negative = inertia(sg);
+        }
+      } else if (!(guess > 0.0)) {
+        double clean = sg;
+        for (;;) {
+          if (sg > 1.0e15) return false;
+          const double next = 8.0 * sg;
+          if (inertia(next) != 0) break;
+          sg = next;
+          clean = sg;
+        }
+        sg = clean;
+        if (inertia(sg) != 0) throw Error(kBreakdown, "inconsistent inertia in the buckling shift search");
+      }
+      res.sigma = sg;
+      res.transformed = true;
+      return true;
+    };
+    if (o.transform == 1 && !choose_sigma(o.shift_hint > 0.0 ? 0.8 * o.shift_hint : 0.0)) {
+      res.no_positive = true;
+      res.converged = true;
+    }
     std::vector<double> previous(static_cast<size_t>(m_req), std::numeric_limits<double>::quiet_NaN());
     std::vector<double> mu_desc;
     int r = 0;
-    for (int it = 1; it <= o.max_iterations; ++it) {
-      // Z = K^-1 G X
-      for (int c = 0; c < q; ++c) apply_g(w0, X.p + static_cast<size_t>(c) * n, Y.p + static_cast<size_t>(c) * n);
-      SIMP_CUDA(cudaMemsetAsync(Z.p, 0, sizeof(double) * n * q, s));
-      SIMP_CUDA(cudaStreamSynchronize(s));
-      for (const GpuAmg::PcgResult& x : solve_columns(amg, works, q, n, Y.p, Z.p))
-        count_solve(x, amg.opt.rtol, res.linear_iterations);
+    for (int it = 1; it <= o.max_iterations && !res.no_positive; ++it) {
+      if (res.transformed) {
+        // Z = (K - sigma G)^-1 K X
+        for (int c = 0; c < q; ++c)
+          apply_k(w0, X.p + static_cast<size_t>(c) * n, Y.p + static_cast<size_t>(c) * n);
+        shifted->apply(Y.p, Z.p, q);
+      } else {
+        // Z = K^-1 G X
+        for (int c = 0; c < q; ++c)
+          apply_g(w0, X.p + static_cast<size_t>(c) * n, Y.p + static_cast<size_t>(c) * n);
+        SIMP_CUDA(cudaMemsetAsync(Z.p, 0, sizeof(double) * n * q, s));
+        SIMP_CUDA(cudaStreamSynchronize(s));
+        for (const GpuAmg::PcgResult& x : solve_columns(amg, works, q, n, Y.p, Z.p))
+          count_solve(x, amg.opt.rtol, res.linear_iterations);
+      }
       // orthonormal basis B of Z, two passes through the Gram matrix
       Mat wz, T;
       gram_of(q, Z.p, Z.p, wz);
@@ -538,14 +663,30 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
         res.converged = true;
         break;
       }
-      int competing = 0;
-      for (int j = 0; j < r; ++j) competing += mu_desc[j] < -mu_m ? 1 : 0;
-      if (competing + m_req > q - 2)
-        throw Error(kBadInput,
-                    "buckling: reversed-load (tensile) modes crowd the subspace, which needs the spectral "
-                    "transformation; it places its shift by the inertia of sparse LDL^T factorisations, which this "
-                    "library does not provide (request more modes, or run this load case on the reference's CPU "
-                    "path)");
+      if (!res.transformed && o.transform == 0) {
+        // reversed-load modes larger than the m-th wanted one take the
+        // slots the wanted ones converge in: once more of them than the
+        // spare slots appear, switch to the transformation
+        int competing = 0;
+        for (int j = 0; j < r; ++j) competing += mu_desc[j] < -mu_m ? 1 : 0;
+        if (competing + m_req > q - 2) {
+          const double estimate = mu_desc[0] > zero ? 0.8 / mu_desc[0] : 0.0;
+          if (!choose_sigma(o.shift_hint > 0.0 ? 0.8 * o.shift_hint : estimate)) {
+            res.no_positive = true;
+            res.converged = true;
+            break;
+          }
+          previous.assign(static_cast<size_t>(m_req), std::numeric_limits<double>::quiet_NaN());
+        }
+      } else if (res.transformed && !refined && mu_desc[0] > zero && change < 1.0e-3 &&
+                 res.sigma < 0.5 / mu_desc[0]) {
+        // a shift from the coarse search can sit far below lambda_1, where
+        // the transformation separates the modes poorly: raise it to 0.8 of
+        // the settled estimate
+        refined = true;
+        if (!choose_sigma(0.8 / mu_desc[0]))
+          throw Error(kBreakdown, "the refined buckling shift found no load factor");
+      }
     }
     if (!res.converged) {
       std::ostringstream os;
@@ -556,8 +697,10 @@ BucklingResult solve_buckling(GpuProblem& p, const BucklingOptions& o, int load_
          << "). Increase buckling.max_iterations, request fewer modes, or loosen buckling.tolerance";
       throw Error(kMaxIter, os.str());
     }
-    mu_top.assign(mu_desc.begin(), mu_desc.begin() + m_req);
-    top_cols = r;
+    if (!res.no_positive) {
+      mu_top.assign(mu_desc.begin(), mu_desc.begin() + m_req);
+      top_cols = r;
+    }
   }
   // the converged subspace (free DOFs, column-major), a warm start for the
   // next analysis

@@ -987,6 +987,7 @@ void simp_default_buckling_options(simp_buckling_options* o) {
   o->poisson = 0.0;
   o->transform = 0;
   o->concurrent_solves = 4;
+  o->shift_hint = 0.0;
 }
 
 int simp_buckling(simp_problem* p, const simp_buckling_options* options, int32_t load_case,
@@ -1005,6 +1006,7 @@ int simp_buckling(simp_problem* p, const simp_buckling_options* options, int32_t
     o.poisson = options->poisson;
     o.transform = options->transform;
     o.concurrent_solves = options->concurrent_solves;
+    o.shift_hint = options->shift_hint;
     p->buckling_warnings.clear();
     const BucklingResult r = solve_buckling(*p->p, o, load_case, stiffness_scale, stress_scale, solid_mask,
                                             start_subspace, start_cols, mode_shapes != nullptr);
@@ -1027,6 +1029,9 @@ int simp_buckling(simp_problem* p, const simp_buckling_options* options, int32_t
       info->linear_iterations = r.linear_iterations;
       info->final_change = r.final_change;
       info->num_warnings = static_cast<int32_t>(r.warnings.size());
+      info->transformed = r.transformed ? 1 : 0;
+      info->sigma = r.sigma;
+      info->factorizations = r.factorizations;
     }
   });
 }

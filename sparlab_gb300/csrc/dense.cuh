@@ -13,6 +13,13 @@
 // scalar pivots met inside the pivot blocks are the squared Cholesky pivots
 // (the D of A = L D L^T), recorded for the singularity check.
 // Row-major n x n storage.
+//
+// The same sweep inverts the indefinite shifted pencil K - sigma G of the
+// buckling spectral transformation (SIGNED pivots: any nonzero finite pivot
+// is taken).  Its pivots are then the D of A = L D L^T in the natural order,
+// so by Sylvester's law of inertia the count of negative pivots is the count
+// of negative eigenvalues whenever no leading minor vanishes -- the number
+// src/fem/Buckling.cpp:190-201 reads off its sparse LDL^T.
 #pragma once
 
 #include "common.h"
@@ -28,7 +35,9 @@ constexpr int kSweepRows = 16;  // rows of U and V per block of k_sweep_pivot
 // few dozen microseconds of FP64 latency in every block, in parallel, so the
 // panel needs no second launch), then writes U_i = M[i, k0:k0+kb] and
 // V_i = U_i S^-1 for its rows i outside the block.  Block 0 records the
-// pivots, the status (1 on a pivot that is not positive and finite) and P.
+// pivots, the status (1 on a pivot that is not positive and finite; SIGNED:
+// zero or not finite) and P.
+template <bool SIGNED = false>
 __global__ void __launch_bounds__(256) k_sweep_pivot(const double* __restrict__ m, int n, int k0, int kb,
                                                      double* __restrict__ u, double* __restrict__ v,
                                                      double* __restrict__ pout, double* __restrict__ piv,
@@ -48,7 +57,7 @@ __global__ void __launch_bounds__(256) k_sweep_pivot(const double* __restrict__ 
   for (int j = 0; j < kb; ++j) {
     if (tid < kNB) {
       const double d = s[j][j];
-      const bool ok = d > 0.0 && isfinite(d);
+      const bool ok = (SIGNED ? d != 0.0 : d > 0.0) && isfinite(d);
       const double p = ok ? 1.0 / d : 1.0;
       const double uc = s[j][tid];
       urow[tid] = uc;
@@ -191,6 +200,48 @@ __global__ void k_dense_from_csr(int n, const i32* __restrict__ ptr, const i32* 
                                  const double* __restrict__ val, double* __restrict__ a) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
     for (i32 k = ptr[r]; k < ptr[r + 1]; ++k) a[(size_t)r * n + col[k]] = val[k];
+}
+
+// a = K - s G densely, K and G on the same CSR pattern (a zeroed before).
+__global__ void k_dense_shifted(int n, const i32* __restrict__ ptr, const i32* __restrict__ col,
+                                const double* __restrict__ kval, const double* __restrict__ gval, double s,
+                                double* __restrict__ a) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    for (i32 k = ptr[r]; k < ptr[r + 1]; ++k) a[(size_t)r * n + col[k]] = kval[k] - s * gval[k];
+}
+
+// Z = F Y for a row-major n x n F and column-major n x q Y, Z: one 32 x 32
+// tile (rows i0.., columns c0..) per block of 256 threads, the inner index
+// staged 32 at a time; every output sums its terms in ascending inner order.
+__global__ void __launch_bounds__(256) k_dense_gemm_cols(const double* __restrict__ f, int n, int q,
+                                                         const double* __restrict__ y, double* __restrict__ z) {
+  __shared__ double fs[kNB][kNB + 1];  // fs[i][k] = F[i0 + i][k0 + k]
+  __shared__ double ys[kNB][kNB + 1];  // ys[c][k] = Y[k0 + k][c0 + c]
+  const int i0 = blockIdx.x * kNB, c0 = blockIdx.y * kNB;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  double acc[kNB / 8] = {};
+  for (int k0 = 0; k0 < n; k0 += kNB) {
+    for (int q2 = ty; q2 < kNB; q2 += 8) {
+      const int i = i0 + q2, k = k0 + tx, c = c0 + q2;
+      fs[q2][tx] = (i < n && k < n) ? f[(size_t)i * n + k] : 0.0;
+      ys[q2][tx] = (c < q && k < n) ? y[(size_t)c * n + k] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int qq = 0; qq < kNB / 8; ++qq) {
+      const int c = ty + 8 * qq;
+      double a = acc[qq];
+#pragma unroll 8
+      for (int k = 0; k < kNB; ++k) a = fma(fs[tx][k], ys[c][k], a);
+      acc[qq] = a;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int qq = 0; qq < kNB / 8; ++qq) {
+    const int i = i0 + tx, c = c0 + ty + 8 * qq;
+    if (i < n && c < q) z[(size_t)c * n + i] = acc[qq];
+  }
 }
 
 }  // namespace

@@ -226,8 +226,9 @@ struct BucklingOptions {
   int max_iterations = 400;
   double tolerance = 1.0e-8, residual_tolerance = 1.0e-6;
   double young = 0.0, poisson = 0.0;
-  int transform = 0;  // 0 auto (plain iteration), 1 shift-invert from the start (not available)
+  int transform = 0;  // 0 auto (plain iteration, transformed when crowded), 1 shift-invert from the start
   int concurrent_solves = 4;
+  double shift_hint = 0.0;  // positive: an estimate of lambda_1 the shift search starts from
 };
 
 // BucklingResult (include/sparlab/fem/Buckling.hpp:111-140)
@@ -237,6 +238,9 @@ struct BucklingResult {
   std::vector<double> subspace;  // free DOFs x subspace_cols, column-major
   int subspace_cols = 0;
   bool no_positive = false, converged = false;
+  bool transformed = false;  // the spectral transformation was used
+  double sigma = 0.0;        // its shift, below lambda_1
+  int factorizations = 0;    // factorisations of K - sigma G
   int iterations = 0, subspace_size = 0;
   double final_change = 0.0;
   i64 linear_iterations = 0;

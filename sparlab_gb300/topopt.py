@@ -125,6 +125,8 @@ class BucklingResult:
     subspace: Optional[np.ndarray]      # free DOFs x columns
     warnings: List[str]
     transformed: bool = False
+    sigma: float = 0.0                  # the transformation's shift, below lambda_1
+    factorizations: int = 0             # factorisations of K - sigma G
     linear_solver: str = "AMG-CG(chebyshev, GPU)"
 
 
@@ -361,7 +363,7 @@ class GpuSimpProblem:
     def buckling(self, load_case=0, num_modes=4, max_iterations=400, tolerance=1e-8,
                  residual_tolerance=1e-6, transform="auto", stiffness_scale=None, stress_scale=None,
                  solid_mask=None, initial_subspace=None, mode_shapes=True,
-                 concurrent_solves=4) -> BucklingResult:
+                 concurrent_solves=4, shift_hint=0.0) -> BucklingResult:
         """``analyse_buckling`` (src/fem/Buckling.cpp:438-466) of one load case
         with the problem's AMG-PCG; the material is ``spec.young`` /
         ``spec.poisson``."""
@@ -372,6 +374,7 @@ class GpuSimpProblem:
         o.young, o.poisson = self.spec.young, self.spec.poisson
         o.transform = {"auto": 0, "shift_invert": 1}[transform]
         o.concurrent_solves = concurrent_solves
+        o.shift_hint = shift_hint
         ks = None if stiffness_scale is None else np.ascontiguousarray(stiffness_scale, np.float64)
         ss = None if stress_scale is None else np.ascontiguousarray(stress_scale, np.float64)
         mask = None if solid_mask is None else np.ascontiguousarray(solid_mask, np.uint8)
@@ -396,7 +399,8 @@ class GpuSimpProblem:
                               frac[:k].copy(), bool(info.no_positive_load_factor), info.iterations,
                               info.subspace_size, bool(info.converged), info.linear_iterations,
                               info.final_change,
-                              sub[:info.subspace_cols].T.copy() if info.subspace_cols else None, warnings)
+                              sub[:info.subspace_cols].T.copy() if info.subspace_cols else None, warnings,
+                              bool(info.transformed), info.sigma, info.factorizations)
 
     def kff(self, scale=None):
         p = np.zeros(self.nfree + 1, np.int32)

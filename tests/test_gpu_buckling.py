@@ -101,25 +101,47 @@ def test_tension_has_no_positive_load_factor():
     gpu.close()
 
 
-def test_crowded_spectrum_reports_the_missing_transformation():
-    """Large axial tension plus a small transverse load: the reversed-load
-    factors crowd the subspace, where the reference needs its LDL^T-based
-    spectral transformation; without the transverse tension the plain
-    iteration matches the oracle."""
-    plain = P.column(2, 60, 6, height=0.1, thickness=0.002, force=0.0, transverse=1.0e6 * 0.1 * 0.002)
-    ref, gpu = pair(plain)
-    o = OB.analyse_buckling(ref, plain, num_modes=3)
-    b = gpu.buckling(num_modes=3)
-    assert not o.transformed
-    np.testing.assert_allclose(b.load_factors, o.load_factors, rtol=1e-7)
-    gpu.close()
-    spec = P.column(2, 60, 6, height=0.1, thickness=0.002, force=2.0e8 * 0.1 * 0.002,
-                    transverse=1.0e6 * 0.1 * 0.002)
-    _, gpu = pair(spec)
-    with pytest.raises(SolverError, match="LDL"):
-        gpu.buckling(num_modes=3)
-    with pytest.raises(SolverError, match="LDL"):
-        gpu.buckling(num_modes=3, transform="shift_invert")
+def test_crowded_spectrum_takes_the_spectral_transformation():
+    """Large axial tension plus a small transverse load (the reference's
+    tests/test_buckling.cpp:301-381): the reversed-load factors crowd the
+    subspace and the iteration switches to (K - sigma G)^-1 K with sigma
+    below lambda_1, placed by the inertia of K - sigma G; without the axial
+    tension the plain iteration runs.  Both reproduce the oracle and the
+    dense eigensolve to 1e-7, as does the transformation from the start."""
+    for tension in (0.0, 2.0e8):
+        spec = P.column(2, 60, 6, height=0.1, thickness=0.002, force=tension * 0.1 * 0.002,
+                        transverse=1.0e6 * 0.1 * 0.002)
+        ref, gpu = pair(spec)
+        assert gpu.nfree > 400
+        o = OB.analyse_buckling(ref, spec, num_modes=3)
+        b = gpu.buckling(num_modes=3)
+        assert b.converged and o.converged
+        assert b.transformed == o.transformed == (tension > 0)
+        assert len(b.load_factors) == len(o.load_factors) >= 1
+        np.testing.assert_allclose(b.load_factors, o.load_factors, rtol=1e-7)
+        if tension > 0:
+            assert 0.0 < b.sigma < b.load_factors[0] and b.factorizations >= 1
+        else:
+            assert b.factorizations == 0
+        s = gpu.buckling(num_modes=3, transform="shift_invert")
+        assert s.converged and s.transformed and 0.0 < s.sigma < s.load_factors[0]
+        np.testing.assert_allclose(s.load_factors, o.load_factors, rtol=1e-7)
+        h = gpu.buckling(num_modes=3, transform="shift_invert", shift_hint=o.load_factors[0])
+        assert h.transformed and 0.0 < h.sigma < h.load_factors[0]
+        np.testing.assert_allclose(h.load_factors, o.load_factors, rtol=1e-7)
+        gpu.close()
+
+
+def test_tension_shift_invert_finds_no_positive_load_factor():
+    """Pure tension past the dense path's size: the shift search grows sigma
+    by factors of 8 up to 1e15 without meeting a load factor."""
+    spec = P.column(2, 60, 6, height=0.1, thickness=0.002, force=2.0e8 * 0.1 * 0.002)
+    ref, gpu = pair(spec)
+    assert gpu.nfree > 400
+    o = OB.analyse_buckling(ref, spec, num_modes=2, transform="shift_invert")
+    b = gpu.buckling(num_modes=2, transform="shift_invert")
+    assert o.no_positive_load_factor and b.no_positive_load_factor
+    assert len(b.load_factors) == 0 and b.converged and b.factorizations == o.factorizations
     gpu.close()
 
 
