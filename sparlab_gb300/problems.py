@@ -331,3 +331,87 @@ def batched_instances(seed: int = 4, count_q4: int = 48, count_hex: int = 16) ->
         spec.weights = np.ones(len(loads))
         out.append(spec)
     return out
+
+
+# ---------------------------------------------------------------------------
+# The reference's published topology benchmarks on structured grids
+# (configs/benchmarks/*.json; their first-iteration and full-solid compliances
+# are in docs/results/benchmarks.csv)
+# ---------------------------------------------------------------------------
+def box_nodes(spec: ProblemSpec, xmin=-math.inf, xmax=math.inf, ymin=-math.inf, ymax=math.inf,
+              zmin=-math.inf, zmax=math.inf) -> np.ndarray:
+    """Nodes inside a box selector, widened by 1e-9 of the mesh diagonal
+    (Selector::contains, src/fem/Selector.cpp:12-19, 52-54)."""
+    tol = 1e-9 * max(_diag(spec), 1e-30)
+    c = spec.node_coords()
+    z = c[:, 2] if spec.dim == 3 else np.zeros(len(c))
+    inside = ((c[:, 0] >= xmin - tol) & (c[:, 0] <= xmax + tol) & (c[:, 1] >= ymin - tol) &
+              (c[:, 1] <= ymax + tol) & (z >= zmin - tol) & (z <= zmax + tol))
+    return np.flatnonzero(inside)
+
+
+def _radius(spec: ProblemSpec, elements: float) -> float:
+    """radius_elements x the mean cell side (Configuration::resolved_filter_radius)."""
+    cells = [spec.lx / spec.nx, spec.ly / spec.ny] + ([spec.lz / spec.nz] if spec.dim == 3 else [])
+    return elements * float(np.prod(cells)) ** (1.0 / spec.dim)
+
+
+def mbb_beam(projection: bool = False, robust: bool = False) -> ProblemSpec:
+    """configs/benchmarks/mbb_beam{,_projected,_robust}.json: the MBB half
+    beam, Q4 180 x 60 unit cells, E = 1, nu = 0.3, t = 1; u_x = 0 on x = 0,
+    a vertical roller at the node nearest (180, 0); (0, -1) N at the node
+    nearest (0, 60); vf 0.5, radius 4.5 cells; the projected variants start
+    at beta 1 (eta 0.5; robust: eta 0.5 +- 0.1)."""
+    spec = ProblemSpec(dim=2, nx=180, ny=60, nz=0, lx=180.0, ly=60.0, lz=0.0, young=1.0, poisson=0.3,
+                       thickness=1.0, volume_fraction=0.5, initial_density=0.5, rtol=1e-10,
+                       projection=projection or robust, eta=0.5, beta_start=1.0,
+                       beta_max=32.0, beta_factor=2.0, beta_interval=40, robust=robust,
+                       robust_delta=0.1, robust_volume_interval=20,
+                       name="mbb_beam" + ("_robust" if robust else "_projected" if projection else ""))
+    spec.filter_radius = _radius(spec, 4.5)
+    fixed = clamp_left(spec, components=[0])
+    fixed[nearest_node(spec, (180.0, 0.0)) * 2 + 1] = 1
+    spec.fixed = fixed
+    spec.loads = point_load(spec, [nearest_node(spec, (0.0, 60.0))], (0.0, -1.0))[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
+def cantilever_beam() -> ProblemSpec:
+    """configs/benchmarks/cantilever_beam.json: Q4 160 x 80 over 0.4 x 0.2 m,
+    Al 7075-T6 (E = 71.7 GPa, nu = 0.33), t = 4 mm; x = 0 clamped; 2000 N
+    down spread over the tip nodes with y in [0.0975, 0.1025]; vf 0.4,
+    radius 2 cells."""
+    spec = ProblemSpec(dim=2, nx=160, ny=80, nz=0, lx=0.4, ly=0.2, lz=0.0, young=71.7e9, poisson=0.33,
+                       thickness=0.004, density=2810.0, volume_fraction=0.4, initial_density=0.4,
+                       rtol=1e-10, name="cantilever_beam")
+    spec.filter_radius = _radius(spec, 2.0)
+    spec.fixed = clamp_left(spec)
+    tip = box_nodes(spec, xmin=0.4, ymin=0.0975, ymax=0.1025)
+    spec.loads = point_load(spec, tip, (0.0, -2000.0))[None, :]
+    spec.weights = np.ones(1)
+    return spec
+
+
+def bracket_3d(projection: bool = False, large: bool = False) -> ProblemSpec:
+    """configs/benchmarks/bracket_3d{,_projected,_large}.json: Hex8 over
+    0.24 x 0.12 x 0.06 m (32 x 16 x 8 cells; large: 96 x 48 x 24), Al
+    7075-T6; x = 0 clamped; load case 1 (weight 1): 3000 N down spread over
+    the tip's bottom edge (x = 0.24, y = 0); load case 2 (weight 0.5): 1200 N
+    along z spread over the tip's mid line (y in [0.0555, 0.0645]; large:
+    [0.0585, 0.0615]); vf 0.3, radius 1.5 cells; the projected and large
+    variants start at beta 1 (eta 0.5)."""
+    n = (96, 48, 24) if large else (32, 16, 8)
+    spec = ProblemSpec(dim=3, nx=n[0], ny=n[1], nz=n[2], lx=0.24, ly=0.12, lz=0.06, young=71.7e9,
+                       poisson=0.33, density=2810.0, volume_fraction=0.3, initial_density=0.3,
+                       rtol=1e-10, projection=projection or large, eta=0.5, beta_start=1.0,
+                       beta_max=16.0, beta_factor=2.0, beta_interval=40,
+                       name="bracket_3d" + ("_large" if large else "_projected" if projection else ""))
+    spec.filter_radius = _radius(spec, 1.5)
+    spec.fixed = clamp_left(spec)
+    edge = box_nodes(spec, xmin=0.24, ymax=0.0)
+    mid = box_nodes(spec, xmin=0.24, ymin=0.0585 if large else 0.0555, ymax=0.0615 if large else 0.0645)
+    spec.loads = np.stack([point_load(spec, edge, (0.0, -3000.0, 0.0)),
+                           point_load(spec, mid, (0.0, 0.0, 1200.0))])
+    spec.weights = np.array([1.0, 0.5])
+    return spec

@@ -1,10 +1,16 @@
-"""Regenerate tests/golden/solver_scaling.json from the reference checkout.
+"""Regenerate tests/golden/solver_scaling.json and tests/golden/benchmarks.json
+from the reference checkout.
 
-Reads the reference's published benchmark table
-(docs/results/solver_scaling.csv: the sparlab_bench model solved by LDL^T,
-AMG-CG and Jacobi-CG) and keeps the columns the parity tests pin: mesh,
-solver, DOF count, stored non-zeros of K, compliance, CG iterations, AMG
-levels and operator complexity.  Run from the repository root:
+Reads the reference's published tables and keeps the columns the parity
+tests pin:
+* docs/results/solver_scaling.csv (the sparlab_bench model solved by LDL^T,
+  AMG-CG and Jacobi-CG): mesh, solver, DOF count, stored non-zeros of K,
+  compliance, CG iterations, AMG levels and operator complexity;
+* docs/results/benchmarks.csv (the topology benchmarks of
+  configs/benchmarks/), the rows on structured Q4/Hex8 grids with point
+  loads: DOF count, volume fraction, the first iteration's compliance and
+  the full-solid compliance.
+Run from the repository root:
 
     python tests/golden/make_golden.py /path/to/reference
 """
@@ -33,6 +39,26 @@ def main(ref):
         json.dump({"source": "docs/results/solver_scaling.csv (sparlab_bench model, "
                              "tolerance 1e-10)", "rows": rows}, f, indent=1)
     print("wrote", out, len(rows), "rows")
+    keep = {"cantilever_beam", "mbb_beam", "mbb_beam_projected", "mbb_beam_robust", "bracket_3d",
+            "bracket_3d_projected", "bracket_3d_large"}
+    bench = []
+    with open(os.path.join(ref, "docs", "results", "benchmarks.csv")) as f:
+        for r in csv.DictReader(f):
+            if r["case"] not in keep:
+                continue
+            bench.append({
+                "case": r["case"], "dim": int(r["dim"]), "element_type": r["element_type"],
+                "elements": int(r["elements"]), "dofs": int(r["dofs"]),
+                "volume_fraction": float(r["volume_fraction_target"]),
+                "initial_compliance": float(r["initial_compliance_J"]),
+                "full_solid_compliance": float(r["full_solid_compliance_J"]),
+                "linear_solver": r["linear_solver"],
+            })
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "benchmarks.json")
+    with open(out, "w") as f:
+        json.dump({"source": "docs/results/benchmarks.csv (configs/benchmarks/<case>.json)",
+                   "rows": bench}, f, indent=1)
+    print("wrote", out, len(bench), "rows")
 
 
 if __name__ == "__main__":
