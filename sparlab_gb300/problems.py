@@ -415,3 +415,67 @@ def bracket_3d(projection: bool = False, large: bool = False) -> ProblemSpec:
                            point_load(spec, mid, (0.0, 0.0, 1200.0))])
     spec.weights = np.array([1.0, 0.5])
     return spec
+
+
+# ---------------------------------------------------------------------------
+# The reference's cross-validation models on structured grids
+# (configs/verification/*.json; SparLab's results are in
+# docs/results/cross_validation.csv)
+# ---------------------------------------------------------------------------
+def face_traction(spec: ProblemSpec, axis: int, at_max: bool, traction) -> np.ndarray:
+    """Consistent nodal forces of a uniform traction on a boundary face of
+    the box grid: each face cell's traction x area shared equally by its
+    corner nodes (exact for bilinear faces)."""
+    f = np.zeros(spec.num_dofs)
+    n = [spec.nx, spec.ny, spec.nz][: spec.dim]
+    h = [spec.lx / spec.nx, spec.ly / spec.ny] + ([spec.lz / spec.nz] if spec.dim == 3 else [])
+    others = [a for a in range(spec.dim) if a != axis]
+    fixed_index = n[axis] if at_max else 0
+    area = float(np.prod([h[a] for a in others])) * (1.0 if spec.dim == 3 else spec.thickness)
+    corners = 2 ** len(others)
+    shape = [n[a] for a in others]
+    for cell in np.ndindex(*shape):
+        for corner in np.ndindex(*([2] * len(others))):
+            idx = [0, 0, 0]
+            idx[axis] = fixed_index
+            for a, c, o in zip(others, cell, corner):
+                idx[a] = c + o
+            node = spec.node_index(idx[0], idx[1], idx[2] if spec.dim == 3 else 0)
+            for k in range(spec.dim):
+                f[node * spec.dim + k] += traction[k] * area / corners
+    return f
+
+
+def cantilever_analysis() -> ProblemSpec:
+    """configs/verification/cantilever_analysis.json: Q4 120 x 12 over
+    1.0 x 0.1 m, E = 70 GPa, nu = 0, t = 10 mm; x = 0 clamped; 1000 N down
+    spread over the tip edge (box xmin = 1.0)."""
+    spec = plane_cantilever(120, 12)
+    spec.name = "cantilever_analysis"
+    return spec
+
+
+def block_3d_analysis() -> ProblemSpec:
+    """configs/verification/block_3d_analysis.json: Hex8 40 x 8 x 4 over
+    0.5 x 0.1 x 0.05 m, E = 68.9 GPa, nu = 0.33; x = 0 clamped; load case
+    tip_load: 1000 N along -y spread over the tip face (box xmin = 0.5);
+    load case top_pressure: a -2e5 Pa traction along z on the top face
+    (box zmin = 0.05)."""
+    spec = ProblemSpec(dim=3, nx=40, ny=8, nz=4, lx=0.5, ly=0.1, lz=0.05, young=68.9e9, poisson=0.33,
+                       density=2700.0, filter_radius=0.0, rtol=1e-12, name="block_3d_analysis")
+    spec.fixed = clamp_left(spec)
+    tip = box_nodes(spec, xmin=0.5)
+    spec.loads = np.stack([point_load(spec, tip, (0.0, -1000.0, 0.0)),
+                           face_traction(spec, 2, True, (0.0, 0.0, -2.0e5))])
+    spec.weights = np.ones(2)
+    return spec
+
+
+def column_hex_buckling_analysis() -> ProblemSpec:
+    """configs/verification/column_hex_buckling_analysis.json: Hex8 40 x 4 x 4
+    over 1.0 x 0.05 x 0.05 m, steel (E = 200 GPa, nu = 0.3); x = 0 clamped;
+    a -400 Pa axial traction on the end face x = 1 (1 N of compression)."""
+    spec = column(3, 40, 4, 4, length=1.0, height=0.05, width=0.05, force=-400.0 * 0.05 * 0.05,
+                  young=200.0e9, poisson=0.3)
+    spec.name = "column_hex_buckling_analysis"
+    return spec

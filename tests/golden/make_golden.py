@@ -9,7 +9,11 @@ tests pin:
 * docs/results/benchmarks.csv (the topology benchmarks of
   configs/benchmarks/), the rows on structured Q4/Hex8 grids with point
   loads: DOF count, volume fraction, the first iteration's compliance and
-  the full-solid compliance.
+  the full-solid compliance;
+* docs/results/cross_validation.csv, the structured-grid models of
+  configs/verification/ (cantilever_analysis, block_3d_analysis,
+  column_hex_buckling_analysis): SparLab's largest displacement per load
+  case and its buckling load factors.
 Run from the repository root:
 
     python tests/golden/make_golden.py /path/to/reference
@@ -59,6 +63,19 @@ def main(ref):
         json.dump({"source": "docs/results/benchmarks.csv (configs/benchmarks/<case>.json)",
                    "rows": bench}, f, indent=1)
     print("wrote", out, len(bench), "rows")
+    static, buckling = {}, {}
+    with open(os.path.join(ref, "docs", "results", "cross_validation.csv")) as f:
+        for r in csv.DictReader(f):
+            if r["case"] in ("cantilever_analysis", "block_3d_analysis") and r["sparlab_max_abs_m"]:
+                static[r["case"] + "/" + r["load_case"]] = float(r["sparlab_max_abs_m"])
+            if r["case"] == "column_hex_buckling_analysis" and r["sparlab_load_factors"]:
+                buckling[r["case"]] = json.loads(r["sparlab_load_factors"])
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "verification.json")
+    with open(out, "w") as f:
+        json.dump({"source": "docs/results/cross_validation.csv (configs/verification/<case>.json), "
+                             "SparLab's own columns",
+                   "max_abs_displacement": static, "buckling_load_factors": buckling}, f, indent=1)
+    print("wrote", out, len(static) + len(buckling), "entries")
 
 
 if __name__ == "__main__":
