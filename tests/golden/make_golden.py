@@ -8,8 +8,9 @@ tests pin:
   compliance, CG iterations, AMG levels and operator complexity;
 * docs/results/benchmarks.csv (the topology benchmarks of
   configs/benchmarks/), the rows on structured Q4/Hex8 grids with point
-  loads: DOF count, volume fraction, the first iteration's compliance and
-  the full-solid compliance;
+  loads: DOF count, volume fraction, the first iteration's compliance, the
+  full-solid compliance and, where published, the full-solid design's first
+  natural frequency (consistent mass) and mass;
 * docs/results/cross_validation.csv, the structured-grid models of
   configs/verification/ (cantilever_analysis, block_3d_analysis,
   column_hex_buckling_analysis): SparLab's largest displacement per load
@@ -57,6 +58,8 @@ def main(ref):
                 "initial_compliance": float(r["initial_compliance_J"]),
                 "full_solid_compliance": float(r["full_solid_compliance_J"]),
                 "linear_solver": r["linear_solver"],
+                "f1_solid_hz": float(r["f1_solid_Hz"]) if r["f1_solid_Hz"] else None,
+                "mass_solid_kg": float(r["mass_solid_kg"]) if r["mass_solid_kg"] else None,
             })
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "benchmarks.json")
     with open(out, "w") as f:

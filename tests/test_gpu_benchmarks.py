@@ -4,7 +4,8 @@ the oracle meets the same numbers in tests/test_oracle_benchmarks.py): the
 first SIMP iteration's compliance and the full-solid compliance of
 configs/benchmarks/{mbb_beam, mbb_beam_projected, mbb_beam_robust,
 cantilever_beam, bracket_3d, bracket_3d_projected, bracket_3d_large}.json
-within 1e-9 relative in FP64, 1e-8 in mixed precision."""
+within 1e-9 relative in FP64, 1e-8 in mixed precision; and the full-solid
+design's first natural frequency and mass where the table publishes them."""
 import json
 import os
 
@@ -33,3 +34,19 @@ def test_first_iteration_and_full_solid_compliance(case, precision):
         c = prob.evaluate().compliance
         prob.close()
         assert abs(c / want - 1.0) <= tol, (c, want)
+
+
+@pytest.mark.parametrize("case", ["cantilever_beam", "bracket_3d", "bracket_3d_large"])
+def test_full_solid_first_frequency_and_mass(case):
+    """The benchmarks' modal post-analysis of the full-solid design on the
+    GPU AMG (consistent mass): the first natural frequency and the total mass
+    within 1e-9 of the published values."""
+    with open(GOLDEN) as f:
+        g = {r["case"]: r for r in json.load(f)["rows"]}[case]
+    spec = SPECS[case]()
+    prob = GpuSimpProblem(spec, element_matrix=oracle.Problem(spec).element_matrix(), precision="fp64")
+    r = prob.modal(num_modes=1, mode_shapes=False)
+    prob.close()
+    assert r.converged
+    assert abs(r.frequencies_hz[0] / g["f1_solid_hz"] - 1.0) <= 1e-9, (r.frequencies_hz[0], g["f1_solid_hz"])
+    assert abs(r.total_mass / g["mass_solid_kg"] - 1.0) <= 1e-9

@@ -5,7 +5,8 @@ cantilever_beam, bracket_3d, bracket_3d_projected, bracket_3d_large}.json
 rebuilt by sparlab_gb300.problems, their DOF counts, the first SIMP
 iteration's compliance (uniform design at the volume fraction: the SIMP law,
 the Heaviside projection at beta = 1 and, for the robust run, the eroded
-design) and the full-solid compliance, within 1e-9 relative.  The published
+design) and the full-solid compliance, within 1e-9 relative, and the
+full-solid design's first natural frequency and mass where published.  The published
 values come from the reference's direct LDL^T (AMG-CG for the large
 bracket); these pin the oracle's restatement of the selectors, point-load
 distribution, load-case weights, element matrices, assembly and solve."""
@@ -45,3 +46,16 @@ def test_first_iteration_and_full_solid_compliance(case):
     c1 = float(oracle.Problem(spec).evaluate(np.ones(spec.num_elements))["compliance"])
     assert abs(c0 / g["initial_compliance"] - 1.0) <= 1e-9, (c0, g["initial_compliance"])
     assert abs(c1 / g["full_solid_compliance"] - 1.0) <= 1e-9, (c1, g["full_solid_compliance"])
+
+
+@pytest.mark.parametrize("case", ["cantilever_beam", "bracket_3d"])
+def test_full_solid_first_frequency_and_mass(case):
+    """The benchmarks' modal post-analysis of the full-solid design
+    (consistent mass, 3-point Gauss; the material densities of the configs):
+    the first natural frequency and the total mass within 1e-9."""
+    from oracle import modal as OM
+    g = golden()[case]
+    spec = SPECS[case]()
+    r = OM.solve_modal(oracle.Problem(spec), spec, num_modes=1, density=spec.density, linear="direct")
+    assert abs(r.frequencies_hz[0] / g["f1_solid_hz"] - 1.0) <= 1e-9, (r.frequencies_hz[0], g["f1_solid_hz"])
+    assert abs(r.total_mass / g["mass_solid_kg"] - 1.0) <= 1e-9
