@@ -479,3 +479,21 @@ def column_hex_buckling_analysis() -> ProblemSpec:
                   young=200.0e9, poisson=0.3)
     spec.name = "column_hex_buckling_analysis"
     return spec
+
+
+def column_buckling() -> ProblemSpec:
+    """configs/benchmarks/column_buckling.json: Q4 40 x 80 over 0.5 x 1.0 m,
+    Al 7075-T6 (E = 71.7 GPa, nu = 0.33), t = 10 mm; the base y = 0 clamped;
+    1e5 N down spread over the top nodes with x in [0.2, 0.3]; vf 0.25,
+    radius 3 cells."""
+    spec = ProblemSpec(dim=2, nx=40, ny=80, nz=0, lx=0.5, ly=1.0, lz=0.0, young=71.7e9, poisson=0.33,
+                       thickness=0.01, density=2810.0, volume_fraction=0.25, initial_density=0.25,
+                       rtol=1e-10, name="column_buckling")
+    spec.filter_radius = _radius(spec, 3.0)
+    fixed = np.zeros(spec.num_dofs, np.uint8)
+    for node in box_nodes(spec, ymax=0.0):
+        fixed[node * 2: node * 2 + 2] = 1
+    spec.fixed = fixed
+    spec.loads = point_load(spec, box_nodes(spec, ymin=1.0, xmin=0.2, xmax=0.3), (0.0, -1.0e5))[None, :]
+    spec.weights = np.ones(1)
+    return spec

@@ -10,7 +10,8 @@ tests pin:
   configs/benchmarks/), the rows on structured Q4/Hex8 grids with point
   loads: DOF count, volume fraction, the first iteration's compliance, the
   full-solid compliance and, where published, the full-solid design's first
-  natural frequency (consistent mass) and mass;
+  natural frequency (consistent mass) and mass, and (docs/results/buckling.csv)
+  its smallest buckling load factor;
 * docs/results/cross_validation.csv, the structured-grid models of
   configs/verification/ (cantilever_analysis, block_3d_analysis,
   column_hex_buckling_analysis): SparLab's largest displacement per load
@@ -45,7 +46,12 @@ def main(ref):
                              "tolerance 1e-10)", "rows": rows}, f, indent=1)
     print("wrote", out, len(rows), "rows")
     keep = {"cantilever_beam", "mbb_beam", "mbb_beam_projected", "mbb_beam_robust", "bracket_3d",
-            "bracket_3d_projected", "bracket_3d_large"}
+            "bracket_3d_projected", "bracket_3d_large", "column_buckling"}
+    lam1 = {}
+    with open(os.path.join(ref, "docs", "results", "buckling.csv")) as f:
+        for r in csv.DictReader(f):
+            if r["full_solid_lambda_1"]:
+                lam1[r["case"]] = float(r["full_solid_lambda_1"])
     bench = []
     with open(os.path.join(ref, "docs", "results", "benchmarks.csv")) as f:
         for r in csv.DictReader(f):
@@ -60,6 +66,7 @@ def main(ref):
                 "linear_solver": r["linear_solver"],
                 "f1_solid_hz": float(r["f1_solid_Hz"]) if r["f1_solid_Hz"] else None,
                 "mass_solid_kg": float(r["mass_solid_kg"]) if r["mass_solid_kg"] else None,
+                "full_solid_lambda_1": lam1.get(r["case"]),
             })
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "benchmarks.json")
     with open(out, "w") as f:

@@ -50,3 +50,21 @@ def test_full_solid_first_frequency_and_mass(case):
     assert r.converged
     assert abs(r.frequencies_hz[0] / g["f1_solid_hz"] - 1.0) <= 1e-9, (r.frequencies_hz[0], g["f1_solid_hz"])
     assert abs(r.total_mass / g["mass_solid_kg"] - 1.0) <= 1e-9
+
+
+def test_column_buckling_full_solid_compliance_and_load_factor():
+    """configs/benchmarks/column_buckling.json on the GPU: the full-solid
+    compliance within 1e-9 and the smallest buckling load factor of the
+    full-solid design (6,560 free DOFs: the subspace iteration on the GPU
+    AMG) within 1e-8 of the published values."""
+    with open(GOLDEN) as f:
+        g = {r["case"]: r for r in json.load(f)["rows"]}["column_buckling"]
+    from sparlab_gb300 import problems as P
+    spec = P.column_buckling()
+    prob = GpuSimpProblem(spec, element_matrix=oracle.Problem(spec).element_matrix(), precision="fp64")
+    prob.set_design(np.ones(spec.num_elements))
+    c = prob.evaluate().compliance
+    b = prob.buckling(num_modes=4, tolerance=1e-8, residual_tolerance=1e-6)
+    prob.close()
+    assert abs(c / g["full_solid_compliance"] - 1.0) <= 1e-9
+    assert b.converged and abs(b.load_factors[0] / g["full_solid_lambda_1"] - 1.0) <= 1e-8

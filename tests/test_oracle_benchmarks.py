@@ -59,3 +59,19 @@ def test_full_solid_first_frequency_and_mass(case):
     r = OM.solve_modal(oracle.Problem(spec), spec, num_modes=1, density=spec.density, linear="direct")
     assert abs(r.frequencies_hz[0] / g["f1_solid_hz"] - 1.0) <= 1e-9, (r.frequencies_hz[0], g["f1_solid_hz"])
     assert abs(r.total_mass / g["mass_solid_kg"] - 1.0) <= 1e-9
+
+
+def test_column_buckling_full_solid_compliance_and_load_factor():
+    """configs/benchmarks/column_buckling.json (Q4 40 x 80, base clamped, a
+    top pad load): the full-solid compliance and the full-solid design's
+    smallest buckling load factor (docs/results/buckling.csv), within 1e-9.
+    Its first-iteration compliance is not pinned: the run holds a solid
+    passive pad under the load and starts from the robust projection."""
+    from oracle import buckling as OB
+    g = golden()["column_buckling"]
+    spec = P.column_buckling()
+    assert spec.num_dofs == g["dofs"] and spec.num_elements == g["elements"]
+    c1 = float(oracle.Problem(spec).evaluate(np.ones(spec.num_elements))["compliance"])
+    assert abs(c1 / g["full_solid_compliance"] - 1.0) <= 1e-9
+    r = OB.analyse_buckling(oracle.Problem(spec), spec, num_modes=4, tolerance=1e-8, residual_tolerance=1e-6)
+    assert r.converged and abs(r.load_factors[0] / g["full_solid_lambda_1"] - 1.0) <= 1e-9
