@@ -11,7 +11,8 @@ tests pin:
   loads: DOF count, volume fraction, the first iteration's compliance, the
   full-solid compliance and, where published, the full-solid design's first
   natural frequency (consistent mass) and mass, and (docs/results/buckling.csv)
-  its smallest buckling load factor;
+  its smallest buckling load factor; and the optimisation's length, stop
+  reason, final compliance and achieved volume fraction;
 * docs/results/cross_validation.csv, the structured-grid models of
   configs/verification/ (cantilever_analysis, block_3d_analysis,
   column_hex_buckling_analysis): SparLab's largest displacement per load
@@ -67,6 +68,9 @@ def main(ref):
                 "f1_solid_hz": float(r["f1_solid_Hz"]) if r["f1_solid_Hz"] else None,
                 "mass_solid_kg": float(r["mass_solid_kg"]) if r["mass_solid_kg"] else None,
                 "full_solid_lambda_1": lam1.get(r["case"]),
+                "iterations": int(r["iterations"]), "stop_reason": r["stop_reason"],
+                "final_compliance": float(r["compliance_J"]),
+                "volume_fraction_achieved": float(r["volume_fraction_achieved"]),
             })
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "benchmarks.json")
     with open(out, "w") as f:
