@@ -4,8 +4,11 @@ the oracle meets the same numbers in tests/test_oracle_benchmarks.py): the
 first SIMP iteration's compliance and the full-solid compliance of
 configs/benchmarks/{mbb_beam, mbb_beam_projected, mbb_beam_robust,
 cantilever_beam, bracket_3d, bracket_3d_projected, bracket_3d_large}.json
-within 1e-9 relative in FP64, 1e-8 in mixed precision; and the full-solid
-design's first natural frequency and mass where the table publishes them."""
+within 1e-9 relative in FP64, 1e-8 in mixed precision; the full-solid
+design's first natural frequency and mass where the table publishes them;
+column_buckling.json's full-solid compliance and buckling load factor; and
+whole OC runs of mbb_beam, cantilever_beam and bracket_3d, which stop at the
+published iteration with the published final compliance."""
 import json
 import os
 

@@ -5,11 +5,14 @@ cantilever_beam, bracket_3d, bracket_3d_projected, bracket_3d_large}.json
 rebuilt by sparlab_gb300.problems, their DOF counts, the first SIMP
 iteration's compliance (uniform design at the volume fraction: the SIMP law,
 the Heaviside projection at beta = 1 and, for the robust run, the eroded
-design) and the full-solid compliance, within 1e-9 relative, and the
-full-solid design's first natural frequency and mass where published.  The published
-values come from the reference's direct LDL^T (AMG-CG for the large
-bracket); these pin the oracle's restatement of the selectors, point-load
-distribution, load-case weights, element matrices, assembly and solve."""
+design) and the full-solid compliance, within 1e-9 relative; the
+full-solid design's first natural frequency and mass where published;
+column_buckling.json's full-solid compliance and buckling load factor; and
+the whole MBB OC run, which stops at the published iteration with the
+published final compliance.  The published values come from the
+reference's direct LDL^T (AMG-CG for the large bracket); these pin the
+oracle's restatement of the selectors, point-load distribution, load-case
+weights, element matrices, assembly, solve, filter and OC update."""
 import json
 import os
 
