@@ -8,8 +8,8 @@ the Heaviside projection at beta = 1 and, for the robust run, the eroded
 design) and the full-solid compliance, within 1e-9 relative; the
 full-solid design's first natural frequency and mass where published;
 column_buckling.json's full-solid compliance and buckling load factor; and
-the whole MBB OC run, which stops at the published iteration with the
-published final compliance.  The published values come from the
+the whole OC runs of mbb_beam and cantilever_beam, which stop at the
+published iteration with the published final compliance.  The published values come from the
 reference's direct LDL^T (AMG-CG for the large bracket); these pin the
 oracle's restatement of the selectors, point-load distribution, load-case
 weights, element matrices, assembly, solve, filter and OC update."""
@@ -80,17 +80,18 @@ def test_column_buckling_full_solid_compliance_and_load_factor():
     assert r.converged and abs(r.load_factors[0] / g["full_solid_lambda_1"] - 1.0) <= 1e-9
 
 
-def test_mbb_optimisation_stops_where_published():
-    """The whole OC run of configs/benchmarks/mbb_beam.json (move 0.2,
-    damping 0.5, density filter of 4.5 cells, change tolerance 1e-2): the
-    design change first falls below the tolerance at the published iteration
-    (434, stop reason design_change), where the compliance is within 1e-5 of
-    the published final value (observed 1.4e-6 after 434 iterations of a
-    solver that differs in rounding: AMG-PCG to 1e-10 against LDL^T) at the
-    volume target."""
-    g = golden()["mbb_beam"]
+@pytest.mark.parametrize("case", ["mbb_beam", "cantilever_beam"])
+def test_optimisation_stops_where_published(case):
+    """The whole OC run of configs/benchmarks/{mbb_beam, cantilever_beam}.json
+    (move 0.2, damping 0.5, density filters of 4.5 and 2 cells, change
+    tolerance 1e-2): the design change first falls below the tolerance at the
+    published iteration (434 and 362, stop reason design_change), where the
+    compliance is within 1e-5 of the published final value (observed 1.4e-6
+    and 1.2e-6 after hundreds of iterations of a solver that differs in
+    rounding: AMG-PCG to 1e-10 against LDL^T) at the volume target."""
+    g = golden()[case]
     assert g["stop_reason"] == "design_change"
-    spec = P.mbb_beam()
+    spec = SPECS[case]()
     _, h = oracle.Problem(spec).run(g["iterations"] + 50, change_tol=1e-2)
     assert len(h) == g["iterations"]
     assert abs(h[-1, 0] / g["final_compliance"] - 1.0) <= 1e-5, (h[-1, 0], g["final_compliance"])
