@@ -12,8 +12,9 @@ from __future__ import annotations
 
 import ctypes as C
 import dataclasses
+import math
 import time
-from typing import List, Optional
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -429,16 +430,42 @@ def optimality_criteria_update(problem: GpuSimpProblem) -> OptimalityCriteriaSte
     return problem.oc_update(apply=False, download=True)
 
 
-class TopologyOptimizer:
-    """``run_oc`` with the evaluation, OC update and clamp on the GPU."""
+def objective_spread(compliances: Sequence[float], window: int) -> float:
+    """Relative spread (max - min) / |c_k| of the last ``window`` + 1
+    compliances, infinite while fewer are known
+    (``objective_spread``, src/topopt/TopologyOptimizer.cpp:124-130)."""
+    w = max(int(window), 1)
+    if len(compliances) <= w:
+        return math.inf
+    last = compliances[-(w + 1):]
+    return (max(last) - min(last)) / max(abs(compliances[-1]), 1e-30)
 
-    def __init__(self, problem: GpuSimpProblem, max_iterations=200, change_tolerance=1e-3):
+
+class TopologyOptimizer:
+    """``run_oc`` with the evaluation, OC update and clamp on the GPU.
+
+    The run stops (src/topopt/TopologyOptimizer.cpp:675-704), once the
+    projection's beta schedule is at its final stage, when the design change
+    is at most ``change_tolerance`` (stop reason "design_change") or, with a
+    positive ``objective_tolerance``, when the compliance's relative spread
+    over the last ``objective_window`` + 1 iterations is at most that
+    ("objective_stall"); otherwise after ``max_iterations``
+    ("iteration_cap").  ``change_tolerance`` <= 0 disables the first rule."""
+
+    def __init__(self, problem: GpuSimpProblem, max_iterations=200, change_tolerance=1e-3,
+                 objective_tolerance=0.0, objective_window=5):
         self.problem = problem
         self.max_iterations = max_iterations
         self.change_tolerance = change_tolerance
+        self.objective_tolerance = objective_tolerance
+        self.objective_window = objective_window
+        self.stop_reason = ""
+        self.final_objective_change = math.inf
 
     def run(self) -> List[TopologyIteration]:
         history = []
+        compliances: List[float] = []
+        self.stop_reason = "iteration_cap"
         for it in range(1, self.max_iterations + 1):
             t0 = time.perf_counter()
             r = self.problem.iterate()
@@ -448,8 +475,14 @@ class TopologyOptimizer:
                                              bool(r.volume_converged), r.beta, bool(r.final_stage),
                                              r.eroded_volume_fraction, r.dilated_volume_fraction,
                                              r.dilated_target_fraction))
+            compliances.append(r.compliance)
+            change_ok = self.change_tolerance > 0 and r.max_change <= self.change_tolerance
+            self.final_objective_change = objective_spread(compliances, self.objective_window)
+            objective_ok = (self.objective_tolerance > 0
+                            and self.final_objective_change <= self.objective_tolerance)
             # during beta continuation only the final stage may stop the run
-            if self.change_tolerance > 0 and r.final_stage and r.max_change <= self.change_tolerance:
+            if r.final_stage and (change_ok or objective_ok):
+                self.stop_reason = "design_change" if change_ok else "objective_stall"
                 break
         return history
 
